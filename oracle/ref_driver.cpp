@@ -1,0 +1,160 @@
+// ref_driver.cpp -- C entry points around the reference's own CPU classes, built with
+// oracle/Makefile.ref into oracle/_ref/libvfref.so from the reference source tree.
+//
+// Test infrastructure only.  It lets the tests and the fixture generator run the
+// reference's TSDFVolume::integrate, MarchingCubes::computeIsoSurface/computePointCloud,
+// af::buildGraph, af::getKnnData, af::filterDisconnected and MotionGraph::warp on
+// in-memory inputs.  Nothing here re-implements the reference; it only marshals arrays.
+#include <af/GraphBuilder.h>
+#include <af/MarchingCubes.h>
+#include <af/Mesh.h>
+#include <af/MotionGraph.h>
+#include <af/TSDFVolume.h>
+
+#include <cstring>
+#include <vector>
+
+namespace {
+
+Mat3f mat3(const float* cm) {
+    Mat3f M;
+    std::memcpy(M.data(), cm, sizeof(float) * 9);
+    return M;
+}
+
+void load_graph(MotionGraph& g, const float* nodes, const float* radii, const float* T, int n) {
+    for (int i = 0; i < n; ++i) {
+        Mat4f M;
+        std::memcpy(M.data(), T + 16 * i, sizeof(float) * 16);
+        g.push_back(Vec3f(nodes[3 * i], nodes[3 * i + 1], nodes[3 * i + 2]), radii[i], M);
+    }
+}
+
+template <int K>
+void knn_impl(const MotionGraph& g, const float* pts, long m, int exclude, unsigned* idx, float* dist) {
+    std::vector<Vec3f> P(m);
+    for (long i = 0; i < m; ++i) P[i] = Vec3f(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+    std::vector<Vecui<K>> I;
+    std::vector<Vecf<K>> D;
+    af::getKnnData(I, D, g, P, exclude != 0);
+    for (long i = 0; i < m; ++i)
+        for (int s = 0; s < K; ++s) {
+            idx[i * K + s] = I[i][s];
+            dist[i * K + s] = D[i][s];
+        }
+}
+
+template <int K>
+void filter_impl(const MotionGraph& g, unsigned* idx, float* dist, int n) {
+    std::vector<Vecui<K>> I(n);
+    std::vector<Vecf<K>> D(n);
+    for (int i = 0; i < n; ++i)
+        for (int s = 0; s < K; ++s) {
+            I[i][s] = idx[i * K + s];
+            D[i][s] = dist[i * K + s];
+        }
+    af::filterDisconnected(I, D, g);
+    for (int i = 0; i < n; ++i)
+        for (int s = 0; s < K; ++s) {
+            idx[i * K + s] = I[i][s];
+            dist[i * K + s] = D[i][s];
+        }
+}
+
+}  // namespace
+
+extern "C" {
+
+// TSDFVolume::integrate (src/TSDFVolume.cpp:55-171); pose = Mat4f column-major
+void ref_integrate(float* tsdf, float* weights, const float* depth, int width, int height, const float* K,
+                   const int* dims, const float* size, float delta, const float* pose) {
+    TSDFVolume vol(Vec3i(dims[0], dims[1], dims[2]), Vec3f(size[0], size[1], size[2]), mat3(K));
+    vol.setDelta(delta);
+    std::vector<unsigned char> color((size_t)width * height * 3, 0);
+    cv::Mat c(height, width, color.data());
+    cv::Mat d(height, width, const_cast<float*>(depth));
+    Mat4f P;
+    std::memcpy(P.data(), pose, sizeof(float) * 16);
+    vol.integrate(P, c, d);
+    std::memcpy(tsdf, vol.tsdf().data(), sizeof(float) * vol.tsdf().size());
+    std::memcpy(weights, vol.tsdfWeights().data(), sizeof(float) * vol.tsdfWeights().size());
+}
+
+// MarchingCubes::computeIsoSurface / computePointCloud (src/MarchingCubes.cpp:297, :484)
+long ref_marching_cubes(const float* tsdf, const float* weights, const int* dims, const float* size, float iso,
+                        int point_cloud, float* verts, long vcap, int* faces, long fcap, long* nfaces) {
+    const size_t S = (size_t)dims[0] * dims[1] * dims[2];
+    std::vector<float> t(tsdf, tsdf + S), w(weights, weights + S);
+    std::vector<unsigned char> col(S + 2, 127);
+    MarchingCubes mc(Vec3i(dims[0], dims[1], dims[2]), Vec3f(size[0], size[1], size[2]));
+    Mesh mesh;
+    if (point_cloud) mc.computePointCloud(mesh, t, w, col, col, col, iso);
+    else mc.computeIsoSurface(mesh, t, w, col, col, col, iso);
+    const auto& V = mesh.vertexCloud().vec_;
+    for (size_t i = 0; i < V.size() && (long)i < vcap; ++i)
+        for (int c = 0; c < 3; ++c) verts[3 * i + c] = V[i][c];
+    const auto& F = mesh.faces();
+    for (size_t i = 0; i < F.size() && (long)i < fcap; ++i)
+        for (int c = 0; c < 3; ++c) faces[3 * i + c] = F[i][c];
+    if (nfaces) *nfaces = (long)F.size();
+    return (long)V.size();
+}
+
+// af::buildGraph (src/GraphBuilder.cpp:12-50)
+int ref_build_graph(float* nodes, float* radii, float* T, int n, int cap, const float* mesh, long m, int knn,
+                    float radius) {
+    MotionGraph g;
+    load_graph(g, nodes, radii, T, n);
+    std::vector<Vec3f> P(m);
+    for (long i = 0; i < m; ++i) P[i] = Vec3f(mesh[3 * i], mesh[3 * i + 1], mesh[3 * i + 2]);
+    af::buildGraph(g, P, (std::size_t)knn, radius);
+    int nn = (int)g.graph().size();
+    if (nn > cap) return -1;
+    for (int i = 0; i < nn; ++i) {
+        for (int c = 0; c < 3; ++c) nodes[3 * i + c] = g.graph().vec_[i][c];
+        radii[i] = g.radiuses()[i];
+        std::memcpy(T + 16 * i, g.transforms()[i].data(), sizeof(float) * 16);
+    }
+    return nn;
+}
+
+// af::getKnnData<K> (include/af/GraphBuilder.h:118-130); K in {4, 6, 8}
+int ref_knn(const float* nodes, const float* radii, int n, const float* pts, long m, int k, int exclude,
+            unsigned* idx, float* dist) {
+    MotionGraph g;
+    std::vector<float> T((size_t)16 * n, 0.f);
+    load_graph(g, nodes, radii, T.data(), n);
+    switch (k) {
+        case 4: knn_impl<4>(g, pts, m, exclude, idx, dist); return 0;
+        case 6: knn_impl<6>(g, pts, m, exclude, idx, dist); return 0;
+        case 8: knn_impl<8>(g, pts, m, exclude, idx, dist); return 0;
+    }
+    return -1;
+}
+
+// af::filterDisconnected<K> (include/af/GraphBuilder.h:132-146)
+int ref_filter_disconnected(const float* nodes, const float* radii, int n, int k, unsigned* idx, float* dist) {
+    MotionGraph g;
+    std::vector<float> T((size_t)16 * n, 0.f);
+    load_graph(g, nodes, radii, T.data(), n);
+    switch (k) {
+        case 4: filter_impl<4>(g, idx, dist, n); return 0;
+        case 6: filter_impl<6>(g, idx, dist, n); return 0;
+        case 8: filter_impl<8>(g, idx, dist, n); return 0;
+    }
+    return -1;
+}
+
+// MotionGraph::warp (src/MotionGraph.cpp:62-90)
+void ref_warp(const float* nodes, const float* radii, const float* T, int n, const float* pts, long m, int k,
+              float* out) {
+    MotionGraph g;
+    load_graph(g, nodes, radii, T, n);
+    std::vector<Vec3f> P(m), W;
+    for (long i = 0; i < m; ++i) P[i] = Vec3f(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]);
+    g.warp(W, P, (size_t)k);
+    for (long i = 0; i < m; ++i)
+        for (int c = 0; c < 3; ++c) out[3 * i + c] = W[i][c];
+}
+
+}  // extern "C"

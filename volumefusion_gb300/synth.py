@@ -1,0 +1,130 @@
+"""Seeded synthetic depth scenes standing in for the reference's recorded sequences.
+
+The reference reads private 16-bit depth PNGs (millimetres) from disk
+(src/dataset.cpp:168-189).  These renderers produce the same kind of frame --
+uint16 millimetres, 0 where a pixel sees nothing -- from analytic scenes, ray-cast in
+float64 through a pinhole camera with pixel (u, v) on the ray ((u-cx)/fx, (v-cy)/fy, 1).
+
+Noise is N(0, (1 mm * (z / 1 m)^2)^2) per pixel.  It is drawn from a counter-based
+generator (splitmix64 of seed and pixel index, Box-Muller), written here in numpy
+integer arithmetic, so that a frame is bit-identical on every machine and numpy version.
+"""
+import math
+
+import numpy as np
+
+_M64 = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+def _splitmix64(x):
+    x = (x + np.uint64(0x9E3779B97F4A7C15)) & _M64
+    z = x
+    z = ((z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)) & _M64
+    z = ((z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)) & _M64
+    return z ^ (z >> np.uint64(31))
+
+
+def gaussian_noise(seed, n, stream=0):
+    """n standard normal samples for (seed, stream), identical on every platform."""
+    with np.errstate(over="ignore"):
+        base = np.uint64((seed * 0x100000001B3 + stream * 0x9E3779B1) & 0xFFFFFFFFFFFFFFFF)
+        idx = np.arange(n, dtype=np.uint64)
+        a = _splitmix64(base ^ (idx * np.uint64(2)))
+        b = _splitmix64(base ^ (idx * np.uint64(2) + np.uint64(1)))
+    u1 = ((a >> np.uint64(11)).astype(np.float64) + 0.5) / float(1 << 53)
+    u2 = ((b >> np.uint64(11)).astype(np.float64) + 0.5) / float(1 << 53)
+    return np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * math.pi * u2)
+
+
+def intrinsics(fx, fy, cx, cy):
+    """3x3 pinhole matrix (row-major numpy; column-major float[9] via .T.ravel())."""
+    return np.array([[fx, 0.0, cx], [0.0, fy, cy], [0.0, 0.0, 1.0]], dtype=np.float64)
+
+
+def _rays(width, height, K):
+    u, v = np.meshgrid(np.arange(width, dtype=np.float64), np.arange(height, dtype=np.float64))
+    dx = (u - K[0, 2]) / K[0, 0]
+    dy = (v - K[1, 2]) / K[1, 1]
+    return np.stack([dx, dy, np.ones_like(dx)], axis=-1)
+
+
+def _hit_sphere(d, c, r):
+    dd = np.einsum("...i,...i->...", d, d)
+    dc = d @ c
+    disc = dc * dc - dd * (c @ c - r * r)
+    t = np.full(dd.shape, np.inf)
+    ok = disc >= 0
+    t[ok] = (dc[ok] - np.sqrt(disc[ok])) / dd[ok]
+    t[t <= 0] = np.inf
+    return t
+
+
+def _hit_capsule(d, a, b, r):
+    """Nearest positive ray parameter for a capsule (segment a-b, radius r), inf on a miss."""
+    ab = b - a
+    L2 = ab @ ab
+    ax = ab / math.sqrt(L2)
+    dd = np.einsum("...i,...i->...", d, d)
+    # infinite cylinder around the axis through a: |(t d - a) x ax|^2 = r^2
+    dpar = d @ ax
+    dperp = d - dpar[..., None] * ax
+    apar = -a @ ax
+    aperp = -a - apar * ax
+    A = np.einsum("...i,...i->...", dperp, dperp)
+    B = 2.0 * (dperp @ aperp)
+    C = aperp @ aperp - r * r
+    disc = B * B - 4 * A * C
+    t = np.full(dd.shape, np.inf)
+    ok = (disc >= 0) & (A > 1e-15)
+    tc = np.full(dd.shape, np.inf)
+    tc[ok] = (-B[ok] - np.sqrt(disc[ok])) / (2 * A[ok])
+    s = np.full(dd.shape, np.nan)
+    s[ok] = tc[ok] * dpar[ok] + apar  # axial coordinate of the hit relative to a
+    body = ok & (tc > 0) & (s >= 0) & (s <= math.sqrt(L2))
+    t[body] = tc[body]
+    t = np.minimum(t, _hit_sphere(d, a, r))
+    t = np.minimum(t, _hit_sphere(d, b, r))
+    return t
+
+
+def _to_mm(z, seed, frame):
+    noise = gaussian_noise(seed, z.size, stream=frame).reshape(z.shape)
+    valid = np.isfinite(z)
+    zz = np.where(valid, z, 0.0)
+    sigma = 0.001 * zz * zz
+    mm = np.rint((zz + sigma * noise) * 1000.0)
+    mm = np.where(valid, np.clip(mm, 0, 65535), 0)
+    return mm.astype(np.uint16)
+
+
+def sphere_frame(width=320, height=288, fx=252.0, fy=252.0, cx=160.0, cy=144.0, radius=0.150,
+                 center=(0.0, 0.0, 0.600), seed=0):
+    """Single depth frame of a sphere (rigid single-frame workload: 320x288, r=150 mm at 600 mm)."""
+    K = intrinsics(fx, fy, cx, cy)
+    d = _rays(width, height, K)
+    t = _hit_sphere(d, np.asarray(center, dtype=np.float64), radius)
+    return _to_mm(t, seed, 0), K
+
+
+def capsule_pair_frame(frame, n_frames=30, width=640, height=576, fx=504.0, fy=504.0, cx=320.0, cy=288.0,
+                       radius=0.060, length=0.300, joint=(0.0, 0.0, 0.800), max_bend_deg=45.0, seed=0):
+    """Frame `frame` of the articulated capsule pair: two capsules of the given radius and length
+    meeting at `joint`; the second one bends linearly from 0 to max_bend_deg about the camera y
+    axis (its free end swings toward the camera) over n_frames frames."""
+    K = intrinsics(fx, fy, cx, cy)
+    d = _rays(width, height, K)
+    j = np.asarray(joint, dtype=np.float64)
+    theta = math.radians(max_bend_deg) * (frame / max(n_frames - 1, 1))
+    a_end = j + length * np.array([-1.0, 0.0, 0.0])
+    b_end = j + length * np.array([math.cos(theta), 0.0, -math.sin(theta)])
+    t = np.minimum(_hit_capsule(d, a_end, j, radius), _hit_capsule(d, j, b_end, radius))
+    return _to_mm(t, seed, frame), K
+
+
+def capsule_pair_sequence(n_frames=30, **kw):
+    frames = []
+    K = None
+    for f in range(n_frames):
+        mm, K = capsule_pair_frame(f, n_frames=n_frames, **kw)
+        frames.append(mm)
+    return np.stack(frames), K
