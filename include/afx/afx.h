@@ -1,0 +1,313 @@
+/*
+ * afx.h -- C ABI of the GB300 (sm_103a) implementation of VolumeFusion's per-frame
+ * non-rigid TSDF depth-fusion hot path.
+ *
+ * Conventions (replacing the reference's af:: free functions and classes):
+ *  - Plain pointers and sizes only.  Array arguments are DEVICE pointers unless the
+ *    name ends in _host.  Layouts are the reference's: Vec3f = 3 packed floats,
+ *    Mat3f / Mat4f = 9 / 16 floats column-major, per-point KNN = K contiguous slots,
+ *    Vec2i = 2 ints, voxel index z*X*Y + y*X + x.
+ *  - Every call takes an explicit stream (cudaStream_t passed as void*, NULL = legacy
+ *    default stream) and is asynchronous unless stated; the reference blocked on
+ *    cudaDeviceSynchronize after every launch.
+ *  - Every call returns an afx_status; no C++ exception crosses the ABI (the reference
+ *    threw std::runtime_error from CUDA_CHECK, src/Helper.cu:7-20).
+ *  - Outputs with a data-dependent length take a capacity and a device counter; a
+ *    launch that would overflow stores at most `capacity` items, keeps counting, and
+ *    the overflow shows as counter > capacity (the reference wrote past the end).
+ *  - Calls that need temporary device memory take (workspace, workspace_bytes); the
+ *    matching *_workspace_size() returns the bytes needed.
+ */
+#ifndef AFX_AFX_H
+#define AFX_AFX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum afx_status {
+    AFX_OK = 0,
+    AFX_ERR_INVALID_ARGUMENT = 1,
+    AFX_ERR_CAPACITY = 2,        /* an output or internal capacity was exceeded */
+    AFX_ERR_CUDA = 3,            /* a CUDA runtime call failed */
+    AFX_ERR_SINGULAR = 4,        /* the Gauss-Newton system has a singular diagonal block */
+    AFX_ERR_WORKSPACE = 5,       /* workspace too small */
+    AFX_ERR_UNSUPPORTED = 6,     /* input outside what this implementation supports */
+    AFX_ERR_TIMEOUT = 7,         /* a bounded device-side wait gave up */
+    AFX_ERR_NO_MEMORY = 8
+} afx_status;
+
+#define AFX_INVALID_INDEX 0xFFFFFFFFu
+
+const char* afx_status_string(int status);
+int afx_version(void);
+/* Last CUDA error seen by the library on this thread (cudaError_t value), 0 if none. */
+int afx_last_cuda_error(void);
+
+/* ------------------------------------------------------------------------------------
+ * Depth pre-processing (src/VertexManipulation.cu, src/BilateralFilter.cu)
+ * ------------------------------------------------------------------------------------ */
+
+/* uint16 millimetres -> float metres (depth.convertTo(CV_32FC1, 1/1000), src/dataset.cpp:188). */
+int afx_depth_from_mm(float* depth, const uint16_t* depth_mm, long n, void* stream);
+
+/* af::runFilterDepthKernel (include/af/VertexManipulation.cuh:11, src/VertexManipulation.cu:17):
+ * values > threshold, < 1e-4 or NaN become +inf. */
+int afx_filter_depth(float* depth, long n, float threshold, void* stream);
+
+/* af::bilateralFilterTextureOpmShared (include/af/BilateralFilter.cuh:8,
+ * src/BilateralFilter.cu:180): radius r, range sigma sigma_i (m), spatial sigma
+ * sigma_s (px), hard range threshold thr (m).  out and in must not alias. */
+int afx_bilateral_filter(float* out, const float* in, int height, int width, int r, double sigma_i, double sigma_s,
+                         float thr, void* stream);
+
+/* af::runDepthToMeshKernel (include/af/VertexManipulation.cuh:13, src/VertexManipulation.cu:65). */
+int afx_depth_to_mesh(float* vertices, const float* depth, int width, int height, const float K[9], void* stream);
+
+/* af::runDepthVerticesNormalsKernel (include/af/VertexManipulation.cuh:23,
+ * src/VertexManipulation.cu:209).  Border pixels get a zero normal (the reference leaves
+ * them unwritten). */
+int afx_depth_vertices_normals(float* normals, const float* vertices, int height, int width, float excl_angle_lo,
+                               float excl_angle_hi, void* stream);
+
+/* af::runRemoveDepthWithoutNormalsKernel (include/af/VertexManipulation.cuh:30, src/VertexManipulation.cu:238). */
+int afx_remove_depth_without_normals(const float* normals, float* vertices, float* depth, int height, int width,
+                                     void* stream);
+
+typedef struct afx_prep_params {
+    float K[9];              /* depth intrinsics, column-major */
+    float depth_threshold;   /* settings.depthThreshold */
+    int bilateral;           /* settings.bilateralFiltr */
+    int bilateral_r;         /* settings.bilateralD (used as the radius) */
+    float sigma_i, sigma_s;  /* settings.bilateralSigmaI / SigmaS */
+    float bilateral_thr;     /* settings.bilateralThreshold */
+    float excl_angle_lo, excl_angle_hi;  /* settings.normExclAngleRange */
+} afx_prep_params;
+
+/* af::loadProcessFrame after the image is in memory (src/VolumeFusion.cu:184-220), fused:
+ * mm -> metres, filter, bilateral, back-projection, normals, removal of pixels without a
+ * normal, and the centroid of the valid vertices (written to centroid[3], device).
+ * One kernel (TMA-staged tiles) plus a 1-thread finaliser. */
+int afx_frame_prep(const uint16_t* depth_mm, int width, int height, const afx_prep_params* params, float* depth,
+                   float* vertices, float* normals, float* centroid, void* stream);
+
+/* ------------------------------------------------------------------------------------
+ * TSDF integration (src/TSDFIntegration.cu)
+ * ------------------------------------------------------------------------------------ */
+
+/* af::runIntegrateTSDFFromFrameKernel (include/af/TSDFIntegration.cuh:8,
+ * src/TSDFIntegration.cu:98); DeviceTsdf::integrate (include/af/DeviceTsdf.cuh:28). */
+int afx_integrate_tsdf(float* tsdf, float* weights, const float* depth, int width, int height, float delta,
+                       const int dims[3], const float voxel_size[3], const float volume_size[3], const float rotate[9],
+                       const float translate[3], const float K[9], void* stream);
+
+/* ------------------------------------------------------------------------------------
+ * Voxel warp and warped integration (src/TSDFWarp.cu, src/TSDFIntegration.cu)
+ * Dense per-voxel forms with the reference's layouts.  The fused session path uses
+ * brick-sparse kernels instead (afx_fusion_*).
+ * ------------------------------------------------------------------------------------ */
+
+/* af::runTsdfKNNGraph (include/af/TSDFWarp.h:9, src/TSDFWarp.cu:70).  Slots hold the K
+ * nearest supporting nodes ordered by (distance, node index); the reference keeps the
+ * first K to arrive, so the two agree where a voxel has at most K supporting nodes.
+ * knn_counts need not be zeroed. */
+int afx_tsdf_knn(uint32_t* knn_idx, float* knn_dist, int* knn_counts, const float* nodes, const float* radii,
+                 int n_nodes, const float voxel_size[3], const float volume_size[3], const int dims[3],
+                 const int voxels_per_node[3], int k, void* workspace, size_t workspace_bytes, void* stream);
+size_t afx_tsdf_knn_workspace_size(const int dims[3], int n_nodes, const int voxels_per_node[3]);
+
+/* af::runComputeTsdfWarpWeightsKernel (include/af/TSDFWarp.h:18, src/TSDFWarp.cu:118). */
+int afx_tsdf_warp_weights(float* knn_weights, const float* radii, const uint32_t* knn_idx, const float* knn_dist,
+                          const int* knn_counts, long n_voxels, int k, void* stream);
+
+/* af::runGenerateTsdfVerticesKernel (include/af/TSDFWarp.h:25, src/TSDFWarp.cu:147). */
+int afx_tsdf_vertices(float* vertices, const float voxel_size[3], const float volume_size[3], const int dims[3],
+                      void* stream);
+
+/* af::runWarpTsdfKernel (include/af/TSDFWarp.h:27, src/TSDFWarp.cu:192). */
+int afx_warp_tsdf(float* vertices, const float* transforms, const uint32_t* knn_idx, const float* knn_weights,
+                  const int* knn_counts, long n_voxels, int k, void* stream);
+
+/* af::runCountCollisionsPerVoxelKernel (include/af/TSDFIntegration.cuh:49,
+ * src/TSDFIntegration.cu:285).  Adds to `counts` (zero it first, as the reference does). */
+int afx_count_collisions(int* counts, const float* vertices, const int* knn_counts, const float voxel_size[3],
+                         const float volume_size[3], const int dims[3], const float rotate[9], const float translate[3],
+                         void* stream);
+
+/* af::runIntegrateWarpedTSDFFromFrameKernel (include/af/TSDFIntegration.cuh:34, src/TSDFIntegration.cu:228). */
+int afx_integrate_warped_tsdf(float* tsdf, float* weights, const float* vertices, const int* collisions,
+                              const int* knn_counts, const float* depth, int width, int height, float delta,
+                              const float voxel_size[3], const float volume_size[3], const int dims[3],
+                              const float rotate[9], const float translate[3], const float K[9], void* stream);
+
+/* ------------------------------------------------------------------------------------
+ * Marching cubes (src/MarchingCubes.cu) and point-cloud de-duplication
+ * ------------------------------------------------------------------------------------ */
+
+/* af::runMarchingCubesMeshKernel (include/af/MarchingCubes.cuh:12, src/MarchingCubes.cu:510):
+ * one vertex per cut edge of every non-trivial cube; *count (device, caller-zeroed) receives
+ * the number produced.  Output order is unspecified, as in the reference. */
+int afx_marching_cubes_points(float* points, unsigned* count, long capacity, const float* tsdf, const float* weights,
+                              const int dims[3], const float voxel_size[3], const float volume_size[3], float iso,
+                              void* stream);
+
+/* af::runMarchingCubesFullKernel (include/af/MarchingCubes.cuh:21, src/MarchingCubes.cu:683):
+ * three vertices and one face per non-degenerate triangle.  Counters are device, caller-zeroed. */
+int afx_marching_cubes_mesh(float* vertices, unsigned* vertex_count, long vertex_capacity, int* faces,
+                            unsigned* face_count, long face_capacity, const float* tsdf, const float* weights,
+                            const int dims[3], const float voxel_size[3], const float volume_size[3], float iso,
+                            void* stream);
+
+/* thrust::sort + thrust::unique of Vec3f with the lexicographic operator<
+ * (src/VolumeFusion.cu:382-384, include/af/eigen_extension.cuh:15-25).  Sorts points[0..*count)
+ * in place and rewrites *count (device) with the number of distinct points.
+ * n_max bounds *count. */
+int afx_sort_unique_points(float* points, unsigned* count, long n_max, void* workspace, size_t workspace_bytes,
+                           void* stream);
+size_t afx_sort_unique_points_workspace_size(long n_max);
+
+/* DeviceTsdf::extractPointCloud (include/af/DeviceTsdf.cuh:34-42): marching-cubes points,
+ * then sort + unique. */
+int afx_extract_point_cloud(float* points, unsigned* count, long capacity, const float* tsdf, const float* weights,
+                            const int dims[3], const float voxel_size[3], const float volume_size[3], float iso,
+                            void* workspace, size_t workspace_bytes, void* stream);
+
+/* af::runTranslateKernel (include/af/VertexManipulation.cuh:16): points += t for
+ * points[0..n) where n = *count if count != NULL else n_max. */
+int afx_translate(float* points, const unsigned* count, long n_max, const float t[3], void* stream);
+
+/* ------------------------------------------------------------------------------------
+ * Motion graph, KNN, skinning, correspondences
+ * (src/GraphBuilder.cpp, include/af/GraphBuilder.h, src/MotionGraph.cpp, src/VertexManipulation.cu,
+ *  src/ComputeCorrespondence.cu)
+ * ------------------------------------------------------------------------------------ */
+
+/* af::buildGraph (include/af/GraphBuilder.h:12, src/GraphBuilder.cpp:12), on the device.
+ * mesh[0..*mesh_count) is the sorted, translated canonical point cloud.  Nodes
+ * (positions, radii, transforms) are appended in place; *n_nodes (device) is read and
+ * updated.  All existing radii must equal `radius` (the pipeline's case); otherwise
+ * AFX_ERR_UNSUPPORTED.  Node selection equals the reference's sequential greedy order. */
+int afx_build_graph(float* nodes, float* radii, float* transforms, int* n_nodes, int node_capacity,
+                    const float* mesh, const unsigned* mesh_count, long mesh_max, int knn, float radius,
+                    void* workspace, size_t workspace_bytes, void* stream);
+size_t afx_build_graph_workspace_size(long mesh_max, int node_capacity);
+
+/* af::getKnnData<K> (include/af/GraphBuilder.h:118): the k nearest nodes of each point
+ * (exclude_closest drops the nearest one, for node-to-node neighbours), ordered by
+ * nanoflann's squared distance, equal distances by node index; distances are sqrt'ed;
+ * missing slots hold AFX_INVALID_INDEX / FLT_MAX.  n_points = *count if count != NULL. */
+int afx_knn(uint32_t* idx, float* dist, const float* nodes, const int* n_nodes, int n_nodes_max, const float* points,
+            const unsigned* count, long n_points_max, int k, int exclude_closest, void* stream);
+
+/* af::filterDisconnected<K> (include/af/GraphBuilder.h:132). */
+int afx_filter_disconnected(uint32_t* idx, float* dist, const int* n_nodes, int n_nodes_max, int k,
+                            const float* radii, void* stream);
+
+/* af::runComputeWarpWeightsKernel (include/af/VertexManipulation.cuh:18, src/VertexManipulation.cu:134). */
+int afx_warp_weights(float* weights, const float* radii, const uint32_t* idx, const float* dist, const unsigned* count,
+                     long n_points_max, int k, const int* n_nodes, void* stream);
+
+/* af::runWarpKernel (include/af/ComputeCorrespondence.cuh:11, src/ComputeCorrespondence.cu:32). */
+int afx_warp(float* warped, const float* points, const float* transforms, const uint32_t* idx, const float* weights,
+             const unsigned* count, long n_points_max, int k, void* stream);
+
+/* af::runCorrespondencePairsKernel (include/af/ComputeCorrespondence.cuh:19,
+ * src/ComputeCorrespondence.cu:83): (vertex, pixel) pairs, ordered by vertex index.
+ * *corr_count (device) is overwritten. */
+int afx_correspondences(int* corr, unsigned* corr_count, long capacity, const float* warped, const unsigned* count,
+                        long n_points_max, const float K[9], const float* depth, int rows, int cols,
+                        const float* frame_vertices, float thresh, void* workspace, size_t workspace_bytes,
+                        void* stream);
+size_t afx_correspondences_workspace_size(long n_points_max);
+
+/* ------------------------------------------------------------------------------------
+ * Whole-frame session: af::runVolumeFusion's per-frame loop (src/VolumeFusion.cu:223-769)
+ * with all state (TSDF, motion graph, solver) resident on the device.
+ * ------------------------------------------------------------------------------------ */
+
+typedef struct afx_fusion_params {
+    int width, height;
+    float K[9];
+    int dims[3];
+    float volume_size[3];
+    float delta;                 /* settings.tsdfDelta */
+    float depth_threshold;
+    int bilateral, bilateral_r;
+    float sigma_i, sigma_s, bilateral_thr;
+    float excl_angle_lo, excl_angle_hi;
+    float graph_radius;          /* settings.motionGraphRadius */
+    int knn;                     /* skinning neighbours (reference: Constants::motionGraphKNN = 6); 1..8 */
+    int kreg;                    /* regularisation neighbours (reference: Constants::energyMRegKNN = 4); 1..8 */
+    int update_graph;
+    int icp_iterations;
+    int gn_iterations;           /* reference: 20 */
+    float lambda_depth, lambda_reg, energy_min_step, corr_thresh;
+    int solver;                  /* 1 = block-Jacobi PCG (fixed iterations); 2 = PCG to pcg_tol */
+    int pcg_iterations;
+    double pcg_tol;
+    int integrate;               /* settings.integrateTsdf */
+    int extract_mesh;            /* run the full marching-cubes mesh each frame */
+    int node_capacity;
+    long mesh_capacity;          /* canonical point cloud capacity */
+    long triangle_capacity;
+} afx_fusion_params;
+
+typedef struct afx_fusion afx_fusion;
+
+typedef struct afx_frame_stats {
+    int frame;
+    int n_nodes;
+    int new_nodes;
+    unsigned mesh_points;        /* canonical point cloud size after de-duplication */
+    unsigned correspondences;
+    int gn_iterations_done;
+    double energy;               /* last evaluated energy */
+    unsigned mesh_vertices, mesh_faces;
+    int error;                   /* device-side error flags (0 = none) */
+} afx_frame_stats;
+
+void afx_fusion_default_params(afx_fusion_params* p);
+int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out);
+int afx_fusion_destroy(afx_fusion* f);
+/* Reset the volume and graph (af::DeviceTsdf::initDefault + MotionGraph::clear). */
+int afx_fusion_reset(afx_fusion* f, void* stream);
+/* Process one frame: the first frame after create/reset initialises the volume by rigid
+ * integration at its centroid (src/VolumeFusion.cu:327-337); later frames run the
+ * non-rigid loop.  depth_mm is a device pointer (use afx_fusion_process_host for host
+ * memory).  Asynchronous on `stream`. */
+int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream);
+/* Same, from host memory: copies the frame to the device on `stream` first. */
+int afx_fusion_process_host(afx_fusion* f, const uint16_t* depth_mm_host, void* stream);
+/* Copy the last frame's statistics to host memory (synchronises `stream`). */
+int afx_fusion_stats(afx_fusion* f, afx_frame_stats* out, void* stream);
+/* Device views of the session state (valid until destroy). */
+int afx_fusion_tsdf(afx_fusion* f, float** tsdf, float** weights);
+int afx_fusion_graph(afx_fusion* f, float** nodes, float** radii, float** transforms, int** n_nodes);
+int afx_fusion_centroid(afx_fusion* f, float** centroid);
+int afx_fusion_point_cloud(afx_fusion* f, float** points, unsigned** count);
+int afx_fusion_mesh(afx_fusion* f, float** vertices, unsigned** vertex_count, int** faces, unsigned** face_count);
+int afx_fusion_frame_views(afx_fusion* f, float** depth, float** vertices, float** normals);
+/* Overwrite the committed node transforms (host memory), e.g. to replay a trajectory. */
+int afx_fusion_set_transforms(afx_fusion* f, const float* transforms_host, int n, void* stream);
+/* Number of kernels the library launched since the session was created. */
+long afx_fusion_kernel_launches(const afx_fusion* f);
+
+/* Per-stage GPU timing (CUDA events around each stage, like the reference's TimeMap).
+ * Stages: 0 prep, 1 rigid integration, 2 point-cloud sort/unique, 3 graph build, 4 KNN +
+ * weights, 5 Gauss-Newton structure, 6 Gauss-Newton iterations, 7 voxel support,
+ * 8 voxel warp + collisions, 9 warped integration, 10 marching cubes.
+ * afx_fusion_stage_times waits for the recorded events, adds milliseconds per stage into
+ * ms[0..n) and returns the number of stages; reset != 0 starts a new accumulation. */
+int afx_fusion_set_timing(afx_fusion* f, int on);
+int afx_fusion_stage_times(afx_fusion* f, double* ms, int n, int reset);
+
+/* Stream-ordered device-to-device copy (helper for bindings that hold raw device views). */
+int afx_copy_device(void* dst, const void* src, size_t bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,257 @@
+"""Per-stage parity of the sm_103a kernels against the CPU oracle (bit-exact where the
+stage is integer/index work or a fixed sequence of IEEE binary32 operations).
+
+All calls go through the C ABI (libafx.so) via volumefusion_gb300.af."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import pyoracle as O  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def cu(a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    if dtype is not None:
+        t = t.to(dtype)
+    return t.cuda()
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def af():
+    from volumefusion_gb300 import af as _af
+    return _af
+
+
+@pytest.fixture(scope="module")
+def frames():
+    from volumefusion_gb300 import synth
+    sphere, Ks = synth.sphere_frame()
+    cap, Kc = synth.capsule_pair_frame(20, width=640, height=576, fx=504.0, fy=504.0, cx=320.0, cy=288.0)
+    return [(sphere, Ks), (cap, Kc)]
+
+
+def test_frame_prep_bit_exact(af, frames):
+    for mm, K in frames:
+        d_o, v_o, n_o, c_o = O.frame_prep(mm, K)
+        d, v, n, c = af.loadProcessFrame(cu(mm.astype(np.int16)), K)
+        assert np.array_equal(host(d), d_o)
+        assert np.array_equal(host(v), v_o)
+        assert np.array_equal(host(n), n_o)
+        assert np.array_equal(host(c), c_o)
+        assert (d_o < np.inf).sum() > 1000
+
+
+def test_stage_kernels_bit_exact(af, frames):
+    mm, K = frames[1]
+    h, w = mm.shape
+    d0 = O.filter_depth(O.depth_from_mm(mm), 1.2)
+    dg = cu(O.depth_from_mm(mm))
+    af.runFilterDepthKernel(dg, 1.2)
+    assert np.array_equal(host(dg), d0)
+    b0 = O.bilateral(d0, 2, float(np.float32(0.03)), 2.0, 0.09)
+    bg = torch.empty_like(dg)
+    af.bilateralFilterTextureOpmShared(bg, dg, h, w, 2, float(np.float32(0.03)), 2.0, 0.09)
+    assert np.array_equal(host(bg), b0)
+    v0 = O.depth_to_mesh(b0, K)
+    vg = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
+    af.runDepthToMeshKernel(vg, bg, w, h, K)
+    assert np.array_equal(host(vg), v0)
+    n0 = O.normals(v0, 1.3, 2.1)
+    ng = torch.empty_like(vg)
+    af.runDepthVerticesNormalsKernel(ng, vg, bg, h, w, (1.3, 2.1))
+    assert np.array_equal(host(ng), n0)
+
+
+def test_rigid_integration_bit_exact(af, frames):
+    for (mm, K), dims, size, delta in ((frames[0], (128, 128, 128), 0.512, 0.016),
+                                       (frames[1], (96, 80, 64), 0.6, 0.02)):
+        d, _, _, c = O.frame_prep(mm, K)
+        dims = np.array(dims, np.int32)
+        vol = np.array([size] * 3, np.float32)
+        vs = vol / dims.astype(np.float32)
+        S = int(np.prod(dims))
+        t0 = np.full(S, -1, np.float32)
+        w0 = np.zeros(S, np.float32)
+        for rep in range(2):  # second pass exercises the running average
+            O.integrate_rigid(t0, w0, d, delta, dims, vs, vol, np.eye(3), c, K)
+        tg = cu(np.full(S, -1, np.float32))
+        wg = cu(np.zeros(S, np.float32))
+        for rep in range(2):
+            af.runIntegrateTSDFFromFrameKernel(tg, wg, cu(d), (mm.shape[1], mm.shape[0]), delta, dims, vs, vol,
+                                               np.eye(3), c, K)
+        assert np.array_equal(host(wg), w0)
+        assert np.array_equal(host(tg), t0)
+        assert (w0 > 0).sum() > 1000
+
+
+def _sorted_rows(a):
+    a = np.ascontiguousarray(a)
+    return a[np.lexsort(a.T[::-1])]
+
+
+def test_marching_cubes_and_sort_unique(af):
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "marching_cubes.npz"))
+    dims, size = g["dims"], g["size"]
+    vs = size / dims.astype(np.float32)
+    pc_o = O.mc_pointcloud(g["tsdf"], g["weights"], dims, vs, size)
+    cap = len(pc_o) + 1000
+    pts = torch.zeros((cap, 3), dtype=torch.float32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    af.runMarchingCubesMeshKernel(pts, cnt, cu(g["tsdf"]), cu(g["weights"]), dims, vs, size)
+    n = int(cnt.item())
+    assert n == len(pc_o)
+    assert np.array_equal(_sorted_rows(host(pts)[:n]), _sorted_rows(pc_o))
+    # sort + unique equals the reference's thrust::sort/unique (and the golden computePointCloud)
+    af.sortUnique(pts, cnt)
+    u = host(pts)[:int(cnt.item())]
+    assert np.array_equal(u, O.sort_unique(pc_o))
+    assert np.array_equal(u, O.sort_unique(g["pointcloud"]))
+    # full mesh: same multiset of triangles as the reference's computeIsoSurface
+    v_o, f_o = O.mc_full(g["tsdf"], g["weights"], dims, vs, size)
+    mv = torch.zeros((len(v_o) + 300, 3), dtype=torch.float32, device="cuda")
+    mf = torch.zeros((len(f_o) + 100, 3), dtype=torch.int32, device="cuda")
+    nv = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nf = torch.zeros(1, dtype=torch.int32, device="cuda")
+    af.runMarchingCubesFullKernel(mv, nv, mf, nf, cu(g["tsdf"]), cu(g["weights"]), dims, vs, size)
+    assert int(nf.item()) == len(f_o) and int(nv.item()) == len(v_o)
+    tri_g = host(mv)[:len(v_o)].reshape(-1, 9)
+    tri_o = v_o.reshape(-1, 9)
+    assert np.array_equal(_sorted_rows(tri_g), _sorted_rows(tri_o))
+    assert np.array_equal(_sorted_rows(tri_g), _sorted_rows(g["iso_verts"].reshape(-1, 9)))
+    fg = host(mf)[:len(f_o)]
+    assert np.array_equal(fg, np.arange(3 * len(f_o), dtype=np.int32).reshape(-1, 3))
+
+
+def test_graph_knn_warp_bit_exact(af):
+    g = np.load(__import__("os").path.join(__import__("os").path.dirname(__file__), "golden", "graph_knn.npz"))
+    mesh = g["mesh"]
+    radius = float(g["radius"])
+    cap = 4096
+    nodes = torch.zeros((cap, 3), dtype=torch.float32, device="cuda")
+    radii = torch.zeros(cap, dtype=torch.float32, device="cuda")
+    T = torch.zeros((cap, 16), dtype=torch.float32, device="cuda")
+    nn = torch.zeros(1, dtype=torch.int32, device="cuda")
+    mcount = cu(np.array([len(mesh)], np.int32))
+    af.buildGraph(nodes, radii, T, nn, cu(mesh), mcount, 4, radius)
+    n = int(nn.item())
+    no, ro, To = O.build_graph(mesh, 4, radius)
+    assert n == len(no)
+    assert np.array_equal(host(nodes)[:n], no)
+    assert np.array_equal(host(T)[:n], To)
+    assert np.array_equal(host(nodes)[:n], g["nodes"])  # the reference's af::buildGraph
+    # incremental build with transformed nodes (transform copy of the nearest node)
+    T.zero_()
+    T[:n] = cu(g["T_rand"])
+    af.buildGraph(nodes, radii, T, nn, cu(g["mesh2"]), cu(np.array([len(g["mesh2"])], np.int32)), 4, radius)
+    n2 = int(nn.item())
+    assert n2 == len(g["nodes2"])
+    assert np.array_equal(host(nodes)[:n2], g["nodes2"])
+    assert np.array_equal(host(T)[:n2], g["transforms2"])
+    # KNN: mesh -> 4 and 6 nodes, node -> 8 nodes excluding itself (ties ordered by index, as the oracle)
+    nodes_g = cu(no)
+    n_g = cu(np.array([len(no)], np.int32))
+    for k in (4, 6):
+        idx = torch.empty((len(mesh), k), dtype=torch.int32, device="cuda")
+        dist = torch.empty((len(mesh), k), dtype=torch.float32, device="cuda")
+        af.getKnnData(idx, dist, nodes_g, n_g, cu(mesh))
+        io, do = O.knn(no, mesh, k)
+        assert np.array_equal(host(idx).view(np.uint32), io)
+        assert np.array_equal(host(dist), do)
+    gi = torch.empty((len(no), 8), dtype=torch.int32, device="cuda")
+    gd = torch.empty((len(no), 8), dtype=torch.float32, device="cuda")
+    af.getKnnData(gi, gd, nodes_g, n_g, nodes_g, excludeClosest=True)
+    gio, gdo = O.knn(no, no, 8, exclude_closest=True)
+    assert np.array_equal(host(gi).view(np.uint32), gio)
+    af.filterDisconnected(gi, gd, n_g, cu(ro))
+    fio, fdo = O.filter_disconnected(gio, gdo, ro)
+    assert np.array_equal(host(gi).view(np.uint32), fio)
+    assert np.array_equal(host(gd), fdo)
+    # weights and warp with non-trivial transforms
+    idx = torch.empty((len(mesh), 4), dtype=torch.int32, device="cuda")
+    dist = torch.empty((len(mesh), 4), dtype=torch.float32, device="cuda")
+    af.getKnnData(idx, dist, nodes_g, n_g, cu(mesh))
+    w = torch.empty_like(dist)
+    af.runComputeWarpWeightsKernel(w, cu(ro), idx, dist, len(mesh), n_g)
+    io, do = O.knn(no, mesh, 4)
+    wo = O.warp_weights(ro, io, do)
+    assert np.array_equal(host(w), wo)
+    out = torch.empty((len(mesh), 3), dtype=torch.float32, device="cuda")
+    af.runWarpKernel(out, cu(mesh), cu(g["T_rand"]), idx, w, len(mesh))
+    assert np.array_equal(host(out), O.warp(mesh, g["T_rand"], io, wo))
+
+
+def test_correspondences_bit_exact(af, frames):
+    mm, K = frames[1]
+    d, v, n, c = O.frame_prep(mm, K)
+    pts = v.reshape(-1, 3)
+    pts = pts[pts[:, 2] > 0][::7] + np.array([0.002, -0.001, 0.003], np.float32)
+    corr_o = O.correspondences(pts, K, d, v, 0.01)
+    corr = torch.empty((len(pts), 2), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+    af.runCorrespondencePairsKernel(corr, cnt, cu(pts), len(pts), K, cu(d), (mm.shape[0], mm.shape[1]), cu(v), 0.01)
+    m = int(cnt.item())
+    assert m == len(corr_o) and m > 100
+    assert np.array_equal(host(corr)[:m], corr_o)
+
+
+def test_voxel_warp_and_warped_integration_bit_exact(af, frames):
+    from volumefusion_gb300 import configs
+    mm, K = frames[1]
+    d, v, n, c = O.frame_prep(mm, K)
+    dims = np.array([64, 64, 48], np.int32)
+    size = np.array([0.512, 0.512, 0.384], np.float32)
+    vs = size / dims.astype(np.float32)
+    S = int(np.prod(dims))
+    t0 = np.full(S, -1, np.float32)
+    w0 = np.zeros(S, np.float32)
+    O.integrate_rigid(t0, w0, d, 0.016, dims, vs, size, np.eye(3), c, K)
+    pc = O.sort_unique(O.mc_pointcloud(t0, w0, dims, vs, size))
+    mesh = O.translate(pc, c)
+    nodes, radii, T = O.build_graph(mesh, 4, 0.025)
+    rng = np.random.default_rng(3)
+    T = T.copy()
+    T[:, 12:15] += rng.normal(0, 0.004, (len(T), 3)).astype(np.float32)
+    per = np.array([2 * (int(np.float32(0.025) / vs[i]) + 1) + 1 for i in range(3)], np.int32)
+    nt = O.translate(nodes, -c)
+    for k in (4, 6):
+        kidx, kdist, kcnt = O.tsdf_knn(nt, radii, vs, size, dims, per, k)
+        gi = torch.empty((S, k), dtype=torch.int32, device="cuda")
+        gd = torch.empty((S, k), dtype=torch.float32, device="cuda")
+        gc = torch.empty(S, dtype=torch.int32, device="cuda")
+        af.runTsdfKNNGraph(gi, gd, gc, cu(nt), cu(radii), len(nt), vs, size, dims, per)
+        assert np.array_equal(host(gc), kcnt)
+        act = kcnt > 0
+        assert act.sum() > 1000
+        assert np.array_equal(host(gi).view(np.uint32)[act], kidx[act])
+        assert np.array_equal(host(gd)[act], kdist[act])
+        kw = O.tsdf_weights(radii, kidx, kdist, kcnt)
+        gw = torch.zeros((S, k), dtype=torch.float32, device="cuda")
+        af.runComputeTsdfWarpWeightsKernel(gw, cu(radii), gi, gd, gc, S)
+        assert np.array_equal(host(gw)[act], kw[act])
+        verts = O.translate(O.tsdf_vertices(vs, size, dims), c)
+        gv = torch.empty((S, 3), dtype=torch.float32, device="cuda")
+        af.runGenerateTsdfVerticesKernel(gv, vs, size, dims)
+        assert np.array_equal(host(gv), O.tsdf_vertices(vs, size, dims))
+        gv = cu(verts)
+        wv = O.warp_tsdf(verts, T, kidx, kw, kcnt)
+        af.runWarpTsdfKernel(gv, cu(T), gi, gw, gc, vs, size, dims)
+        assert np.array_equal(host(gv), wv)
+        coll = O.count_collisions(wv, kcnt, vs, size, dims, np.eye(3), c)
+        gcoll = torch.zeros(S, dtype=torch.int32, device="cuda")
+        af.runCountCollisionsPerVoxelKernel(gcoll, gv, gc, vs, size, dims, np.eye(3), c)
+        assert np.array_equal(host(gcoll), coll)
+        t1, w1 = t0.copy(), w0.copy()
+        O.integrate_warped(t1, w1, wv, coll, kcnt, d, 0.016, vs, size, dims, np.eye(3), c, K)
+        tg, wg = cu(t0), cu(w0)
+        af.runIntegrateWarpedTSDFFromFrameKernel(tg, wg, gv, gcoll, gc, cu(d), (mm.shape[1], mm.shape[0]), 0.016, vs,
+                                                 size, dims, np.eye(3), c, K)
+        assert np.array_equal(host(tg), t1)
+        assert np.array_equal(host(wg), w1)

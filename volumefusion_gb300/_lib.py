@@ -1,0 +1,122 @@
+"""ctypes binding of libafx.so (the sm_103a CUDA library, C ABI in include/afx/afx.h).
+
+Loading fails loudly when the library is missing: there is no CPU fallback.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libafx.so")
+
+vp = C.c_void_p
+i32 = C.c_int
+i64 = C.c_long
+f32 = C.c_float
+f64 = C.c_double
+sz = C.c_size_t
+
+
+class PrepParams(C.Structure):
+    _fields_ = [("K", f32 * 9), ("depth_threshold", f32), ("bilateral", i32), ("bilateral_r", i32), ("sigma_i", f32),
+                ("sigma_s", f32), ("bilateral_thr", f32), ("excl_angle_lo", f32), ("excl_angle_hi", f32)]
+
+
+class FusionParams(C.Structure):
+    _fields_ = [("width", i32), ("height", i32), ("K", f32 * 9), ("dims", i32 * 3), ("volume_size", f32 * 3),
+                ("delta", f32), ("depth_threshold", f32), ("bilateral", i32), ("bilateral_r", i32), ("sigma_i", f32),
+                ("sigma_s", f32), ("bilateral_thr", f32), ("excl_angle_lo", f32), ("excl_angle_hi", f32),
+                ("graph_radius", f32), ("knn", i32), ("kreg", i32), ("update_graph", i32), ("icp_iterations", i32),
+                ("gn_iterations", i32), ("lambda_depth", f32), ("lambda_reg", f32), ("energy_min_step", f32),
+                ("corr_thresh", f32), ("solver", i32), ("pcg_iterations", i32), ("pcg_tol", f64), ("integrate", i32),
+                ("extract_mesh", i32), ("node_capacity", i32), ("mesh_capacity", i64), ("triangle_capacity", i64)]
+
+
+class FrameStats(C.Structure):
+    _fields_ = [("frame", i32), ("n_nodes", i32), ("new_nodes", i32), ("mesh_points", C.c_uint),
+                ("correspondences", C.c_uint), ("gn_iterations_done", i32), ("energy", f64),
+                ("mesh_vertices", C.c_uint), ("mesh_faces", C.c_uint), ("error", i32)]
+
+
+SIGNATURES = {
+    "afx_status_string": (C.c_char_p, [i32]),
+    "afx_version": (i32, []),
+    "afx_last_cuda_error": (i32, []),
+    "afx_depth_from_mm": (i32, [vp, vp, i64, vp]),
+    "afx_filter_depth": (i32, [vp, i64, f32, vp]),
+    "afx_bilateral_filter": (i32, [vp, vp, i32, i32, i32, f64, f64, f32, vp]),
+    "afx_depth_to_mesh": (i32, [vp, vp, i32, i32, vp, vp]),
+    "afx_depth_vertices_normals": (i32, [vp, vp, i32, i32, f32, f32, vp]),
+    "afx_remove_depth_without_normals": (i32, [vp, vp, vp, i32, i32, vp]),
+    "afx_frame_prep": (i32, [vp, i32, i32, C.POINTER(PrepParams), vp, vp, vp, vp, vp]),
+    "afx_integrate_tsdf": (i32, [vp, vp, vp, i32, i32, f32, vp, vp, vp, vp, vp, vp, vp]),
+    "afx_tsdf_knn": (i32, [vp, vp, vp, vp, vp, i32, vp, vp, vp, vp, i32, vp, sz, vp]),
+    "afx_tsdf_knn_workspace_size": (sz, [vp, i32, vp]),
+    "afx_tsdf_warp_weights": (i32, [vp, vp, vp, vp, vp, i64, i32, vp]),
+    "afx_tsdf_vertices": (i32, [vp, vp, vp, vp, vp]),
+    "afx_warp_tsdf": (i32, [vp, vp, vp, vp, vp, i64, i32, vp]),
+    "afx_count_collisions": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+    "afx_integrate_warped_tsdf": (i32, [vp, vp, vp, vp, vp, vp, i32, i32, f32, vp, vp, vp, vp, vp, vp, vp]),
+    "afx_marching_cubes_points": (i32, [vp, vp, i64, vp, vp, vp, vp, vp, f32, vp]),
+    "afx_marching_cubes_mesh": (i32, [vp, vp, i64, vp, vp, i64, vp, vp, vp, vp, vp, f32, vp]),
+    "afx_sort_unique_points": (i32, [vp, vp, i64, vp, sz, vp]),
+    "afx_sort_unique_points_workspace_size": (sz, [i64]),
+    "afx_extract_point_cloud": (i32, [vp, vp, i64, vp, vp, vp, vp, vp, f32, vp, sz, vp]),
+    "afx_translate": (i32, [vp, vp, i64, vp, vp]),
+    "afx_build_graph": (i32, [vp, vp, vp, vp, i32, vp, vp, i64, i32, f32, vp, sz, vp]),
+    "afx_build_graph_workspace_size": (sz, [i64, i32]),
+    "afx_knn": (i32, [vp, vp, vp, vp, i32, vp, vp, i64, i32, i32, vp]),
+    "afx_filter_disconnected": (i32, [vp, vp, vp, i32, i32, vp, vp]),
+    "afx_warp_weights": (i32, [vp, vp, vp, vp, vp, i64, i32, vp, vp]),
+    "afx_warp": (i32, [vp, vp, vp, vp, vp, vp, i64, i32, vp]),
+    "afx_correspondences": (i32, [vp, vp, i64, vp, vp, i64, vp, vp, i32, i32, vp, f32, vp, sz, vp]),
+    "afx_correspondences_workspace_size": (sz, [i64]),
+    "afx_fusion_default_params": (None, [C.POINTER(FusionParams)]),
+    "afx_fusion_create": (i32, [C.POINTER(FusionParams), C.POINTER(vp)]),
+    "afx_fusion_destroy": (i32, [vp]),
+    "afx_fusion_reset": (i32, [vp, vp]),
+    "afx_fusion_process": (i32, [vp, vp, vp]),
+    "afx_fusion_process_host": (i32, [vp, vp, vp]),
+    "afx_fusion_stats": (i32, [vp, C.POINTER(FrameStats), vp]),
+    "afx_fusion_tsdf": (i32, [vp, C.POINTER(vp), C.POINTER(vp)]),
+    "afx_fusion_graph": (i32, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
+    "afx_fusion_centroid": (i32, [vp, C.POINTER(vp)]),
+    "afx_fusion_point_cloud": (i32, [vp, C.POINTER(vp), C.POINTER(vp)]),
+    "afx_fusion_mesh": (i32, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
+    "afx_fusion_frame_views": (i32, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
+    "afx_fusion_set_transforms": (i32, [vp, vp, i32, vp]),
+    "afx_fusion_kernel_launches": (i64, [vp]),
+    "afx_copy_device": (i32, [vp, vp, sz, vp]),
+    "afx_fusion_set_timing": (i32, [vp, i32]),
+    "afx_fusion_stage_times": (i32, [vp, C.POINTER(f64), i32, i32]),
+}
+
+_lib = None
+
+
+class AfxError(RuntimeError):
+    def __init__(self, status, what):
+        self.status = status
+        msg = lib().afx_status_string(status).decode()
+        super().__init__("%s failed: %s (status %d, last CUDA error %d)" % (what, msg, status,
+                                                                            lib().afx_last_cuda_error()))
+
+
+def lib():
+    """The loaded libafx.so.  Raises if it has not been built (python -m volumefusion_gb300.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libafx.so is missing (%s); build it with `python -m volumefusion_gb300.build`"
+                               % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status, what):
+    if status != 0:
+        raise AfxError(status, what)

@@ -1,0 +1,230 @@
+"""The reference's af:: operator API over torch CUDA tensors, backed by libafx.so.
+
+Names, argument order and meaning follow the reference's free functions
+(include/af/*.cuh, include/af/*.h); tensors stand in for its raw device pointers and
+Eigen values (Vec3f -> 3 floats, Mat3f/Mat4f -> column-major floats).  Like the
+reference, every call here blocks until the GPU work is done and raises on failure
+(the reference's CUDA_CHECK throws std::runtime_error, src/Helper.cu:7-20).  The C ABI
+underneath is asynchronous and stream-ordered.
+"""
+import ctypes as C
+
+import numpy as np
+import torch
+
+from ._lib import PrepParams, check, lib
+
+INVALID_INDEX = 0xFFFFFFFF
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t):
+    if t is None:
+        return None
+    assert t.is_cuda and t.is_contiguous(), "expected a contiguous CUDA tensor"
+    return C.c_void_p(t.data_ptr())
+
+
+def _f(vals, n):
+    arr = (C.c_float * n)(*[float(v) for v in np.asarray(vals, dtype=np.float64).ravel()])
+    return arr
+
+
+def _i(vals, n):
+    return (C.c_int * n)(*[int(v) for v in np.asarray(vals).ravel()])
+
+
+def kcol(M):
+    """3x3 / 4x4 matrix (numpy, row-major) -> column-major float list (Eigen layout)."""
+    return np.asarray(M, dtype=np.float64).T.ravel()
+
+
+def _sync(status, what):
+    check(status, what)
+    torch.cuda.current_stream().synchronize()
+
+
+def _u32(n=1):
+    return torch.zeros(n, dtype=torch.int32, device="cuda")
+
+
+def _workspace(nbytes):
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device="cuda")
+
+
+# ---- include/af/VertexManipulation.cuh, include/af/BilateralFilter.cuh ----
+
+def runFilterDepthKernel(depth, threshold):
+    _sync(lib().afx_filter_depth(_p(depth), depth.numel(), threshold, _stream()), "runFilterDepthKernel")
+
+
+def bilateralFilterTextureOpmShared(output, input, height, width, r, sI, sS, thr):
+    _sync(lib().afx_bilateral_filter(_p(output), _p(input), height, width, r, sI, sS, thr, _stream()),
+          "bilateralFilterTextureOpmShared")
+
+
+def runDepthToMeshKernel(mesh, depth, width, height, K):
+    _sync(lib().afx_depth_to_mesh(_p(mesh), _p(depth), width, height, _f(kcol(K), 9), _stream()),
+          "runDepthToMeshKernel")
+
+
+def runDepthVerticesNormalsKernel(normals, vertices, depth, h, w, normExclAngleRange):
+    del depth  # unused by the reference kernel as well
+    lo, hi = normExclAngleRange
+    _sync(lib().afx_depth_vertices_normals(_p(normals), _p(vertices), h, w, lo, hi, _stream()),
+          "runDepthVerticesNormalsKernel")
+
+
+def runRemoveDepthWithoutNormalsKernel(normals, vertices, depth, h, w):
+    _sync(lib().afx_remove_depth_without_normals(_p(normals), _p(vertices), _p(depth), h, w, _stream()),
+          "runRemoveDepthWithoutNormalsKernel")
+
+
+def loadProcessFrame(depth_mm, K, depth_threshold=1.2, bilateral=True, bilateral_r=2, sigma_i=0.03, sigma_s=2.0,
+                     bilateral_thr=0.09, norm_excl_angle_range=(1.3, 2.1)):
+    """af::loadProcessFrame after the image is in memory (src/VolumeFusion.cu:184-220):
+    returns (depth, vertices, normals, centroid) device tensors."""
+    h, w = depth_mm.shape
+    p = PrepParams()
+    p.K[:] = list(kcol(K))
+    p.depth_threshold = depth_threshold
+    p.bilateral = int(bilateral)
+    p.bilateral_r = bilateral_r
+    p.sigma_i = sigma_i
+    p.sigma_s = sigma_s
+    p.bilateral_thr = bilateral_thr
+    p.excl_angle_lo, p.excl_angle_hi = norm_excl_angle_range
+    mm = depth_mm.to(device="cuda", dtype=torch.int16).contiguous()
+    depth = torch.empty((h, w), dtype=torch.float32, device="cuda")
+    verts = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
+    nrm = torch.empty((h, w, 3), dtype=torch.float32, device="cuda")
+    cen = torch.empty(3, dtype=torch.float32, device="cuda")
+    _sync(lib().afx_frame_prep(_p(mm), w, h, C.byref(p), _p(depth), _p(verts), _p(nrm), _p(cen), _stream()),
+          "loadProcessFrame")
+    return depth, verts, nrm, cen
+
+
+# ---- include/af/TSDFIntegration.cuh ----
+
+def runIntegrateTSDFFromFrameKernel(tsdf, tsdfWeights, depthFrame, frameDims, delta, dims, voxelSize, volumeSize,
+                                    volumeRotate, volumeTranslate, depthIntrinsics):
+    _sync(lib().afx_integrate_tsdf(_p(tsdf), _p(tsdfWeights), _p(depthFrame), int(frameDims[0]), int(frameDims[1]),
+                                   delta, _i(dims, 3), _f(voxelSize, 3), _f(volumeSize, 3), _f(kcol(volumeRotate), 9),
+                                   _f(volumeTranslate, 3), _f(kcol(depthIntrinsics), 9), _stream()),
+          "runIntegrateTSDFFromFrameKernel")
+
+
+def runCountCollisionsPerVoxelKernel(collisionCounts, tsdfVertices, knnCounts, voxelSize, volumeSize, volumeDim,
+                                     volumeRotate, volumeTranslate):
+    _sync(lib().afx_count_collisions(_p(collisionCounts), _p(tsdfVertices), _p(knnCounts), _f(voxelSize, 3),
+                                     _f(volumeSize, 3), _i(volumeDim, 3), _f(kcol(volumeRotate), 9),
+                                     _f(volumeTranslate, 3), _stream()), "runCountCollisionsPerVoxelKernel")
+
+
+def runIntegrateWarpedTSDFFromFrameKernel(tsdf, tsdfWeights, tsdfVertices, collisionCounts, knnCounts, depthFrame,
+                                          frameDims, delta, voxelSize, volumeSize, volumeDim, volumeRotate,
+                                          volumeTranslate, depthIntrinsics):
+    _sync(lib().afx_integrate_warped_tsdf(_p(tsdf), _p(tsdfWeights), _p(tsdfVertices), _p(collisionCounts),
+                                          _p(knnCounts), _p(depthFrame), int(frameDims[0]), int(frameDims[1]), delta,
+                                          _f(voxelSize, 3), _f(volumeSize, 3), _i(volumeDim, 3),
+                                          _f(kcol(volumeRotate), 9), _f(volumeTranslate, 3),
+                                          _f(kcol(depthIntrinsics), 9), _stream()),
+          "runIntegrateWarpedTSDFFromFrameKernel")
+
+
+# ---- include/af/TSDFWarp.h ----
+
+def runTsdfKNNGraph(knnIdxs, knnDists, knnCounts, graph, graphRadiuses, graphSize, voxelSize, volumeSize, volumeDim,
+                    voxelsPerNode):
+    k = knnIdxs.shape[-1]
+    ws_bytes = lib().afx_tsdf_knn_workspace_size(_i(volumeDim, 3), int(graphSize), _i(voxelsPerNode, 3))
+    ws = _workspace(ws_bytes)
+    _sync(lib().afx_tsdf_knn(_p(knnIdxs), _p(knnDists), _p(knnCounts), _p(graph), _p(graphRadiuses), int(graphSize),
+                             _f(voxelSize, 3), _f(volumeSize, 3), _i(volumeDim, 3), _i(voxelsPerNode, 3), k, _p(ws),
+                             ws.numel(), _stream()), "runTsdfKNNGraph")
+
+
+def runComputeTsdfWarpWeightsKernel(knnWeights, graphRadiuses, knnIdxs, knnDists, knnCounts, gridSize):
+    _sync(lib().afx_tsdf_warp_weights(_p(knnWeights), _p(graphRadiuses), _p(knnIdxs), _p(knnDists), _p(knnCounts),
+                                      int(gridSize), knnIdxs.shape[-1], _stream()), "runComputeTsdfWarpWeightsKernel")
+
+
+def runGenerateTsdfVerticesKernel(tsdfVertices, voxelSize, volumeSize, volumeDim):
+    _sync(lib().afx_tsdf_vertices(_p(tsdfVertices), _f(voxelSize, 3), _f(volumeSize, 3), _i(volumeDim, 3), _stream()),
+          "runGenerateTsdfVerticesKernel")
+
+
+def runWarpTsdfKernel(tsdfVertices, motionGraph, knnIdxs, knnWeights, knnCounts, voxelSize, volumeSize, volumeDim):
+    del voxelSize, volumeSize
+    n = int(np.prod(volumeDim))
+    _sync(lib().afx_warp_tsdf(_p(tsdfVertices), _p(motionGraph), _p(knnIdxs), _p(knnWeights), _p(knnCounts), n,
+                              knnIdxs.shape[-1], _stream()), "runWarpTsdfKernel")
+
+
+# ---- include/af/MarchingCubes.cuh, include/af/DeviceTsdf.cuh ----
+
+def runMarchingCubesMeshKernel(mesh, meshSize, tsdf, tsdfWeights, dims, voxelSize, volSize, isoValue=0.0):
+    _sync(lib().afx_marching_cubes_points(_p(mesh), _p(meshSize), mesh.shape[0], _p(tsdf), _p(tsdfWeights),
+                                          _i(dims, 3), _f(voxelSize, 3), _f(volSize, 3), isoValue, _stream()),
+          "runMarchingCubesMeshKernel")
+
+
+def runMarchingCubesFullKernel(mesh, meshSize, faces, facesSize, tsdf, tsdfWeights, dims, voxelSize, volSize,
+                               isoValue=0.0):
+    _sync(lib().afx_marching_cubes_mesh(_p(mesh), _p(meshSize), mesh.shape[0], _p(faces), _p(facesSize),
+                                        faces.shape[0], _p(tsdf), _p(tsdfWeights), _i(dims, 3), _f(voxelSize, 3),
+                                        _f(volSize, 3), isoValue, _stream()), "runMarchingCubesFullKernel")
+
+
+def sortUnique(points, count):
+    """thrust::sort + thrust::unique of Vec3f (src/VolumeFusion.cu:382-384) in place."""
+    n_max = points.shape[0]
+    ws = _workspace(lib().afx_sort_unique_points_workspace_size(n_max))
+    _sync(lib().afx_sort_unique_points(_p(points), _p(count), n_max, _p(ws), ws.numel(), _stream()), "sortUnique")
+
+
+def runTranslateKernel(mesh, meshSize, translation):
+    _sync(lib().afx_translate(_p(mesh), None, int(meshSize), _f(translation, 3), _stream()), "runTranslateKernel")
+
+
+# ---- include/af/GraphBuilder.h, include/af/VertexManipulation.cuh, include/af/ComputeCorrespondence.cuh ----
+
+def buildGraph(nodes, radii, transforms, n_nodes, mesh, mesh_count, knn, radius):
+    """af::buildGraph on the device; node arrays are capacity-sized and n_nodes is a 1-element int32 tensor."""
+    ws = _workspace(lib().afx_build_graph_workspace_size(mesh.shape[0], nodes.shape[0]))
+    _sync(lib().afx_build_graph(_p(nodes), _p(radii), _p(transforms), _p(n_nodes), nodes.shape[0], _p(mesh),
+                                _p(mesh_count), mesh.shape[0], knn, radius, _p(ws), ws.numel(), _stream()),
+          "buildGraph")
+
+
+def getKnnData(idx, dist, nodes, n_nodes, points, count=None, excludeClosest=False):
+    _sync(lib().afx_knn(_p(idx), _p(dist), _p(nodes), _p(n_nodes), nodes.shape[0], _p(points), _p(count),
+                        points.shape[0], idx.shape[-1], int(excludeClosest), _stream()), "getKnnData")
+
+
+def filterDisconnected(idx, dist, n_nodes, radii):
+    _sync(lib().afx_filter_disconnected(_p(idx), _p(dist), _p(n_nodes), idx.shape[0], idx.shape[-1], _p(radii),
+                                        _stream()), "filterDisconnected")
+
+
+def runComputeWarpWeightsKernel(knnWeights, motionGraphRadiuses, knnIdxs, knnDists, meshSize, n_nodes):
+    _sync(lib().afx_warp_weights(_p(knnWeights), _p(motionGraphRadiuses), _p(knnIdxs), _p(knnDists), None,
+                                 int(meshSize), knnIdxs.shape[-1], _p(n_nodes), _stream()),
+          "runComputeWarpWeightsKernel")
+
+
+def runWarpKernel(warpedMesh, mesh, motionGraph, knnIdxs, knnWeights, meshSize):
+    _sync(lib().afx_warp(_p(warpedMesh), _p(mesh), _p(motionGraph), _p(knnIdxs), _p(knnWeights), None, int(meshSize),
+                         knnIdxs.shape[-1], _stream()), "runWarpKernel")
+
+
+def runCorrespondencePairsKernel(corrIdxs, corrIdxsSize, warpedMesh, warpedMeshSize, K, depth, depthDim, frameMesh,
+                                 thresholdDist):
+    rows, cols = int(depthDim[0]), int(depthDim[1])
+    ws = _workspace(lib().afx_correspondences_workspace_size(int(warpedMeshSize)))
+    _sync(lib().afx_correspondences(_p(corrIdxs), _p(corrIdxsSize), corrIdxs.shape[0], _p(warpedMesh), None,
+                                    int(warpedMeshSize), _f(kcol(K), 9), _p(depth), rows, cols, _p(frameMesh),
+                                    thresholdDist, _p(ws), ws.numel(), _stream()), "runCorrespondencePairsKernel")

@@ -1,0 +1,713 @@
+// afx_fusion.cu -- the per-frame non-rigid fusion loop (af::runVolumeFusion,
+// src/VolumeFusion.cu:223-769) as a device-resident session, plus the library's
+// status / error plumbing.
+//
+// Every stage runs on the session's stream with its sizes kept in device memory, so a
+// frame needs no host synchronisation: the canonical point cloud, motion graph,
+// correspondences and Gauss-Newton control (energy test, commit of pending transforms)
+// all stay on the GPU.  The reference blocks on cudaDeviceSynchronize and copies the
+// point cloud and graph to the host every frame.
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "afx_gn.h"
+#include "afx_voxel.h"
+
+namespace afx {
+
+static thread_local int g_last_cuda_error = 0;
+static std::atomic<long> g_launches{0};
+
+int note_cuda_error(cudaError_t e) {
+    if (e == cudaSuccess) return AFX_OK;
+    g_last_cuda_error = (int)e;
+    return AFX_ERR_CUDA;
+}
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+long launches_total() { return g_launches.load(std::memory_order_relaxed); }
+
+struct FrameStats {
+    int frame;
+    int n_nodes;
+    int new_nodes;
+    unsigned mesh_points;
+    unsigned correspondences;
+    int gn_iterations_done;
+    double energy;
+    unsigned mesh_vertices, mesh_faces;
+    int error;
+};
+
+}  // namespace afx
+
+using namespace afx;
+
+struct afx_fusion {
+    afx_fusion_params p;
+    Volume vol;
+    long S = 0, P = 0;
+    int per[3];
+    int frame = 0;
+    long launches_at_create = 0;
+    // device buffers
+    void* arena = nullptr;
+    size_t arena_bytes = 0;
+    float* tsdf;
+    float* weights;
+    unsigned* coll;
+    uint16_t* depth_mm;
+    float* depth;
+    float* verts;
+    float* normals;
+    float* centroid0;      // frame-0 centroid (volume translation)
+    float* centroid;       // current frame centroid
+    unsigned long long* acc;
+    int* error;
+    unsigned* epoch;
+    float* points;         // canonical point cloud
+    unsigned* npoints;
+    float* nodes_host;     // positions used for graph build / KNN (the reference's CPU copy)
+    float* nodes_dev;      // positions used on the device (the reference's motionGraph_d)
+    float* nodes_t;        // translated copy for the voxel support
+    float* radii;
+    float* T;              // committed transforms
+    float* Tp;             // pending transforms
+    int* n_nodes;
+    int* n_old;
+    uint32_t* midx;
+    float* mdist;
+    float* mw;
+    uint32_t* gidx;
+    float* gdist;
+    float* warped;
+    int* corr;
+    unsigned* ncorr;
+    int* corr_of_vertex;
+    float* mverts;
+    int* mfaces;
+    unsigned* nmverts;
+    unsigned* nmfaces;
+    WarpedVoxel* wvox;
+    unsigned char* wcount;
+    FrameStats* stats;
+    void* ws_sort;
+    size_t ws_sort_bytes;
+    void* ws_graph;
+    size_t ws_graph_bytes;
+    void* ws_corr;
+    size_t ws_corr_bytes;
+    void* ws_support;
+    size_t ws_support_bytes;
+    void* ws_gn;
+    size_t ws_gn_bytes;
+    SupportWorkspace sup;
+    GnBuffers gn;
+    // optional per-stage timing (the reference's TimeMap, include/af/TimeMap.h)
+    bool timing = false;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_used;
+    cudaEvent_t ev_open = nullptr;
+    int ev_stage = -1;
+};
+
+namespace afx {
+
+__global__ void copy_new_nodes_kernel(float* dst, const float* src, const int* n_old, const int* n_nodes, int cap) {
+    int i = *n_old + blockIdx.x * blockDim.x + threadIdx.x;
+    int n = min(*n_nodes, cap);
+    if (i < n) {
+        dst[3 * i] = src[3 * i];
+        dst[3 * i + 1] = src[3 * i + 1];
+        dst[3 * i + 2] = src[3 * i + 2];
+    }
+}
+
+__global__ void record_n_old_kernel(const int* n_nodes, int* n_old) { *n_old = *n_nodes; }
+
+__global__ void frame_begin_kernel(unsigned* epoch, unsigned* ncorr, int* error, unsigned* nmverts, unsigned* nmfaces) {
+    unsigned e = *epoch + 1;
+    if (e >= (1u << 24)) e = 1;  // collision words are cleared by the host when this wraps
+    *epoch = e;
+    *ncorr = 0;
+    *nmverts = 0;
+    *nmfaces = 0;
+}
+
+__global__ void stats_kernel(FrameStats* s, int frame, const int* n_nodes, const int* n_old, const unsigned* npoints,
+                             const unsigned* ncorr, const GnState* gn, const unsigned* nv, const unsigned* nf,
+                             const int* error, int nonrigid) {
+    s->frame = frame;
+    s->n_nodes = *n_nodes;
+    s->new_nodes = nonrigid ? *n_nodes - *n_old : 0;
+    s->mesh_points = *npoints;
+    s->correspondences = nonrigid ? *ncorr : 0;
+    s->gn_iterations_done = nonrigid ? gn->iters : 0;
+    s->energy = nonrigid ? gn->e_last : 0.0;
+    s->mesh_vertices = *nv;
+    s->mesh_faces = *nf;
+    s->error = *error;
+}
+
+static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace afx
+
+enum Stage { ST_PREP, ST_INTEGRATE_RIGID, ST_SORT, ST_GRAPH, ST_KNN, ST_GN_SETUP, ST_GN_LOOP, ST_SUPPORT, ST_VOXEL_WARP,
+             ST_WARPED_INTEGRATE, ST_MC, ST_COUNT };
+
+static cudaEvent_t take_event(afx_fusion* f) {
+    if (!f->ev_pool.empty()) {
+        cudaEvent_t e = f->ev_pool.back();
+        f->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Marks the start of `stage` (closing the previous one) when timing is on.
+static void stage_mark(afx_fusion* f, int stage, cudaStream_t st) {
+    if (!f->timing) return;
+    cudaEvent_t e = take_event(f);
+    cudaEventRecord(e, st);
+    if (f->ev_open) f->ev_used.push_back({f->ev_stage, {f->ev_open, e}});
+    if (stage < 0) {
+        f->ev_pool.push_back(e);  // closing mark only
+        f->ev_open = nullptr;
+        f->ev_stage = -1;
+        return;
+    }
+    // the closing event of the previous stage doubles as this stage's opening event
+    cudaEvent_t e2 = take_event(f);
+    cudaEventRecord(e2, st);
+    f->ev_open = e2;
+    f->ev_stage = stage;
+}
+
+extern "C" {
+
+const char* afx_status_string(int s) {
+    switch (s) {
+        case AFX_OK: return "ok";
+        case AFX_ERR_INVALID_ARGUMENT: return "invalid argument";
+        case AFX_ERR_CAPACITY: return "capacity exceeded";
+        case AFX_ERR_CUDA: return "CUDA error";
+        case AFX_ERR_SINGULAR: return "singular Gauss-Newton block";
+        case AFX_ERR_WORKSPACE: return "workspace too small";
+        case AFX_ERR_UNSUPPORTED: return "unsupported input";
+        case AFX_ERR_TIMEOUT: return "device wait timed out";
+        case AFX_ERR_NO_MEMORY: return "out of device memory";
+    }
+    return "unknown status";
+}
+
+int afx_version(void) { return 100; }
+
+int afx_last_cuda_error(void) { return g_last_cuda_error; }
+
+void afx_fusion_default_params(afx_fusion_params* p) {
+    std::memset(p, 0, sizeof(*p));
+    p->width = 640;
+    p->height = 576;
+    const float K[9] = {504.f, 0.f, 0.f, 0.f, 504.f, 0.f, 320.f, 288.f, 1.f};
+    std::memcpy(p->K, K, sizeof(K));
+    p->dims[0] = p->dims[1] = p->dims[2] = 256;
+    p->volume_size[0] = p->volume_size[1] = p->volume_size[2] = 1.024f;
+    p->delta = 0.016f;
+    p->depth_threshold = 1.2f;
+    p->bilateral = 1;
+    p->bilateral_r = 2;
+    p->sigma_i = 0.03f;
+    p->sigma_s = 2.f;
+    p->bilateral_thr = 0.09f;
+    p->excl_angle_lo = 1.3f;
+    p->excl_angle_hi = 2.1f;
+    p->graph_radius = 0.025f;
+    p->knn = 4;
+    p->kreg = 8;
+    p->update_graph = 1;
+    p->icp_iterations = 1;
+    p->gn_iterations = 5;
+    p->lambda_depth = 1.f;
+    p->lambda_reg = 14.142135623730951f;
+    p->energy_min_step = 1e-4f;
+    p->corr_thresh = 0.01f;
+    p->solver = 1;
+    p->pcg_iterations = 10;
+    p->pcg_tol = 0.0;
+    p->integrate = 1;
+    p->extract_mesh = 1;
+    p->node_capacity = 16384;
+    p->mesh_capacity = 2000000;
+    p->triangle_capacity = 4000000;
+}
+
+int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
+    if (!params || !out) return AFX_ERR_INVALID_ARGUMENT;
+    const afx_fusion_params& p = *params;
+    if (p.width < 3 || p.height < 3 || p.dims[0] < 3 || p.dims[1] < 3 || p.dims[2] < 3 || p.knn < 1 || p.knn > 8 ||
+        p.kreg < 1 || p.kreg > 8 || p.node_capacity < 1 || p.mesh_capacity < 1 || p.triangle_capacity < 1 ||
+        !(p.graph_radius > 0.f) || p.icp_iterations < 0 || p.gn_iterations < 0 || p.pcg_iterations < 0)
+        return AFX_ERR_INVALID_ARGUMENT;
+    afx_fusion* f = new (std::nothrow) afx_fusion();
+    if (!f) return AFX_ERR_NO_MEMORY;
+    f->p = p;
+    float vs[3];
+    for (int c = 0; c < 3; ++c) vs[c] = p.volume_size[c] / (float)p.dims[c];
+    f->vol = make_volume(p.dims, vs, p.volume_size);
+    f->S = (long)p.dims[0] * p.dims[1] * p.dims[2];
+    f->P = (long)p.width * p.height;
+    // voxels per node cube: 2 * ((r / voxelSize).cast<int>() + 1) + 1 (src/VolumeFusion.cu:702-706)
+    for (int c = 0; c < 3; ++c) f->per[c] = 2 * ((int)(p.graph_radius / vs[c]) + 1) + 1;
+    const long M = p.mesh_capacity, N = p.node_capacity, S = f->S, Pp = f->P;
+    const long nbricks = brick_count_total(f->vol);
+    f->ws_sort_bytes = sort_unique_workspace_size(M);
+    f->ws_graph_bytes = build_graph_ws(M);
+    f->ws_corr_bytes = corr_ws(M);
+    f->ws_support_bytes = support_workspace_size(f->vol, (int)N, f->per);
+    f->ws_gn_bytes = gn_workspace_size(M, (int)N, p.knn, p.kreg);
+    size_t sz = 0;
+    auto add = [&](size_t n) { sz += al(n); };
+    add(S * 4); add(S * 4); add(S * 4);                  // tsdf weights coll
+    add(Pp * 2); add(Pp * 4); add(Pp * 12); add(Pp * 12);  // frame buffers
+    add(64); add(64); add(64); add(64); add(64);          // centroids acc error epoch
+    add(M * 12); add(64);                                 // points
+    add(N * 12); add(N * 12); add(N * 12); add(N * 4); add(N * 64); add(N * 64); add(64); add(64);
+    add(M * p.knn * 4); add(M * p.knn * 4); add(M * p.knn * 4);
+    add(N * p.kreg * 4); add(N * p.kreg * 4);
+    add(M * 12); add(M * 8); add(64); add(M * 4);
+    add(p.triangle_capacity * 36); add(p.triangle_capacity * 12); add(64); add(64);
+    add(nbricks * 512 * sizeof(WarpedVoxel)); add(nbricks * 512);
+    add(sizeof(FrameStats));
+    add(f->ws_sort_bytes); add(f->ws_graph_bytes); add(f->ws_corr_bytes); add(f->ws_support_bytes); add(f->ws_gn_bytes);
+    f->arena_bytes = sz + 4096;
+    cudaError_t e = cudaMalloc(&f->arena, f->arena_bytes);
+    if (e != cudaSuccess) {
+        note_cuda_error(e);
+        delete f;
+        return AFX_ERR_NO_MEMORY;
+    }
+    char* q = static_cast<char*>(f->arena);
+    auto take = [&](size_t n) {
+        char* r = q;
+        q += al(n);
+        return r;
+    };
+    f->tsdf = (float*)take(S * 4);
+    f->weights = (float*)take(S * 4);
+    f->coll = (unsigned*)take(S * 4);
+    f->depth_mm = (uint16_t*)take(Pp * 2);
+    f->depth = (float*)take(Pp * 4);
+    f->verts = (float*)take(Pp * 12);
+    f->normals = (float*)take(Pp * 12);
+    f->centroid0 = (float*)take(64);
+    f->centroid = (float*)take(64);
+    f->acc = (unsigned long long*)take(64);
+    f->error = (int*)take(64);
+    f->epoch = (unsigned*)take(64);
+    f->points = (float*)take(M * 12);
+    f->npoints = (unsigned*)take(64);
+    f->nodes_host = (float*)take(N * 12);
+    f->nodes_dev = (float*)take(N * 12);
+    f->nodes_t = (float*)take(N * 12);
+    f->radii = (float*)take(N * 4);
+    f->T = (float*)take(N * 64);
+    f->Tp = (float*)take(N * 64);
+    f->n_nodes = (int*)take(64);
+    f->n_old = (int*)take(64);
+    f->midx = (uint32_t*)take(M * p.knn * 4);
+    f->mdist = (float*)take(M * p.knn * 4);
+    f->mw = (float*)take(M * p.knn * 4);
+    f->gidx = (uint32_t*)take(N * p.kreg * 4);
+    f->gdist = (float*)take(N * p.kreg * 4);
+    f->warped = (float*)take(M * 12);
+    f->corr = (int*)take(M * 8);
+    f->ncorr = (unsigned*)take(64);
+    f->corr_of_vertex = (int*)take(M * 4);
+    f->mverts = (float*)take(p.triangle_capacity * 36);
+    f->mfaces = (int*)take(p.triangle_capacity * 12);
+    f->nmverts = (unsigned*)take(64);
+    f->nmfaces = (unsigned*)take(64);
+    f->wvox = (WarpedVoxel*)take(nbricks * 512 * sizeof(WarpedVoxel));
+    f->wcount = (unsigned char*)take(nbricks * 512);
+    f->stats = (FrameStats*)take(sizeof(FrameStats));
+    f->ws_sort = take(f->ws_sort_bytes);
+    f->ws_graph = take(f->ws_graph_bytes);
+    f->ws_corr = take(f->ws_corr_bytes);
+    f->ws_support = take(f->ws_support_bytes);
+    f->ws_gn = take(f->ws_gn_bytes);
+    if (!carve_support(f->ws_support, f->ws_support_bytes, f->vol, (int)N, f->per, &f->sup) ||
+        !gn_carve(f->ws_gn, f->ws_gn_bytes, M, (int)N, p.knn, p.kreg, &f->gn)) {
+        cudaFree(f->arena);
+        delete f;
+        return AFX_ERR_WORKSPACE;
+    }
+    f->launches_at_create = launches_total();
+    int rc = afx_fusion_reset(f, nullptr);
+    if (rc) {
+        cudaFree(f->arena);
+        delete f;
+        return rc;
+    }
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        note_cuda_error(e);
+        cudaFree(f->arena);
+        delete f;
+        return AFX_ERR_CUDA;
+    }
+    *out = f;
+    return AFX_OK;
+}
+
+int afx_fusion_destroy(afx_fusion* f) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    for (auto& u : f->ev_used) {
+        cudaEventDestroy(u.second.first);
+        cudaEventDestroy(u.second.second);
+    }
+    for (auto e : f->ev_pool) cudaEventDestroy(e);
+    if (f->ev_open) cudaEventDestroy(f->ev_open);
+    cudaError_t e = cudaFree(f->arena);
+    delete f;
+    return note_cuda_error(e);
+}
+
+__global__ void fill_kernel(float* p, long n, float v) {
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+int afx_fusion_reset(afx_fusion* f, void* stream) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    fill_kernel<<<blocks_for(f->S, 256), 256, 0, st>>>(f->tsdf, f->S, -1.f);  // DeviceTsdf::initDefault
+    AFX_LAUNCH_CHECK();
+    AFX_CUDA(cudaMemsetAsync(f->weights, 0, f->S * 4, st));
+    AFX_CUDA(cudaMemsetAsync(f->coll, 0, f->S * 4, st));
+    AFX_CUDA(cudaMemsetAsync(f->centroid0, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->acc, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->error, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->epoch, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->npoints, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->n_nodes, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->n_old, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->ncorr, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->nmverts, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->nmfaces, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->stats, 0, sizeof(FrameStats), st));
+    gn_init_barrier(f->gn, st);
+    f->frame = 0;
+    return AFX_OK;
+}
+
+static int extract_frame_mesh(afx_fusion* f, cudaStream_t st) {
+    // canonical point cloud for the next frame (runMarchingCubesMeshKernel on the volume the next
+    // frame starts from) and, if asked, the output mesh (runMarchingCubesFullKernel), in one pass
+    AFX_CUDA(cudaMemsetAsync(f->npoints, 0, 4, st));
+    const bool mesh = f->p.extract_mesh != 0;
+    return mc_fused_impl(f->tsdf, f->weights, f->vol, 0.f, f->points, f->npoints, f->p.mesh_capacity,
+                         mesh ? f->mverts : nullptr, mesh ? f->nmverts : nullptr, f->p.triangle_capacity * 3,
+                         mesh ? f->mfaces : nullptr, mesh ? f->nmfaces : nullptr, f->p.triangle_capacity, st);
+}
+
+int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
+    if (!f || !depth_mm) return AFX_ERR_INVALID_ARGUMENT;
+    const afx_fusion_params& p = f->p;
+    cudaStream_t st = as_stream(stream);
+    int rc;
+    static const float I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    frame_begin_kernel<<<1, 1, 0, st>>>(f->epoch, f->ncorr, f->error, f->nmverts, f->nmfaces);
+    AFX_LAUNCH_CHECK();
+    // af::loadProcessFrame (src/VolumeFusion.cu:151-220)
+    afx_prep_params pp;
+    std::memcpy(pp.K, p.K, sizeof(pp.K));
+    pp.depth_threshold = p.depth_threshold;
+    pp.bilateral = p.bilateral;
+    pp.bilateral_r = p.bilateral_r;
+    pp.sigma_i = p.sigma_i;
+    pp.sigma_s = p.sigma_s;
+    pp.bilateral_thr = p.bilateral_thr;
+    pp.excl_angle_lo = p.excl_angle_lo;
+    pp.excl_angle_hi = p.excl_angle_hi;
+    stage_mark(f, ST_PREP, st);
+    rc = frame_prep_impl(depth_mm, p.width, p.height, &pp, f->depth, f->verts, f->normals,
+                         f->frame == 0 ? f->centroid0 : f->centroid, f->acc, f->error, st);
+    if (rc) return rc;
+    if (f->frame == 0) {
+        stage_mark(f, ST_INTEGRATE_RIGID, st);
+        // rigid integration at the frame-0 centroid (src/VolumeFusion.cu:334-336)
+        rc = integrate_rigid_impl(f->tsdf, f->weights, f->depth, p.width, p.height, p.delta, f->vol, I3, nullptr, p.K,
+                                  st, f->centroid0);
+        if (rc) return rc;
+        stage_mark(f, ST_MC, st);
+        rc = extract_frame_mesh(f, st);
+        if (rc) return rc;
+        stage_mark(f, -1, st);
+        stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame, f->n_nodes, f->n_old, f->npoints, f->ncorr, f->gn.state,
+                                      f->nmverts, f->nmfaces, f->error, 0);
+        AFX_LAUNCH_CHECK();
+        f->frame++;
+        return AFX_OK;
+    }
+    const long M = p.mesh_capacity;
+    const int N = p.node_capacity;
+    // canonical point cloud: sort + unique, then + frame-0 centroid (src/VolumeFusion.cu:382-389)
+    stage_mark(f, ST_SORT, st);
+    rc = sort_unique_impl(f->points, f->npoints, M, f->ws_sort, f->ws_sort_bytes, st);
+    if (rc) return rc;
+    rc = translate_dev_impl(f->points, f->points, f->npoints, M, f->centroid0, 1.f, st);
+    if (rc) return rc;
+    // motion graph (src/VolumeFusion.cu:394-404)
+    stage_mark(f, ST_GRAPH, st);
+    record_n_old_kernel<<<1, 1, 0, st>>>(f->n_nodes, f->n_old);
+    AFX_LAUNCH_CHECK();
+    if (f->frame == 1 || p.update_graph) {
+        rc = build_graph_impl(f->nodes_host, f->radii, f->T, f->n_nodes, N, f->points, f->npoints, M, p.graph_radius,
+                              f->ws_graph, f->ws_graph_bytes, f->error, st);
+        if (rc) return rc;
+        copy_new_nodes_kernel<<<blocks_for(N, 256), 256, 0, st>>>(f->nodes_dev, f->nodes_host, f->n_old, f->n_nodes, N);
+        AFX_LAUNCH_CHECK();
+    }
+    // KNN and weights (src/VolumeFusion.cu:410-424)
+    stage_mark(f, ST_KNN, st);
+    rc = knn_impl(f->midx, f->mdist, f->nodes_host, f->n_nodes, N, f->points, f->npoints, M, p.knn, 0, st);
+    if (rc) return rc;
+    rc = knn_impl(f->gidx, f->gdist, f->nodes_host, f->n_nodes, N, f->nodes_host, nullptr, N, p.kreg, 1, st);
+    if (rc) return rc;
+    rc = afx_filter_disconnected(f->gidx, f->gdist, f->n_nodes, N, p.kreg, f->radii, st);
+    if (rc) return rc;
+    rc = warp_weights_impl(f->mw, f->radii, f->midx, f->mdist, f->npoints, M, p.knn, f->n_nodes, st);
+    if (rc) return rc;
+    GnArgs g;
+    std::memset(&g, 0, sizeof(g));
+    g.mesh = f->points;
+    g.mesh_count = f->npoints;
+    g.m_max = M;
+    g.midx = f->midx;
+    g.mw = f->mw;
+    g.k = p.knn;
+    g.normals = f->normals;
+    g.frame = f->verts;
+    g.corr = f->corr;
+    g.corr_count = f->ncorr;
+    g.c_max = M;
+    g.corr_of_vertex = f->corr_of_vertex;
+    g.nodes = f->nodes_dev;
+    g.n_nodes = f->n_nodes;
+    g.n_max = N;
+    g.gidx = f->gidx;
+    g.kreg = p.kreg;
+    g.lam_d = p.lambda_depth;
+    g.lam_r = p.lambda_reg;
+    g.min_step = p.energy_min_step;
+    g.b = f->gn;
+    g.error = f->error;
+    stage_mark(f, ST_GN_SETUP, st);
+    rc = gn_frame_setup(g, st);
+    if (rc) return rc;
+    const double tol = p.solver == 2 ? p.pcg_tol : 0.0;
+    for (int icp = 0; icp < p.icp_iterations; ++icp) {
+        // warp with the committed transforms, then projective correspondences (src/VolumeFusion.cu:439-447)
+        rc = warp_impl(f->warped, f->points, f->T, f->midx, f->mw, f->npoints, M, p.knn, st);
+        if (rc) return rc;
+        rc = correspondences_impl(f->corr, f->ncorr, M, f->warped, f->npoints, M, p.K, f->depth, p.height, p.width,
+                                  f->verts, p.corr_thresh, f->corr_of_vertex, f->ws_corr, f->ws_corr_bytes, st);
+        if (rc) return rc;
+        rc = gn_icp_setup(g, f->Tp, f->T, st);
+        if (rc) return rc;
+        stage_mark(f, ST_GN_LOOP, st);
+        for (int it = 0; it < p.gn_iterations; ++it) {
+            rc = gn_iteration(g, it, f->warped, f->T, f->Tp, p.pcg_iterations, tol, st);
+            if (rc) return rc;
+            rc = warp_impl(f->warped, f->points, f->Tp, f->midx, f->mw, f->npoints, M, p.knn, st);
+            if (rc) return rc;
+        }
+    }
+    // voxel support, warp, collisions and warped integration (src/VolumeFusion.cu:702-741)
+    stage_mark(f, ST_SUPPORT, st);
+    rc = translate_dev_impl(f->nodes_t, f->nodes_dev, nullptr, N, f->centroid0, -1.f, st);
+    if (rc) return rc;
+    rc = build_support(f->sup, f->vol, f->per, f->nodes_t, f->radii, f->n_nodes, N, f->error, st);
+    if (rc) return rc;
+    // the reference translates its device graph back in place: p = (p - c) + c (src/VolumeFusion.cu:721)
+    rc = translate_dev_impl(f->nodes_dev, f->nodes_t, nullptr, N, f->centroid0, 1.f, st);
+    if (rc) return rc;
+    WarpArgs wa;
+    std::memset(&wa, 0, sizeof(wa));
+    wa.vol = f->vol;
+    wa.bg = make_bricks(f->vol);
+    wa.k = p.knn;
+    wa.nodes_t = f->nodes_t;
+    wa.radii = f->radii;
+    wa.transforms = f->T;
+    wa.brick_offset = f->sup.brick_offset;
+    wa.brick_count = f->sup.brick_count;
+    wa.brick_nodes = f->sup.brick_nodes;
+    wa.active = f->sup.active;
+    wa.n_active = f->sup.n_active;
+    for (int c = 0; c < 3; ++c) wa.per[c] = f->per[c];
+    wa.centroid_dev = f->centroid0;
+    std::memcpy(wa.Rinv, I3, sizeof(I3));
+    wa.out = f->wvox;
+    wa.out_count = f->wcount;
+    wa.coll = f->coll;
+    wa.epoch_dev = f->epoch;
+    wa.error = f->error;
+    stage_mark(f, ST_VOXEL_WARP, st);
+    rc = launch_brick_warp(wa, wa.bg.n, st);
+    if (rc) return rc;
+    stage_mark(f, ST_WARPED_INTEGRATE, st);
+    if (p.integrate) {
+        WarpedIntegrateArgs ia;
+        ia.vol = f->vol;
+        ia.bg = wa.bg;
+        ia.active = f->sup.active;
+        ia.n_active = f->sup.n_active;
+        ia.in = f->wvox;
+        ia.in_count = f->wcount;
+        ia.coll = f->coll;
+        ia.epoch_dev = f->epoch;
+        ia.tsdf = f->tsdf;
+        ia.weights = f->weights;
+        ia.depth = f->depth;
+        ia.W = p.width;
+        ia.H = p.height;
+        ia.delta = p.delta;
+        ia.K = make_intrinsics(p.K);
+        rc = launch_brick_integrate(ia, wa.bg.n, st);
+        if (rc) return rc;
+    }
+    stage_mark(f, ST_MC, st);
+    rc = extract_frame_mesh(f, st);
+    if (rc) return rc;
+    stage_mark(f, -1, st);
+    stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame, f->n_nodes, f->n_old, f->npoints, f->ncorr, f->gn.state,
+                                  f->nmverts, f->nmfaces, f->error, 1);
+    AFX_LAUNCH_CHECK();
+    f->frame++;
+    return AFX_OK;
+}
+
+int afx_fusion_process_host(afx_fusion* f, const uint16_t* depth_mm_host, void* stream) {
+    if (!f || !depth_mm_host) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    AFX_CUDA(cudaMemcpyAsync(f->depth_mm, depth_mm_host, f->P * 2, cudaMemcpyHostToDevice, st));
+    return afx_fusion_process(f, f->depth_mm, stream);
+}
+
+int afx_fusion_stats(afx_fusion* f, afx_frame_stats* out, void* stream) {
+    if (!f || !out) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    FrameStats s;
+    AFX_CUDA(cudaMemcpyAsync(&s, f->stats, sizeof(s), cudaMemcpyDeviceToHost, st));
+    AFX_CUDA(cudaStreamSynchronize(st));
+    out->frame = s.frame;
+    out->n_nodes = s.n_nodes;
+    out->new_nodes = s.new_nodes;
+    out->mesh_points = s.mesh_points;
+    out->correspondences = s.correspondences;
+    out->gn_iterations_done = s.gn_iterations_done;
+    out->energy = s.energy;
+    out->mesh_vertices = s.mesh_vertices;
+    out->mesh_faces = s.mesh_faces;
+    out->error = s.error;
+    if (s.error & ERRF_TIMEOUT) return AFX_ERR_TIMEOUT;
+    if (s.error & ERRF_SINGULAR) return AFX_ERR_SINGULAR;
+    if (s.error & ERRF_UNSUPPORTED) return AFX_ERR_UNSUPPORTED;
+    if (s.error & ERRF_CAPACITY) return AFX_ERR_CAPACITY;
+    return AFX_OK;
+}
+
+int afx_fusion_tsdf(afx_fusion* f, float** tsdf, float** weights) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    if (tsdf) *tsdf = f->tsdf;
+    if (weights) *weights = f->weights;
+    return AFX_OK;
+}
+
+int afx_fusion_graph(afx_fusion* f, float** nodes, float** radii, float** transforms, int** n_nodes) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    if (nodes) *nodes = f->nodes_host;
+    if (radii) *radii = f->radii;
+    if (transforms) *transforms = f->T;
+    if (n_nodes) *n_nodes = f->n_nodes;
+    return AFX_OK;
+}
+
+int afx_fusion_centroid(afx_fusion* f, float** centroid) {
+    if (!f || !centroid) return AFX_ERR_INVALID_ARGUMENT;
+    *centroid = f->centroid0;
+    return AFX_OK;
+}
+
+int afx_fusion_point_cloud(afx_fusion* f, float** points, unsigned** count) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    if (points) *points = f->points;
+    if (count) *count = f->npoints;
+    return AFX_OK;
+}
+
+int afx_fusion_mesh(afx_fusion* f, float** vertices, unsigned** vertex_count, int** faces, unsigned** face_count) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    if (vertices) *vertices = f->mverts;
+    if (vertex_count) *vertex_count = f->nmverts;
+    if (faces) *faces = f->mfaces;
+    if (face_count) *face_count = f->nmfaces;
+    return AFX_OK;
+}
+
+int afx_fusion_frame_views(afx_fusion* f, float** depth, float** vertices, float** normals) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    if (depth) *depth = f->depth;
+    if (vertices) *vertices = f->verts;
+    if (normals) *normals = f->normals;
+    return AFX_OK;
+}
+
+int afx_fusion_set_transforms(afx_fusion* f, const float* transforms_host, int n, void* stream) {
+    if (!f || !transforms_host || n < 0 || n > f->p.node_capacity) return AFX_ERR_INVALID_ARGUMENT;
+    AFX_CUDA(cudaMemcpyAsync(f->T, transforms_host, (size_t)n * 64, cudaMemcpyHostToDevice, as_stream(stream)));
+    return AFX_OK;
+}
+
+long afx_fusion_kernel_launches(const afx_fusion* f) { return f ? launches_total() - f->launches_at_create : 0; }
+
+int afx_fusion_set_timing(afx_fusion* f, int on) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    f->timing = on != 0;
+    return AFX_OK;
+}
+
+int afx_fusion_stage_times(afx_fusion* f, double* ms, int n, int reset) {
+    if (!f || !ms || n < 1) return AFX_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < n; ++i) ms[i] = 0.0;
+    for (auto& u : f->ev_used) {
+        cudaEventSynchronize(u.second.second);
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, u.second.first, u.second.second) == cudaSuccess && u.first >= 0 && u.first < n)
+            ms[u.first] += t;
+    }
+    cudaGetLastError();
+    if (reset) {
+        for (auto& u : f->ev_used) {
+            f->ev_pool.push_back(u.second.first);
+            f->ev_pool.push_back(u.second.second);
+        }
+        f->ev_used.clear();
+    }
+    return ST_COUNT;
+}
+
+int afx_copy_device(void* dst, const void* src, size_t bytes, void* stream) {
+    if ((!dst || !src) && bytes) return AFX_ERR_INVALID_ARGUMENT;
+    if (!bytes) return AFX_OK;
+    AFX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, as_stream(stream)));
+    return AFX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,59 @@
+// afx_internal.h -- functions shared between the library's translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "afx_common.cuh"
+
+namespace afx {
+
+// ---- scans (afx_scan.cu) ----
+// Exclusive prefix sum of n unsigned values; out may alias in.  If total != nullptr the
+// sum of all n values is written there (device).  Workspace: scan_workspace_size(n).
+size_t scan_workspace_size(long n);
+int scan_exclusive(const unsigned* in, unsigned* out, long n, unsigned* total, void* ws, cudaStream_t st);
+// Same, with the element count read from the device (n = min(*count, n_max)).
+int scan_exclusive_dev(const unsigned* in, unsigned* out, const unsigned* count, long n_max, unsigned* total, void* ws,
+                       cudaStream_t st);
+
+// ---- prep (afx_prep.cu) ----
+int frame_prep_impl(const uint16_t* mm, int width, int height, const afx_prep_params* p, float* depth, float* vertices,
+                    float* normals, float* centroid, unsigned long long* acc, int* error, cudaStream_t st);
+
+// ---- integration (afx_integrate.cu) ----
+int integrate_rigid_impl(float* tsdf, float* weights, const float* depth, int W, int H, float delta, const Volume& vol,
+                         const float* R, const float* t, const float* K, cudaStream_t st, const float* t_dev = nullptr);
+void rotation_inverse(const float* R, float* Rinv);
+
+// ---- marching cubes and sorting (afx_mc.cu) ----
+size_t sort_unique_workspace_size(long n_max);
+int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, cudaStream_t st);
+int mc_fused_impl(const float* tsdf, const float* weights, const Volume& vol, float iso, float* points,
+                  unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
+                  unsigned* face_count, long face_cap, cudaStream_t st);
+int translate_impl(float* pts, const unsigned* count, long n_max, const float* t, cudaStream_t st);
+// pts += sign * t_dev (t_dev in device memory); dst may differ from src
+int translate_dev_impl(float* dst, const float* src, const unsigned* count, long n_max, const float* t_dev, float sign,
+                       cudaStream_t st);
+
+}  // namespace afx
+
+namespace afx {
+// ---- graph (afx_graph.cu) ----
+size_t build_graph_ws(long mesh_max);
+int build_graph_impl(float* nodes, float* radii, float* T, int* n_nodes, int cap, const float* mesh,
+                     const unsigned* mesh_count, long mesh_max, float r, void* ws, size_t ws_bytes, int* error,
+                     cudaStream_t st);
+int knn_impl(uint32_t* idx, float* dist, const float* nodes, const int* n_nodes, int n_max, const float* pts,
+             const unsigned* count, long m_max, int k, int excl, cudaStream_t st);
+int warp_weights_impl(float* w, const float* radii, const uint32_t* idx, const float* dist, const unsigned* count,
+                      long m_max, int k, const int* n_nodes, cudaStream_t st);
+int warp_impl(float* out, const float* pts, const float* T, const uint32_t* idx, const float* w, const unsigned* count,
+              long m_max, int k, cudaStream_t st);
+size_t corr_ws(long m_max);
+int correspondences_impl(int* corr, unsigned* corr_count, long cap, const float* warped, const unsigned* count,
+                         long m_max, const float* K, const float* depth, int rows, int cols, const float* frame,
+                         float thresh, int* corr_of_vertex, void* ws, size_t ws_bytes, cudaStream_t st);
+}  // namespace afx
