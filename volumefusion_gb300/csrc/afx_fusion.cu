@@ -107,10 +107,14 @@ struct afx_fusion {
     GnBuffers gn;
     // optional per-stage timing (the reference's TimeMap, include/af/TimeMap.h)
     bool timing = false;
-    std::vector<cudaEvent_t> ev_pool;
-    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_used;
-    cudaEvent_t ev_open = nullptr;
-    int ev_stage = -1;
+    std::vector<cudaEvent_t> ev_pool;                  // recorded-and-read events for reuse
+    std::vector<std::pair<int, cudaEvent_t>> marks;    // (stage started at this event, event); -1 = stage end
+    // canonical point cloud double buffer: marching cubes at the end of a frame writes the
+    // next frame's raw points into points_buf[cur ^ 1] while points_buf[cur] keeps this frame's
+    int cur = 0;
+    float* points_buf[2];
+    unsigned* npoints_buf[2];
+    unsigned* mesh_used;   // canonical point count used by the last frame
 };
 
 namespace afx {
@@ -169,23 +173,13 @@ static cudaEvent_t take_event(afx_fusion* f) {
     return e;
 }
 
-// Marks the start of `stage` (closing the previous one) when timing is on.
+// Records an event that ends the running stage and starts `stage` (-1: no new stage).
 static void stage_mark(afx_fusion* f, int stage, cudaStream_t st) {
     if (!f->timing) return;
     cudaEvent_t e = take_event(f);
+    if (!e) return;
     cudaEventRecord(e, st);
-    if (f->ev_open) f->ev_used.push_back({f->ev_stage, {f->ev_open, e}});
-    if (stage < 0) {
-        f->ev_pool.push_back(e);  // closing mark only
-        f->ev_open = nullptr;
-        f->ev_stage = -1;
-        return;
-    }
-    // the closing event of the previous stage doubles as this stage's opening event
-    cudaEvent_t e2 = take_event(f);
-    cudaEventRecord(e2, st);
-    f->ev_open = e2;
-    f->ev_stage = stage;
+    f->marks.push_back({stage, e});
 }
 
 extern "C" {
@@ -275,7 +269,7 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     add(S * 4); add(S * 4); add(S * 4);                  // tsdf weights coll
     add(Pp * 2); add(Pp * 4); add(Pp * 12); add(Pp * 12);  // frame buffers
     add(64); add(64); add(64); add(64); add(64);          // centroids acc error epoch
-    add(M * 12); add(64);                                 // points
+    add(M * 12); add(64); add(M * 12); add(64); add(64);  // point-cloud double buffer + used count
     add(N * 12); add(N * 12); add(N * 12); add(N * 4); add(N * 64); add(N * 64); add(64); add(64);
     add(M * p.knn * 4); add(M * p.knn * 4); add(M * p.knn * 4);
     add(N * p.kreg * 4); add(N * p.kreg * 4);
@@ -309,8 +303,13 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     f->acc = (unsigned long long*)take(64);
     f->error = (int*)take(64);
     f->epoch = (unsigned*)take(64);
-    f->points = (float*)take(M * 12);
-    f->npoints = (unsigned*)take(64);
+    f->points_buf[0] = (float*)take(M * 12);
+    f->npoints_buf[0] = (unsigned*)take(64);
+    f->points_buf[1] = (float*)take(M * 12);
+    f->npoints_buf[1] = (unsigned*)take(64);
+    f->mesh_used = (unsigned*)take(64);
+    f->points = f->points_buf[0];
+    f->npoints = f->npoints_buf[0];
     f->nodes_host = (float*)take(N * 12);
     f->nodes_dev = (float*)take(N * 12);
     f->nodes_t = (float*)take(N * 12);
@@ -366,12 +365,9 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
 
 int afx_fusion_destroy(afx_fusion* f) {
     if (!f) return AFX_ERR_INVALID_ARGUMENT;
-    for (auto& u : f->ev_used) {
-        cudaEventDestroy(u.second.first);
-        cudaEventDestroy(u.second.second);
-    }
+    cudaDeviceSynchronize();
+    for (auto& m : f->marks) cudaEventDestroy(m.second);
     for (auto e : f->ev_pool) cudaEventDestroy(e);
-    if (f->ev_open) cudaEventDestroy(f->ev_open);
     cudaError_t e = cudaFree(f->arena);
     delete f;
     return note_cuda_error(e);
@@ -393,7 +389,12 @@ int afx_fusion_reset(afx_fusion* f, void* stream) {
     AFX_CUDA(cudaMemsetAsync(f->acc, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->error, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->epoch, 0, 64, st));
-    AFX_CUDA(cudaMemsetAsync(f->npoints, 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->npoints_buf[0], 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->npoints_buf[1], 0, 64, st));
+    AFX_CUDA(cudaMemsetAsync(f->mesh_used, 0, 64, st));
+    f->cur = 0;
+    f->points = f->points_buf[0];
+    f->npoints = f->npoints_buf[0];
     AFX_CUDA(cudaMemsetAsync(f->n_nodes, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->n_old, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->ncorr, 0, 64, st));
@@ -408,9 +409,10 @@ int afx_fusion_reset(afx_fusion* f, void* stream) {
 static int extract_frame_mesh(afx_fusion* f, cudaStream_t st) {
     // canonical point cloud for the next frame (runMarchingCubesMeshKernel on the volume the next
     // frame starts from) and, if asked, the output mesh (runMarchingCubesFullKernel), in one pass
-    AFX_CUDA(cudaMemsetAsync(f->npoints, 0, 4, st));
+    const int next = f->cur ^ 1;
+    AFX_CUDA(cudaMemsetAsync(f->npoints_buf[next], 0, 4, st));
     const bool mesh = f->p.extract_mesh != 0;
-    return mc_fused_impl(f->tsdf, f->weights, f->vol, 0.f, f->points, f->npoints, f->p.mesh_capacity,
+    return mc_fused_impl(f->tsdf, f->weights, f->vol, 0.f, f->points_buf[next], f->npoints_buf[next], f->p.mesh_capacity,
                          mesh ? f->mverts : nullptr, mesh ? f->nmverts : nullptr, f->p.triangle_capacity * 3,
                          mesh ? f->mfaces : nullptr, mesh ? f->nmfaces : nullptr, f->p.triangle_capacity, st);
 }
@@ -448,7 +450,7 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
         rc = extract_frame_mesh(f, st);
         if (rc) return rc;
         stage_mark(f, -1, st);
-        stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame, f->n_nodes, f->n_old, f->npoints, f->ncorr, f->gn.state,
+        stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame, f->n_nodes, f->n_old, f->mesh_used, f->ncorr, f->gn.state,
                                       f->nmverts, f->nmfaces, f->error, 0);
         AFX_LAUNCH_CHECK();
         f->frame++;
@@ -458,7 +460,12 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
     const int N = p.node_capacity;
     // canonical point cloud: sort + unique, then + frame-0 centroid (src/VolumeFusion.cu:382-389)
     stage_mark(f, ST_SORT, st);
+    f->cur ^= 1;
+    f->points = f->points_buf[f->cur];
+    f->npoints = f->npoints_buf[f->cur];
     rc = sort_unique_impl(f->points, f->npoints, M, f->ws_sort, f->ws_sort_bytes, st);
+    if (rc) return rc;
+    AFX_CUDA(cudaMemcpyAsync(f->mesh_used, f->npoints, 4, cudaMemcpyDeviceToDevice, st));
     if (rc) return rc;
     rc = translate_dev_impl(f->points, f->points, f->npoints, M, f->centroid0, 1.f, st);
     if (rc) return rc;
@@ -586,7 +593,7 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
     rc = extract_frame_mesh(f, st);
     if (rc) return rc;
     stage_mark(f, -1, st);
-    stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame, f->n_nodes, f->n_old, f->npoints, f->ncorr, f->gn.state,
+    stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame, f->n_nodes, f->n_old, f->mesh_used, f->ncorr, f->gn.state,
                                   f->nmverts, f->nmfaces, f->error, 1);
     AFX_LAUNCH_CHECK();
     f->frame++;
@@ -686,19 +693,17 @@ int afx_fusion_set_timing(afx_fusion* f, int on) {
 int afx_fusion_stage_times(afx_fusion* f, double* ms, int n, int reset) {
     if (!f || !ms || n < 1) return AFX_ERR_INVALID_ARGUMENT;
     for (int i = 0; i < n; ++i) ms[i] = 0.0;
-    for (auto& u : f->ev_used) {
-        cudaEventSynchronize(u.second.second);
+    if (!f->marks.empty()) cudaEventSynchronize(f->marks.back().second);
+    for (size_t i = 0; i + 1 < f->marks.size(); ++i) {
+        int stage = f->marks[i].first;
+        if (stage < 0 || stage >= n) continue;
         float t = 0.f;
-        if (cudaEventElapsedTime(&t, u.second.first, u.second.second) == cudaSuccess && u.first >= 0 && u.first < n)
-            ms[u.first] += t;
+        if (cudaEventElapsedTime(&t, f->marks[i].second, f->marks[i + 1].second) == cudaSuccess) ms[stage] += t;
     }
     cudaGetLastError();
     if (reset) {
-        for (auto& u : f->ev_used) {
-            f->ev_pool.push_back(u.second.first);
-            f->ev_pool.push_back(u.second.second);
-        }
-        f->ev_used.clear();
+        for (auto& m : f->marks) f->ev_pool.push_back(m.second);
+        f->marks.clear();
     }
     return ST_COUNT;
 }

@@ -115,7 +115,11 @@ __global__ void graph_setup_kernel(GraphState s, Grid* gout) {
         ext = fmaxf(ext, hi[c] - lo[c]);
     }
     float cell = s.r > 0.f ? s.r : 1.f;
-    for (;;) {
+    if (!(ext < 1e6f)) {  // non-finite coordinates: refuse rather than size a grid from them
+        atomicOr(s.error, ERRF_UNSUPPORTED);
+        for (int c = 0; c < 3; ++c) lo[c] = hi[c] = 0.f;
+    }
+    for (int guard = 0; guard < 200; ++guard) {
         long cells = 1;
         for (int c = 0; c < 3; ++c) cells *= (long)((hi[c] - lo[c]) / cell) + 2;
         if (cells <= kGridMaxCells) break;
