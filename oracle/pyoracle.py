@@ -90,6 +90,7 @@ def lib():
             "vfo_fusion_centroid": (C.c_void_p, [C.c_void_p]),
             "vfo_fusion_mesh": (C.c_void_p, [C.c_void_p]),
             "vfo_fusion_set_transforms": (None, [C.c_void_p, f32p, C.c_int]),
+            "vfo_fusion_set_tsdf": (None, [C.c_void_p, f32p, f32p]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -448,3 +449,6 @@ class Fusion:
     def set_transforms(self, T):
         T = _f32(T).reshape(-1, 16)
         lib().vfo_fusion_set_transforms(self.h, T, len(T))
+
+    def set_tsdf(self, tsdf, weights):
+        lib().vfo_fusion_set_tsdf(self.h, _f32(tsdf).ravel(), _f32(weights).ravel())

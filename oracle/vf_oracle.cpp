@@ -1208,4 +1208,9 @@ void vfo_fusion_set_transforms(vfo_fusion* f, const float* T, int n) {
     std::memcpy(f->T.data(), T, 64 * (size_t)std::min(n, f->n));
 }
 
+void vfo_fusion_set_tsdf(vfo_fusion* f, const float* tsdf, const float* weights) {
+    std::memcpy(f->tsdf.data(), tsdf, sizeof(float) * f->S);
+    std::memcpy(f->weights.data(), weights, sizeof(float) * f->S);
+}
+
 }  // extern "C"

@@ -137,6 +137,8 @@ const float* vfo_fusion_centroid(const vfo_fusion* f);
 const float* vfo_fusion_mesh(const vfo_fusion* f);
 /* Replace the committed node transforms (used to feed a GPU solution back for stage-wise parity). */
 void vfo_fusion_set_transforms(vfo_fusion* f, const float* transforms, int n);
+/* Replace the volume (stage-wise parity: continue from the GPU's volume). */
+void vfo_fusion_set_tsdf(vfo_fusion* f, const float* tsdf, const float* weights);
 
 #ifdef __cplusplus
 }

@@ -89,3 +89,35 @@ def test_mc_tables_match_reference_when_present():
     edges = [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4), (0, 4), (1, 5), (2, 6), (3, 7)]
     mine = [sum(1 << i for i, (a, b) in enumerate(edges) if ((c >> a) & 1) != ((c >> b) & 1)) for c in range(256)]
     assert mine == ref_et
+
+
+def test_cpp_shims_compile_against_reference_style_callers(tmp_path):
+    """A caller using the reference's names and Eigen-like value types compiles against the
+    header-only shims (syntax and template instantiation only; nothing runs)."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("no g++")
+    src = tmp_path / "caller.cpp"
+    src.write_text(r'''
+#include <af/afx_shims.h>
+struct V3f { float v[3]; float operator[](int i) const { return v[i]; } };
+struct V3i { int v[3]; int operator[](int i) const { return v[i]; } };
+struct V2i { int v[2]; int operator[](int i) const { return v[i]; } };
+struct M3f { float m[9]; const float* data() const { return m; } };
+void caller(float* tsdf, float* w, const float* depth, int* coll, const int* cnt, const float* verts) {
+    V2i fd{{640, 576}}; V3i dims{{256, 256, 256}}; V3f vs{{0.004f, 0.004f, 0.004f}}, size{{1.024f, 1.024f, 1.024f}},
+        t{{0, 0, 0.8f}};
+    M3f R{{1, 0, 0, 0, 1, 0, 0, 0, 1}}, K{{504, 0, 0, 0, 504, 0, 320, 288, 1}};
+    af::runIntegrateTSDFFromFrameKernel(tsdf, w, depth, fd, 0.016f, dims, vs, size, R, t, K);
+    af::runCountCollisionsPerVoxelKernel(coll, verts, cnt, vs, size, dims, R, t);
+    af::runIntegrateWarpedTSDFFromFrameKernel(tsdf, w, verts, coll, cnt, depth, fd, 0.016f, vs, size, dims, R, t, K);
+    afx_fusion_params p; afx_fusion_default_params(&p);
+    af::VolumeFusionSession s(p);
+    (void)s;
+}
+''')
+    r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"),
+                        "-I", "/usr/local/cuda/include", str(src)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

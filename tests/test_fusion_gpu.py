@@ -32,6 +32,10 @@ def test_first_frame_rigid_bit_exact():
 
 
 def test_session_tracks_oracle_small_sequence():
+    """Frame by frame from a common state: after every frame the oracle continues from the GPU's
+    volume and warp field, so each frame's stages are compared from identical inputs.  Point
+    cloud, graph and correspondences are then bit-identical; the solve agrees to 1e-4 (PCG
+    in FP32/FP64 vs FP64) and the integrated volume differs only where that moves a projection."""
     from volumefusion_gb300 import configs
     cfg = configs.small_nonrigid(n_frames=6)
     frames = configs.small_frames(cfg)
@@ -41,26 +45,25 @@ def test_session_tracks_oracle_small_sequence():
         s.process(mm)
         o.process(mm)
         st = s.stats()
-        if i == 0:
-            continue
-        assert st["error"] == 0
-        assert st["n_nodes"] == o.num_nodes, (i, st, o.num_nodes)
-        assert st["mesh_points"] == o.mesh_size
-        nodes, radii, T = s.graph()
-        assert np.array_equal(nodes.cpu().numpy(), o.nodes())
-        if i == 1:
-            # frame 1 starts from bit-identical state: point cloud, graph, correspondences agree exactly
-            assert np.array_equal(s.point_cloud().cpu().numpy(), o.mesh())
-            assert st["correspondences"] == o.num_corr
-        dT = np.abs(T.cpu().numpy() - o.transforms()).max()
-        assert dT < 1e-4, (i, dT)
+        assert st["error"] == 0, st
         t, w = s.tsdf()
         t, w = t.cpu().numpy(), w.cpu().numpy()
-        ot, ow = o.tsdf(), o.weights()
-        bad = (np.abs(t - ot) > 1e-5 * np.maximum(1.0, np.abs(ot))) | (w != ow)
-        assert bad.mean() < 1e-3, (i, bad.sum())
-        # continue both from the same warp field so later frames compare stage by stage
-        o.set_transforms(T.cpu().numpy())
+        if i == 0:
+            assert np.array_equal(t, o.tsdf()) and np.array_equal(w, o.weights())
+        else:
+            assert st["n_nodes"] == o.num_nodes, (i, st, o.num_nodes)
+            assert st["mesh_points"] == o.mesh_size, (i, st, o.mesh_size)
+            assert np.array_equal(s.point_cloud().cpu().numpy(), o.mesh())
+            nodes, radii, T = s.graph()
+            assert np.array_equal(nodes.cpu().numpy(), o.nodes())
+            assert st["correspondences"] == o.num_corr, (i, st, o.num_corr)
+            dT = np.abs(T.cpu().numpy() - o.transforms()).max()
+            assert dT < 1e-4, (i, dT)
+            ot, ow = o.tsdf(), o.weights()
+            bad = (np.abs(t - ot) > 1e-5 * np.maximum(1.0, np.abs(ot))) | (w != ow)
+            assert bad.mean() < 1e-3, (i, int(bad.sum()))
+            o.set_transforms(T.cpu().numpy())
+        o.set_tsdf(t, w)
     s.close()
 
 

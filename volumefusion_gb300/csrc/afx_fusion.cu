@@ -484,7 +484,8 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
     stage_mark(f, ST_KNN, st);
     rc = knn_impl(f->midx, f->mdist, f->nodes_host, f->n_nodes, N, f->points, f->npoints, M, p.knn, 0, st);
     if (rc) return rc;
-    rc = knn_impl(f->gidx, f->gdist, f->nodes_host, f->n_nodes, N, f->nodes_host, nullptr, N, p.kreg, 1, st);
+    rc = knn_impl(f->gidx, f->gdist, f->nodes_host, f->n_nodes, N, f->nodes_host,
+                  reinterpret_cast<const unsigned*>(f->n_nodes), N, p.kreg, 1, st);
     if (rc) return rc;
     rc = afx_filter_disconnected(f->gidx, f->gdist, f->n_nodes, N, p.kreg, f->radii, st);
     if (rc) return rc;

@@ -245,6 +245,7 @@ __global__ void __launch_bounds__(32 * kGnWarps) jtj_assemble_kernel(GnArgs a) {
         long v = ent / a.k;
         int s = (int)(ent % a.k);
         int c = a.corr_of_vertex[v];
+        if (lane == 0) a.b.jc[t] = c;
         if (c < 0) continue;
         touched = true;
         int px = a.corr[2 * (long)c + 1];
@@ -253,6 +254,8 @@ __global__ void __launch_bounds__(32 * kGnWarps) jtj_assemble_kernel(GnArgs a) {
         grad_rows(a.mesh + 3 * v, G);
         float Ja[6];
         jdepth(nrm, a.mw[v * a.k + s], G, a.lam_d, Ja);
+        if (lane == 0)
+            for (int q = 0; q < 6; ++q) a.b.jrow[(long)t * 6 + q] = Ja[q];
         for (int tt = 0; tt < a.k; ++tt) {
             float wt = a.mw[v * a.k + tt];
             if (wt == 0.f) continue;
@@ -426,13 +429,24 @@ __global__ void __launch_bounds__(256) residual_kernel(GnArgs a, const float* wa
 }
 
 // Energy test and commit decision (src/VolumeFusion.cu:589-598).
-__global__ void energy_kernel(GnArgs a, int iter) {
+__global__ void __launch_bounds__(kEnergyBlocks) energy_kernel(GnArgs a, int iter) {
     GnState* s = a.b.state;
     if (s->done) return;
-    double ed = 0, er = 0;
-    for (int i = 0; i < kEnergyBlocks; ++i) {
-        ed += a.b.epart[2 * i];
-        er += a.b.epart[2 * i + 1];
+    __shared__ double sd[kEnergyBlocks / 32], sr[kEnergyBlocks / 32];
+    // one partial pair per thread, fixed-order tree: the same totals on every run
+    double ed = warp_sum(a.b.epart[2 * threadIdx.x]);
+    double er = warp_sum(a.b.epart[2 * threadIdx.x + 1]);
+    if ((threadIdx.x & 31) == 0) {
+        sd[threadIdx.x >> 5] = ed;
+        sr[threadIdx.x >> 5] = er;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return;
+    ed = 0;
+    er = 0;
+    for (int i = 0; i < kEnergyBlocks / 32; ++i) {
+        ed += sd[i];
+        er += sr[i];
     }
     double e = ed + er;
     s->e_last = e;
@@ -464,18 +478,11 @@ __global__ void __launch_bounds__(32 * kGnWarps) jtr_kernel(GnArgs a) {
     const int q = lane < 6 ? lane : 0;
     float acc = 0.f;
     const unsigned o = a.b.loff[node], e = a.b.loff[node + 1];
+    // J rows were formed once per ICP iteration by jtj_assemble_kernel (same values, same order)
     for (unsigned t = o; t < e; ++t) {
-        unsigned ent = a.b.lst[t];
-        long v = ent / a.k;
-        int s = (int)(ent % a.k);
-        int c = a.corr_of_vertex[v];
+        int c = a.b.jc[t];
         if (c < 0) continue;
-        int px = a.corr[2 * (long)c + 1];
-        float G[3][6];
-        grad_rows(a.mesh + 3 * v, G);
-        float J[6];
-        jdepth(a.normals + 3 * (long)px, a.mw[v * a.k + s], G, a.lam_d, J);
-        acc = acc + J[q] * a.b.rdepth[c];
+        acc = acc + a.b.jrow[(long)t * 6 + q] * a.b.rdepth[c];
     }
     const unsigned io = a.b.ioff[node], ie = a.b.ioff[node + 1];
     unsigned it = io;
@@ -505,6 +512,13 @@ __global__ void __launch_bounds__(32 * kGnWarps) jtr_kernel(GnArgs a) {
 }
 
 // ---- PCG (cooperative, persistent) ----
+//
+// Only ceil(n / kGnWarps) CTAs (at most the launched grid) take part; the others leave at once.
+// Each iteration has two grid barriers: after A p (reduces p.Ap) and after the r / z update
+// (reduces r.z and r.r).  The new search direction p_k = z_k + beta p_{k-1} is formed in the
+// A p phase (double-buffered p, so neighbours' values are computed on the fly from z and the
+// previous p without a third barrier).  Reductions are finished by the last CTA to arrive, in
+// CTA order, so every CTA sees the same FP64 totals.
 
 struct PcgArgs {
     GnArgs g;
@@ -513,66 +527,49 @@ struct PcgArgs {
     double tol;  // <= 0: run exactly `iters` iterations
 };
 
-AFX_D bool grid_sync(unsigned* bar, int* err) {
-    __syncthreads();
+constexpr int kRed = 4;  // reduction slots per CTA
+
+// Arrive at the barrier with this CTA's partials; the last CTA sums all partials (fixed order)
+// into totals and releases the others.  Returns false if the bounded wait gave up.
+AFX_D bool grid_reduce_sync(unsigned* bar, int active, double* partial, double* totals, const double* mine, int nslots,
+                            double* out, int* err) {
     __shared__ int s_ok;
+    __shared__ double s_tot[kRed];
+    __syncthreads();
     if (threadIdx.x == 0) {
+        for (int i = 0; i < nslots; ++i) __stcg(partial + (long)blockIdx.x * kRed + i, mine[i]);
         volatile unsigned* gen = bar + 1;
         unsigned g = *gen;
         __threadfence();
         unsigned arrived = atomicAdd(bar, 1u) + 1;
         s_ok = 1;
-        if (arrived == gridDim.x) {
+        if (arrived == (unsigned)active) {
+            __threadfence();
+            for (int i = 0; i < nslots; ++i) {
+                double t = 0;
+                for (int c = 0; c < active; ++c) t += __ldcg(partial + (long)c * kRed + i);
+                __stcg(totals + i, t);
+            }
             bar[0] = 0;
             __threadfence();
             atomicAdd(bar + 1, 1u);
         } else {
-            long i = 0;
+            long k = 0;
             while (*gen == g) {
-                if (++i > (1L << 24)) {
+                if (++k > (1L << 24)) {
                     atomicOr(err, ERRF_TIMEOUT);
                     s_ok = 0;
                     break;
                 }
                 __nanosleep(32);
             }
+            __threadfence();
         }
-        __threadfence();
+        for (int i = 0; i < nslots; ++i) s_tot[i] = __ldcg(totals + i);
     }
     __syncthreads();
+    for (int i = 0; i < nslots; ++i) out[i] = s_tot[i];
     return s_ok != 0;
-}
-
-// y = A x for node `node`, computed by one warp; returns the 6 entries in lanes 0..5.
-AFX_D void spmv_row(const GnBuffers& b, int node, const float* x, float* y6) {
-    const int lane = threadIdx.x & 31;
-    const int cnt = b.nbr_cnt[node];
-    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int u = lane; u <= cnt; u += 32) {
-        const float* blk;
-        const float* xv;
-        bool tr = false;
-        if (u == 0) {
-            blk = b.diag + (long)node * 36;
-            xv = x + (long)node * 6;
-        } else {
-            int ref = b.nbr_ref[(long)node * kMaxNbr + u - 1];
-            int other = b.nbr[(long)node * kMaxNbr + u - 1];
-            xv = x + (long)other * 6;
-            if (ref >= 0) blk = b.blocks + (long)ref * 36;
-            else {
-                blk = b.blocks + (long)(-ref - 1) * 36;
-                tr = true;
-            }
-        }
-        for (int i = 0; i < 6; ++i) {
-            float s = 0.f;
-            for (int j = 0; j < 6; ++j) s = s + (tr ? blk[j * 6 + i] : blk[i * 6 + j]) * xv[j];
-            acc[i] = acc[i] + s;
-        }
-    }
-    for (int i = 0; i < 6; ++i) acc[i] = warp_sum(acc[i]);
-    for (int i = 0; i < 6; ++i) y6[i] = acc[i];
 }
 
 AFX_D double block_sum_d(double v, double* sh) {
@@ -586,105 +583,152 @@ AFX_D double block_sum_d(double v, double* sh) {
     return s;  // valid in thread 0
 }
 
-AFX_D double grid_total(const double* partial, int idx, int stride) {
-    double s = 0;
-    for (int i = 0; i < (int)gridDim.x; ++i) s += partial[(long)i * stride + idx];
-    return s;
+// Search direction entry for this iteration: z (first iteration) or z + beta * p_prev.
+AFX_D float pdir(const float* z, const float* pprev, long i, double beta, bool first) {
+    float zi = __ldcg(z + i);
+    return first ? zi : (float)((double)zi + beta * (double)__ldcg(pprev + i));
+}
+
+// y = A p for node `node` (one warp), p formed on the fly; returns the 6 entries in every lane.
+AFX_D void spmv_row(const GnBuffers& b, int node, const float* z, const float* pprev, double beta, bool first,
+                    float* y6) {
+    const int lane = threadIdx.x & 31;
+    const int cnt = b.nbr_cnt[node];
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int u = lane; u <= cnt; u += 32) {
+        const float* blk;
+        long xo;
+        bool tr = false;
+        if (u == 0) {
+            blk = b.diag + (long)node * 36;
+            xo = (long)node * 6;
+        } else {
+            int ref = b.nbr_ref[(long)node * kMaxNbr + u - 1];
+            int other = b.nbr[(long)node * kMaxNbr + u - 1];
+            xo = (long)other * 6;
+            if (ref >= 0) blk = b.blocks + (long)ref * 36;
+            else {
+                blk = b.blocks + (long)(-ref - 1) * 36;
+                tr = true;
+            }
+        }
+        float xv[6];
+#pragma unroll
+        for (int j = 0; j < 6; ++j) xv[j] = pdir(z, pprev, xo + j, beta, first);
+#pragma unroll
+        for (int i = 0; i < 6; ++i) {
+            float s = 0.f;
+#pragma unroll
+            for (int j = 0; j < 6; ++j) s = s + (tr ? blk[j * 6 + i] : blk[i * 6 + j]) * xv[j];
+            acc[i] = acc[i] + s;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 6; ++i) y6[i] = warp_sum(acc[i]);
 }
 
 __global__ void __launch_bounds__(32 * kGnWarps) pcg_kernel(PcgArgs P) {
     GnArgs& a = P.g;
     GnBuffers& b = a.b;
     if (b.state->done) return;
-    __shared__ double sh[kGnWarps];
     const int n = min(*a.n_nodes, a.n_max);
+    const int active = max(1, min((int)gridDim.x, (n + kGnWarps - 1) / kGnWarps));
+    if ((int)blockIdx.x >= active) return;
+    __shared__ double sh[kGnWarps];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int gw = blockIdx.x * kGnWarps + w, nw = gridDim.x * kGnWarps;
-    const long nv = (long)n * 6;
-    const long tid = blockIdx.x * (long)blockDim.x + threadIdx.x, nthreads = (long)gridDim.x * blockDim.x;
+    const int gw = blockIdx.x * kGnWarps + w, nw = active * kGnWarps;
     int* err = a.error;
-    // x = 0, r = b, z = M^-1 r, p = z, rz = r.z, bb = b.b
-    double rz = 0, bb = 0;
-    for (long t = tid; t < (long)n; t += nthreads) {
-        const double* Mi = b.minv + t * 36;
-        for (int i = 0; i < 6; ++i) {
+    float* pbuf[2] = {b.p, b.ap + (long)a.n_max * 6};  // second direction buffer follows A p
+    // x = 0, r = b, z = M^-1 r; rz = r.z, bb = b.b  (one node per warp, lanes 0..5 own one entry)
+    double rz_part = 0, bb_part = 0;
+    for (int node = gw; node < n; node += nw) {
+        if (lane < 6) {
+            const long o = (long)node * 6;
+            const double* Mi = b.minv + (long)node * 36 + lane * 6;
             double s = 0;
-            for (int j = 0; j < 6; ++j) s += Mi[i * 6 + j] * (double)b.jtr[t * 6 + j];
-            float zi = (float)s, ri = b.jtr[t * 6 + i];
-            b.x[t * 6 + i] = 0.f;
-            b.r[t * 6 + i] = ri;
-            b.z[t * 6 + i] = zi;
-            b.p[t * 6 + i] = zi;
-            rz += (double)ri * (double)zi;
-            bb += (double)ri * (double)ri;
+            for (int j = 0; j < 6; ++j) s += Mi[j] * (double)b.jtr[o + j];
+            float zi = (float)s, ri = b.jtr[o + lane];
+            b.x[o + lane] = 0.f;
+            __stcg(b.r + o + lane, ri);
+            __stcg(b.z + o + lane, zi);
+            rz_part += (double)ri * (double)zi;
+            bb_part += (double)ri * (double)ri;
         }
     }
-    double s1 = block_sum_d(rz, sh), s2 = block_sum_d(bb, sh);
-    if (threadIdx.x == 0) {
-        b.partial[blockIdx.x * 4 + 0] = s1;
-        b.partial[blockIdx.x * 4 + 1] = s2;
-    }
-    if (!grid_sync(b.bar, err)) return;
-    rz = grid_total(b.partial, 0, 4);
-    const double bnorm2 = grid_total(b.partial, 1, 4);
+    double mine[kRed] = {block_sum_d(rz_part, sh), block_sum_d(bb_part, sh), 0, 0};
+    double tot[kRed];
+    if (!grid_reduce_sync(b.bar, active, b.partial, b.partial + 4096 * kRed, mine, 2, tot, err)) return;
+    double rz = tot[0];
+    const double bnorm2 = tot[1];
+    double beta = 0;
     int it = 0;
     for (; it < P.iters; ++it) {
-        // Ap = A p, pAp
+        const bool first = it == 0;
+        const float* pprev = pbuf[(it + 1) & 1];
+        float* pcur = pbuf[it & 1];
+        // p_it = z + beta p_{it-1}; Ap = A p_it; p.Ap
         double pap = 0;
         for (int node = gw; node < n; node += nw) {
             float y[6];
-            spmv_row(b, node, b.p, y);
-            if (lane == 0)
-                for (int i = 0; i < 6; ++i) {
-                    b.ap[(long)node * 6 + i] = y[i];
-                    pap += (double)b.p[(long)node * 6 + i] * (double)y[i];
-                }
+            spmv_row(b, node, b.z, pprev, beta, first, y);
+            if (lane < 6) {
+                const long o = (long)node * 6 + lane;
+                float pi = pdir(b.z, pprev, o, beta, first);
+                __stcg(pcur + o, pi);
+                float yi = y[0];
+#pragma unroll
+                for (int q = 1; q < 6; ++q)
+                    if (lane == q) yi = y[q];
+                __stcg(b.ap + o, yi);
+                pap += (double)pi * (double)yi;
+            }
         }
-        double s = block_sum_d(pap, sh);
-        if (threadIdx.x == 0) b.partial[blockIdx.x * 4 + 2] = s;
-        if (!grid_sync(b.bar, err)) return;
-        pap = grid_total(b.partial, 2, 4);
+        mine[0] = block_sum_d(pap, sh);
+        if (!grid_reduce_sync(b.bar, active, b.partial, b.partial + 4096 * kRed, mine, 1, tot, err)) return;
+        pap = tot[0];
         if (pap == 0.0 || !(pap == pap)) break;
         const double alpha = rz / pap;
-        double rz2 = 0, rr = 0;
-        for (long t = tid; t < (long)n; t += nthreads) {
-            for (int i = 0; i < 6; ++i) {
-                b.x[t * 6 + i] = (float)((double)b.x[t * 6 + i] + alpha * (double)b.p[t * 6 + i]);
-                b.r[t * 6 + i] = (float)((double)b.r[t * 6 + i] - alpha * (double)b.ap[t * 6 + i]);
+        // x += alpha p; r -= alpha Ap; z = M^-1 r; r.z, r.r
+        double rz_p = 0, rr_p = 0;
+        for (int node = gw; node < n; node += nw) {
+            const long o = (long)node * 6;
+            float rv = 0.f;
+            if (lane < 6) {
+                b.x[o + lane] = (float)((double)b.x[o + lane] + alpha * (double)__ldcg(pcur + o + lane));
+                rv = (float)((double)__ldcg(b.r + o + lane) - alpha * (double)__ldcg(b.ap + o + lane));
+                __stcg(b.r + o + lane, rv);
             }
-            const double* Mi = b.minv + t * 36;
-            for (int i = 0; i < 6; ++i) {
+            float rr6[6];
+#pragma unroll
+            for (int j = 0; j < 6; ++j) rr6[j] = __shfl_sync(0xffffffffu, rv, j);
+            if (lane < 6) {
+                const double* Mi = b.minv + (long)node * 36 + lane * 6;
                 double zs = 0;
-                for (int j = 0; j < 6; ++j) zs += Mi[i * 6 + j] * (double)b.r[t * 6 + j];
+                for (int j = 0; j < 6; ++j) zs += Mi[j] * (double)rr6[j];
                 float zi = (float)zs;
-                b.z[t * 6 + i] = zi;
-                rz2 += (double)b.r[t * 6 + i] * (double)zi;
-                rr += (double)b.r[t * 6 + i] * (double)b.r[t * 6 + i];
+                __stcg(b.z + o + lane, zi);
+                rz_p += (double)rv * (double)zi;
+                rr_p += (double)rv * (double)rv;
             }
         }
-        double q1 = block_sum_d(rz2, sh), q2 = block_sum_d(rr, sh);
-        if (threadIdx.x == 0) {
-            b.partial[blockIdx.x * 4 + 0] = q1;
-            b.partial[blockIdx.x * 4 + 3] = q2;
-        }
-        if (!grid_sync(b.bar, err)) return;
-        rz2 = grid_total(b.partial, 0, 4);
-        rr = grid_total(b.partial, 3, 4);
-        const double beta = rz2 / rz;
-        rz = rz2;
-        for (long t = tid; t < nv; t += nthreads) b.p[t] = (float)((double)b.z[t] + beta * (double)b.p[t]);
-        if (!grid_sync(b.bar, err)) return;
-        if (P.tol > 0 && rr <= P.tol * P.tol * bnorm2) {
+        mine[0] = block_sum_d(rz_p, sh);
+        mine[1] = block_sum_d(rr_p, sh);
+        if (!grid_reduce_sync(b.bar, active, b.partial, b.partial + 4096 * kRed, mine, 2, tot, err)) return;
+        beta = tot[0] / rz;
+        rz = tot[0];
+        if (P.tol > 0 && tot[1] <= P.tol * P.tol * bnorm2) {
             ++it;
             break;
         }
     }
     // pending transforms -= [[x_rot]x, x_t; 0] (updateTransformsKernel, src/MotionOptimization.cu:483-498)
-    for (long t = tid; t < (long)n; t += nthreads) {
-        const float* u = b.x + t * 6;
-        float* T = P.T_pending + t * 16;
-        const float U[16] = {0.f, u[2], -u[1], 0.f, -u[2], 0.f, u[0], 0.f, u[1], -u[0], 0.f, 0.f, u[3], u[4], u[5], 0.f};
-        for (int e = 0; e < 16; ++e) T[e] = T[e] - U[e];
+    for (int node = gw; node < n; node += nw) {
+        if (lane == 0) {
+            const float* u = b.x + (long)node * 6;
+            float* T = P.T_pending + (long)node * 16;
+            const float U[16] = {0.f, u[2], -u[1], 0.f, -u[2], 0.f, u[0], 0.f, u[1], -u[0], 0.f, 0.f, u[3], u[4], u[5], 0.f};
+            for (int e = 0; e < 16; ++e) T[e] = T[e] - U[e];
+        }
     }
 }
 
@@ -722,9 +766,10 @@ size_t gn_workspace_size(long m_max, int n_max, int k, int kreg) {
     s += 3 * al((n_max + 1) * 4) + al((size_t)n_max * kreg * 4);  // icnt ioff icur ilst
     s += al(n_max * 4) + 2 * al((size_t)n_max * kMaxNbr * 4);     // nbr_cnt nbr nbr_ref
     s += al((size_t)n_max * kMaxNbr * 36 * 4) + al((size_t)n_max * 36 * 4) + al((size_t)n_max * 36 * 8);
-    s += al((size_t)n_max * 6 * 4) * 6;                           // jtr x r z p ap
+    s += al((size_t)m_max * k * 6 * 4) + al((size_t)m_max * k * 4);  // jrow jc
+    s += al((size_t)n_max * 6 * 4) * 5 + al((size_t)n_max * 6 * 4 * 2);  // jtr x r z p, ap + p2
     s += al(m_max * 4) + al((size_t)n_max * kreg * 3 * 4);        // rdepth rreg
-    s += al((size_t)4096 * 4 * 8) + al(64) + al(kEnergyBlocks * 2 * 8) + al(sizeof(GnState));
+    s += al((size_t)(4096 + 1) * kRed * 8) + al(64) + al(kEnergyBlocks * 2 * 8) + al(sizeof(GnState));
     s += al(scan_workspace_size(m_max > n_max ? m_max : n_max));
     return s + 1024;
 }
@@ -751,15 +796,17 @@ bool gn_carve(void* ws, size_t bytes, long m_max, int n_max, int k, int kreg, Gn
     b->blocks = (float*)take((size_t)n_max * kMaxNbr * 36 * 4);
     b->diag = (float*)take((size_t)n_max * 36 * 4);
     b->minv = (double*)take((size_t)n_max * 36 * 8);
+    b->jrow = (float*)take((size_t)m_max * k * 6 * 4);
+    b->jc = (int*)take((size_t)m_max * k * 4);
     b->jtr = (float*)take((size_t)n_max * 6 * 4);
     b->x = (float*)take((size_t)n_max * 6 * 4);
     b->r = (float*)take((size_t)n_max * 6 * 4);
     b->z = (float*)take((size_t)n_max * 6 * 4);
     b->p = (float*)take((size_t)n_max * 6 * 4);
-    b->ap = (float*)take((size_t)n_max * 6 * 4);
+    b->ap = (float*)take((size_t)n_max * 6 * 4 * 2);  // A p, then the second search-direction buffer
     b->rdepth = (float*)take(m_max * 4);
     b->rreg = (float*)take((size_t)n_max * kreg * 3 * 4);
-    b->partial = (double*)take((size_t)4096 * 4 * 8);
+    b->partial = (double*)take((size_t)(4096 + 1) * kRed * 8);
     b->bar = (unsigned*)take(64);
     b->epart = (double*)take(kEnergyBlocks * 2 * 8);
     b->state = (GnState*)take(sizeof(GnState));
@@ -839,7 +886,7 @@ int gn_iteration(const GnArgs& a, int iter, const float* warped, float* T_commit
     const GnBuffers& b = a.b;
     residual_kernel<<<kEnergyBlocks, 256, 0, st>>>(a, warped, T_pending);
     AFX_LAUNCH_CHECK();
-    energy_kernel<<<1, 1, 0, st>>>(a, iter);
+    energy_kernel<<<1, kEnergyBlocks, 0, st>>>(a, iter);
     AFX_LAUNCH_CHECK();
     commit_kernel<<<blocks_for((long)a.n_max * 16, 256), 256, 0, st>>>(a, T_committed, T_pending);
     AFX_LAUNCH_CHECK();

@@ -36,6 +36,8 @@ struct GnBuffers {
     float* blocks;         // [N*kMaxNbr*36] upper blocks (a,b), b > a, row-major
     float* diag;           // [N*36]
     double* minv;          // [N*36]
+    float* jrow;           // [M*K*6] depth-row Jacobian block of each node-list entry (per ICP iteration)
+    int* jc;               // [M*K]   its correspondence index, -1 if the vertex has none
     // per GN iteration
     float* jtr;            // [N*6]
     float* rdepth;         // [C_max]

@@ -72,20 +72,21 @@ __global__ void graph_bbox_init(int* bbox) {
     }
 }
 
-__global__ void graph_bbox_kernel(GraphState s) {
-    long m = min((long)*s.mesh_count, s.mesh_max);
-    int n = min(*s.n_nodes, s.cap);
-    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+// Bounding box of the point cloud and the existing nodes: grid-stride over the live counts,
+// block reduction, one atomic per block and axis.
+__global__ void __launch_bounds__(256) graph_bbox_kernel(GraphState s) {
+    __shared__ int smn[3][8], smx[3][8];
+    const long m = min((long)*s.mesh_count, s.mesh_max);
+    const int n = min(*s.n_nodes, s.cap);
     int mn[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, mx[3] = {(int)0x80000000, (int)0x80000000, (int)0x80000000};
-    const float* p = nullptr;
-    if (i < m) p = s.mesh + 3 * i;
-    else if (i - m < n) p = s.nodes + 3 * (i - m);
-    if (p)
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < m + n; i += (long)gridDim.x * blockDim.x) {
+        const float* p = i < m ? s.mesh + 3 * i : s.nodes + 3 * (i - m);
         for (int c = 0; c < 3; ++c) {
             int o = ford(p[c]);
-            mn[c] = o;
-            mx[c] = o;
+            mn[c] = min(mn[c], o);
+            mx[c] = max(mx[c], o);
         }
+    }
     for (int c = 0; c < 3; ++c) {
 #pragma unroll
         for (int off = 16; off > 0; off >>= 1) {
@@ -95,9 +96,19 @@ __global__ void graph_bbox_kernel(GraphState s) {
     }
     if ((threadIdx.x & 31) == 0)
         for (int c = 0; c < 3; ++c) {
-            atomicMin(s.bbox + c, mn[c]);
-            atomicMax(s.bbox + 3 + c, mx[c]);
+            smn[c][threadIdx.x >> 5] = mn[c];
+            smx[c][threadIdx.x >> 5] = mx[c];
         }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        int a = 0x7fffffff, b = (int)0x80000000;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            a = min(a, smn[threadIdx.x][w]);
+            b = max(b, smx[threadIdx.x][w]);
+        }
+        atomicMin(s.bbox + threadIdx.x, a);
+        atomicMax(s.bbox + 3 + threadIdx.x, b);
+    }
 }
 
 // Chooses the grid from the bounding box, seeds the first node when the graph is empty
@@ -361,7 +372,7 @@ int build_graph_impl(float* nodes, float* radii, float* T, int* n_nodes, int cap
     AFX_CUDA(cudaMemsetAsync(s.g.cnt, 0, (size_t)kGridMaxCells * 4, st));
     graph_bbox_init<<<1, 32, 0, st>>>(s.bbox);
     AFX_LAUNCH_CHECK();
-    graph_bbox_kernel<<<blocks_for(mesh_max + cap, 256), 256, 0, st>>>(s);
+    graph_bbox_kernel<<<128, 256, 0, st>>>(s);
     AFX_LAUNCH_CHECK();
     graph_check_radii_kernel<<<blocks_for(cap, 256), 256, 0, st>>>(s);
     AFX_LAUNCH_CHECK();
