@@ -223,6 +223,20 @@ int afx_correspondences(int* corr, unsigned* corr_count, long capacity, const fl
                         void* stream);
 size_t afx_correspondences_workspace_size(long n_points_max);
 
+/* afx_correspondences without a workspace and without allocating: for callers that must
+ * not allocate device memory during the frame (real-time loops on a preallocated memory
+ * budget, code running under an allocator lock or inside a host callback).  This entry
+ * point has no counterpart in the reference.  Scratch is a fixed device array of the
+ * library sized for AFX_CORR_STATIC_MAX_POINTS vertices (about 3 MiB); n_points_max above
+ * that returns AFX_ERR_CAPACITY before any work.  The first call on each device looks up
+ * the array's address (make that first call before any stream capture).  All calls on a
+ * device share the one array: calls that overlap in time (other streams, other host
+ * threads) race and must be ordered by the caller.  Results equal afx_correspondences. */
+#define AFX_CORR_STATIC_MAX_POINTS 262144L
+int afx_correspondences_static(int* corr, unsigned* corr_count, long capacity, const float* warped,
+                               const unsigned* count, long n_points_max, const float K[9], const float* depth,
+                               int rows, int cols, const float* frame_vertices, float thresh, void* stream);
+
 /* ------------------------------------------------------------------------------------
  * Whole-frame session: af::runVolumeFusion's per-frame loop (src/VolumeFusion.cu:223-769)
  * with all state (TSDF, motion graph, solver) resident on the device.

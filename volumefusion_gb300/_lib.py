@@ -70,6 +70,7 @@ SIGNATURES = {
     "afx_warp": (i32, [vp, vp, vp, vp, vp, vp, i64, i32, vp]),
     "afx_correspondences": (i32, [vp, vp, i64, vp, vp, i64, vp, vp, i32, i32, vp, f32, vp, sz, vp]),
     "afx_correspondences_workspace_size": (sz, [i64]),
+    "afx_correspondences_static": (i32, [vp, vp, i64, vp, vp, i64, vp, vp, i32, i32, vp, f32, vp]),
     "afx_fusion_default_params": (None, [C.POINTER(FusionParams)]),
     "afx_fusion_create": (i32, [C.POINTER(FusionParams), C.POINTER(vp)]),
     "afx_fusion_destroy": (i32, [vp]),

@@ -5,6 +5,7 @@
 // copying the point cloud down and the results up every frame (src/VolumeFusion.cu:392-419).
 #include <cfloat>
 #include <cstring>
+#include <mutex>
 
 #include "afx_internal.h"
 
@@ -728,3 +729,56 @@ int afx_correspondences(int* corr, unsigned* corr_count, long capacity, const fl
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------
+// Correspondence search without any allocation: the same three steps as
+// afx_correspondences (flag kernel, exclusive scan, scatter kernel), with the scratch in a
+// fixed file-scope device array instead of a caller-provided workspace.  Every scratch word
+// is written before it is read within one call (flags and pixels for every live vertex,
+// scan block sums, scan output), so nothing has to start at zero and nothing is cleared.
+// The array is shared by all calls on a device: calls that overlap in time race on it.
+// ------------------------------------------------------------------------------------
+
+namespace afx {
+
+constexpr long kCorrStaticMaxPoints = AFX_CORR_STATIC_MAX_POINTS;
+// flags, pixels, scan output (4 bytes each per vertex) + scan block sums + alignment slack
+constexpr size_t kCorrStaticBytes = 3 * (size_t)kCorrStaticMaxPoints * 4 + 64 * 1024;
+
+static __device__ __align__(256) unsigned char g_corr_static_scratch[kCorrStaticBytes];
+
+constexpr int kCorrStaticMaxDevices = 64;
+static std::mutex g_corr_static_mu;
+static void* g_corr_static_ptr[kCorrStaticMaxDevices];
+
+// Device address of the scratch array on the current device, looked up once per device.
+static int corr_static_scratch(void** out) {
+    int dev = 0;
+    AFX_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kCorrStaticMaxDevices) return AFX_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lock(g_corr_static_mu);
+    if (!g_corr_static_ptr[dev]) {
+        void* p = nullptr;
+        AFX_CUDA(cudaGetSymbolAddress(&p, g_corr_static_scratch));
+        g_corr_static_ptr[dev] = p;
+    }
+    *out = g_corr_static_ptr[dev];
+    return AFX_OK;
+}
+
+}  // namespace afx
+
+extern "C" int afx_correspondences_static(int* corr, unsigned* corr_count, long capacity, const float* warped,
+                                          const unsigned* count, long n_points_max, const float K[9],
+                                          const float* depth, int rows, int cols, const float* frame_vertices,
+                                          float thresh, void* stream) {
+    if (!corr || !corr_count || !warped || !K || !depth || !frame_vertices || rows <= 0 || cols <= 0)
+        return AFX_ERR_INVALID_ARGUMENT;
+    if (n_points_max > kCorrStaticMaxPoints) return AFX_ERR_CAPACITY;
+    if (corr_ws(n_points_max) > kCorrStaticBytes) return AFX_ERR_CAPACITY;
+    void* scratch = nullptr;
+    int rc = corr_static_scratch(&scratch);
+    if (rc) return rc;
+    return correspondences_impl(corr, corr_count, capacity, warped, count, n_points_max, K, depth, rows, cols,
+                                frame_vertices, thresh, nullptr, scratch, kCorrStaticBytes, as_stream(stream));
+}
