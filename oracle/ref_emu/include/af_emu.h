@@ -87,3 +87,9 @@ void launch(dim3 grid, dim3 block, size_t smem, const std::function<void()>& bod
 void launch_sync(dim3 grid, dim3 block, size_t smem, const std::function<void()>& body);
 void* dynamic_smem();
 }  // namespace af_emu
+
+// the reference's device code calls these unqualified, as CUDA's headers allow
+using std::abs;
+using std::isinf;
+using std::isnan;
+using std::pow;
