@@ -1,13 +1,16 @@
 """Benchmark: non-rigid fusion frames/s on the 256^3 articulated-capsule sequence.
 
-A step is one non-rigid frame of the 30-frame 640x576 capsule-pair sequence (256^3 FP32
+A step fuses the 30-frame 640x576 capsule-pair sequence from an empty volume (256^3 FP32
 TSDF at 4 mm, 25 mm motion graph, K=4, 8-NN regularisation, 1 ICP x 5 Gauss-Newton x 10
-PCG), played forward and back so that any number of steps sees continuous motion.
+PCG): afx_fusion_reset, then frames 0..29 (frame 0 rigid, 29 non-rigid).  Every step is the
+same work.  L2 is flushed (a 256 MiB write) between steps.
 
   value : frames/s with the depth frames already resident in HBM (afx_fusion_process)
   e2e   : frames/s through the C ABI with host depth buffers (afx_fusion_process_host from
           pinned memory + a device-to-host read of the frame statistics every frame)
   p50/p99 frame latency from the e2e loop.
+  dense_graph : the same sequence with the graph radius lowered to 7 mm (about 1500 nodes),
+          device-resident, for the solver at the stated graph size.
 
 --impl reference times the reference's CPU path (the oracle port of it: this box has no
 build of the reference) with all host threads.  Under torchrun each rank runs an
@@ -30,18 +33,13 @@ sys.path.insert(0, ROOT)
 N_FRAMES = 30
 
 
-def seq_index(f):
-    """Forward-backward play of the 30-frame sequence: 0..29, 28..1, 0..29, ..."""
-    period = 2 * (N_FRAMES - 1)
-    r = f % period
-    return r if r < N_FRAMES else period - r
-
-
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--clip", type=int, default=N_FRAMES, help="frames of the sequence per step")
+    ap.add_argument("--no-dense-graph", action="store_true")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frames", type=int, default=3)
@@ -108,19 +106,23 @@ def dist_setup(n):
 def cpu_baseline(cfg, frames_np, n_frames):
     """Oracle port of the reference path on the host cores (all threads)."""
     from oracle import pyoracle as O
-    ocfg = dict(cfg)
-    ocfg["solver"] = 1
-    o = O.Fusion(ocfg)
+    o = O.Fusion(dict(cfg))
     o.process(frames_np[0])
     t0 = time.perf_counter()
-    for f in range(1, n_frames + 1):
-        o.process(frames_np[seq_index(f)])
+    for f in range(1, min(n_frames, N_FRAMES - 1) + 1):
+        o.process(frames_np[f])
     dt = time.perf_counter() - t0
     o.close()
     return n_frames / dt, dt
 
 
+REF_FRAMES_PER_STEP = 4
+
+
 def run_reference(args):
+    """The reference's CPU path (its oracle port; see DESIGN) on the host cores.  A step is a
+    bounded sample of the workload: the first REF_FRAMES_PER_STEP frames of the sequence from
+    an empty volume (frame 0 rigid, then non-rigid frames)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -128,27 +130,48 @@ def run_reference(args):
     cfg = configs.nonrigid_capsules_256(n_frames=N_FRAMES)
     frames_np = configs.capsule_frames(cfg)
     from oracle import pyoracle as O
-    o = O.Fusion(dict(cfg))
-    o.process(frames_np[0])
-    for f in range(1, 1 + args.warmup):
-        o.process(frames_np[seq_index(f)])
-    t0 = time.perf_counter()
-    for f in range(1 + args.warmup, 1 + args.warmup + args.steps):
-        o.process(frames_np[seq_index(f)])
-    dt = time.perf_counter() - t0
-    fps = args.steps / dt
+
+    def step():
+        o = O.Fusion(dict(cfg))
+        t0 = time.perf_counter()
+        for f in range(REF_FRAMES_PER_STEP):
+            o.process(frames_np[f])
+        dt = time.perf_counter() - t0
+        o.close()
+        return dt
+
+    for _ in range(args.warmup):
+        step()
+    dt = sum(step() for _ in range(args.steps))
+    n = args.steps * REF_FRAMES_PER_STEP
+    fps = n / dt
     cores = os.cpu_count()
     line = {
         "impl": "reference", "metric": "nonrigid_frames_per_s_256", "value": fps, "unit": "frames/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": cfg["name"], "frames": "640x576 capsule pair, 30-frame sequence played back and forth",
-                   "volume": "256^3 FP32 @ 4 mm", "parallelism": "replicas"},
+        "config": {"workload": cfg["name"], "frames": "640x576 capsule pair, 30-frame sequence",
+                   "volume": "256^3 FP32 TSDF @ 4 mm", "graph_radius_mm": 25, "knn": 4, "kreg": 8,
+                   "gn": "1 ICP x 5 GN x 10 PCG", "parallelism": "single"},
         "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
-                         "sample": "%d frames of the workload after %d warm-up frames" % (args.steps, args.warmup)},
+                         "sample": "%d steps of the first %d frames of the sequence from an empty volume, after %d "
+                                   "warm-up steps, all host threads (OpenMP)" % (args.steps, REF_FRAMES_PER_STEP,
+                                                                                 args.warmup)},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def stage_bytes(cfg, st):
+    """Algorithmic bytes per frame of the stages with an exact HBM figure."""
+    S = int(np.prod(cfg["dims"]))
+    P = cfg["width"] * cfg["height"]
+    A = st.get("active_voxels", 0)
+    return {
+        "prep": P * (2.0 + 4.0 + 24.0),
+        "marching_cubes": 8.0 * S + 12.0 * st["mesh_points"] * 4 + 48.0 * st["mesh_faces"],
+        "warped_integrate": 16.0 * A if A else None,
+    }
 
 
 def main():
@@ -157,6 +180,7 @@ def main():
         return run_reference(args)
     import torch
     from volumefusion_gb300 import configs
+    from volumefusion_gb300._lib import FrameStats
     from volumefusion_gb300.fusion import FusionSession
 
     dist = dist_setup(args.gpus)
@@ -169,100 +193,130 @@ def main():
     frames_dev = [torch.from_numpy(f.astype(np.int16)).cuda() for f in frames_np]
     pinned = [torch.from_numpy(f.astype(np.int16)).pin_memory() for f in frames_np]
     stream = torch.cuda.Stream()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    clip = max(1, min(args.clip, N_FRAMES))
 
     def barrier():
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
 
+    def reduce_max(x):
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        if dist:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def run_device(session, steps):
+        """`steps` passes over the sequence, each from an empty volume."""
+        with torch.cuda.stream(stream):
+            for step in range(steps):
+                if step:
+                    flush.fill_(step & 0xFF)  # L2 flush between steps
+                session.reset()
+                for f in range(clip):
+                    session.process(frames_dev[f])
+
     # ---- device-resident arm ----
     s = FusionSession(cfg, stream=stream)
-    with torch.cuda.stream(stream):
-        s.process(frames_dev[0])
-        for f in range(1, 1 + args.warmup):
-            s.process(frames_dev[seq_index(f)])
+    run_device(s, args.warmup)
     s.stats()
     barrier()
     sampler = ClockSampler(local)
     sampler.start()
     l0 = s.kernel_launches()
-    s.set_timing(True)
-    s.stage_times(reset=True)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    with torch.cuda.stream(stream):
-        for f in range(1 + args.warmup, 1 + args.warmup + args.steps):
-            s.process(frames_dev[seq_index(f)])
+    run_device(s, args.steps)
     ev1.record(stream)
     barrier()
     sampler.stop()
     launches = s.kernel_launches() - l0
-    ms = ev0.elapsed_time(ev1)
+    ms = reduce_max(ev0.elapsed_time(ev1))
+    frames = args.steps * clip
+    fps = world * frames / (ms / 1000.0)
+    # per-stage breakdown: the same number of steps again, with CUDA events around each stage
+    s.set_timing(True)
+    s.stage_times(reset=True)
+    run_device(s, args.steps)
+    barrier()
     stage_ms = s.stage_times(reset=True)
     s.set_timing(False)
     st = s.stats(check_errors=False)
-    tmax = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-    ms = float(tmax.item())
-    fps = world * args.steps / (ms / 1000.0)
     s.close()
 
     # ---- end-to-end arm: host buffers through the C ABI, per-frame latency ----
     s2 = FusionSession(cfg, stream=stream)
-    s2.process_host_ptr(pinned[0].data_ptr())
-    s2.stats()
-    for f in range(1, 1 + args.warmup):
-        s2.process_host_ptr(pinned[seq_index(f)].data_ptr())
-        s2.stats()
+
+    def run_e2e(steps, lat=None):
+        for _ in range(steps):
+            s2.reset()
+            for f in range(clip):
+                a = time.perf_counter()
+                s2.process_host_ptr(pinned[f].data_ptr())
+                s2.stats(check_errors=False)  # device-to-host read of the frame result
+                if lat is not None:
+                    lat.append(time.perf_counter() - a)
+
+    run_e2e(args.warmup)
     barrier()
     lat = []
     t0 = time.perf_counter()
-    for f in range(1 + args.warmup, 1 + args.warmup + args.steps):
-        a = time.perf_counter()
-        s2.process_host_ptr(pinned[seq_index(f)].data_ptr())
-        s2.stats(check_errors=False)  # device-to-host read of the frame result
-        lat.append(time.perf_counter() - a)
+    run_e2e(args.steps, lat)
     barrier()
-    e2e_s = time.perf_counter() - t0
-    te = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-    if dist:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_fps = world * args.steps / float(te.item())
+    e2e_fps = world * frames / reduce_max(time.perf_counter() - t0)
     s2.close()
 
+    # ---- the same sequence with a ~1500-node graph (device-resident) ----
+    dense = None
+    if not args.no_dense_graph:
+        dcfg = dict(cfg)
+        dcfg["graph_radius"] = 0.007
+        sd = FusionSession(dcfg, stream=stream)
+        run_device(sd, 1)
+        barrier()
+        dsteps = max(1, args.steps // 2)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        run_device(sd, dsteps)
+        e1.record(stream)
+        barrier()
+        dms = reduce_max(e0.elapsed_time(e1))
+        sd.set_timing(True)
+        sd.stage_times(reset=True)
+        run_device(sd, 1)
+        barrier()
+        dstage = {k: v / clip for k, v in sd.stage_times(reset=True).items()}
+        sd.set_timing(False)
+        dst = sd.stats(check_errors=False)
+        sd.close()
+        dense = {"graph_radius_mm": 7, "value": world * dsteps * clip / (dms / 1000.0), "unit": "frames/s",
+                 "n_nodes_last_frame": dst["n_nodes"], "correspondences_last_frame": dst["correspondences"],
+                 "stage_ms_per_frame": dstage}
+
     # ---- roofline of the dominant stage ----
-    S = int(np.prod(cfg["dims"]))
-    dom = max(stage_ms, key=stage_ms.get)
-    per_frame = {k: v / args.steps for k, v in stage_ms.items()}
+    per_frame = {k: v / frames for k, v in stage_ms.items()}
+    dom = max(per_frame, key=per_frame.get)
     peaks = {}
     pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):
         peaks = json.load(open(pk_path))
     hbm = peaks.get("hbm_gbs", 6800.0)
-    # algorithmic bytes per launch of the stages we can state exactly
-    tri = st["mesh_faces"]
-    algo = {
-        "marching_cubes": 8.0 * S + 12.0 * st["mesh_points"] * 4 + 48.0 * tri,
-    }
-    roof = None
-    if dom in algo:
-        achieved = algo[dom] / (per_frame[dom] / 1000.0) / 1e9
-        roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": achieved / hbm, "traffic": None, "peak_source": "measured" if peaks else "fallback"}
-    else:
-        mc = per_frame.get("marching_cubes", 0)
-        if mc > 0:
-            achieved = algo["marching_cubes"] / (mc / 1000.0) / 1e9
-            roof = {"bound": "hbm", "kernel": "marching_cubes", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                    "frac": achieved / hbm, "traffic": None, "peak_source": "measured" if peaks else "fallback",
-                    "note": "dominant stage is %s (%.3f ms/frame), latency-bound" % (dom, per_frame[dom])}
+    algo = {k: v for k, v in stage_bytes(cfg, st).items() if v}
+    pick = dom if dom in algo else max(algo, key=lambda k: per_frame.get(k, 0.0))
+    achieved = algo[pick] / (per_frame[pick] / 1000.0) / 1e9
+    roof = {"bound": "hbm", "kernel": pick, "achieved": achieved, "peak": hbm, "unit": "GB/s",
+            "frac": achieved / hbm, "traffic": None,
+            "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"}
+    if pick != dom:
+        roof["note"] = "dominant stage is %s (%.3f ms/frame), latency-bound" % (dom, per_frame[dom])
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and args.cpu_frames > 0:
         v, dt = cpu_baseline(cfg, frames_np, args.cpu_frames)
         cpu = {"value": v, "unit": "frames/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "%d non-rigid frames of the workload (%.1f s) on all host threads" % (args.cpu_frames, dt)}
+               "sample": "frames 1..%d of the sequence after the rigid frame 0 (%.1f s), all host threads"
+                         % (args.cpu_frames, dt)}
 
     if rank == 0:
         line = {
@@ -270,18 +324,21 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": cfg["name"],
-                       "frames": "640x576 capsule pair, 30-frame sequence played back and forth",
+                       "frames": "640x576 capsule pair, 30-frame sequence",
+                       "step": "reset + frames 0..%d (frame 0 rigid)" % (clip - 1),
                        "volume": "256^3 FP32 TSDF @ 4 mm (134 MB tsdf+weights, larger than L2)",
                        "graph_radius_mm": 25, "knn": 4, "kreg": 8, "gn": "1 ICP x 5 GN x 10 PCG",
-                       "parallelism": "replicas" if world > 1 else "single", "l2": "working set larger than L2"},
-            "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": int(frames_np[0].nbytes),
-                    "d2h_bytes_per_step": int(C.sizeof(__import__("volumefusion_gb300._lib", fromlist=["x"]).FrameStats)),
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "flushed between steps (256 MiB write)"},
+            "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": int(frames_np[0].nbytes) * clip,
+                    "d2h_bytes_per_step": int(C.sizeof(FrameStats)) * clip,
                     "latency_ms_p50": 1000 * float(np.percentile(lat, 50)),
                     "latency_ms_p99": 1000 * float(np.percentile(lat, 99))},
             "gpu_launches": int(launches),
             "stage_ms_per_frame": per_frame,
-            "frame_stats": {k: st[k] for k in ("n_nodes", "mesh_points", "correspondences", "gn_iterations_done",
+            "last_frame_stats": {k: st[k] for k in ("n_nodes", "mesh_points", "correspondences", "gn_iterations_done",
                                                 "mesh_faces", "error")},
+            "dense_graph": dense,
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": sampler.summary(),

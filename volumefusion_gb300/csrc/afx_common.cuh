@@ -49,6 +49,19 @@ inline unsigned blocks_for(long n, int threads) {
     return (unsigned)(b < 1 ? 1 : b);
 }
 
+// Grid for a grid-stride kernel over at most n items whose live count is read on the device:
+// enough blocks to cover n, capped at kStrideBlocks so that a large capacity with few live
+// items costs a few waves of immediately-exiting blocks, not one block per 256 slots.
+constexpr long kStrideBlocks = 1216;  // 8 blocks per SM on 152 SMs
+inline unsigned grid_for(long n, int threads) {
+    long b = (n + threads - 1) / threads;
+    return (unsigned)(b < 1 ? 1 : (b > kStrideBlocks ? kStrideBlocks : b));
+}
+
+// for (i in [start, n)) over the whole grid
+#define AFX_GRID_STRIDE(i, n) \
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < (n); i += (long)gridDim.x * blockDim.x)
+
 // ---- Eigen-order small vector arithmetic ----
 AFX_HD float dot3(const float* a, const float* b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
 AFX_HD float sqnorm3(const float* a) { return a[0] * a[0] + (a[1] * a[1] + a[2] * a[2]); }

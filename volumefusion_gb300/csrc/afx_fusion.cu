@@ -401,7 +401,6 @@ int afx_fusion_reset(afx_fusion* f, void* stream) {
     AFX_CUDA(cudaMemsetAsync(f->nmverts, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->nmfaces, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->stats, 0, sizeof(FrameStats), st));
-    gn_init_barrier(f->gn, st);
     f->frame = 0;
     return AFX_OK;
 }
@@ -529,12 +528,8 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
         rc = gn_icp_setup(g, f->Tp, f->T, st);
         if (rc) return rc;
         stage_mark(f, ST_GN_LOOP, st);
-        for (int it = 0; it < p.gn_iterations; ++it) {
-            rc = gn_iteration(g, it, f->warped, f->T, f->Tp, p.pcg_iterations, tol, st);
-            if (rc) return rc;
-            rc = warp_impl(f->warped, f->points, f->Tp, f->midx, f->mw, f->npoints, M, p.knn, st);
-            if (rc) return rc;
-        }
+        rc = gn_loop(g, f->points, f->warped, f->T, f->Tp, p.gn_iterations, p.pcg_iterations, tol, st);
+        if (rc) return rc;
     }
     // voxel support, warp, collisions and warped integration (src/VolumeFusion.cu:702-741)
     stage_mark(f, ST_SUPPORT, st);

@@ -41,61 +41,51 @@ AFX_D void jdepth(const float* n, float w, const float G[3][6], float lam, float
 // ---- per-frame node lists ----
 
 __global__ void lst_count_kernel(GnArgs a) {
-    long m = min((long)*a.mesh_count, a.m_max);
-    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= m * a.k) return;
-    if (a.mw[t] == 0.f) return;
-    uint32_t node = a.midx[t];
-    if (node >= (uint32_t)*a.n_nodes) return;
-    atomicAdd(a.b.lcnt + node, 1u);
+    const long m = min((long)*a.mesh_count, a.m_max);
+    const uint32_t n = (uint32_t)*a.n_nodes;
+    AFX_GRID_STRIDE(t, m * a.k) {
+        if (a.mw[t] == 0.f) continue;
+        const uint32_t node = a.midx[t];
+        if (node < n) atomicAdd(a.b.lcnt + node, 1u);
+    }
 }
 
 __global__ void lst_fill_kernel(GnArgs a) {
-    long m = min((long)*a.mesh_count, a.m_max);
-    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= m * a.k) return;
-    if (a.mw[t] == 0.f) return;
-    uint32_t node = a.midx[t];
-    if (node >= (uint32_t)*a.n_nodes) return;
-    unsigned p = a.b.loff[node] + atomicAdd(a.b.lcur + node, 1u);
-    a.b.lst[p] = (unsigned)t;
+    const long m = min((long)*a.mesh_count, a.m_max);
+    const uint32_t n = (uint32_t)*a.n_nodes;
+    AFX_GRID_STRIDE(t, m * a.k) {
+        if (a.mw[t] == 0.f) continue;
+        const uint32_t node = a.midx[t];
+        if (node >= n) continue;
+        const unsigned p = a.b.loff[node] + atomicAdd(a.b.lcur + node, 1u);
+        a.b.lst[p] = (unsigned)t;
+    }
 }
 
 __global__ void in_count_kernel(GnArgs a) {
-    int n = min(*a.n_nodes, a.n_max);
-    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= (long)n * a.kreg) return;
-    uint32_t nb = a.gidx[t];
-    if (nb >= (uint32_t)n) return;
-    atomicAdd(a.b.icnt + nb, 1u);
+    const int n = min(*a.n_nodes, a.n_max);
+    AFX_GRID_STRIDE(t, (long)n * a.kreg) {
+        const uint32_t nb = a.gidx[t];
+        if (nb < (uint32_t)n) atomicAdd(a.b.icnt + nb, 1u);
+    }
 }
 
 __global__ void in_fill_kernel(GnArgs a) {
-    int n = min(*a.n_nodes, a.n_max);
-    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= (long)n * a.kreg) return;
-    uint32_t nb = a.gidx[t];
-    if (nb >= (uint32_t)n) return;
-    unsigned p = a.b.ioff[nb] + atomicAdd(a.b.icur + nb, 1u);
-    a.b.ilst[p] = (unsigned)t;
+    const int n = min(*a.n_nodes, a.n_max);
+    AFX_GRID_STRIDE(t, (long)n * a.kreg) {
+        const uint32_t nb = a.gidx[t];
+        if (nb >= (uint32_t)n) continue;
+        const unsigned p = a.b.ioff[nb] + atomicAdd(a.b.icur + nb, 1u);
+        a.b.ilst[p] = (unsigned)t;
+    }
 }
 
-// Sort each node's list ascending (bitonic in shared memory); one CTA per node.
-__global__ void __launch_bounds__(256) seg_sort_kernel(unsigned* lst, const unsigned* off, const int* n_nodes, int n_max,
-                                                       int* error) {
-    __shared__ unsigned s[kSegMax];
-    const int a = blockIdx.x;
-    if (a >= min(*n_nodes, n_max)) return;
-    const unsigned o = off[a];
-    const int len = (int)(off[a + 1] - o);
-    if (len <= 1) return;
-    if (len > kSegMax) {
-        if (threadIdx.x == 0) atomicOr(error, ERRF_CAPACITY);
-        return;
-    }
+// Bitonic sort of one list (len <= kSegMax) through shared memory, by the whole CTA.
+AFX_D void seg_sort_one(unsigned* lst, int len, unsigned* s) {
     int P = 1;
     while (P < len) P <<= 1;
-    for (int i = threadIdx.x; i < P; i += blockDim.x) s[i] = i < len ? lst[o + i] : 0xffffffffu;
+    __syncthreads();  // the previous list's write-back is done with s
+    for (int i = threadIdx.x; i < P; i += blockDim.x) s[i] = i < len ? lst[i] : 0xffffffffu;
     __syncthreads();
     for (int size = 2; size <= P; size <<= 1)
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
@@ -110,8 +100,25 @@ __global__ void __launch_bounds__(256) seg_sort_kernel(unsigned* lst, const unsi
             }
             __syncthreads();
         }
-    for (int i = threadIdx.x; i < len; i += blockDim.x) lst[o + i] = s[i];
+    for (int i = threadIdx.x; i < len; i += blockDim.x) lst[i] = s[i];
 }
+
+// Sort each node's list ascending (bitonic in shared memory); one CTA per node at a time.
+__global__ void __launch_bounds__(256) seg_sort_kernel(unsigned* lst, const unsigned* off, const int* n_nodes, int n_max,
+                                                       int* error) {
+    __shared__ unsigned s[kSegMax];
+    const int n = min(*n_nodes, n_max);
+    for (int a = blockIdx.x; a < n; a += gridDim.x) {
+        const unsigned o = off[a];
+        const int len = (int)(off[a + 1] - o);
+        if (len > kSegMax) {
+            if (threadIdx.x == 0) atomicOr(error, ERRF_CAPACITY);
+            continue;
+        }
+        if (len > 1) seg_sort_one(lst + o, len, s);
+    }
+}
+
 
 // ---- per-ICP assembly ----
 
@@ -179,33 +186,52 @@ __global__ void __launch_bounds__(32 * kGnWarps) nbr_discover_kernel(GnArgs a, i
 // For neighbour slots below the diagonal, find the owner's slot (binary search).
 __global__ void nbr_ref_kernel(GnArgs a) {
     const int n = min(*a.n_nodes, a.n_max);
-    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= (long)n * kMaxNbr) return;
-    int node = (int)(t / kMaxNbr), u = (int)(t % kMaxNbr);
-    if (u >= a.b.nbr_cnt[node]) return;
-    int bnode = a.b.nbr[t];
-    if (bnode > node) {
-        a.b.nbr_ref[t] = (int)t;
-        return;
-    }
-    const int* L = a.b.nbr + (long)bnode * kMaxNbr;
-    int lo = 0, hi = a.b.nbr_cnt[bnode] - 1, f = -1;
-    while (lo <= hi) {
-        int mid = (lo + hi) >> 1;
-        if (L[mid] == node) {
-            f = mid;
-            break;
+    AFX_GRID_STRIDE(t, (long)n * kMaxNbr) {
+        const int node = (int)(t / kMaxNbr), u = (int)(t % kMaxNbr);
+        if (u >= a.b.nbr_cnt[node]) continue;
+        const int bnode = a.b.nbr[t];
+        if (bnode > node) {
+            a.b.nbr_ref[t] = (int)t;
+            continue;
         }
-        if (L[mid] < node) lo = mid + 1;
-        else hi = mid - 1;
+        const int* L = a.b.nbr + (long)bnode * kMaxNbr;
+        int lo = 0, hi = a.b.nbr_cnt[bnode] - 1, f = -1;
+        while (lo <= hi) {
+            const int mid = (lo + hi) >> 1;
+            if (L[mid] == node) {
+                f = mid;
+                break;
+            }
+            if (L[mid] < node) lo = mid + 1;
+            else hi = mid - 1;
+        }
+        if (f < 0) {
+            atomicOr(a.error, ERRF_CAPACITY);
+            a.b.nbr_ref[t] = 0;
+            continue;
+        }
+        a.b.nbr_ref[t] = -((int)((long)bnode * kMaxNbr + f) + 1);
     }
-    if (f < 0) {
-        atomicOr(a.error, ERRF_CAPACITY);
-        a.b.nbr_ref[t] = 0;
-        return;
-    }
-    a.b.nbr_ref[t] = -((int)((long)bnode * kMaxNbr + f) + 1);
 }
+
+// J^T J: node a's warp accumulates D_a and its upper blocks (a, b > a).  Lane l owns block
+// entries l and l + 32 of every block; each entry is summed in a fixed sequential order:
+// depth rows by ascending node-list entry, then regularisation rows by ascending row.  The
+// per-row inputs (normals, points, weights, target slots) are staged 32 rows at a time by the
+// whole warp, the upper blocks accumulate in shared memory, so the ordered loop touches no
+// global memory.
+constexpr int kJtjWarps = 2;
+constexpr int kJtjMaxK = 8;
+
+struct JtjStage {
+    float blk[kMaxNbr * 36];   // upper blocks of this node
+    int L[kMaxNbr];            // sorted neighbour ids
+    float nrm[32][3];          // depth rows: frame normal
+    float pt[32][3];           //             canonical vertex (or node position for a reg row)
+    float w[32][kJtjMaxK];     //             skinning weights
+    signed char slot[32][kJtjMaxK];  // -1: diagonal, >= 0: upper block, -2: no contribution
+    int own[32];               // depth rows: the row's own slot s, or -1 without correspondence
+};
 
 AFX_D int find_slot(const int* L, int cnt, int b) {
     int lo = 0, hi = cnt - 1;
@@ -218,518 +244,939 @@ AFX_D int find_slot(const int* L, int cnt, int b) {
     return -1;
 }
 
-// J^T J: node a's warp accumulates D_a and its upper blocks (a, b > a).  Lane l owns block
-// entries l and l + 32 of every block; each entry is summed in a fixed sequential order.
-__global__ void __launch_bounds__(32 * kGnWarps) jtj_assemble_kernel(GnArgs a) {
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int node = blockIdx.x * kGnWarps + w;
-    const int n = min(*a.n_nodes, a.n_max);
-    if (node >= n) return;
-    const int* L = a.b.nbr + (long)node * kMaxNbr;
-    const int cnt = a.b.nbr_cnt[node];
-    float* D = a.b.diag + (long)node * 36;
-    float* B = a.b.blocks + (long)node * kMaxNbr * 36;
-    const int e0 = lane, e1 = lane + 32;  // entries this lane owns (e1 valid for lanes 0..3)
-    const int i0 = e0 / 6, j0 = e0 % 6, i1 = e1 / 6, j1 = e1 % 6;
-    // zero this node's accumulators
-    float d0 = 0.f, d1 = 0.f;
-    for (int u = 0; u < cnt; ++u) {
-        if (L[u] <= node) continue;
-        B[u * 36 + e0] = 0.f;
-        if (e1 < 36) B[u * 36 + e1] = 0.f;
+// Column q of grad_rows(p): (G[0][q], G[1][q], G[2][q]).
+AFX_D void gcol(const float* p, int q, float c[3]) {
+    switch (q) {
+        case 0: c[0] = 0.f; c[1] = -p[2]; c[2] = p[1]; break;
+        case 1: c[0] = p[2]; c[1] = 0.f; c[2] = -p[0]; break;
+        case 2: c[0] = -p[1]; c[1] = p[0]; c[2] = 0.f; break;
+        case 3: c[0] = 1.f; c[1] = 0.f; c[2] = 0.f; break;
+        case 4: c[0] = 0.f; c[1] = 1.f; c[2] = 0.f; break;
+        default: c[0] = 0.f; c[1] = 0.f; c[2] = 1.f; break;
     }
-    bool touched = false;
-    const unsigned o = a.b.loff[node], e = a.b.loff[node + 1];
-    for (unsigned t = o; t < e; ++t) {
-        unsigned ent = a.b.lst[t];
-        long v = ent / a.k;
-        int s = (int)(ent % a.k);
-        int c = a.corr_of_vertex[v];
-        if (lane == 0) a.b.jc[t] = c;
-        if (c < 0) continue;
-        touched = true;
-        int px = a.corr[2 * (long)c + 1];
-        const float* nrm = a.normals + 3 * (long)px;
-        float G[3][6];
-        grad_rows(a.mesh + 3 * v, G);
-        float Ja[6];
-        jdepth(nrm, a.mw[v * a.k + s], G, a.lam_d, Ja);
-        if (lane == 0)
-            for (int q = 0; q < 6; ++q) a.b.jrow[(long)t * 6 + q] = Ja[q];
-        for (int tt = 0; tt < a.k; ++tt) {
-            float wt = a.mw[v * a.k + tt];
-            if (wt == 0.f) continue;
-            uint32_t bnode = a.midx[v * a.k + tt];
-            if (bnode < (uint32_t)node) continue;
-            float Jb[6];
-            jdepth(nrm, wt, G, a.lam_d, Jb);
-            if (bnode == (uint32_t)node) {
-                d0 = d0 + Ja[i0] * Jb[j0];
-                if (e1 < 36) d1 = d1 + Ja[i1] * Jb[j1];
-            } else {
-                int u = find_slot(L, cnt, (int)bnode);
-                if (u < 0) continue;
-                float* blk = B + u * 36;
-                blk[e0] = blk[e0] + Ja[i0] * Jb[j0];
-                if (e1 < 36) blk[e1] = blk[e1] + Ja[i1] * Jb[j1];
-            }
-        }
-    }
-    // regularisation rows in ascending row order: incoming edges x -> node with x < node,
-    // then node's own edges, then incoming edges with x > node (src/MotionOptimization.cu:298-340)
-    const unsigned io = a.b.ioff[node], ie = a.b.ioff[node + 1];
-    unsigned it = io;
-    auto reg_row = [&](int src, int kk) {
-        uint32_t nb = a.gidx[(long)src * a.kreg + kk];
-        float G[3][6];
-        grad_rows(a.nodes + 3 * (long)src, G);
-        for (int ax = 0; ax < 3; ++ax) {
-            float g[6], gn[6];
-#pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                g[q] = G[ax][q] * a.lam_r;
-                gn[q] = -g[q];
-            }
-            // this node is `src` (coefficient +g) or `nb` (coefficient -g)
-            const float* Jn = (src == node) ? g : gn;
-            d0 = d0 + Jn[i0] * Jn[j0];
-            if (e1 < 36) d1 = d1 + Jn[i1] * Jn[j1];
-            int other = (src == node) ? (int)nb : src;
-            if (other > node) {
-                const float* Jo = (src == node) ? gn : g;
-                int u = find_slot(L, cnt, other);
-                if (u >= 0) {
-                    float* blk = B + u * 36;
-                    blk[e0] = blk[e0] + Jn[i0] * Jo[j0];
-                    if (e1 < 36) blk[e1] = blk[e1] + Jn[i1] * Jo[j1];
-                }
-            }
-        }
-        touched = true;
-    };
-    while (it < ie && a.b.ilst[it] / a.kreg < (unsigned)node) {
-        unsigned ent = a.b.ilst[it++];
-        reg_row((int)(ent / a.kreg), (int)(ent % a.kreg));
-    }
-    for (int kk = 0; kk < a.kreg; ++kk) {
-        uint32_t nb = a.gidx[(long)node * a.kreg + kk];
-        if (nb >= (uint32_t)n) continue;
-        reg_row(node, kk);
-    }
-    while (it < ie) {
-        unsigned ent = a.b.ilst[it++];
-        reg_row((int)(ent / a.kreg), (int)(ent % a.kreg));
-    }
-    if (!touched) {  // identity diagonal block (src/VolumeFusion.cu:637-640)
-        d0 = (i0 == j0) ? 1.f : 0.f;
-        d1 = (i1 == j1) ? 1.f : 0.f;
-    }
-    D[e0] = d0;
-    if (e1 < 36) D[e1] = d1;
 }
 
-// FP64 inverse of each diagonal block (Gauss-Jordan with partial pivoting).
-__global__ void diag_inverse_kernel(GnArgs a) {
-    int node = blockIdx.x * blockDim.x + threadIdx.x;
-    int n = min(*a.n_nodes, a.n_max);
+// Component q of jdepth(n, w, G, lam), from column q of G (zero below the weight cut-off).
+AFX_D float jdepth_q(const float* n, float w, const float c[3], float lam) {
+    if (w < 1.e-4f) return 0.f;
+    const float nw0 = n[0] * w, nw1 = n[1] * w, nw2 = n[2] * w;
+    return (nw0 * c[0] + (nw1 * c[1] + nw2 * c[2])) * lam;
+}
+
+__global__ void __launch_bounds__(32 * kJtjWarps) jtj_assemble_kernel(GnArgs a) {
+    __shared__ JtjStage stage[kJtjWarps];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    JtjStage& S = stage[w];
+    const int n = min(*a.n_nodes, a.n_max);
+    const int k = a.k;
+    const int e0 = lane, e1 = lane + 32;  // entries this lane owns (e1 valid for lanes 0..3)
+    const int i0 = e0 / 6, j0 = e0 % 6, i1 = e1 / 6, j1 = e1 % 6;
+    const bool has1 = e1 < 36;
+    for (int node = blockIdx.x * kJtjWarps + w; node < n; node += gridDim.x * kJtjWarps) {
+        const int cnt = a.b.nbr_cnt[node];
+        for (int u = lane; u < cnt; u += 32) S.L[u] = a.b.nbr[(long)node * kMaxNbr + u];
+        for (int x = lane; x < cnt * 36; x += 32) S.blk[x] = 0.f;
+        __syncwarp();
+        float d0 = 0.f, d1 = 0.f;
+        bool touched = false;
+        const unsigned o = a.b.loff[node], e = a.b.loff[node + 1];
+        for (unsigned base = o; base < e; base += 32) {
+            // stage up to 32 depth rows, one per lane
+            const unsigned t = base + lane;
+            if (t < e) {
+                const unsigned ent = a.b.lst[t];
+                const long v = ent / k;
+                const int s = (int)(ent % k);
+                const int c = a.corr_of_vertex[v];
+                a.b.jc[t] = c;
+                S.own[lane] = c < 0 ? -1 : s;
+                if (c >= 0) {
+                    const int px = a.corr[2 * (long)c + 1];
+                    float nrm[3], p[3];
+                    for (int q = 0; q < 3; ++q) {
+                        nrm[q] = a.normals[3 * (long)px + q];
+                        p[q] = a.mesh[3 * v + q];
+                        S.nrm[lane][q] = nrm[q];
+                        S.pt[lane][q] = p[q];
+                    }
+                    for (int tt = 0; tt < k; ++tt) {
+                        const float wt = a.mw[v * k + tt];
+                        const uint32_t bnode = a.midx[v * k + tt];
+                        S.w[lane][tt] = wt;
+                        int sl = -2;
+                        if (wt != 0.f && bnode >= (uint32_t)node) {
+                            if (bnode == (uint32_t)node) sl = -1;
+                            else {
+                                const int f = find_slot(S.L, cnt, (int)bnode);
+                                if (f >= 0) sl = f;
+                            }
+                        }
+                        S.slot[lane][tt] = (signed char)sl;
+                    }
+                    // this row's J block for J^T r (jtr_node)
+                    float G[3][6];
+                    grad_rows(p, G);
+                    float Ja[6];
+                    jdepth(nrm, S.w[lane][s], G, a.lam_d, Ja);
+                    for (int q = 0; q < 6; ++q) a.b.jrow[(long)t * 6 + q] = Ja[q];
+                }
+            }
+            __syncwarp();
+            // ordered accumulation over the staged rows
+            const int nb = (int)min(32u, e - base);
+            for (int r = 0; r < nb; ++r) {
+                const int s = S.own[r];
+                if (s < 0) continue;
+                touched = true;
+                float ci0[3], cj0[3], ci1[3], cj1[3];
+                gcol(S.pt[r], i0, ci0);
+                gcol(S.pt[r], j0, cj0);
+                gcol(S.pt[r], i1 < 6 ? i1 : 0, ci1);
+                gcol(S.pt[r], j1, cj1);
+                const float* nrm = S.nrm[r];
+                const float wa = S.w[r][s];
+                const float ja0 = jdepth_q(nrm, wa, ci0, a.lam_d);
+                const float ja1 = has1 ? jdepth_q(nrm, wa, ci1, a.lam_d) : 0.f;
+                for (int tt = 0; tt < k; ++tt) {
+                    const int sl = S.slot[r][tt];
+                    if (sl == -2) continue;
+                    const float wt = S.w[r][tt];
+                    const float jb0 = jdepth_q(nrm, wt, cj0, a.lam_d);
+                    const float jb1 = has1 ? jdepth_q(nrm, wt, cj1, a.lam_d) : 0.f;
+                    if (sl == -1) {
+                        d0 = d0 + ja0 * jb0;
+                        if (has1) d1 = d1 + ja1 * jb1;
+                    } else {
+                        float* blk = S.blk + sl * 36;
+                        blk[e0] = blk[e0] + ja0 * jb0;
+                        if (has1) blk[e1] = blk[e1] + ja1 * jb1;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        // regularisation rows in ascending row order: incoming edges x -> node with x < node,
+        // then node's own edges, then incoming edges with x > node (src/MotionOptimization.cu:298-340)
+        const unsigned io = a.b.ioff[node], nin = a.b.ioff[node + 1] - io;
+        unsigned nlo = 0;  // incoming rows with source below node (ilst is ascending)
+        for (unsigned x = lane; x < nin; x += 32) nlo += (a.b.ilst[io + x] / a.kreg < (unsigned)node) ? 1u : 0u;
+        nlo = warp_sum(nlo);
+        const unsigned nrows = nin + (unsigned)a.kreg;
+        for (unsigned base = 0; base < nrows; base += 32) {
+            const unsigned r = base + lane;
+            if (r < nrows) {
+                int src, kk;
+                if (r < nlo) {
+                    const unsigned ent = a.b.ilst[io + r];
+                    src = (int)(ent / a.kreg);
+                    kk = (int)(ent % a.kreg);
+                } else if (r < nlo + (unsigned)a.kreg) {
+                    src = node;
+                    kk = (int)(r - nlo);
+                } else {
+                    const unsigned ent = a.b.ilst[io + r - a.kreg];
+                    src = (int)(ent / a.kreg);
+                    kk = (int)(ent % a.kreg);
+                }
+                const uint32_t nbk = a.gidx[(long)src * a.kreg + kk];
+                bool live = true;
+                if (src == node && nbk >= (uint32_t)n) live = false;  // own edge filtered out
+                S.own[lane] = live ? (src == node ? 1 : 0) : -1;
+                for (int q = 0; q < 3; ++q) S.pt[lane][q] = a.nodes[3 * (long)src + q];
+                const int other = (src == node) ? (int)nbk : src;
+                int sl = -2;
+                if (other > node) {
+                    const int f = find_slot(S.L, cnt, other);
+                    if (f >= 0) sl = f;
+                }
+                S.slot[lane][0] = (signed char)sl;
+            }
+            __syncwarp();
+            const int nb = (int)min(32u, nrows - base);
+            for (int rr = 0; rr < nb; ++rr) {
+                const int self = S.own[rr];
+                if (self < 0) continue;
+                touched = true;
+                float ci0[3], cj0[3], ci1[3], cj1[3];
+                gcol(S.pt[rr], i0, ci0);
+                gcol(S.pt[rr], j0, cj0);
+                gcol(S.pt[rr], i1 < 6 ? i1 : 0, ci1);
+                gcol(S.pt[rr], j1, cj1);
+                const int sl = S.slot[rr][0];
+#pragma unroll
+                for (int ax = 0; ax < 3; ++ax) {
+                    const float g_i0 = ci0[ax] * a.lam_r, g_j0 = cj0[ax] * a.lam_r;
+                    const float g_i1 = has1 ? ci1[ax] * a.lam_r : 0.f, g_j1 = has1 ? cj1[ax] * a.lam_r : 0.f;
+                    // this node is `src` (coefficient +g) or the edge's target (coefficient -g)
+                    const float n_i0 = self ? g_i0 : -g_i0, n_j0 = self ? g_j0 : -g_j0;
+                    const float n_i1 = self ? g_i1 : -g_i1, n_j1 = self ? g_j1 : -g_j1;
+                    d0 = d0 + n_i0 * n_j0;
+                    if (has1) d1 = d1 + n_i1 * n_j1;
+                    if (sl >= 0) {
+                        const float o_j0 = self ? -g_j0 : g_j0, o_j1 = self ? -g_j1 : g_j1;
+                        float* blk = S.blk + sl * 36;
+                        blk[e0] = blk[e0] + n_i0 * o_j0;
+                        if (has1) blk[e1] = blk[e1] + n_i1 * o_j1;
+                    }
+                }
+            }
+            __syncwarp();
+        }
+        if (!touched) {  // identity diagonal block (src/VolumeFusion.cu:637-640)
+            d0 = (i0 == j0) ? 1.f : 0.f;
+            d1 = (i1 == j1) ? 1.f : 0.f;
+        }
+        float* D = a.b.diag + (long)node * 36;
+        D[e0] = d0;
+        if (has1) D[e1] = d1;
+        float* B = a.b.blocks + (long)node * kMaxNbr * 36;
+        for (int u = 0; u < cnt; ++u) {
+            if (S.L[u] <= node) continue;
+            B[u * 36 + e0] = S.blk[u * 36 + e0];
+            if (has1) B[u * 36 + e1] = S.blk[u * 36 + e1];
+        }
+        __syncwarp();
+    }
+}
+
+// Inverse of each diagonal block: Gauss-Jordan with partial pivoting in FP64, one warp per
+// node with lane j < 12 owning column j of [D | I]; stored rounded to FP32 (the preconditioner
+// is applied in FP32).
+__global__ void __launch_bounds__(128) diag_inverse_kernel(GnArgs a) {
+    const int lane = threadIdx.x & 31;
+    const int node = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int n = min(*a.n_nodes, a.n_max);
     if (node >= n) return;
-    double m[6][12];
     const float* D = a.b.diag + (long)node * 36;
-    for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 12; ++j) m[i][j] = j < 6 ? (double)D[i * 6 + j] : (j - 6 == i ? 1.0 : 0.0);
+    const bool own = lane < 12;
+    double col[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) col[i] = !own ? 0.0 : (lane < 6 ? (double)D[i * 6 + lane] : (lane - 6 == i ? 1.0 : 0.0));
     bool ok = true;
-    for (int c = 0; c < 6 && ok; ++c) {
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        // pivot: the largest |m[r][c]|, r >= c (first on ties), read from lane c
         int p = c;
-        for (int r = c + 1; r < 6; ++r)
-            if (fabs(m[r][c]) > fabs(m[p][c])) p = r;
-        if (m[p][c] == 0.0) {
+        double best = fabs(__shfl_sync(0xffffffffu, col[c], c));
+#pragma unroll
+        for (int r = c + 1; r < 6; ++r) {
+            double v = fabs(__shfl_sync(0xffffffffu, col[r], c));
+            if (v > best) {
+                best = v;
+                p = r;
+            }
+        }
+        if (best == 0.0) {
             ok = false;
             break;
         }
-        if (p != c)
-            for (int j = 0; j < 12; ++j) {
-                double t = m[p][j];
-                m[p][j] = m[c][j];
-                m[c][j] = t;
-            }
-        double d = m[c][c];
-        for (int j = 0; j < 12; ++j) m[c][j] /= d;
+        if (p != c) {
+#pragma unroll
+            for (int r = c + 1; r < 6; ++r)
+                if (r == p) {
+                    double t = col[r];
+                    col[r] = col[c];
+                    col[c] = t;
+                }
+        }
+        const double d = __shfl_sync(0xffffffffu, col[c], c);
+        col[c] /= d;
+#pragma unroll
         for (int r = 0; r < 6; ++r)
             if (r != c) {
-                double f = m[r][c];
-                for (int j = 0; j < 12; ++j) m[r][j] -= f * m[c][j];
+                double f = __shfl_sync(0xffffffffu, col[r], c);
+                col[r] -= f * col[c];
             }
     }
-    double* out = a.b.minv + (long)node * 36;
+    float* out = a.b.minv + (long)node * 36;
     if (!ok) {
-        atomicOr(a.error, ERRF_SINGULAR);
-        for (int i = 0; i < 36; ++i) out[i] = 0.0;
+        if (lane == 0) atomicOr(a.error, ERRF_SINGULAR);
+        if (lane < 6)
+            for (int i = 0; i < 6; ++i) out[i * 6 + lane] = 0.f;
         return;
     }
-    for (int i = 0; i < 6; ++i)
-        for (int j = 0; j < 6; ++j) out[i * 6 + j] = m[i][j + 6];
+    if (lane >= 6 && lane < 12)
+#pragma unroll
+        for (int i = 0; i < 6; ++i) out[i * 6 + lane - 6] = (float)col[i];
 }
 
-// ---- per-GN-iteration kernels ----
-
-constexpr int kEnergyBlocks = 256;
-
-// fill_r_DepthKernel / fill_r_MRegKernel + runSquareKernel + reductions
-// (src/MotionOptimization.cu:163-227, src/VolumeFusion.cu:575-588); energies in FP64.
-__global__ void __launch_bounds__(256) residual_kernel(GnArgs a, const float* warped, const float* T_pending) {
-    if (a.b.state->done) return;
-    __shared__ double sd[8], sr[8];
-    const long C = min((long)*a.corr_count, a.c_max);
-    const int n = min(*a.n_nodes, a.n_max);
-    const long R = (long)n * a.kreg;
-    double ed = 0.0, er = 0.0;
-    const long stride = (long)gridDim.x * blockDim.x;
-    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < C; c += stride) {
-        long v = a.corr[2 * c], px = a.corr[2 * c + 1];
-        const float* wv = warped + 3 * v;
-        const float* f = a.frame + 3 * px;
-        float d[3] = {wv[0] - f[0], wv[1] - f[1], wv[2] - f[2]};
-        float r = a.lam_d * dot3(a.normals + 3 * px, d);
-        a.b.rdepth[c] = r;
-        ed += (double)(r * r);
-    }
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < R; t += stride) {
-        int i = (int)(t / a.kreg);
-        uint32_t nb = a.gidx[t];
-        float* rr = a.b.rreg + 3 * t;
-        if (nb >= (uint32_t)n) {
-            rr[0] = rr[1] = rr[2] = 0.f;
-            continue;
-        }
-        float tc[3], tn[3];
-        mat4_point(T_pending + 16 * (long)i, a.nodes + 3 * (long)i, tc);
-        mat4_point(T_pending + 16 * (long)nb, a.nodes + 3 * (long)i, tn);
-        for (int ax = 0; ax < 3; ++ax) {
-            float r = (tc[ax] - tn[ax]) * a.lam_r;
-            rr[ax] = r;
-            er += (double)(r * r);
-        }
-    }
-    ed = warp_sum(ed);
-    er = warp_sum(er);
-    if ((threadIdx.x & 31) == 0) {
-        sd[threadIdx.x >> 5] = ed;
-        sr[threadIdx.x >> 5] = er;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double x = 0, y = 0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-            x += sd[i];
-            y += sr[i];
-        }
-        a.b.epart[2 * blockIdx.x] = x;
-        a.b.epart[2 * blockIdx.x + 1] = y;
-    }
-}
-
-// Energy test and commit decision (src/VolumeFusion.cu:589-598).
-__global__ void __launch_bounds__(kEnergyBlocks) energy_kernel(GnArgs a, int iter) {
-    GnState* s = a.b.state;
-    if (s->done) return;
-    __shared__ double sd[kEnergyBlocks / 32], sr[kEnergyBlocks / 32];
-    // one partial pair per thread, fixed-order tree: the same totals on every run
-    double ed = warp_sum(a.b.epart[2 * threadIdx.x]);
-    double er = warp_sum(a.b.epart[2 * threadIdx.x + 1]);
-    if ((threadIdx.x & 31) == 0) {
-        sd[threadIdx.x >> 5] = ed;
-        sr[threadIdx.x >> 5] = er;
-    }
-    __syncthreads();
-    if (threadIdx.x != 0) return;
-    ed = 0;
-    er = 0;
-    for (int i = 0; i < kEnergyBlocks / 32; ++i) {
-        ed += sd[i];
-        er += sr[i];
-    }
-    double e = ed + er;
-    s->e_last = e;
-    s->e_depth = ed;
-    s->e_reg = er;
-    if (s->e_prev - e < (double)a.min_step) {
-        s->done = 1;
-        return;
-    }
-    s->e_prev = e;
-    s->commit = iter != 0;
-    s->iters = iter + 1;
-}
-
-__global__ void commit_kernel(GnArgs a, float* T_committed, const float* T_pending) {
-    if (a.b.state->done || !a.b.state->commit) return;
-    const int n = min(*a.n_nodes, a.n_max);
-    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t < (long)n * 16) T_committed[t] = T_pending[t];
-}
-
-// J^T r, one warp per node: lanes 0..5 each own one entry and sum in the fixed order.
-__global__ void __launch_bounds__(32 * kGnWarps) jtr_kernel(GnArgs a) {
-    if (a.b.state->done) return;
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int node = blockIdx.x * kGnWarps + w;
-    const int n = min(*a.n_nodes, a.n_max);
-    if (node >= n) return;
-    const int q = lane < 6 ? lane : 0;
-    float acc = 0.f;
-    const unsigned o = a.b.loff[node], e = a.b.loff[node + 1];
-    // J rows were formed once per ICP iteration by jtj_assemble_kernel (same values, same order)
-    for (unsigned t = o; t < e; ++t) {
-        int c = a.b.jc[t];
-        if (c < 0) continue;
-        acc = acc + a.b.jrow[(long)t * 6 + q] * a.b.rdepth[c];
-    }
-    const unsigned io = a.b.ioff[node], ie = a.b.ioff[node + 1];
-    unsigned it = io;
-    auto reg_row = [&](int src, int kk) {
-        float G[3][6];
-        grad_rows(a.nodes + 3 * (long)src, G);
-        for (int ax = 0; ax < 3; ++ax) {
-            float g = G[ax][q] * a.lam_r;
-            float jn = (src == node) ? g : -g;
-            acc = acc + jn * a.b.rreg[((long)src * a.kreg + kk) * 3 + ax];
-        }
-    };
-    while (it < ie && a.b.ilst[it] / a.kreg < (unsigned)node) {
-        unsigned ent = a.b.ilst[it++];
-        reg_row((int)(ent / a.kreg), (int)(ent % a.kreg));
-    }
-    for (int kk = 0; kk < a.kreg; ++kk) {
-        uint32_t nb = a.gidx[(long)node * a.kreg + kk];
-        if (nb >= (uint32_t)n) continue;
-        reg_row(node, kk);
-    }
-    while (it < ie) {
-        unsigned ent = a.b.ilst[it++];
-        reg_row((int)(ent / a.kreg), (int)(ent % a.kreg));
-    }
-    if (lane < 6) a.b.jtr[(long)node * 6 + lane] = acc;
-}
-
-// ---- PCG (cooperative, persistent) ----
+// ---- Gauss-Newton loop: one thread-block cluster per ICP iteration ----
 //
-// Only ceil(n / kGnWarps) CTAs (at most the launched grid) take part; the others leave at once.
-// Each iteration has two grid barriers: after A p (reduces p.Ap) and after the r / z update
-// (reduces r.z and r.r).  The new search direction p_k = z_k + beta p_{k-1} is formed in the
-// A p phase (double-buffered p, so neighbours' values are computed on the fly from z and the
-// previous p without a third barrier).  Reductions are finished by the last CTA to arrive, in
-// CTA order, so every CTA sees the same FP64 totals.
+// All Gauss-Newton iterations of one ICP iteration (src/VolumeFusion.cu:571-691) run in one
+// launch of a single cluster of kGnClusterMax CTAs (16 where the device allows non-portable
+// cluster sizes, else 8).  Phases are separated by the hardware cluster barrier
+// (barrier.cluster.arrive.release / wait.acquire), so no CTA spins on memory.  FP64
+// reductions go through distributed shared memory: each CTA writes its block sum into a slot
+// of its own shared memory and, after the barrier, reads every CTA's slot in rank order, so
+// all CTAs hold bit-identical totals and take identical branches.  Values exchanged between
+// CTAs through global memory (residuals, pending transforms, PCG vectors, warped vertices)
+// are stored with st.global.cg and loaded with ld.global.cg, i.e. always from L2.
+// Per iteration:
+//   residuals + energies -> energy test and commit -> J^T r -> PCG (x = 0, block-Jacobi,
+//   FP32 block SpMV, FP64 dots, two cluster barriers per PCG iteration)
+//   -> T_pending -= [[x_rot]x, x_t; 0] -> re-warp the canonical vertices with T_pending.
 
-struct PcgArgs {
-    GnArgs g;
-    float* T_pending;
-    int iters;
-    double tol;  // <= 0: run exactly `iters` iterations
+constexpr int kLoopThreads = 512;
+constexpr int kLoopWarps = kLoopThreads / 32;
+
+AFX_D unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+
+AFX_D unsigned cluster_size() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+
+// All threads of all CTAs of the cluster; orders every prior memory access before every later one.
+AFX_D void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Load a double from the shared memory of CTA `rank` of this cluster, at the offset of `p` here.
+AFX_D double dsmem_load(const double* p, unsigned rank) {
+    unsigned local = (unsigned)__cvta_generic_to_shared(p), remote;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(rank));
+    double v;
+    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(remote) : "memory");
+    return v;
+}
+
+struct ClusterSums {
+    double slot[2][4];            // this CTA's block sums, double-buffered across calls
+    double warp[kLoopWarps * 4];  // per-warp sums
+    double total[4];
+    int phase;
 };
 
-constexpr int kRed = 4;  // reduction slots per CTA
-
-// Arrive at the barrier with this CTA's partials; the last CTA sums all partials (fixed order)
-// into totals and releases the others.  Returns false if the bounded wait gave up.
-AFX_D bool grid_reduce_sync(unsigned* bar, int active, double* partial, double* totals, const double* mine, int nslots,
-                            double* out, int* err) {
-    __shared__ int s_ok;
-    __shared__ double s_tot[kRed];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < nslots; ++i) __stcg(partial + (long)blockIdx.x * kRed + i, mine[i]);
-        volatile unsigned* gen = bar + 1;
-        unsigned g = *gen;
-        __threadfence();
-        unsigned arrived = atomicAdd(bar, 1u) + 1;
-        s_ok = 1;
-        if (arrived == (unsigned)active) {
-            __threadfence();
-            for (int i = 0; i < nslots; ++i) {
-                double t = 0;
-                for (int c = 0; c < active; ++c) t += __ldcg(partial + (long)c * kRed + i);
-                __stcg(totals + i, t);
-            }
-            bar[0] = 0;
-            __threadfence();
-            atomicAdd(bar + 1, 1u);
-        } else {
-            long k = 0;
-            while (*gen == g) {
-                if (++k > (1L << 24)) {
-                    atomicOr(err, ERRF_TIMEOUT);
-                    s_ok = 0;
-                    break;
-                }
-                __nanosleep(32);
-            }
-            __threadfence();
-        }
-        for (int i = 0; i < nslots; ++i) s_tot[i] = __ldcg(totals + i);
-    }
-    __syncthreads();
-    for (int i = 0; i < nslots; ++i) out[i] = s_tot[i];
-    return s_ok != 0;
-}
-
-AFX_D double block_sum_d(double v, double* sh) {
-    v = warp_sum(v);
-    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-    __syncthreads();
-    double s = 0;
-    if (threadIdx.x == 0)
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
-    __syncthreads();
-    return s;  // valid in thread 0
-}
-
-// Search direction entry for this iteration: z (first iteration) or z + beta * p_prev.
-AFX_D float pdir(const float* z, const float* pprev, long i, double beta, bool first) {
-    float zi = __ldcg(z + i);
-    return first ? zi : (float)((double)zi + beta * (double)__ldcg(pprev + i));
-}
-
-// y = A p for node `node` (one warp), p formed on the fly; returns the 6 entries in every lane.
-AFX_D void spmv_row(const GnBuffers& b, int node, const float* z, const float* pprev, double beta, bool first,
-                    float* y6) {
-    const int lane = threadIdx.x & 31;
-    const int cnt = b.nbr_cnt[node];
-    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int u = lane; u <= cnt; u += 32) {
-        const float* blk;
-        long xo;
-        bool tr = false;
-        if (u == 0) {
-            blk = b.diag + (long)node * 36;
-            xo = (long)node * 6;
-        } else {
-            int ref = b.nbr_ref[(long)node * kMaxNbr + u - 1];
-            int other = b.nbr[(long)node * kMaxNbr + u - 1];
-            xo = (long)other * 6;
-            if (ref >= 0) blk = b.blocks + (long)ref * 36;
-            else {
-                blk = b.blocks + (long)(-ref - 1) * 36;
-                tr = true;
-            }
-        }
-        float xv[6];
-#pragma unroll
-        for (int j = 0; j < 6; ++j) xv[j] = pdir(z, pprev, xo + j, beta, first);
-#pragma unroll
-        for (int i = 0; i < 6; ++i) {
-            float s = 0.f;
-#pragma unroll
-            for (int j = 0; j < 6; ++j) s = s + (tr ? blk[j * 6 + i] : blk[i * 6 + j]) * xv[j];
-            acc[i] = acc[i] + s;
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 6; ++i) y6[i] = warp_sum(acc[i]);
-}
-
-__global__ void __launch_bounds__(32 * kGnWarps) pcg_kernel(PcgArgs P) {
-    GnArgs& a = P.g;
-    GnBuffers& b = a.b;
-    if (b.state->done) return;
-    const int n = min(*a.n_nodes, a.n_max);
-    const int active = max(1, min((int)gridDim.x, (n + kGnWarps - 1) / kGnWarps));
-    if ((int)blockIdx.x >= active) return;
-    __shared__ double sh[kGnWarps];
+// Sums v[0..NV) over every thread of the cluster; all threads of all CTAs get identical totals.
+// Fixed-shape FP64 trees: butterfly within each warp, then over the CTA's warps, then over the
+// CTAs by rank.  Contains one cluster barrier.
+template <int NV>
+AFX_D void cluster_sum(double (&v)[NV], ClusterSums& cs) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int gw = blockIdx.x * kGnWarps + w, nw = active * kGnWarps;
-    int* err = a.error;
-    float* pbuf[2] = {b.p, b.ap + (long)a.n_max * 6};  // second direction buffer follows A p
-    // x = 0, r = b, z = M^-1 r; rz = r.z, bb = b.b  (one node per warp, lanes 0..5 own one entry)
-    double rz_part = 0, bb_part = 0;
-    for (int node = gw; node < n; node += nw) {
-        if (lane < 6) {
-            const long o = (long)node * 6;
-            const double* Mi = b.minv + (long)node * 36 + lane * 6;
-            double s = 0;
-            for (int j = 0; j < 6; ++j) s += Mi[j] * (double)b.jtr[o + j];
-            float zi = (float)s, ri = b.jtr[o + lane];
-            b.x[o + lane] = 0.f;
-            __stcg(b.r + o + lane, ri);
-            __stcg(b.z + o + lane, zi);
-            rz_part += (double)ri * (double)zi;
-            bb_part += (double)ri * (double)ri;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        double s = warp_sum(v[i]);
+        if (lane == 0) cs.warp[w * 4 + i] = s;
+    }
+    __syncthreads();
+    const int ph = cs.phase;
+    if (w == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double s = lane < kLoopWarps ? cs.warp[lane * 4 + i] : 0.0;
+#pragma unroll
+            for (int o = kLoopWarps / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) cs.slot[ph][i] = s;
         }
     }
-    double mine[kRed] = {block_sum_d(rz_part, sh), block_sum_d(bb_part, sh), 0, 0};
-    double tot[kRed];
-    if (!grid_reduce_sync(b.bar, active, b.partial, b.partial + 4096 * kRed, mine, 2, tot, err)) return;
-    double rz = tot[0];
-    const double bnorm2 = tot[1];
-    double beta = 0;
-    int it = 0;
-    for (; it < P.iters; ++it) {
-        const bool first = it == 0;
-        const float* pprev = pbuf[(it + 1) & 1];
-        float* pcur = pbuf[it & 1];
-        // p_it = z + beta p_{it-1}; Ap = A p_it; p.Ap
-        double pap = 0;
-        for (int node = gw; node < n; node += nw) {
-            float y[6];
-            spmv_row(b, node, b.z, pprev, beta, first, y);
-            if (lane < 6) {
-                const long o = (long)node * 6 + lane;
-                float pi = pdir(b.z, pprev, o, beta, first);
-                __stcg(pcur + o, pi);
-                float yi = y[0];
+    cluster_barrier();
+    if (w == 0) {
+        const unsigned ncta = cluster_size();
 #pragma unroll
-                for (int q = 1; q < 6; ++q)
-                    if (lane == q) yi = y[q];
-                __stcg(b.ap + o, yi);
-                pap += (double)pi * (double)yi;
+        for (int i = 0; i < NV; ++i) {
+            double t = lane < (int)ncta ? dsmem_load(&cs.slot[ph][i], lane) : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) cs.total[i] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = cs.total[i];
+    if (threadIdx.x == 0) cs.phase = ph ^ 1;
+}
+
+struct LoopArgs {
+    GnArgs g;
+    const float* points;  // canonical vertices
+    float* warped;
+    float* T_committed;
+    float* T_pending;
+    int gn_iters, pcg_iters;
+    double tol;  // <= 0: run exactly pcg_iters PCG iterations
+};
+
+// J^T r of one node, one warp: lane l sums the node-list entries l, l+32, ... (depth rows, J
+// rows formed once per ICP iteration by jtj_assemble_kernel) and then the regularisation rows
+// l, l+32, ... (incoming edges, then the node's own); the 32 partial sums are combined by a
+// butterfly, so every lane returns the same six totals.
+AFX_D void jtr_node(const GnArgs& a, int node, int n, float (&acc)[6]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) acc[q] = 0.f;
+    const unsigned o = a.b.loff[node], e = a.b.loff[node + 1];
+#pragma unroll 4
+    for (unsigned t = o + lane; t < e; t += 32) {
+        const int c = a.b.jc[t];
+        if (c < 0) continue;
+        const float rd = __ldcg(a.b.rdepth + c);
+        const float* J = a.b.jrow + (long)t * 6;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) acc[q] = acc[q] + J[q] * rd;
+    }
+    const unsigned io = a.b.ioff[node], nin = a.b.ioff[node + 1] - io;
+    for (unsigned u = lane; u < nin + (unsigned)a.kreg; u += 32) {
+        int src, kk;
+        if (u < nin) {
+            const unsigned ent = a.b.ilst[io + u];
+            src = (int)(ent / a.kreg);
+            kk = (int)(ent % a.kreg);
+        } else {
+            src = node;
+            kk = (int)(u - nin);
+            if (a.gidx[(long)node * a.kreg + kk] >= (uint32_t)n) continue;
+        }
+        float G[3][6];
+        grad_rows(a.nodes + 3 * (long)src, G);
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+            const float r = __ldcg(a.b.rreg + ((long)src * a.kreg + kk) * 3 + ax);
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const float g = G[ax][q] * a.lam_r;
+                const float jn = (src == node) ? g : -g;
+                acc[q] = acc[q] + jn * r;
             }
         }
-        mine[0] = block_sum_d(pap, sh);
-        if (!grid_reduce_sync(b.bar, active, b.partial, b.partial + 4096 * kRed, mine, 1, tot, err)) return;
-        pap = tot[0];
-        if (pap == 0.0 || !(pap == pap)) break;
-        const double alpha = rz / pap;
-        // x += alpha p; r -= alpha Ap; z = M^-1 r; r.z, r.r
-        double rz_p = 0, rr_p = 0;
-        for (int node = gw; node < n; node += nw) {
-            const long o = (long)node * 6;
-            float rv = 0.f;
-            if (lane < 6) {
-                b.x[o + lane] = (float)((double)b.x[o + lane] + alpha * (double)__ldcg(pcur + o + lane));
-                rv = (float)((double)__ldcg(b.r + o + lane) - alpha * (double)__ldcg(b.ap + o + lane));
-                __stcg(b.r + o + lane, rv);
-            }
-            float rr6[6];
+    }
 #pragma unroll
-            for (int j = 0; j < 6; ++j) rr6[j] = __shfl_sync(0xffffffffu, rv, j);
-            if (lane < 6) {
-                const double* Mi = b.minv + (long)node * 36 + lane * 6;
-                double zs = 0;
-                for (int j = 0; j < 6; ++j) zs += Mi[j] * (double)rr6[j];
-                float zi = (float)zs;
-                __stcg(b.z + o + lane, zi);
-                rz_p += (double)rv * (double)zi;
-                rr_p += (double)rv * (double)rv;
+    for (int q = 0; q < 6; ++q) acc[q] = warp_sum(acc[q]);
+}
+
+// Row `i` of A z for node `node`: the node's blocks (diagonal first, then the neighbours in
+// ascending order) times z, FP32.
+AFX_D float spmv_entry(const GnBuffers& b, int node, int i, const float* z) {
+    const int cnt = b.nbr_cnt[node];
+    float acc = 0.f;
+    {
+        const float* B = b.diag + (long)node * 36 + i * 6;
+        const float* x = z + (long)node * 6;
+        float s = 0.f;
+#pragma unroll
+        for (int j = 0; j < 6; ++j) s = s + B[j] * __ldcg(x + j);
+        acc = acc + s;
+    }
+#pragma unroll 2
+    for (int u = 0; u < cnt; ++u) {
+        const int ref = b.nbr_ref[(long)node * kMaxNbr + u];
+        const float* x = z + (long)b.nbr[(long)node * kMaxNbr + u] * 6;
+        float s = 0.f;
+        if (ref >= 0) {
+            const float* B = b.blocks + (long)ref * 36 + i * 6;
+#pragma unroll
+            for (int j = 0; j < 6; ++j) s = s + B[j] * __ldcg(x + j);
+        } else {
+            const float* B = b.blocks + (long)(-ref - 1) * 36 + i;
+#pragma unroll
+            for (int j = 0; j < 6; ++j) s = s + B[j * 6] * __ldcg(x + j);
+        }
+        acc = acc + s;
+    }
+    return acc;
+}
+
+// ---- PCG with the system resident in distributed shared memory ----
+//
+// For graphs up to kDsNpc nodes per CTA, each CTA of the cluster owns a contiguous node range
+// and keeps, in its shared memory, the rows of J^T J for its nodes (diagonal block, then the
+// neighbour blocks in ascending neighbour order, lower ones stored transposed so every block
+// is row-major B_ij), their block inverses, its slices of x, r, p, A p, and a full copy of z.
+// After each update a CTA writes its new z slice into every CTA's copy (st.shared::cluster), so
+// the SpMV reads only local shared memory.  Partial sums are written into every CTA's slot
+// array and summed locally in rank order after the cluster barrier: identical totals in all
+// CTAs.  J^T J does not change during the Gauss-Newton loop, so the rows are staged once.
+
+constexpr int kDsNodes = 1024;   // node limit of this path (full z copy)
+constexpr int kDsNpc = 64;       // nodes per CTA
+constexpr int kDsBlocks = 1024;  // blocks per CTA (diagonal included)
+constexpr int kDsMaxCta = 16;
+
+struct DsLayout {
+    float* z;       // [kDsNodes * 6] full copy
+    float* x;       // [kDsNpc * 6] own slices
+    float* r;
+    float* p;
+    float* ap;
+    float* minv;    // [kDsNpc * 36]
+    float* blk;     // [kDsBlocks * 36]
+    int* col;       // [kDsBlocks] neighbour node of each block
+    int* rowptr;    // [kDsNpc + 1]
+    double* slot;   // [2][kDsMaxCta][4]
+    int* misc;      // [4]
+};
+
+constexpr size_t kDsSmem = sizeof(float) * ((size_t)kDsNodes * 6 + 4 * kDsNpc * 6 + kDsNpc * 36 + (size_t)kDsBlocks * 36) +
+                           sizeof(int) * (kDsBlocks + kDsNpc + 1 + 4) + sizeof(double) * 2 * kDsMaxCta * 4 + 64;
+
+AFX_D DsLayout ds_layout(void* base) {
+    DsLayout d;
+    double* dp = static_cast<double*>(base);
+    d.slot = dp;
+    float* f = reinterpret_cast<float*>(dp + 2 * kDsMaxCta * 4);
+    d.z = f;
+    f += kDsNodes * 6;
+    d.x = f;
+    f += kDsNpc * 6;
+    d.r = f;
+    f += kDsNpc * 6;
+    d.p = f;
+    f += kDsNpc * 6;
+    d.ap = f;
+    f += kDsNpc * 6;
+    d.minv = f;
+    f += kDsNpc * 36;
+    d.blk = f;
+    f += (size_t)kDsBlocks * 36;
+    int* ip = reinterpret_cast<int*>(f);
+    d.col = ip;
+    ip += kDsBlocks;
+    d.rowptr = ip;
+    ip += kDsNpc + 1;
+    d.misc = ip;
+    return d;
+}
+
+// Store to the same shared-memory offset in CTA `rank` of this cluster.
+AFX_D void dsmem_store_f32(float* local, unsigned rank, float v) {
+    unsigned a = (unsigned)__cvta_generic_to_shared(local), ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(ra), "f"(v) : "memory");
+}
+AFX_D void dsmem_store_f64(double* local, unsigned rank, double v) {
+    unsigned a = (unsigned)__cvta_generic_to_shared(local), ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+    asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(ra), "d"(v) : "memory");
+}
+
+// Cluster sum through the slot arrays: the CTA's block total is written into slot[ph][rank] of
+// every CTA; after the barrier each CTA adds the slots in rank order.
+template <int NV>
+AFX_D void ds_sum(double (&v)[NV], const DsLayout& d, ClusterSums& cs, int& ph) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned rank = cluster_rank(), ncta = cluster_size();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        double s = warp_sum(v[i]);
+        if (lane == 0) cs.warp[w * 4 + i] = s;
+    }
+    __syncthreads();
+    if (w == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double s = lane < kLoopWarps ? cs.warp[lane * 4 + i] : 0.0;
+#pragma unroll
+            for (int o = kLoopWarps / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            // lane q < ncta sends the total to CTA q
+            if (lane < (int)ncta) dsmem_store_f64(d.slot + (ph * kDsMaxCta + rank) * 4 + i, lane, s);
+        }
+    }
+    cluster_barrier();
+    if (w == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double t = lane < (int)ncta ? d.slot[(ph * kDsMaxCta + lane) * 4 + i] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            if (lane == 0) cs.total[i] = t;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = cs.total[i];
+    ph ^= 1;
+}
+
+// Stage this CTA's rows; returns (uniformly over the cluster) whether every CTA's rows fit.
+AFX_D bool ds_stage(const GnBuffers& b, int n, const DsLayout& d, ClusterSums& cs, int& ph) {
+    const unsigned rank = cluster_rank(), ncta = cluster_size();
+    const int npc = (n + (int)ncta - 1) / (int)ncta;
+    const int start = min(n, (int)rank * npc), own = min(n, start + npc) - start;
+    if (threadIdx.x < 32) {
+        // row pointers: diagonal + neighbour blocks per own node (one warp, inclusive scan)
+        int carry = 0;
+        for (int base = 0; base < own; base += 32) {
+            const int li = base + (int)threadIdx.x;
+            const int c = li < own ? 1 + b.nbr_cnt[start + li] : 0;
+            int incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int)threadIdx.x >= o) incl += y;
+            }
+            if (li < own) d.rowptr[li] = carry + incl - c;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        if (threadIdx.x == 0) {
+            d.rowptr[own] = carry;
+            d.misc[0] = carry;
+        }
+    }
+    __syncthreads();
+    double need[1] = {d.misc[0] > kDsBlocks ? 1.0 : 0.0};
+    ds_sum<1>(need, d, cs, ph);
+    if (need[0] != 0.0) return false;
+    // copy the rows (block-major, 36 floats each) and the inverses
+    for (int li = threadIdx.x >> 5; li < own; li += kLoopWarps) {
+        const int node = start + li;
+        const int lane = threadIdx.x & 31;
+        const int r0 = d.rowptr[li], cnt = d.rowptr[li + 1] - r0 - 1;
+        for (int e = lane; e < 36; e += 32) {
+            d.blk[r0 * 36 + e] = b.diag[(long)node * 36 + e];
+            d.minv[li * 36 + e] = b.minv[(long)node * 36 + e];
+        }
+        if (lane == 0) d.col[r0] = node;
+        for (int u = 0; u < cnt; ++u) {
+            const int ref = b.nbr_ref[(long)node * kMaxNbr + u];
+            const float* src = b.blocks + (long)(ref >= 0 ? ref : -ref - 1) * 36;
+            float* dst = d.blk + (r0 + 1 + u) * 36;
+            for (int e = lane; e < 36; e += 32) dst[e] = ref >= 0 ? src[e] : src[(e % 6) * 6 + e / 6];
+            if (lane == 0) d.col[r0 + 1 + u] = b.nbr[(long)node * kMaxNbr + u];
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
+// One PCG solve (same recurrences and arithmetic as the global-memory path), then
+// T_pending -= [x] for the own nodes.  J^T r is read from b.jtr.
+AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, int& ph) {
+    const GnBuffers& b = L.g.b;
+    const unsigned rank = cluster_rank(), ncta = cluster_size();
+    const int npc = (n + (int)ncta - 1) / (int)ncta;
+    const int start = min(n, (int)rank * npc), own = min(n, start + npc) - start;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int grp = lane / 6, ei = lane - 6 * grp;
+    const int li = w * 5 + grp;  // kLoopWarps * 5 >= kDsNpc: one own node per lane group
+    const bool act = lane < 30 && li < own;
+    const int o = li * 6 + ei;
+    const int gnode = start + li;
+    // x = 0, r = b, z = M^-1 r
+    double d2[2] = {0.0, 0.0};
+    {
+        const float ji = act ? __ldcg(b.jtr + (long)gnode * 6 + ei) : 0.f;
+        float zi = 0.f;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const float rq = __shfl_sync(0xffffffffu, ji, lane < 30 ? grp * 6 + q : q);
+            if (act) zi = zi + d.minv[li * 36 + ei * 6 + q] * rq;
+        }
+        if (act) {
+            d.x[o] = 0.f;
+            d.r[o] = ji;
+            for (unsigned q = 0; q < ncta; ++q) dsmem_store_f32(d.z + (long)gnode * 6 + ei, q, zi);
+            d2[0] += (double)ji * (double)zi;
+            d2[1] += (double)ji * (double)ji;
+        }
+    }
+    ds_sum<2>(d2, d, cs, ph);
+    double rz = d2[0];
+    const double bnorm2 = d2[1];
+    float beta = 0.f;
+    for (int it = 0; it < L.pcg_iters; ++it) {
+        double pap[1] = {0.0};
+        if (act) {
+            const int r0 = d.rowptr[li], r1 = d.rowptr[li + 1];
+            float acc = 0.f;
+            for (int bk = r0; bk < r1; ++bk) {
+                const float* B = d.blk + bk * 36 + ei * 6;
+                const float* x = d.z + d.col[bk] * 6;
+                float s = 0.f;
+#pragma unroll
+                for (int j = 0; j < 6; ++j) s = s + B[j] * x[j];
+                acc = acc + s;
+            }
+            const float zi = d.z[(long)gnode * 6 + ei];
+            float pi = zi, api = acc;
+            if (it) {
+                pi = zi + beta * d.p[o];
+                api = acc + beta * d.ap[o];
+            }
+            d.p[o] = pi;
+            d.ap[o] = api;
+            pap[0] += (double)pi * (double)api;
+        }
+        ds_sum<1>(pap, d, cs, ph);
+        if (pap[0] == 0.0 || !(pap[0] == pap[0])) break;
+        const float alpha = (float)(rz / pap[0]);
+        double q2[2] = {0.0, 0.0};
+        float rv = 0.f;
+        if (act) {
+            d.x[o] = d.x[o] + alpha * d.p[o];
+            rv = d.r[o] - alpha * d.ap[o];
+            d.r[o] = rv;
+        }
+        float zi = 0.f;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const float rq = __shfl_sync(0xffffffffu, rv, lane < 30 ? grp * 6 + q : q);
+            if (act) zi = zi + d.minv[li * 36 + ei * 6 + q] * rq;
+        }
+        if (act) {
+            for (unsigned q = 0; q < ncta; ++q) dsmem_store_f32(d.z + (long)gnode * 6 + ei, q, zi);
+            q2[0] += (double)rv * (double)zi;
+            q2[1] += (double)rv * (double)rv;
+        }
+        ds_sum<2>(q2, d, cs, ph);
+        beta = (float)(q2[0] / rz);
+        rz = q2[0];
+        if (L.tol > 0 && q2[1] <= L.tol * L.tol * bnorm2) break;
+    }
+    // T_pending -= [[x_rot]x, x_t; 0] for the own nodes (updateTransformsKernel,
+    // src/MotionOptimization.cu:483-498); x also to global memory for inspection
+    __syncthreads();
+    for (int t = threadIdx.x; t < own * 16; t += blockDim.x) {
+        const int l = t >> 4, e = t & 15;
+        const float* u = d.x + l * 6;
+        float U;
+        switch (e) {
+            case 1: U = u[2]; break;
+            case 2: U = -u[1]; break;
+            case 4: U = -u[2]; break;
+            case 6: U = u[0]; break;
+            case 8: U = u[1]; break;
+            case 9: U = -u[0]; break;
+            case 12: U = u[3]; break;
+            case 13: U = u[4]; break;
+            case 14: U = u[5]; break;
+            default: U = 0.f;
+        }
+        float* T = L.T_pending + (long)(start + l) * 16 + e;
+        __stcg(T, __ldcg(T) - U);
+    }
+    for (int t = threadIdx.x; t < own * 6; t += blockDim.x) __stcg(b.x + (long)start * 6 + t, d.x[t]);
+}
+
+__global__ void __launch_bounds__(kLoopThreads, 1) gn_loop_kernel(LoopArgs L) {
+    const GnArgs& a = L.g;
+    const GnBuffers& b = a.b;
+    __shared__ ClusterSums cs;
+    extern __shared__ double ds_smem[];
+    if (threadIdx.x == 0) cs.phase = 0;
+    __syncthreads();
+    const unsigned rank = cluster_rank(), ncta = cluster_size();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const long gt = (long)rank * kLoopThreads + threadIdx.x, gstride = (long)ncta * kLoopThreads;
+    const int gw = (int)rank * kLoopWarps + w, nw = (int)ncta * kLoopWarps;
+    const bool leader = rank == 0 && threadIdx.x == 0;
+    const int n = min(*a.n_nodes, a.n_max);
+    const long ncorr = min((long)*a.corr_count, a.c_max);
+    const long nreg = (long)n * a.kreg;
+    const long m = min((long)*a.mesh_count, a.m_max);
+    GnState* s = b.state;
+    double e_prev = s->e_prev;
+    bool done = s->done != 0;
+    // small graphs: the system lives in distributed shared memory for the whole loop
+    const DsLayout dsl = ds_layout(ds_smem);
+    int ds_ph = 0;
+    const bool ds = !done && n > 0 && (n + (int)ncta - 1) / (int)ncta <= kDsNpc && ds_stage(b, n, dsl, cs, ds_ph);
+    for (int iter = 0; iter < L.gn_iters && !done; ++iter) {
+        // ---- residuals and energies (fill_r_DepthKernel / fill_r_MRegKernel + runSquareKernel,
+        //      src/MotionOptimization.cu:163-227, src/VolumeFusion.cu:575-588), FP64 sums
+        double e2[2] = {0.0, 0.0};
+        for (long c = gt; c < ncorr; c += gstride) {
+            long v = a.corr[2 * c], px = a.corr[2 * c + 1];
+            const float* f = a.frame + 3 * px;
+            float d[3] = {__ldcg(L.warped + 3 * v) - f[0], __ldcg(L.warped + 3 * v + 1) - f[1],
+                          __ldcg(L.warped + 3 * v + 2) - f[2]};
+            float r = a.lam_d * dot3(a.normals + 3 * px, d);
+            __stcg(b.rdepth + c, r);
+            e2[0] += (double)(r * r);
+        }
+        for (long t = gt; t < nreg; t += gstride) {
+            int i = (int)(t / a.kreg);
+            uint32_t nb = a.gidx[t];
+            float* rr = b.rreg + 3 * t;
+            if (nb >= (uint32_t)n) {
+                __stcg(rr, 0.f);
+                __stcg(rr + 1, 0.f);
+                __stcg(rr + 2, 0.f);
+                continue;
+            }
+            float Ti[16], Tn[16], tc[3], tn[3];
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                Ti[e] = __ldcg(L.T_pending + 16 * (long)i + e);
+                Tn[e] = __ldcg(L.T_pending + 16 * (long)nb + e);
+            }
+            mat4_point(Ti, a.nodes + 3 * (long)i, tc);
+            mat4_point(Tn, a.nodes + 3 * (long)i, tn);
+            for (int ax = 0; ax < 3; ++ax) {
+                float r = (tc[ax] - tn[ax]) * a.lam_r;
+                __stcg(rr + ax, r);
+                e2[1] += (double)(r * r);
             }
         }
-        mine[0] = block_sum_d(rz_p, sh);
-        mine[1] = block_sum_d(rr_p, sh);
-        if (!grid_reduce_sync(b.bar, active, b.partial, b.partial + 4096 * kRed, mine, 2, tot, err)) return;
-        beta = tot[0] / rz;
-        rz = tot[0];
-        if (P.tol > 0 && tot[1] <= P.tol * P.tol * bnorm2) {
-            ++it;
+        cluster_sum<2>(e2, cs);
+        // ---- energy test and commit decision (src/VolumeFusion.cu:589-598)
+        const double e = e2[0] + e2[1];
+        if (leader) {
+            s->e_last = e;
+            s->e_depth = e2[0];
+            s->e_reg = e2[1];
+        }
+        if (e_prev - e < (double)a.min_step) {
+            if (leader) s->done = 1;
+            done = true;
             break;
         }
-    }
-    // pending transforms -= [[x_rot]x, x_t; 0] (updateTransformsKernel, src/MotionOptimization.cu:483-498)
-    for (int node = gw; node < n; node += nw) {
-        if (lane == 0) {
-            const float* u = b.x + (long)node * 6;
-            float* T = P.T_pending + (long)node * 16;
-            const float U[16] = {0.f, u[2], -u[1], 0.f, -u[2], 0.f, u[0], 0.f, u[1], -u[0], 0.f, 0.f, u[3], u[4], u[5], 0.f};
-            for (int e = 0; e < 16; ++e) T[e] = T[e] - U[e];
+        e_prev = e;
+        const bool commit = iter != 0;
+        if (leader) {
+            s->e_prev = e;
+            s->commit = commit;
+            s->iters = iter + 1;
         }
+        if (commit)
+            for (long t = gt; t < (long)n * 16; t += gstride) L.T_committed[t] = __ldcg(L.T_pending + t);
+        if (ds) {
+            // ---- J^T r over the cluster, one node per warp; then the solve in CTA 0
+            for (int node = gw; node < n; node += nw) {
+                float jv[6];
+                jtr_node(a, node, n, jv);
+                if (lane < 6) {
+                    float ji = jv[0];
+#pragma unroll
+                    for (int q = 1; q < 6; ++q)
+                        if (lane == q) ji = jv[q];
+                    __stcg(b.jtr + (long)node * 6 + lane, ji);
+                }
+            }
+            cluster_barrier();
+            pcg_ds(L, n, dsl, cs, ds_ph);
+            cluster_barrier();
+        } else {
+        // ---- J^T r (one node per warp), then x = 0, r = b, z = M^-1 r; rz = r.z, bb = b.b
+        double d2[2] = {0.0, 0.0};
+        for (int node = gw; node < n; node += nw) {
+            float jv[6];
+            jtr_node(a, node, n, jv);
+            if (lane < 6) {
+                const long o = (long)node * 6;
+                const float* Mi = b.minv + (long)node * 36 + lane * 6;
+                float zi = 0.f;
+#pragma unroll
+                for (int q = 0; q < 6; ++q) zi = zi + Mi[q] * jv[q];
+                float ji = jv[0];
+#pragma unroll
+                for (int q = 1; q < 6; ++q)
+                    if (lane == q) ji = jv[q];
+                b.jtr[o + lane] = ji;
+                __stcg(b.x + o + lane, 0.f);
+                __stcg(b.r + o + lane, ji);
+                __stcg(b.z + o + lane, zi);
+                d2[0] += (double)ji * (double)zi;
+                d2[1] += (double)ji * (double)ji;
+            }
+        }
+        cluster_sum<2>(d2, cs);
+        // ---- PCG, six lanes per node (entry i = lane % 6 of node group lane / 6, five groups per
+        // warp).  Pipelined recurrences: A p_k = A z_k + beta_k A p_{k-1} and
+        // p_k = z_k + beta_k p_{k-1}, so the SpMV reads z, complete at the barrier that gave beta_k.
+        const int grp = lane / 6, ei = lane - 6 * grp;
+        const bool glane = lane < 30;
+        const int g0 = gw * 5 + grp, gstep = nw * 5;
+        double rz = d2[0];
+        const double bnorm2 = d2[1];
+        float beta = 0.f;
+        for (int it = 0; it < L.pcg_iters; ++it) {
+            double pap[1] = {0.0};
+            if (glane)
+                for (int node = g0; node < n; node += gstep) {
+                    const long o = (long)node * 6 + ei;
+                    const float az = spmv_entry(b, node, ei, b.z);
+                    const float zi = __ldcg(b.z + o);
+                    float pi = zi, api = az;
+                    if (it) {
+                        pi = zi + beta * __ldcg(b.p + o);
+                        api = az + beta * __ldcg(b.ap + o);
+                    }
+                    __stcg(b.p + o, pi);
+                    __stcg(b.ap + o, api);
+                    pap[0] += (double)pi * (double)api;
+                }
+            cluster_sum<1>(pap, cs);
+            if (pap[0] == 0.0 || !(pap[0] == pap[0])) break;
+            const float alpha = (float)(rz / pap[0]);
+            // x += alpha p; r -= alpha A p; z = M^-1 r; r.z, r.r
+            double q2[2] = {0.0, 0.0};
+            for (int base = gw * 5; base < n; base += gstep) {  // warp-uniform trip count
+                const int node = base + grp;
+                const bool act = glane && node < n;
+                const long o = (long)node * 6 + ei;
+                float rv = 0.f;
+                if (act) {
+                    __stcg(b.x + o, __ldcg(b.x + o) + alpha * __ldcg(b.p + o));
+                    rv = __ldcg(b.r + o) - alpha * __ldcg(b.ap + o);
+                    __stcg(b.r + o, rv);
+                }
+                float zi = 0.f;
+                const float* Mi = b.minv + (long)(act ? node : 0) * 36 + ei * 6;
+#pragma unroll
+                for (int q = 0; q < 6; ++q) {
+                    const float rq = __shfl_sync(0xffffffffu, rv, glane ? grp * 6 + q : q);
+                    if (act) zi = zi + Mi[q] * rq;
+                }
+                if (act) {
+                    __stcg(b.z + o, zi);
+                    q2[0] += (double)rv * (double)zi;
+                    q2[1] += (double)rv * (double)rv;
+                }
+            }
+            cluster_sum<2>(q2, cs);
+            beta = (float)(q2[0] / rz);
+            rz = q2[0];
+            if (L.tol > 0 && q2[1] <= L.tol * L.tol * bnorm2) break;
+        }
+        cluster_barrier();  // x complete
+        // ---- T_pending -= [[x_rot]x, x_t; 0] (updateTransformsKernel, src/MotionOptimization.cu:483-498)
+        for (int node = gw; node < n; node += nw) {
+            if (lane < 16) {
+                float u[6];
+#pragma unroll
+                for (int q = 0; q < 6; ++q) u[q] = __ldcg(b.x + (long)node * 6 + q);
+                const float U[16] = {0.f, u[2], -u[1], 0.f, -u[2], 0.f, u[0], 0.f,
+                                     u[1], -u[0], 0.f, 0.f, u[3], u[4], u[5], 0.f};
+                float* T = L.T_pending + (long)node * 16 + lane;
+                __stcg(T, __ldcg(T) - U[lane]);
+            }
+        }
+        cluster_barrier();
+        }
+        // ---- re-warp the canonical vertices with T_pending (warpKernel, src/ComputeCorrespondence.cu:13-30)
+        for (long i = gt; i < m; i += gstride) {
+            const float p[3] = {L.points[3 * i], L.points[3 * i + 1], L.points[3 * i + 2]};
+            bool zero = true;
+            for (int j = 0; j < a.k; ++j)
+                if (!(fabsf(a.mw[i * a.k + j]) <= 1e-5f)) zero = false;
+            float acc[3] = {p[0], p[1], p[2]};
+            if (!zero) {
+                acc[0] = acc[1] = acc[2] = 0.f;
+                for (int j = 0; j < a.k; ++j) {
+                    uint32_t nb = a.midx[i * a.k + j];
+                    if (nb == AFX_INVALID_INDEX) continue;
+                    float T[16], o[3];
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) T[e] = __ldcg(L.T_pending + 16 * (long)nb + e);
+                    mat4_point(T, p, o);
+                    float wj = a.mw[i * a.k + j];
+                    acc[0] = acc[0] + wj * o[0];
+                    acc[1] = acc[1] + wj * o[1];
+                    acc[2] = acc[2] + wj * o[2];
+                }
+            }
+            __stcg(L.warped + 3 * i, acc[0]);
+            __stcg(L.warped + 3 * i + 1, acc[1]);
+            __stcg(L.warped + 3 * i + 2, acc[2]);
+        }
+        cluster_barrier();
     }
+    // no CTA leaves while another may still read its shared memory
+    cluster_barrier();
 }
 
 }  // namespace afx
@@ -747,17 +1194,36 @@ struct GnSizes {
 
 static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
-static int pcg_grid(int n_max) {
-    static int cached = -1;
-    if (cached < 0) {
-        int dev = 0, sms = 0, per = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pcg_kernel, 32 * kGnWarps, 0);
-        cached = sms * (per < 1 ? 1 : (per > 4 ? 4 : per));
+// Cluster size for gn_loop_kernel: 16 CTAs where the device runs non-portable clusters of
+// that size, else the portable 8.
+static int gn_cluster_size() {
+    static int cached = 0;
+    if (!cached) {
+        cudaFuncSetAttribute(gn_loop_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(gn_loop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDsSmem);
+        const int sizes[2] = {16, 8};
+        for (int c : sizes) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(c);
+            cfg.blockDim = dim3(kLoopThreads);
+            cfg.dynamicSmemBytes = kDsSmem;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = c;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int clusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&clusters, gn_loop_kernel, &cfg) == cudaSuccess && clusters > 0) {
+                cached = c;
+                break;
+            }
+            cudaGetLastError();
+        }
+        if (!cached) cached = 8;
     }
-    int need = (n_max + kGnWarps - 1) / kGnWarps;
-    return need < 1 ? 1 : (need < cached ? need : cached);
+    return cached;
 }
 
 size_t gn_workspace_size(long m_max, int n_max, int k, int kreg) {
@@ -765,11 +1231,11 @@ size_t gn_workspace_size(long m_max, int n_max, int k, int kreg) {
     s += 3 * al((n_max + 1) * 4) + al(m_max * k * 4);           // lcnt loff lcur lst
     s += 3 * al((n_max + 1) * 4) + al((size_t)n_max * kreg * 4);  // icnt ioff icur ilst
     s += al(n_max * 4) + 2 * al((size_t)n_max * kMaxNbr * 4);     // nbr_cnt nbr nbr_ref
-    s += al((size_t)n_max * kMaxNbr * 36 * 4) + al((size_t)n_max * 36 * 4) + al((size_t)n_max * 36 * 8);
+    s += al((size_t)n_max * kMaxNbr * 36 * 4) + al((size_t)n_max * 36 * 4) + al((size_t)n_max * 36 * 4);
     s += al((size_t)m_max * k * 6 * 4) + al((size_t)m_max * k * 4);  // jrow jc
     s += al((size_t)n_max * 6 * 4) * 5 + al((size_t)n_max * 6 * 4 * 2);  // jtr x r z p, ap + p2
     s += al(m_max * 4) + al((size_t)n_max * kreg * 3 * 4);        // rdepth rreg
-    s += al((size_t)(4096 + 1) * kRed * 8) + al(64) + al(kEnergyBlocks * 2 * 8) + al(sizeof(GnState));
+    s += al(sizeof(GnState));
     s += al(scan_workspace_size(m_max > n_max ? m_max : n_max));
     return s + 1024;
 }
@@ -795,7 +1261,7 @@ bool gn_carve(void* ws, size_t bytes, long m_max, int n_max, int k, int kreg, Gn
     b->nbr_ref = (int*)take((size_t)n_max * kMaxNbr * 4);
     b->blocks = (float*)take((size_t)n_max * kMaxNbr * 36 * 4);
     b->diag = (float*)take((size_t)n_max * 36 * 4);
-    b->minv = (double*)take((size_t)n_max * 36 * 8);
+    b->minv = (float*)take((size_t)n_max * 36 * 4);
     b->jrow = (float*)take((size_t)m_max * k * 6 * 4);
     b->jc = (int*)take((size_t)m_max * k * 4);
     b->jtr = (float*)take((size_t)n_max * 6 * 4);
@@ -806,15 +1272,10 @@ bool gn_carve(void* ws, size_t bytes, long m_max, int n_max, int k, int kreg, Gn
     b->ap = (float*)take((size_t)n_max * 6 * 4 * 2);  // A p, then the second search-direction buffer
     b->rdepth = (float*)take(m_max * 4);
     b->rreg = (float*)take((size_t)n_max * kreg * 3 * 4);
-    b->partial = (double*)take((size_t)(4096 + 1) * kRed * 8);
-    b->bar = (unsigned*)take(64);
-    b->epart = (double*)take(kEnergyBlocks * 2 * 8);
     b->state = (GnState*)take(sizeof(GnState));
     b->scan_ws = take(scan_workspace_size(m_max > n_max ? m_max : n_max));
     return true;
 }
-
-void gn_init_barrier(const GnBuffers& b, cudaStream_t st) { cudaMemsetAsync(b.bar, 0, 64, st); }
 
 // Per frame: node -> vertex lists and incoming regularisation edges.
 int gn_frame_setup(const GnArgs& a, cudaStream_t st) {
@@ -825,25 +1286,25 @@ int gn_frame_setup(const GnArgs& a, cudaStream_t st) {
     AFX_CUDA(cudaMemsetAsync(b.icur, 0, (a.n_max + 1) * 4, st));
     const long mk = a.m_max * a.k;
     if (mk > 0) {
-        lst_count_kernel<<<blocks_for(mk, 256), 256, 0, st>>>(a);
+        lst_count_kernel<<<grid_for(mk, 256), 256, 0, st>>>(a);
         AFX_LAUNCH_CHECK();
     }
     int rc = scan_exclusive(b.lcnt, b.loff, a.n_max + 1, nullptr, b.scan_ws, st);
     if (rc) return rc;
     if (mk > 0) {
-        lst_fill_kernel<<<blocks_for(mk, 256), 256, 0, st>>>(a);
+        lst_fill_kernel<<<grid_for(mk, 256), 256, 0, st>>>(a);
         AFX_LAUNCH_CHECK();
     }
-    seg_sort_kernel<<<(unsigned)a.n_max, 256, 0, st>>>(b.lst, b.loff, a.n_nodes, a.n_max, a.error);
+    seg_sort_kernel<<<grid_for(a.n_max, 1), 256, 0, st>>>(b.lst, b.loff, a.n_nodes, a.n_max, a.error);
     AFX_LAUNCH_CHECK();
     const long nk = (long)a.n_max * a.kreg;
-    in_count_kernel<<<blocks_for(nk, 256), 256, 0, st>>>(a);
+    in_count_kernel<<<grid_for(nk, 256), 256, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
     rc = scan_exclusive(b.icnt, b.ioff, a.n_max + 1, nullptr, b.scan_ws, st);
     if (rc) return rc;
-    in_fill_kernel<<<blocks_for(nk, 256), 256, 0, st>>>(a);
+    in_fill_kernel<<<grid_for(nk, 256), 256, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
-    seg_sort_kernel<<<(unsigned)a.n_max, 256, 0, st>>>(b.ilst, b.ioff, a.n_nodes, a.n_max, a.error);
+    seg_sort_kernel<<<grid_for(a.n_max, 1), 256, 0, st>>>(b.ilst, b.ioff, a.n_nodes, a.n_max, a.error);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
@@ -870,39 +1331,45 @@ int gn_icp_setup(const GnArgs& a, float* T_pending, const float* T_committed, cu
     if (smem > 48 * 1024) cudaFuncSetAttribute(nbr_discover_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     nbr_discover_kernel<<<nb, 32 * kGnWarps, smem, st>>>(a, words);
     AFX_LAUNCH_CHECK();
-    nbr_ref_kernel<<<blocks_for((long)a.n_max * kMaxNbr, 256), 256, 0, st>>>(a);
+    nbr_ref_kernel<<<grid_for((long)a.n_max * kMaxNbr, 256), 256, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
-    jtj_assemble_kernel<<<nb, 32 * kGnWarps, 0, st>>>(a);
+    jtj_assemble_kernel<<<grid_for(a.n_max, kJtjWarps), 32 * kJtjWarps, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
-    diag_inverse_kernel<<<blocks_for(a.n_max, 128), 128, 0, st>>>(a);
+    diag_inverse_kernel<<<(unsigned)((a.n_max + 3) / 4), 128, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
 
-// One Gauss-Newton iteration (src/VolumeFusion.cu:571-691); `warped` is re-warped with the
-// pending transforms by the caller after this returns.
-int gn_iteration(const GnArgs& a, int iter, const float* warped, float* T_committed, float* T_pending, int pcg_iters,
-                 double tol, cudaStream_t st) {
-    const GnBuffers& b = a.b;
-    residual_kernel<<<kEnergyBlocks, 256, 0, st>>>(a, warped, T_pending);
+// All Gauss-Newton iterations of one ICP iteration (src/VolumeFusion.cu:571-691): one launch
+// of gn_loop_kernel.  On return (stream order) T_committed holds the last accepted transforms,
+// T_pending the last update and `warped` the canonical vertices warped by T_pending.
+int gn_loop(const GnArgs& a, const float* points, float* warped, float* T_committed, float* T_pending, int gn_iters,
+            int pcg_iters, double tol, cudaStream_t st) {
+    if (gn_iters <= 0) return AFX_OK;
+    LoopArgs L;
+    L.g = a;
+    L.points = points;
+    L.warped = warped;
+    L.T_committed = T_committed;
+    L.T_pending = T_pending;
+    L.gn_iters = gn_iters;
+    L.pcg_iters = pcg_iters;
+    L.tol = tol;
+    const int c = gn_cluster_size();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(c);
+    cfg.blockDim = dim3(kLoopThreads);
+    cfg.dynamicSmemBytes = kDsSmem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    AFX_CUDA(cudaLaunchKernelEx(&cfg, gn_loop_kernel, L));
     AFX_LAUNCH_CHECK();
-    energy_kernel<<<1, kEnergyBlocks, 0, st>>>(a, iter);
-    AFX_LAUNCH_CHECK();
-    commit_kernel<<<blocks_for((long)a.n_max * 16, 256), 256, 0, st>>>(a, T_committed, T_pending);
-    AFX_LAUNCH_CHECK();
-    const unsigned nb = (unsigned)((a.n_max + kGnWarps - 1) / kGnWarps);
-    jtr_kernel<<<nb, 32 * kGnWarps, 0, st>>>(a);
-    AFX_LAUNCH_CHECK();
-    PcgArgs P;
-    P.g = a;
-    P.T_pending = T_pending;
-    P.iters = pcg_iters;
-    P.tol = tol;
-    int grid = pcg_grid(a.n_max);
-    void* args[] = {&P};
-    AFX_CUDA(cudaLaunchCooperativeKernel((void*)pcg_kernel, dim3(grid), dim3(32 * kGnWarps), args, 0, st));
-    AFX_LAUNCH_CHECK();
-    (void)b;
     return AFX_OK;
 }
 

@@ -35,7 +35,7 @@ struct GnBuffers {
     int* nbr_ref;          // [N*kMaxNbr] block index (owner*kMaxNbr + slot), negative = transpose of -(ref+1)
     float* blocks;         // [N*kMaxNbr*36] upper blocks (a,b), b > a, row-major
     float* diag;           // [N*36]
-    double* minv;          // [N*36]
+    float* minv;           // [N*36] inverse diagonal blocks (FP64 Gauss-Jordan, stored FP32)
     float* jrow;           // [M*K*6] depth-row Jacobian block of each node-list entry (per ICP iteration)
     int* jc;               // [M*K]   its correspondence index, -1 if the vertex has none
     // per GN iteration
@@ -43,9 +43,6 @@ struct GnBuffers {
     float* rdepth;         // [C_max]
     float* rreg;           // [N*kreg*3]
     float* x, *r, *z, *p, *ap;  // PCG vectors [N*6]
-    double* partial;       // [grid * 4]
-    unsigned* bar;         // grid barrier words [2]
-    double* epart;         // energy partials [kEnergyBlocks * 2]
     void* scan_ws;
     GnState* state;
 };
@@ -77,10 +74,9 @@ struct GnArgs {
 
 size_t gn_workspace_size(long m_max, int n_max, int k, int kreg);
 bool gn_carve(void* ws, size_t bytes, long m_max, int n_max, int k, int kreg, GnBuffers* b);
-void gn_init_barrier(const GnBuffers& b, cudaStream_t st);
 int gn_frame_setup(const GnArgs& a, cudaStream_t st);
 int gn_icp_setup(const GnArgs& a, float* T_pending, const float* T_committed, cudaStream_t st);
-int gn_iteration(const GnArgs& a, int iter, const float* warped, float* T_committed, float* T_pending, int pcg_iters,
-                 double tol, cudaStream_t st);
+int gn_loop(const GnArgs& a, const float* points, float* warped, float* T_committed, float* T_pending, int gn_iters,
+            int pcg_iters, double tol, cudaStream_t st);
 
 }  // namespace afx

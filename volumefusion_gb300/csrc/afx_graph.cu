@@ -173,15 +173,13 @@ AFX_D void grid_insert(const Grid& g, const float* p, int idx, int* error) {
 }
 
 __global__ void graph_check_radii_kernel(GraphState s) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int n = min(*s.n_nodes, s.cap);
-    if (i < n && s.radii[i] != s.r) atomicOr(s.error, ERRF_UNSUPPORTED);
+    const int n = min(*s.n_nodes, s.cap);
+    AFX_GRID_STRIDE(i, n) if (s.radii[i] != s.r) atomicOr(s.error, ERRF_UNSUPPORTED);
 }
 
 __global__ void graph_insert_existing_kernel(GraphState s, const Grid* gp) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int n = min(*s.n_nodes, s.cap);
-    if (i < n) grid_insert(*gp, s.nodes + 3 * i, i, s.error);
+    const int n = min(*s.n_nodes, s.cap);
+    AFX_GRID_STRIDE(i, n) grid_insert(*gp, s.nodes + 3 * i, (int)i, s.error);
 }
 
 // Any node in the grid with distance < r?  (radius test of src/GraphBuilder.cpp:28-34)
@@ -203,20 +201,16 @@ AFX_D bool grid_covered(const Grid& g, const float* nodes, const float* p, float
     return false;
 }
 
+// flags[i] = 1 for live points no node covers (only the live range is read afterwards)
 __global__ void graph_candidates_kernel(GraphState s, const Grid* gp) {
-    long m = min((long)*s.mesh_count, s.mesh_max);
-    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (i >= s.mesh_max) return;
-    unsigned f = 0;
-    if (i < m) f = grid_covered(*gp, s.nodes, s.mesh + 3 * i, s.r) ? 0u : 1u;
-    s.flags[i] = f;
+    const long m = min((long)*s.mesh_count, s.mesh_max);
+    AFX_GRID_STRIDE(i, m) s.flags[i] = grid_covered(*gp, s.nodes, s.mesh + 3 * i, s.r) ? 0u : 1u;
 }
 
 __global__ void graph_compact_kernel(GraphState s, const unsigned* total) {
-    long m = min((long)*s.mesh_count, s.mesh_max);
-    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (i < m && s.flags[i]) s.cand[s.pos[i]] = (unsigned)i;
-    if (i == 0) *s.ncand = *total;
+    const long m = min((long)*s.mesh_count, s.mesh_max);
+    AFX_GRID_STRIDE(i, m) if (s.flags[i]) s.cand[s.pos[i]] = (unsigned)i;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *s.ncand = *total;
 }
 
 // Exact nearest node by expanding rings of grid cells; ties to the lower index.
@@ -255,6 +249,9 @@ __global__ void __launch_bounds__(kChunk) graph_greedy_kernel(GraphState s, cons
     __shared__ unsigned uncovered[kChunk];
     __shared__ int s_nu;
     __shared__ int s_sel[kChunk];
+    __shared__ float s_fac[kChunk];
+    __shared__ float s_upos[kChunk * 3];  // positions of the uncovered candidates
+    __shared__ float s_spos[kChunk * 3];  // positions of the points selected in this chunk
     __shared__ int s_nsel;
     __shared__ int s_stop;
     const Grid g = *gp;
@@ -283,48 +280,80 @@ __global__ void __launch_bounds__(kChunk) graph_greedy_kernel(GraphState s, cons
             s_nu = acc;
         }
         __syncthreads();
-        if (unc) uncovered[wcount[tid >> 5] + __popc(bal & ((1u << lane) - 1))] = s.cand[ci];
-        __syncthreads();
-        // (b) in-order resolution against the nodes selected earlier in this chunk (warp 0)
-        if (tid < 32) {
-            for (int u = 0; u < s_nu; ++u) {
-                const float* p = s.mesh + 3 * (long)uncovered[u];
-                bool hit = false;
-                for (int k = lane; k < s_nsel; k += 32) {
-                    const float* q = s.mesh + 3 * (long)s_sel[k];
-                    if (sqrtf(l2sq_nanoflann(p, q)) < s.r) hit = true;
-                }
-                hit = __any_sync(0xffffffffu, hit);
-                if (!hit && lane == 0) s_sel[s_nsel++] = (int)uncovered[u];
-                __syncwarp();
-            }
+        if (unc) {
+            const int slot = wcount[tid >> 5] + __popc(bal & ((1u << lane) - 1));
+            const unsigned v = s.cand[ci];
+            uncovered[slot] = v;
+            s_upos[3 * slot] = s.mesh[3 * (long)v];
+            s_upos[3 * slot + 1] = s.mesh[3 * (long)v + 1];
+            s_upos[3 * slot + 2] = s.mesh[3 * (long)v + 2];
         }
         __syncthreads();
-        // (c) append the selected points as nodes, in order, with their nearest node's transform
-        if (tid == 0) {
-            int n = *s.n_nodes;
-            for (int k = 0; k < s_nsel; ++k) {
-                if (n >= s.cap) {
-                    atomicOr(s.error, ERRF_CAPACITY);
-                    s_stop = 1;
-                    break;
+        // (b) in-order resolution against the nodes selected earlier in this chunk (warp 0, all
+        // positions in shared memory)
+        if (tid < 32) {
+            int nsel = 0;
+            for (int u = 0; u < s_nu; ++u) {
+                const float* p = s_upos + 3 * u;
+                bool hit = false;
+                for (int k = lane; k < nsel; k += 32)
+                    if (sqrtf(l2sq_nanoflann(p, s_spos + 3 * k)) < s.r) hit = true;
+                hit = __any_sync(0xffffffffu, hit);
+                if (!hit) {
+                    if (lane < 3) s_spos[3 * nsel + lane] = p[lane];
+                    if (lane == 0) s_sel[nsel] = (int)uncovered[u];
+                    ++nsel;
                 }
-                const float* p = s.mesh + 3 * (long)s_sel[k];
-                float bs;
-                int j = nearest_node(g, s.nodes, p, &bs);
-                float d = sqrtf(bs);
-                float factor = d / (0.f + d);
-                for (int e = 0; e < 16; ++e) s.T[16 * (long)n + e] = 0.f + s.T[16 * (long)j + e] * factor;
-                s.nodes[3 * n] = p[0];
-                s.nodes[3 * n + 1] = p[1];
-                s.nodes[3 * n + 2] = p[2];
-                s.radii[n] = s.r;
-                __threadfence();
-                grid_insert(g, p, n, s.error);
-                __threadfence();
-                ++n;
+                __syncwarp();
             }
-            *s.n_nodes = n;
+            if (lane == 0) s_nsel = nsel;
+        }
+        __syncthreads();
+        // (c) append the selected points as nodes, in order, each with the transform of its nearest
+        // node among all nodes before it.  The nearest node is found in parallel: the grid holds
+        // the nodes from before this chunk; the ones selected earlier in the chunk are scanned
+        // directly, after them, so equal distances still go to the lower index.
+        const int n0 = *s.n_nodes;
+        const int take = min(s_nsel, max(s.cap - n0, 0));
+        if (tid < take) {
+            const float* p = s_spos + 3 * tid;
+            float bs;
+            int j = nearest_node(g, s.nodes, p, &bs);
+            for (int q = 0; q < tid; ++q) {
+                const float d = l2sq_nanoflann(p, s_spos + 3 * q);
+                if (d < bs) {
+                    bs = d;
+                    j = n0 + q;
+                }
+            }
+            uncovered[tid] = (unsigned)j;  // reuse: nearest node of selected point tid
+            const float d = sqrtf(bs);
+            s_fac[tid] = d / (0.f + d);
+            const int n = n0 + tid;
+            s.nodes[3 * n] = p[0];
+            s.nodes[3 * n + 1] = p[1];
+            s.nodes[3 * n + 2] = p[2];
+            s.radii[n] = s.r;
+        }
+        __syncthreads();
+        // transforms in order (a node may copy from one selected earlier in the chunk): lane e of
+        // warp 0 owns entry e, so each copy reads what the same lane wrote before
+        if (tid < 16)
+            for (int k = 0; k < take; ++k) {
+                const long j = (long)uncovered[k];
+                s.T[16 * (long)(n0 + k) + tid] = 0.f + s.T[16 * j + tid] * s_fac[k];
+            }
+        __threadfence();
+        __syncthreads();
+        if (tid < take) grid_insert(g, s.mesh + 3 * (long)s_sel[tid], n0 + tid, s.error);
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            *s.n_nodes = n0 + take;
+            if (take < s_nsel) {
+                atomicOr(s.error, ERRF_CAPACITY);
+                s_stop = 1;
+            }
         }
         __syncthreads();
     }
@@ -375,17 +404,17 @@ int build_graph_impl(float* nodes, float* radii, float* T, int* n_nodes, int cap
     AFX_LAUNCH_CHECK();
     graph_bbox_kernel<<<128, 256, 0, st>>>(s);
     AFX_LAUNCH_CHECK();
-    graph_check_radii_kernel<<<blocks_for(cap, 256), 256, 0, st>>>(s);
+    graph_check_radii_kernel<<<grid_for(cap, 256), 256, 0, st>>>(s);
     AFX_LAUNCH_CHECK();
     graph_setup_kernel<<<1, 1, 0, st>>>(s, gdev);
     AFX_LAUNCH_CHECK();
-    graph_insert_existing_kernel<<<blocks_for(cap, 256), 256, 0, st>>>(s, gdev);
+    graph_insert_existing_kernel<<<grid_for(cap, 256), 256, 0, st>>>(s, gdev);
     AFX_LAUNCH_CHECK();
-    graph_candidates_kernel<<<blocks_for(mesh_max, 256), 256, 0, st>>>(s, gdev);
+    graph_candidates_kernel<<<grid_for(mesh_max, 256), 256, 0, st>>>(s, gdev);
     AFX_LAUNCH_CHECK();
     int rc = scan_exclusive_dev(s.flags, s.pos, mesh_count, mesh_max, total, scan_ws, st);
     if (rc) return rc;
-    graph_compact_kernel<<<blocks_for(mesh_max, 256), 256, 0, st>>>(s, total);
+    graph_compact_kernel<<<grid_for(mesh_max, 256), 256, 0, st>>>(s, total);
     AFX_LAUNCH_CHECK();
     graph_greedy_kernel<<<1, kChunk, 0, st>>>(s, gdev);
     AFX_LAUNCH_CHECK();
@@ -398,104 +427,142 @@ int build_graph_impl(float* nodes, float* radii, float* T, int* n_nodes, int cap
 // ------------------------------------------------------------------------------------
 
 constexpr int kKnnTile = 1024;
+constexpr int kKnnThreads = 128;
 
+// One thread per query point (grid-stride over blocks of points, so a block that has no points
+// left loads no nodes).  The running list holds the best KK (distance, index) pairs in
+// registers: a candidate that beats the last entry (or fills an empty slot) replaces it and
+// bubbles up past strictly larger distances, so equal distances keep the earlier index, as the
+// ordered insertion did.  Empty slots carry index -1 and sort last.
 template <int KK>
-__global__ void __launch_bounds__(256) knn_kernel(uint32_t* idx, float* dist, const float* __restrict__ nodes,
-                                                  const int* n_nodes, int n_max, const float* __restrict__ pts,
-                                                  const unsigned* count, long m_max, int k, int excl) {
+__global__ void __launch_bounds__(kKnnThreads) knn_kernel(uint32_t* idx, float* dist, const float* __restrict__ nodes,
+                                                          const int* n_nodes, int n_max, const float* __restrict__ pts,
+                                                          const unsigned* count, long m_max, int k, int excl) {
     __shared__ float s_n[kKnnTile * 3];
     const int n = min(*n_nodes, n_max);
     const long m = count ? min((long)*count, m_max) : m_max;
-    const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    float q[3] = {0.f, 0.f, 0.f};
-    if (i < m) {
-        q[0] = pts[3 * i];
-        q[1] = pts[3 * i + 1];
-        q[2] = pts[3 * i + 2];
-    }
-    const int kk = k + excl;
-    float bd[KK];
-    int bi[KK];
-    int cnt = 0;
-    for (int base = 0; base < n; base += kKnnTile) {
-        const int nt = min(kKnnTile, n - base);
-        __syncthreads();
-        for (int t = threadIdx.x; t < nt * 3; t += blockDim.x) s_n[t] = nodes[3 * (long)base + t];
-        __syncthreads();
-        if (i < m)
-            for (int j = 0; j < nt; ++j) {
-                float d = l2sq_nanoflann(q, s_n + 3 * j);
-                int id = base + j;
-                if (cnt == kk && !(d < bd[kk - 1])) continue;  // equal distance: the earlier index stays
-                int p = (cnt < kk) ? cnt++ : kk - 1;
-                while (p > 0 && d < bd[p - 1]) {
-                    bd[p] = bd[p - 1];
-                    bi[p] = bi[p - 1];
-                    --p;
-                }
-                bd[p] = d;
-                bi[p] = id;
-            }
-    }
-    if (i >= m) return;
-    for (int s = 0; s < k; ++s) {
-        int src = s + excl;
-        if (src < cnt) {
-            idx[i * k + s] = (uint32_t)bi[src];
-            dist[i * k + s] = sqrtf(bd[src]);
-        } else {
-            idx[i * k + s] = AFX_INVALID_INDEX;
-            dist[i * k + s] = FLT_MAX;
+    for (long blk = blockIdx.x; blk * kKnnThreads < m; blk += gridDim.x) {
+        const long i = blk * kKnnThreads + threadIdx.x;
+        float q[3] = {0.f, 0.f, 0.f};
+        if (i < m) {
+            q[0] = pts[3 * i];
+            q[1] = pts[3 * i + 1];
+            q[2] = pts[3 * i + 2];
         }
+        float bd[KK];
+        int bi[KK];
+#pragma unroll
+        for (int s = 0; s < KK; ++s) {
+            bd[s] = 0.f;
+            bi[s] = -1;
+        }
+        for (int base = 0; base < n; base += kKnnTile) {
+            const int nt = min(kKnnTile, n - base);
+            __syncthreads();
+            for (int t = threadIdx.x; t < nt * 3; t += blockDim.x) s_n[t] = nodes[3 * (long)base + t];
+            __syncthreads();
+            if (i < m)
+                for (int j = 0; j < nt; ++j) {
+                    const float d = l2sq_nanoflann(q, s_n + 3 * j);
+                    if (bi[KK - 1] >= 0 && !(d < bd[KK - 1])) continue;
+                    bd[KK - 1] = d;
+                    bi[KK - 1] = base + j;
+#pragma unroll
+                    for (int p = KK - 1; p > 0; --p) {
+                        if (bi[p - 1] < 0 || bd[p] < bd[p - 1]) {
+                            const float td = bd[p];
+                            bd[p] = bd[p - 1];
+                            bd[p - 1] = td;
+                            const int ti = bi[p];
+                            bi[p] = bi[p - 1];
+                            bi[p - 1] = ti;
+                        }
+                    }
+                }
+        }
+        if (i < m)
+#pragma unroll
+            for (int s = 0; s < KK; ++s) {
+                const int o = s - excl;
+                if (o < 0 || o >= k) continue;
+                if (bi[s] >= 0) {
+                    idx[i * k + o] = (uint32_t)bi[s];
+                    dist[i * k + o] = sqrtf(bd[s]);
+                } else {
+                    idx[i * k + o] = AFX_INVALID_INDEX;
+                    dist[i * k + o] = FLT_MAX;
+                }
+            }
     }
 }
 
 int knn_impl(uint32_t* idx, float* dist, const float* nodes, const int* n_nodes, int n_max, const float* pts,
              const unsigned* count, long m_max, int k, int excl, cudaStream_t st) {
     if (m_max <= 0) return AFX_OK;
-    const int kk = k + (excl ? 1 : 0);
-    unsigned blocks = blocks_for(m_max, 256);
-    if (kk <= 4) knn_kernel<4><<<blocks, 256, 0, st>>>(idx, dist, nodes, n_nodes, n_max, pts, count, m_max, k, excl ? 1 : 0);
-    else if (kk <= 9) knn_kernel<9><<<blocks, 256, 0, st>>>(idx, dist, nodes, n_nodes, n_max, pts, count, m_max, k, excl ? 1 : 0);
-    else if (kk <= 17) knn_kernel<17><<<blocks, 256, 0, st>>>(idx, dist, nodes, n_nodes, n_max, pts, count, m_max, k, excl ? 1 : 0);
-    else return AFX_ERR_UNSUPPORTED;
+    const int e = excl ? 1 : 0;
+    const int kk = k + e;
+    const long want = (m_max + kKnnThreads - 1) / kKnnThreads;
+    const unsigned blocks = (unsigned)(want < 4096 ? want : 4096);
+#define AFX_KNN(KK)                                                                                              \
+    knn_kernel<KK><<<blocks, kKnnThreads, 0, st>>>(idx, dist, nodes, n_nodes, n_max, pts, count, m_max, k, e); \
+    break
+    switch (kk) {
+        case 1: AFX_KNN(1);
+        case 2: AFX_KNN(2);
+        case 3: AFX_KNN(3);
+        case 4: AFX_KNN(4);
+        case 5: AFX_KNN(5);
+        case 6: AFX_KNN(6);
+        case 7: AFX_KNN(7);
+        case 8: AFX_KNN(8);
+        case 9: AFX_KNN(9);
+        default:
+            if (kk <= 12) {
+                AFX_KNN(12);
+            } else if (kk <= 17) {
+                AFX_KNN(17);
+            } else {
+                return AFX_ERR_UNSUPPORTED;
+            }
+    }
+#undef AFX_KNN
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
 
 __global__ void filter_disconnected_kernel(uint32_t* idx, float* dist, const int* n_nodes, int n_max, int k,
                                            const float* radii) {
-    int n = min(*n_nodes, n_max);
-    long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (t >= (long)n * k) return;
-    long i = t / k;
-    uint32_t nb = idx[t];
-    if (nb >= (uint32_t)n) return;
-    if (dist[t] <= radii[i] * 1.3f) return;
-    idx[t] = AFX_INVALID_INDEX;
-    dist[t] = FLT_MAX;
+    const int n = min(*n_nodes, n_max);
+    AFX_GRID_STRIDE(t, (long)n * k) {
+        const long i = t / k;
+        const uint32_t nb = idx[t];
+        if (nb >= (uint32_t)n) continue;
+        if (dist[t] <= radii[i] * 1.3f) continue;
+        idx[t] = AFX_INVALID_INDEX;
+        dist[t] = FLT_MAX;
+    }
 }
 
 // computeWarpWeightsKernel (src/VertexManipulation.cu:105-132)
 __global__ void warp_weights_kernel(float* w, const float* radii, const uint32_t* idx, const float* dist,
                                     const unsigned* count, long m_max, int k, const int* n_nodes) {
-    long m = count ? min((long)*count, m_max) : m_max;
-    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    int n = *n_nodes;
-    float ws[17];
-    float sum = 0.f;
-    for (int j = 0; j < k; ++j) {
-        uint32_t nb = idx[i * k + j];
-        float wj = 0.f;
-        if (nb < (uint32_t)n) {
-            float r = radii[nb], d = dist[i * k + j];
-            wj = (d >= r) ? 0.f : afx_expf(-(d * d) / (2.0f * (r * r)));
+    const long m = count ? min((long)*count, m_max) : m_max;
+    const int n = *n_nodes;
+    AFX_GRID_STRIDE(i, m) {
+        float ws[17];
+        float sum = 0.f;
+        for (int j = 0; j < k; ++j) {
+            uint32_t nb = idx[i * k + j];
+            float wj = 0.f;
+            if (nb < (uint32_t)n) {
+                float r = radii[nb], d = dist[i * k + j];
+                wj = (d >= r) ? 0.f : afx_expf(-(d * d) / (2.0f * (r * r)));
+            }
+            ws[j] = wj;
+            sum = sum + wj;
         }
-        ws[j] = wj;
-        sum = sum + wj;
+        for (int j = 0; j < k; ++j) w[i * k + j] = (sum != 0.f) ? ws[j] / sum : ws[j];
     }
-    for (int j = 0; j < k; ++j) w[i * k + j] = (sum != 0.f) ? ws[j] / sum : ws[j];
 }
 
 // warpKernel (src/ComputeCorrespondence.cu:5-30)
@@ -503,36 +570,36 @@ __global__ void warp_kernel(float* out, const float* __restrict__ pts, const flo
                             const uint32_t* __restrict__ idx, const float* __restrict__ w, const unsigned* count,
                             long m_max, int k) {
     long m = count ? min((long)*count, m_max) : m_max;
-    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    float p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
-    bool zero = true;
-    for (int j = 0; j < k; ++j)
-        if (!(fabsf(w[i * k + j]) <= 1e-5f)) zero = false;
-    float acc[3] = {p[0], p[1], p[2]};
-    if (!zero) {
-        acc[0] = acc[1] = acc[2] = 0.f;
-        for (int j = 0; j < k; ++j) {
-            uint32_t nb = idx[i * k + j];
-            if (nb == AFX_INVALID_INDEX) continue;
-            float o[3];
-            mat4_point(T + 16 * (long)nb, p, o);
-            float wj = w[i * k + j];
-            acc[0] = acc[0] + wj * o[0];
-            acc[1] = acc[1] + wj * o[1];
-            acc[2] = acc[2] + wj * o[2];
+    AFX_GRID_STRIDE(i, m) {
+        float p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+        bool zero = true;
+        for (int j = 0; j < k; ++j)
+            if (!(fabsf(w[i * k + j]) <= 1e-5f)) zero = false;
+        float acc[3] = {p[0], p[1], p[2]};
+        if (!zero) {
+            acc[0] = acc[1] = acc[2] = 0.f;
+            for (int j = 0; j < k; ++j) {
+                uint32_t nb = idx[i * k + j];
+                if (nb == AFX_INVALID_INDEX) continue;
+                float o[3];
+                mat4_point(T + 16 * (long)nb, p, o);
+                float wj = w[i * k + j];
+                acc[0] = acc[0] + wj * o[0];
+                acc[1] = acc[1] + wj * o[1];
+                acc[2] = acc[2] + wj * o[2];
+            }
         }
+        out[3 * i] = acc[0];
+        out[3 * i + 1] = acc[1];
+        out[3 * i + 2] = acc[2];
     }
-    out[3 * i] = acc[0];
-    out[3 * i + 1] = acc[1];
-    out[3 * i + 2] = acc[2];
 }
 
 int warp_weights_impl(float* w, const float* radii, const uint32_t* idx, const float* dist, const unsigned* count,
                       long m_max, int k, const int* n_nodes, cudaStream_t st) {
     if (m_max <= 0) return AFX_OK;
     if (k > 17) return AFX_ERR_UNSUPPORTED;
-    warp_weights_kernel<<<blocks_for(m_max, 256), 256, 0, st>>>(w, radii, idx, dist, count, m_max, k, n_nodes);
+    warp_weights_kernel<<<grid_for(m_max, 256), 256, 0, st>>>(w, radii, idx, dist, count, m_max, k, n_nodes);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
@@ -540,7 +607,7 @@ int warp_weights_impl(float* w, const float* radii, const uint32_t* idx, const f
 int warp_impl(float* out, const float* pts, const float* T, const uint32_t* idx, const float* w, const unsigned* count,
               long m_max, int k, cudaStream_t st) {
     if (m_max <= 0) return AFX_OK;
-    warp_kernel<<<blocks_for(m_max, 256), 256, 0, st>>>(out, pts, T, idx, w, count, m_max, k);
+    warp_kernel<<<grid_for(m_max, 256), 256, 0, st>>>(out, pts, T, idx, w, count, m_max, k);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
@@ -578,27 +645,27 @@ AFX_D int corr_pixel(const CorrArgs& a, long i) {
 
 __global__ void corr_flags_kernel(CorrArgs a, unsigned* flags, int* pix) {
     long m = a.count ? min((long)*a.count, a.m_max) : a.m_max;
-    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    int px = corr_pixel(a, i);
-    pix[i] = px;
-    flags[i] = px >= 0 ? 1u : 0u;
+    AFX_GRID_STRIDE(i, m) {
+        int px = corr_pixel(a, i);
+        pix[i] = px;
+        flags[i] = px >= 0 ? 1u : 0u;
+    }
 }
 
 __global__ void corr_scatter_kernel(CorrArgs a, const unsigned* flags, const int* pix, const unsigned* pos, int* corr,
                                     long cap, int* corr_of_vertex) {
     long m = a.count ? min((long)*a.count, a.m_max) : a.m_max;
-    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    if (flags[i]) {
-        unsigned p = pos[i];
-        if (p < cap) {
-            corr[2 * (long)p] = (int)i;
-            corr[2 * (long)p + 1] = pix[i];
+    AFX_GRID_STRIDE(i, m) {
+        if (flags[i]) {
+            unsigned p = pos[i];
+            if (p < cap) {
+                corr[2 * (long)p] = (int)i;
+                corr[2 * (long)p + 1] = pix[i];
+            }
+            if (corr_of_vertex) corr_of_vertex[i] = (int)p;
+        } else if (corr_of_vertex) {
+            corr_of_vertex[i] = -1;
         }
-        if (corr_of_vertex) corr_of_vertex[i] = (int)p;
-    } else if (corr_of_vertex) {
-        corr_of_vertex[i] = -1;
     }
 }
 
@@ -630,11 +697,11 @@ int correspondences_impl(int* corr, unsigned* corr_count, long cap, const float*
     a.cols = cols;
     a.frame = frame;
     a.thresh = thresh;
-    corr_flags_kernel<<<blocks_for(m_max, 256), 256, 0, st>>>(a, flags, pix);
+    corr_flags_kernel<<<grid_for(m_max, 256), 256, 0, st>>>(a, flags, pix);
     AFX_LAUNCH_CHECK();
     int rc = scan_exclusive_dev(flags, pos, count, m_max, corr_count, scan_ws, st);
     if (rc) return rc;
-    corr_scatter_kernel<<<blocks_for(m_max, 256), 256, 0, st>>>(a, flags, pix, pos, corr, cap, corr_of_vertex);
+    corr_scatter_kernel<<<grid_for(m_max, 256), 256, 0, st>>>(a, flags, pix, pos, corr, cap, corr_of_vertex);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
@@ -698,7 +765,7 @@ int afx_filter_disconnected(uint32_t* idx, float* dist, const int* n_nodes, int 
                             void* stream) {
     if (!idx || !dist || !n_nodes || !radii || k < 1) return AFX_ERR_INVALID_ARGUMENT;
     if (n_nodes_max <= 0) return AFX_OK;
-    filter_disconnected_kernel<<<blocks_for((long)n_nodes_max * k, 256), 256, 0, as_stream(stream)>>>(
+    filter_disconnected_kernel<<<grid_for((long)n_nodes_max * k, 256), 256, 0, as_stream(stream)>>>(
         idx, dist, n_nodes, n_nodes_max, k, radii);
     AFX_LAUNCH_CHECK();
     return AFX_OK;

@@ -140,21 +140,22 @@ AFX_D bool node_cube(const float* node_t, const Volume& vol, const int* per, Nod
 }
 
 __global__ void brick_count_kernel(SupportArgs a) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= min(*a.n_nodes, a.n_max)) return;
+    const int n = min(*a.n_nodes, a.n_max);
+    AFX_GRID_STRIDE(j, n) {
     NodeCube c;
-    if (!node_cube(a.nodes + 3 * j, a.vol, a.per, &c)) return;
+    if (!node_cube(a.nodes + 3 * j, a.vol, a.per, &c)) continue;
     for (int bz = c.lo[2] / kBrick; bz <= c.hi[2] / kBrick; ++bz)
         for (int by = c.lo[1] / kBrick; by <= c.hi[1] / kBrick; ++by)
             for (int bx = c.lo[0] / kBrick; bx <= c.hi[0] / kBrick; ++bx)
                 atomicAdd(a.brick_count + ((long)bz * a.bg.nb[1] + by) * a.bg.nb[0] + bx, 1u);
+    }
 }
 
 __global__ void brick_fill_kernel(SupportArgs a) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= min(*a.n_nodes, a.n_max)) return;
+    const int n = min(*a.n_nodes, a.n_max);
+    AFX_GRID_STRIDE(j, n) {
     NodeCube c;
-    if (!node_cube(a.nodes + 3 * j, a.vol, a.per, &c)) return;
+    if (!node_cube(a.nodes + 3 * j, a.vol, a.per, &c)) continue;
     for (int bz = c.lo[2] / kBrick; bz <= c.hi[2] / kBrick; ++bz)
         for (int by = c.lo[1] / kBrick; by <= c.hi[1] / kBrick; ++by)
             for (int bx = c.lo[0] / kBrick; bx <= c.hi[0] / kBrick; ++bx) {
@@ -163,12 +164,12 @@ __global__ void brick_fill_kernel(SupportArgs a) {
                 if (pos < a.pair_capacity) a.brick_nodes[pos] = (unsigned)j;
                 else atomicOr(a.error, ERRF_CAPACITY);
             }
+    }
 }
 
 __global__ void brick_active_kernel(const unsigned* brick_count, long nb, unsigned* active, unsigned* n_active) {
-    long b = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (b >= nb) return;
-    bool on = brick_count[b] > 0;
+    const long b = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    const bool on = b < nb && brick_count[b] > 0;  // every lane takes part in the ballot
     unsigned m = __ballot_sync(0xffffffffu, on);
     unsigned base = 0;
     int lane = threadIdx.x & 31;
@@ -209,8 +210,10 @@ __global__ void __launch_bounds__(kBrickVox) brick_warp_kernel(WarpArgs a) {
     __shared__ float s_rad[kMaxBrickNodes];
     __shared__ int s_lo[kMaxBrickNodes * 3], s_hi[kMaxBrickNodes * 3];
     __shared__ int s_id[kMaxBrickNodes];
-    const unsigned slot = blockIdx.x;
-    if (slot >= *a.n_active) return;
+    const unsigned n_active = *a.n_active;
+    for (unsigned slot = blockIdx.x; slot < n_active; slot += gridDim.x) {
+    __syncthreads();  // the previous brick's staged nodes are no longer read
+    [&] {
     const unsigned b = a.active[slot];
     const unsigned off = a.brick_offset[b];
     const int nc = min((int)a.brick_count[b], kMaxBrickNodes);
@@ -308,12 +311,14 @@ __global__ void __launch_bounds__(kBrickVox) brick_warp_kernel(WarpArgs a) {
     wv.p[2] = q[2];
     wv.target = target;
     a.out[local] = wv;
+    }();
+    }
 }
 
 // integrateWarpedTSDFFromFrameKernel (src/TSDFIntegration.cu:173-226) over the active bricks
 __global__ void __launch_bounds__(kBrickVox) brick_integrate_kernel(WarpedIntegrateArgs a) {
-    const unsigned slot = blockIdx.x;
-    if (slot >= *a.n_active) return;
+    const unsigned n_active = *a.n_active;
+    for (unsigned slot = blockIdx.x; slot < n_active; slot += gridDim.x) [&] {
     const long local = (long)slot * kBrickVox + threadIdx.x;
     if (a.in_count[local] == 0) return;
     const WarpedVoxel wv = a.in[local];
@@ -330,6 +335,7 @@ __global__ void __launch_bounds__(kBrickVox) brick_integrate_kernel(WarpedIntegr
     tsdf_blend(t, w, tn);
     a.tsdf[v] = t;
     a.weights[v] = w;
+    }();
 }
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -393,13 +399,13 @@ int build_support(const SupportWorkspace& s, const Volume& vol, const int* per, 
     a.pair_capacity = s.pair_capacity;
     a.error = error;
     if (n_max > 0) {
-        brick_count_kernel<<<blocks_for(n_max, 128), 128, 0, st>>>(a);
+        brick_count_kernel<<<grid_for(n_max, 128), 128, 0, st>>>(a);
         AFX_LAUNCH_CHECK();
     }
     int rc = scan_exclusive(s.brick_count, s.brick_offset, bg.n, nullptr, s.scan_tmp, st);
     if (rc) return rc;
     if (n_max > 0) {
-        brick_fill_kernel<<<blocks_for(n_max, 128), 128, 0, st>>>(a);
+        brick_fill_kernel<<<grid_for(n_max, 128), 128, 0, st>>>(a);
         AFX_LAUNCH_CHECK();
     }
     brick_active_kernel<<<blocks_for(bg.n, 256), 256, 0, st>>>(s.brick_count, bg.n, s.active, s.n_active);
@@ -407,11 +413,14 @@ int build_support(const SupportWorkspace& s, const Volume& vol, const int* per, 
     return AFX_OK;
 }
 
+// Block-stride grid over the active bricks (their number is on the device).
+static unsigned brick_grid(long max_active) { return (unsigned)(max_active < 608 ? max_active : 608); }
+
 int launch_brick_warp(const WarpArgs& a, long max_active, cudaStream_t st) {
     if (max_active <= 0) return AFX_OK;
     switch (a.k <= 4 ? 4 : 8) {
-        case 4: brick_warp_kernel<4><<<(unsigned)max_active, kBrickVox, 0, st>>>(a); break;
-        default: brick_warp_kernel<8><<<(unsigned)max_active, kBrickVox, 0, st>>>(a); break;
+        case 4: brick_warp_kernel<4><<<brick_grid(max_active), kBrickVox, 0, st>>>(a); break;
+        default: brick_warp_kernel<8><<<brick_grid(max_active), kBrickVox, 0, st>>>(a); break;
     }
     AFX_LAUNCH_CHECK();
     return AFX_OK;
@@ -419,7 +428,7 @@ int launch_brick_warp(const WarpArgs& a, long max_active, cudaStream_t st) {
 
 int launch_brick_integrate(const WarpedIntegrateArgs& a, long max_active, cudaStream_t st) {
     if (max_active <= 0) return AFX_OK;
-    brick_integrate_kernel<<<(unsigned)max_active, kBrickVox, 0, st>>>(a);
+    brick_integrate_kernel<<<brick_grid(max_active), kBrickVox, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }

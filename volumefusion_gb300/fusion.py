@@ -64,6 +64,10 @@ class FusionSession:
         s = self.stream if self.stream is not None else torch.cuda.current_stream()
         return C.c_void_p(s.cuda_stream)
 
+    def reset(self):
+        """Start a new sequence: empty volume and graph (stream-ordered, no allocation)."""
+        check(lib().afx_fusion_reset(self.h, self._st()), "afx_fusion_reset")
+
     def process(self, depth_mm):
         """depth_mm: uint16/int16 CUDA tensor (H, W) or host numpy uint16 array."""
         if isinstance(depth_mm, np.ndarray):
