@@ -217,20 +217,19 @@ __global__ void nbr_ref_kernel(GnArgs a) {
 // J^T J: node a's warp accumulates D_a and its upper blocks (a, b > a).  Lane l owns block
 // entries l and l + 32 of every block; each entry is summed in a fixed sequential order:
 // depth rows by ascending node-list entry, then regularisation rows by ascending row.  The
-// per-row inputs (normals, points, weights, target slots) are staged 32 rows at a time by the
-// whole warp, the upper blocks accumulate in shared memory, so the ordered loop touches no
-// global memory.
+// rows are staged 32 at a time, one per lane, with their Jacobian blocks already formed
+// (jdepth for every contributing slot, or lam_r * G for a regularisation row), so the ordered
+// loop is shared-memory loads and adds only; the upper blocks accumulate in shared memory.
 constexpr int kJtjWarps = 2;
 constexpr int kJtjMaxK = 8;
 
 struct JtjStage {
-    float blk[kMaxNbr * 36];   // upper blocks of this node
-    int L[kMaxNbr];            // sorted neighbour ids
-    float nrm[32][3];          // depth rows: frame normal
-    float pt[32][3];           //             canonical vertex (or node position for a reg row)
-    float w[32][kJtjMaxK];     //             skinning weights
-    signed char slot[32][kJtjMaxK];  // -1: diagonal, >= 0: upper block, -2: no contribution
-    int own[32];               // depth rows: the row's own slot s, or -1 without correspondence
+    float blk[kMaxNbr * 36];           // upper blocks of this node
+    int L[kMaxNbr];                    // sorted neighbour ids
+    float J[32][kJtjMaxK][6];          // depth rows: jdepth of each slot; reg rows: lam_r * G (3 x 6)
+    signed char slot[32][kJtjMaxK];    // -1: diagonal, >= 0: upper block, -2: no contribution
+    int own[32];                       // depth rows: the row's own slot, -1 without correspondence;
+                                       // reg rows: 1 own edge, 0 incoming edge, -1 skipped
 };
 
 AFX_D int find_slot(const int* L, int cnt, int b) {
@@ -242,25 +241,6 @@ AFX_D int find_slot(const int* L, int cnt, int b) {
         else hi = mid - 1;
     }
     return -1;
-}
-
-// Column q of grad_rows(p): (G[0][q], G[1][q], G[2][q]).
-AFX_D void gcol(const float* p, int q, float c[3]) {
-    switch (q) {
-        case 0: c[0] = 0.f; c[1] = -p[2]; c[2] = p[1]; break;
-        case 1: c[0] = p[2]; c[1] = 0.f; c[2] = -p[0]; break;
-        case 2: c[0] = -p[1]; c[1] = p[0]; c[2] = 0.f; break;
-        case 3: c[0] = 1.f; c[1] = 0.f; c[2] = 0.f; break;
-        case 4: c[0] = 0.f; c[1] = 1.f; c[2] = 0.f; break;
-        default: c[0] = 0.f; c[1] = 0.f; c[2] = 1.f; break;
-    }
-}
-
-// Component q of jdepth(n, w, G, lam), from column q of G (zero below the weight cut-off).
-AFX_D float jdepth_q(const float* n, float w, const float c[3], float lam) {
-    if (w < 1.e-4f) return 0.f;
-    const float nw0 = n[0] * w, nw1 = n[1] * w, nw2 = n[2] * w;
-    return (nw0 * c[0] + (nw1 * c[1] + nw2 * c[2])) * lam;
 }
 
 __global__ void __launch_bounds__(32 * kJtjWarps) jtj_assemble_kernel(GnArgs a) {
@@ -292,17 +272,14 @@ __global__ void __launch_bounds__(32 * kJtjWarps) jtj_assemble_kernel(GnArgs a) 
                 S.own[lane] = c < 0 ? -1 : s;
                 if (c >= 0) {
                     const int px = a.corr[2 * (long)c + 1];
-                    float nrm[3], p[3];
-                    for (int q = 0; q < 3; ++q) {
-                        nrm[q] = a.normals[3 * (long)px + q];
-                        p[q] = a.mesh[3 * v + q];
-                        S.nrm[lane][q] = nrm[q];
-                        S.pt[lane][q] = p[q];
-                    }
+                    const float nrm[3] = {a.normals[3 * (long)px], a.normals[3 * (long)px + 1],
+                                          a.normals[3 * (long)px + 2]};
+                    const float p[3] = {a.mesh[3 * v], a.mesh[3 * v + 1], a.mesh[3 * v + 2]};
+                    float G[3][6];
+                    grad_rows(p, G);
                     for (int tt = 0; tt < k; ++tt) {
                         const float wt = a.mw[v * k + tt];
                         const uint32_t bnode = a.midx[v * k + tt];
-                        S.w[lane][tt] = wt;
                         int sl = -2;
                         if (wt != 0.f && bnode >= (uint32_t)node) {
                             if (bnode == (uint32_t)node) sl = -1;
@@ -312,13 +289,16 @@ __global__ void __launch_bounds__(32 * kJtjWarps) jtj_assemble_kernel(GnArgs a) 
                             }
                         }
                         S.slot[lane][tt] = (signed char)sl;
+                        if (sl != -2 || tt == s) {
+                            float Jt[6];
+                            jdepth(nrm, wt, G, a.lam_d, Jt);
+#pragma unroll
+                            for (int q = 0; q < 6; ++q) S.J[lane][tt][q] = Jt[q];
+                            if (tt == s)  // this row's J block, for J^T r
+#pragma unroll
+                                for (int q = 0; q < 6; ++q) a.b.jrow[(long)t * 6 + q] = Jt[q];
+                        }
                     }
-                    // this row's J block for J^T r (jtr_node)
-                    float G[3][6];
-                    grad_rows(p, G);
-                    float Ja[6];
-                    jdepth(nrm, S.w[lane][s], G, a.lam_d, Ja);
-                    for (int q = 0; q < 6; ++q) a.b.jrow[(long)t * 6 + q] = Ja[q];
                 }
             }
             __syncwarp();
@@ -328,21 +308,13 @@ __global__ void __launch_bounds__(32 * kJtjWarps) jtj_assemble_kernel(GnArgs a) 
                 const int s = S.own[r];
                 if (s < 0) continue;
                 touched = true;
-                float ci0[3], cj0[3], ci1[3], cj1[3];
-                gcol(S.pt[r], i0, ci0);
-                gcol(S.pt[r], j0, cj0);
-                gcol(S.pt[r], i1 < 6 ? i1 : 0, ci1);
-                gcol(S.pt[r], j1, cj1);
-                const float* nrm = S.nrm[r];
-                const float wa = S.w[r][s];
-                const float ja0 = jdepth_q(nrm, wa, ci0, a.lam_d);
-                const float ja1 = has1 ? jdepth_q(nrm, wa, ci1, a.lam_d) : 0.f;
+                const float ja0 = S.J[r][s][i0];
+                const float ja1 = has1 ? S.J[r][s][i1] : 0.f;
                 for (int tt = 0; tt < k; ++tt) {
                     const int sl = S.slot[r][tt];
                     if (sl == -2) continue;
-                    const float wt = S.w[r][tt];
-                    const float jb0 = jdepth_q(nrm, wt, cj0, a.lam_d);
-                    const float jb1 = has1 ? jdepth_q(nrm, wt, cj1, a.lam_d) : 0.f;
+                    const float jb0 = S.J[r][tt][j0];
+                    const float jb1 = S.J[r][tt][j1];
                     if (sl == -1) {
                         d0 = d0 + ja0 * jb0;
                         if (has1) d1 = d1 + ja1 * jb1;
@@ -379,10 +351,14 @@ __global__ void __launch_bounds__(32 * kJtjWarps) jtj_assemble_kernel(GnArgs a) 
                     kk = (int)(ent % a.kreg);
                 }
                 const uint32_t nbk = a.gidx[(long)src * a.kreg + kk];
-                bool live = true;
-                if (src == node && nbk >= (uint32_t)n) live = false;  // own edge filtered out
+                const bool live = !(src == node && nbk >= (uint32_t)n);  // own edge filtered out
                 S.own[lane] = live ? (src == node ? 1 : 0) : -1;
-                for (int q = 0; q < 3; ++q) S.pt[lane][q] = a.nodes[3 * (long)src + q];
+                float G[3][6];
+                grad_rows(a.nodes + 3 * (long)src, G);
+#pragma unroll
+                for (int ax = 0; ax < 3; ++ax)
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) S.J[lane][ax][q] = G[ax][q] * a.lam_r;
                 const int other = (src == node) ? (int)nbk : src;
                 int sl = -2;
                 if (other > node) {
@@ -397,16 +373,11 @@ __global__ void __launch_bounds__(32 * kJtjWarps) jtj_assemble_kernel(GnArgs a) 
                 const int self = S.own[rr];
                 if (self < 0) continue;
                 touched = true;
-                float ci0[3], cj0[3], ci1[3], cj1[3];
-                gcol(S.pt[rr], i0, ci0);
-                gcol(S.pt[rr], j0, cj0);
-                gcol(S.pt[rr], i1 < 6 ? i1 : 0, ci1);
-                gcol(S.pt[rr], j1, cj1);
                 const int sl = S.slot[rr][0];
 #pragma unroll
                 for (int ax = 0; ax < 3; ++ax) {
-                    const float g_i0 = ci0[ax] * a.lam_r, g_j0 = cj0[ax] * a.lam_r;
-                    const float g_i1 = has1 ? ci1[ax] * a.lam_r : 0.f, g_j1 = has1 ? cj1[ax] * a.lam_r : 0.f;
+                    const float g_i0 = S.J[rr][ax][i0], g_j0 = S.J[rr][ax][j0];
+                    const float g_i1 = has1 ? S.J[rr][ax][i1] : 0.f, g_j1 = S.J[rr][ax][j1];
                     // this node is `src` (coefficient +g) or the edge's target (coefficient -g)
                     const float n_i0 = self ? g_i0 : -g_i0, n_j0 = self ? g_j0 : -g_j0;
                     const float n_i1 = self ? g_i1 : -g_i1, n_j1 = self ? g_j1 : -g_j1;
@@ -755,13 +726,15 @@ AFX_D void dsmem_store_f64(double* local, unsigned rank, double v) {
 
 // Cluster sum through the slot arrays: the CTA's block total is written into slot[ph][rank] of
 // every CTA; after the barrier each CTA adds the slots in rank order.
+// `live` (warp-uniform) is false for warps whose lanes hold only zeros: they skip the FP64
+// butterfly (FP64 issue is scarce on this part) and contribute an exact 0.
 template <int NV>
-AFX_D void ds_sum(double (&v)[NV], const DsLayout& d, ClusterSums& cs, int& ph) {
+AFX_D void ds_sum(double (&v)[NV], const DsLayout& d, ClusterSums& cs, int& ph, bool live = true) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned rank = cluster_rank(), ncta = cluster_size();
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-        double s = warp_sum(v[i]);
+        const double s = live ? warp_sum(v[i]) : 0.0;
         if (lane == 0) cs.warp[w * 4 + i] = s;
     }
     __syncthreads();
@@ -781,7 +754,7 @@ AFX_D void ds_sum(double (&v)[NV], const DsLayout& d, ClusterSums& cs, int& ph) 
         for (int i = 0; i < NV; ++i) {
             double t = lane < (int)ncta ? d.slot[(ph * kDsMaxCta + lane) * 4 + i] : 0.0;
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+            for (int o = kDsMaxCta / 2; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
             if (lane == 0) cs.total[i] = t;
         }
     }
@@ -853,6 +826,7 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
     const int grp = lane / 6, ei = lane - 6 * grp;
     const int li = w * 5 + grp;  // kLoopWarps * 5 >= kDsNpc: one own node per lane group
     const bool act = lane < 30 && li < own;
+    const bool live = w * 5 < own;  // this warp owns at least one node
     const int o = li * 6 + ei;
     const int gnode = start + li;
     // x = 0, r = b, z = M^-1 r
@@ -873,7 +847,7 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
             d2[1] += (double)ji * (double)ji;
         }
     }
-    ds_sum<2>(d2, d, cs, ph);
+    ds_sum<2>(d2, d, cs, ph, live);
     double rz = d2[0];
     const double bnorm2 = d2[1];
     float beta = 0.f;
@@ -900,7 +874,7 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
             d.ap[o] = api;
             pap[0] += (double)pi * (double)api;
         }
-        ds_sum<1>(pap, d, cs, ph);
+        ds_sum<1>(pap, d, cs, ph, live);
         if (pap[0] == 0.0 || !(pap[0] == pap[0])) break;
         const float alpha = (float)(rz / pap[0]);
         double q2[2] = {0.0, 0.0};
@@ -921,7 +895,7 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
             q2[0] += (double)rv * (double)zi;
             q2[1] += (double)rv * (double)rv;
         }
-        ds_sum<2>(q2, d, cs, ph);
+        ds_sum<2>(q2, d, cs, ph, live);
         beta = (float)(q2[0] / rz);
         rz = q2[0];
         if (L.tol > 0 && q2[1] <= L.tol * L.tol * bnorm2) break;

@@ -31,6 +31,7 @@ namespace afx {
 constexpr int kGridSlots = 32;
 constexpr int kGridMaxCells = 1 << 18;
 constexpr int kChunk = 1024;
+constexpr int kNearestBrute = 1024;  // nearest existing node by a scan below this many nodes
 
 struct Grid {
     float org[3];
@@ -317,8 +318,19 @@ __global__ void __launch_bounds__(kChunk) graph_greedy_kernel(GraphState s, cons
         const int take = min(s_nsel, max(s.cap - n0, 0));
         if (tid < take) {
             const float* p = s_spos + 3 * tid;
-            float bs;
-            int j = nearest_node(g, s.nodes, p, &bs);
+            float bs = FLT_MAX;
+            int j = -1;
+            if (n0 <= kNearestBrute) {  // few nodes: a scan beats expanding rings over a sparse grid
+                for (int q = 0; q < n0; ++q) {
+                    const float d = l2sq_nanoflann(p, s.nodes + 3 * (long)q);
+                    if (d < bs) {
+                        bs = d;
+                        j = q;
+                    }
+                }
+            } else {
+                j = nearest_node(g, s.nodes, p, &bs);
+            }
             for (int q = 0; q < tid; ++q) {
                 const float d = l2sq_nanoflann(p, s_spos + 3 * q);
                 if (d < bs) {

@@ -90,23 +90,6 @@ AFX_D void edge_vertex(const float* __restrict__ tsdf, const Volume& vol, int x,
     for (int c = 0; c < 3; ++c) o[c] = (float)__dadd_rn((double)p0[c], __dmul_rn(mu, (double)(p1[c] - p0[c])));
 }
 
-AFX_D int cube_index(const float* __restrict__ tsdf, const float* __restrict__ w, const Volume& vol, int x, int y,
-                     int z, float iso) {
-    const int X = vol.dims[0], Y = vol.dims[1];
-    long off[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) off[c] = ((long)(z + c_corner[c][2]) * Y + (y + c_corner[c][1])) * X + x + c_corner[c][0];
-    bool any_zero = false;
-#pragma unroll
-    for (int c = 0; c < 8; ++c) any_zero |= (__ldg(w + off[c]) == 0.0f);
-    if (any_zero) return 0;
-    int idx = 0;
-#pragma unroll
-    for (int c = 0; c < 8; ++c)
-        if (__ldg(tsdf + off[c]) > iso) idx |= 1 << c;
-    return idx;
-}
-
 AFX_D bool vne(const float* a, const float* b) { return a[0] != b[0] || a[1] != b[1] || a[2] != b[2]; }
 
 // Warp-aggregated append: returns this lane's base index for `n` items.
@@ -125,24 +108,59 @@ AFX_D unsigned warp_append(unsigned* counter, unsigned n) {
     return base + x - n;
 }
 
-// One thread per cube, x fastest.  Emits the point-cloud vertices (marchingCubesMeshKernel)
-// and/or the triangles (marchingCubesFullKernel) of its cube.
+// A CTA covers a 32 x 8 patch of cube columns and a run of kMcZ cubes along z; each thread
+// marches its column, keeping the four corner values of the slice it shares with the next cube
+// (one new tsdf/weight row pair per step instead of eight corners, no index divisions).  Warps
+// are aligned to x rows, so the loads are coalesced and the warp-level append stays converged.
+// Emits the point-cloud vertices (marchingCubesMeshKernel) and/or the triangles
+// (marchingCubesFullKernel) of each cube.
+constexpr int kMcX = 32, kMcY = 8, kMcZ = 16;
+
+// tsdf/weight of the corners (x, y), (x+1, y), (x, y+1), (x+1, y+1) of slice z
+AFX_D void mc_slice(const float* __restrict__ tsdf, const float* __restrict__ w, long row0, long X, float t[4],
+                    float ww[4]) {
+    t[0] = __ldg(tsdf + row0);
+    t[1] = __ldg(tsdf + row0 + 1);
+    t[2] = __ldg(tsdf + row0 + X);
+    t[3] = __ldg(tsdf + row0 + X + 1);
+    ww[0] = __ldg(w + row0);
+    ww[1] = __ldg(w + row0 + 1);
+    ww[2] = __ldg(w + row0 + X);
+    ww[3] = __ldg(w + row0 + X + 1);
+}
+
 template <bool kPoints, bool kMesh>
-__global__ void __launch_bounds__(256) mc_kernel(const float* __restrict__ tsdf, const float* __restrict__ weights,
-                                                 McArgs a) {
+__global__ void __launch_bounds__(kMcX * kMcY) mc_kernel(const float* __restrict__ tsdf,
+                                                        const float* __restrict__ weights, McArgs a) {
     const int nx = a.vol.dims[0] - 2, ny = a.vol.dims[1] - 2, nz = a.vol.dims[2] - 2;
-    const long ncubes = (long)nx * ny * nz;
-    const long stride = (long)gridDim.x * blockDim.x;
-    const long start = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    // all lanes of a warp iterate together so the warp-level append stays converged
-    for (long base = start - (threadIdx.x & 31); base < ncubes; base += stride) {
-        long cid = base + (threadIdx.x & 31);
-        int ci = 0, x = 0, y = 0, z = 0;
-        if (cid < ncubes) {
-            x = (int)(cid % nx);
-            y = (int)((cid / nx) % ny);
-            z = (int)(cid / ((long)nx * ny));
-            ci = cube_index(tsdf, weights, a.vol, x, y, z, a.iso);
+    const long X = a.vol.dims[0], XY = X * a.vol.dims[1];
+    const int x = blockIdx.x * kMcX + threadIdx.x, y = blockIdx.y * kMcY + threadIdx.y;
+    const int z0 = blockIdx.z * kMcZ, z1 = min(z0 + kMcZ, nz);
+    const bool col = x < nx && y < ny;
+    const long base = (long)y * X + x;
+    float t0[4] = {0.f, 0.f, 0.f, 0.f}, w0[4] = {0.f, 0.f, 0.f, 0.f};
+    if (col) mc_slice(tsdf, weights, (long)z0 * XY + base, X, t0, w0);
+    for (int z = z0; z < z1; ++z) {
+        float t1[4] = {0.f, 0.f, 0.f, 0.f}, w1[4] = {0.f, 0.f, 0.f, 0.f};
+        if (col) mc_slice(tsdf, weights, (long)(z + 1) * XY + base, X, t1, w1);
+        int ci = 0;
+        if (col) {
+            // corners (src/MarchingCubes.cu:338-379): c0 (1,1,0) c1 (1,0,0) c2 (0,0,0) c3 (0,1,0),
+            // c4..c7 the same one slice up; slot s of a slice is (x + (s & 1), y + (s >> 1))
+            const float ct[8] = {t0[3], t0[1], t0[0], t0[2], t1[3], t1[1], t1[0], t1[2]};
+            const float cw[8] = {w0[3], w0[1], w0[0], w0[2], w1[3], w1[1], w1[0], w1[2]};
+            bool any_zero = false;
+#pragma unroll
+            for (int c = 0; c < 8; ++c) any_zero |= (cw[c] == 0.0f);
+            if (!any_zero)
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    if (ct[c] > a.iso) ci |= 1 << c;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            t0[q] = t1[q];
+            w0[q] = w1[q];
         }
         const bool active = ci != 0 && ci != 255;
         if (!__any_sync(0xffffffffu, active)) continue;
@@ -223,15 +241,13 @@ int mc_fused_impl(const float* tsdf, const float* weights, const Volume& vol, fl
     a.faces = faces;
     const long ncubes = (long)(vol.dims[0] - 2) * (vol.dims[1] - 2) * (vol.dims[2] - 2);
     if (ncubes <= 0) return AFX_OK;
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    long want = (ncubes + 255) / 256;
-    unsigned grid = (unsigned)(want < (long)sms * 16 ? want : (long)sms * 16);
+    const dim3 grid((unsigned)((vol.dims[0] - 2 + kMcX - 1) / kMcX), (unsigned)((vol.dims[1] - 2 + kMcY - 1) / kMcY),
+                    (unsigned)((vol.dims[2] - 2 + kMcZ - 1) / kMcZ));
+    const dim3 block(kMcX, kMcY);
     const bool P = points != nullptr, M = verts != nullptr;
-    if (P && M) mc_kernel<true, true><<<grid, 256, 0, st>>>(tsdf, weights, a);
-    else if (P) mc_kernel<true, false><<<grid, 256, 0, st>>>(tsdf, weights, a);
-    else if (M) mc_kernel<false, true><<<grid, 256, 0, st>>>(tsdf, weights, a);
+    if (P && M) mc_kernel<true, true><<<grid, block, 0, st>>>(tsdf, weights, a);
+    else if (P) mc_kernel<true, false><<<grid, block, 0, st>>>(tsdf, weights, a);
+    else if (M) mc_kernel<false, true><<<grid, block, 0, st>>>(tsdf, weights, a);
     else return AFX_OK;
     AFX_LAUNCH_CHECK();
     if (M && vert_count) {
@@ -262,17 +278,28 @@ AFX_D bool key_less(const Key3& a, const Key3& b) {
 AFX_D bool key_le(const Key3& a, const Key3& b) { return !key_less(b, a); }
 
 constexpr int kSortTile = 2048;
+constexpr int kSortThreads = 1024;
+constexpr int kSortCluster = 16;
 
-__device__ __forceinline__ long dev_n(const unsigned* count, long n_max) { return min((long)*count, n_max); }
+AFX_D unsigned sort_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+AFX_D unsigned sort_ncta() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+AFX_D void sort_cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
 
-__global__ void __launch_bounds__(1024) sort_tiles_kernel(const float* __restrict__ pts, Key3* out,
-                                                          const unsigned* count, long n_max) {
-    __shared__ Key3 s[kSortTile];
-    const long n = dev_n(count, n_max);
-    const long base = (long)blockIdx.x * kSortTile;
-    if (base >= n) return;
+// Bitonic sort of one tile of up to kSortTile points (padding sorts last) into `out`.
+AFX_D void sort_tile(const float* __restrict__ pts, Key3* out, long base, long n, Key3* s) {
+    __syncthreads();
     for (int i = threadIdx.x; i < kSortTile; i += blockDim.x) {
-        long j = base + i;
+        const long j = base + i;
         Key3 k;
         if (j < n) {
             k.k[0] = f2key(pts[3 * j]);
@@ -284,45 +311,38 @@ __global__ void __launch_bounds__(1024) sort_tiles_kernel(const float* __restric
         s[i] = k;
     }
     __syncthreads();
-    for (int size = 2; size <= kSortTile; size <<= 1) {
+    for (int size = 2; size <= kSortTile; size <<= 1)
         for (int stride = size >> 1; stride > 0; stride >>= 1) {
-            int p = threadIdx.x;  // one pair per thread (1024 pairs)
-            int i = 2 * stride * (p / stride) + (p % stride);
-            int j = i + stride;
-            bool asc = (i & size) == 0;
-            Key3 a = s[i], b = s[j];
-            if (key_less(b, a) == asc) {
-                s[i] = b;
-                s[j] = a;
+            for (int p = threadIdx.x; p < kSortTile / 2; p += blockDim.x) {
+                const int i = 2 * stride * (p / stride) + (p % stride), j = i + stride;
+                const bool asc = (i & size) == 0;
+                const Key3 a = s[i], b = s[j];
+                if (key_less(b, a) == asc) {
+                    s[i] = b;
+                    s[j] = a;
+                }
             }
             __syncthreads();
         }
-    }
     for (int i = threadIdx.x; i < kSortTile; i += blockDim.x) {
-        long j = base + i;
+        const long j = base + i;
         if (j < n) out[j] = s[i];
     }
 }
 
-// One merge pass: runs of length L in `in` merged pairwise into `out`.  Each CTA produces
-// kSortTile outputs; a pass with L >= n leaves the data where it is (flag in *state).
-__global__ void __launch_bounds__(512) merge_pass_kernel(const Key3* __restrict__ in, Key3* __restrict__ out,
-                                                         const unsigned* count, long n_max, long L) {
-    __shared__ Key3 s[kSortTile];
-    const long n = dev_n(count, n_max);
-    if (L >= n) return;
-    const long o0 = (long)blockIdx.x * kSortTile;
-    if (o0 >= n) return;
+// Outputs [o0, o0 + kSortTile) of merging the sorted runs of length L around o0 (merge path).
+AFX_D void merge_chunk(const Key3* __restrict__ in, Key3* __restrict__ out, long n, long L, long o0, Key3* s,
+                       long* split) {
     const long pair = o0 / (2 * L) * (2 * L);
     const long a0 = pair, na = min(L, n - a0);
     const long b0 = pair + L, nb = max(0L, min(L, n - b0));
     const long d0 = o0 - pair, d1 = min(d0 + kSortTile, na + nb);
-    __shared__ long split[2];
+    __syncthreads();
     if (threadIdx.x < 2) {
-        long d = threadIdx.x == 0 ? d0 : d1;
+        const long d = threadIdx.x == 0 ? d0 : d1;
         long lo = max(0L, d - nb), hi = min(d, na);
         while (lo < hi) {
-            long mid = (lo + hi) >> 1;
+            const long mid = (lo + hi) >> 1;
             if (key_le(in[a0 + mid], in[b0 + d - 1 - mid])) lo = mid + 1;
             else hi = mid;
         }
@@ -334,67 +354,146 @@ __global__ void __launch_bounds__(512) merge_pass_kernel(const Key3* __restrict_
     const int la = (int)(i1 - i0), lb = (int)(j1 - j0);
     for (int t = threadIdx.x; t < la + lb; t += blockDim.x) s[t] = t < la ? in[a0 + i0 + t] : in[b0 + j0 + (t - la)];
     __syncthreads();
-    // each thread merges 4 consecutive outputs of the tile
     const int tot = la + lb;
-    const int q0 = threadIdx.x * 4;
-    if (q0 >= tot) return;
-    int lo = max(0, q0 - lb), hi = min(q0, la);
-    while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if (key_le(s[mid], s[la + q0 - 1 - mid])) lo = mid + 1;
-        else hi = mid;
-    }
-    int ia = lo, ib = q0 - lo;
-    for (int q = q0; q < q0 + 4 && q < tot; ++q) {
-        bool takeA = ib >= lb || (ia < la && key_le(s[ia], s[la + ib]));
-        out[o0 + q] = takeA ? s[ia++] : s[la + ib++];
-    }
-}
-
-__global__ void unique_flags_kernel(const Key3* buf0, const Key3* buf1, const unsigned* count, long n_max, int passes,
-                                    unsigned* flags) {
-    const long n = dev_n(count, n_max);
-    // the sorted data is in buf0 after an even number of effective passes, else in buf1
-    int eff = 0;
-    for (long L = kSortTile; L < n && eff < passes; L <<= 1) ++eff;
-    const Key3* buf = (eff & 1) ? buf1 : buf0;
-    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    unsigned f = 1;
-    if (i > 0) {
-        Key3 a = buf[i - 1], b = buf[i];
-        float ax = key2f(a.k[0]), ay = key2f(a.k[1]), az = key2f(a.k[2]);
-        float bx = key2f(b.k[0]), by = key2f(b.k[1]), bz = key2f(b.k[2]);
-        f = (ax == bx && ay == by && az == bz) ? 0u : 1u;
-    }
-    flags[i] = f;
-}
-
-__global__ void unique_scatter_kernel(const Key3* buf0, const Key3* buf1, unsigned* count, long n_max, int passes,
-                                      const unsigned* flags, const unsigned* pos, const unsigned* total, float* pts) {
-    const long n = dev_n(count, n_max);
-    int eff = 0;
-    for (long L = kSortTile; L < n && eff < passes; L <<= 1) ++eff;
-    const Key3* buf = (eff & 1) ? buf1 : buf0;
-    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (i < n && flags[i]) {
-        Key3 k = buf[i];
-        float* o = pts + 3 * (long)pos[i];
-        o[0] = key2f(k.k[0]);
-        o[1] = key2f(k.k[1]);
-        o[2] = key2f(k.k[2]);
+    const int per = kSortTile / kSortThreads;
+    const int q0 = threadIdx.x * per;
+    if (q0 < tot) {
+        int lo = max(0, q0 - lb), hi = min(q0, la);
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (key_le(s[mid], s[la + q0 - 1 - mid])) lo = mid + 1;
+            else hi = mid;
+        }
+        int ia = lo, ib = q0 - lo;
+        for (int q = q0; q < q0 + per && q < tot; ++q) {
+            const bool takeA = ib >= lb || (ia < la && key_le(s[ia], s[la + ib]));
+            out[o0 + q] = takeA ? s[ia++] : s[la + ib++];
+        }
     }
 }
 
-__global__ void set_count_kernel(unsigned* count, const unsigned* total, long n_max) {
-    if (min((long)*count, n_max) > 0) *count = *total;
+AFX_D bool key_same_point(const Key3& a, const Key3& b) {
+    return key2f(a.k[0]) == key2f(b.k[0]) && key2f(a.k[1]) == key2f(b.k[1]) && key2f(a.k[2]) == key2f(b.k[2]);
+}
+
+// Lexicographic sort + unique of the point cloud in one launch of one thread-block cluster:
+// tiles of kSortTile sorted in shared memory, merge-path passes until one run remains (the
+// pass count follows the live count on the device), then unique by float equality of
+// consecutive points and an ordered compaction back into `pts`.  Phases are separated by the
+// hardware cluster barrier.
+__global__ void __launch_bounds__(kSortThreads, 1) sort_unique_kernel(float* pts, unsigned* count, long n_max,
+                                                                     Key3* buf0, Key3* buf1, unsigned* tile_cnt) {
+    __shared__ Key3 s[kSortTile];
+    __shared__ long split[2];
+    __shared__ unsigned wsum[kSortThreads / 32];
+    __shared__ unsigned s_base;
+    const long n = min((long)*count, n_max);
+    const unsigned rank = sort_rank(), ncta = sort_ncta();
+    const long tiles = (n + kSortTile - 1) / kSortTile;
+    for (long t = rank; t < tiles; t += ncta) sort_tile(pts, buf0, t * kSortTile, n, s);
+    sort_cluster_barrier();
+    Key3* src = buf0;
+    Key3* dst = buf1;
+    for (long L = kSortTile; L < n; L <<= 1) {
+        for (long t = rank; t < tiles; t += ncta) merge_chunk(src, dst, n, L, t * kSortTile, s, split);
+        sort_cluster_barrier();
+        Key3* tmp = src;
+        src = dst;
+        dst = tmp;
+    }
+    // unique flags and per-tile counts
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (long t = rank; t < tiles; t += ncta) {
+        unsigned c = 0;
+        for (long i = t * kSortTile + threadIdx.x; i < min(n, (t + 1) * kSortTile); i += blockDim.x)
+            c += (i == 0 || !key_same_point(src[i - 1], src[i])) ? 1u : 0u;
+        c = warp_sum(c);
+        __syncthreads();
+        if (lane == 0) wsum[w] = c;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned tot = 0;
+            for (int k = 0; k < kSortThreads / 32; ++k) tot += wsum[k];
+            tile_cnt[t] = tot;
+        }
+    }
+    sort_cluster_barrier();
+    // ordered compaction: tile base = exclusive prefix of the tile counts
+    for (long t = rank; t < tiles; t += ncta) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned b = 0;
+            for (long k = 0; k < t; ++k) b += __ldcg(tile_cnt + k);
+            s_base = b;
+        }
+        __syncthreads();
+        // one element per thread per round, kSortTile / kSortThreads rounds, in index order
+        unsigned run = s_base;
+        for (long r0 = t * kSortTile; r0 < min(n, (t + 1) * kSortTile); r0 += blockDim.x) {
+            const long i = r0 + threadIdx.x;
+            const bool keep = i < n && (i == 0 || !key_same_point(src[i - 1], src[i]));
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            __syncthreads();
+            if (lane == 0) wsum[w] = __popc(bal);
+            __syncthreads();
+            unsigned before = 0, all = 0;
+            for (int k = 0; k < kSortThreads / 32; ++k) {
+                const unsigned v = wsum[k];
+                if (k < w) before += v;
+                all += v;
+            }
+            if (keep) {
+                const unsigned pos = run + before + __popc(bal & ((1u << lane) - 1));
+                const Key3 k = src[i];
+                float* o = pts + 3 * (long)pos;
+                o[0] = key2f(k.k[0]);
+                o[1] = key2f(k.k[1]);
+                o[2] = key2f(k.k[2]);
+            }
+            run += all;
+        }
+    }
+    sort_cluster_barrier();
+    if (rank == 0 && threadIdx.x == 0 && n > 0) {
+        unsigned tot = 0;
+        for (long k = 0; k < tiles; ++k) tot += __ldcg(tile_cnt + k);
+        *count = tot;
+    }
 }
 
 static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 
 size_t sort_unique_workspace_size(long n_max) {
     if (n_max < 1) n_max = 1;
-    return 2 * al(n_max * sizeof(Key3)) + 2 * al(n_max * 4) + al(scan_workspace_size(n_max)) + 256;
+    return 2 * al(n_max * sizeof(Key3)) + al(((n_max + kSortTile - 1) / kSortTile) * 4) + 256;
+}
+
+static int sort_cluster_size() {
+    static int cached = 0;
+    if (!cached) {
+        cudaFuncSetAttribute(sort_unique_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        const int sizes[2] = {kSortCluster, 8};
+        for (int c : sizes) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(c);
+            cfg.blockDim = dim3(kSortThreads);
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = c;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int clusters = 0;
+            if (cudaOccupancyMaxActiveClusters(&clusters, sort_unique_kernel, &cfg) == cudaSuccess && clusters > 0) {
+                cached = c;
+                break;
+            }
+            cudaGetLastError();
+        }
+        if (!cached) cached = 8;
+    }
+    return cached;
 }
 
 int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, cudaStream_t st) {
@@ -405,34 +504,20 @@ int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t w
     p += al(n_max * sizeof(Key3));
     Key3* buf1 = reinterpret_cast<Key3*>(p);
     p += al(n_max * sizeof(Key3));
-    unsigned* flags = reinterpret_cast<unsigned*>(p);
-    p += al(n_max * 4);
-    unsigned* pos = reinterpret_cast<unsigned*>(p);
-    p += al(n_max * 4);
-    void* scan_ws = p;
-    p += al(scan_workspace_size(n_max));
-    unsigned* total = reinterpret_cast<unsigned*>(p);
-    const long tiles = (n_max + kSortTile - 1) / kSortTile;
-    sort_tiles_kernel<<<(unsigned)tiles, 1024, 0, st>>>(pts, buf0, count, n_max);
-    AFX_LAUNCH_CHECK();
-    int passes = 0;
-    Key3* src = buf0;
-    Key3* dst = buf1;
-    for (long L = kSortTile; L < n_max; L <<= 1, ++passes) {
-        merge_pass_kernel<<<(unsigned)tiles, 512, 0, st>>>(src, dst, count, n_max, L);
-        AFX_LAUNCH_CHECK();
-        Key3* t = src;
-        src = dst;
-        dst = t;
-    }
-    unique_flags_kernel<<<blocks_for(n_max, 256), 256, 0, st>>>(buf0, buf1, count, n_max, passes, flags);
-    AFX_LAUNCH_CHECK();
-    int rc = scan_exclusive_dev(flags, pos, count, n_max, total, scan_ws, st);
-    if (rc) return rc;
-    unique_scatter_kernel<<<blocks_for(n_max, 256), 256, 0, st>>>(buf0, buf1, count, n_max, passes, flags, pos, total,
-                                                                  pts);
-    AFX_LAUNCH_CHECK();
-    set_count_kernel<<<1, 1, 0, st>>>(count, total, n_max);
+    unsigned* tile_cnt = reinterpret_cast<unsigned*>(p);
+    const int c = sort_cluster_size();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(c);
+    cfg.blockDim = dim3(kSortThreads);
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = c;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    AFX_CUDA(cudaLaunchKernelEx(&cfg, sort_unique_kernel, pts, count, n_max, buf0, buf1, tile_cnt));
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
