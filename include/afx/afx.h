@@ -238,6 +238,45 @@ int afx_correspondences_static(int* corr, unsigned* corr_count, long capacity, c
                                int rows, int cols, const float* frame_vertices, float thresh, void* stream);
 
 /* ------------------------------------------------------------------------------------
+ * Gauss-Newton for the motion graph, step by step (src/VolumeFusion.cu:454-691 drives these
+ * kernels of src/MotionOptimization.cu with a dense J and a cuSOLVER LU).  Here J is never
+ * stored: J^T J is assembled block-sparse per node (the session uses the same code).
+ * ------------------------------------------------------------------------------------ */
+typedef struct afx_gn afx_gn;
+
+/* Workspace for graphs of up to n_nodes_max nodes, n_points_max canonical vertices and as many
+ * correspondences, k skinning and kreg regularisation neighbours (<= 8 each). */
+int afx_gn_create(long n_points_max, int n_nodes_max, int k, int kreg, afx_gn** out);
+int afx_gn_destroy(afx_gn* g);
+
+/* Residuals and system for correspondences `corr` ((vertex, pixel) pairs, *n_corr of them):
+ * fill_r_DepthKernel / fill_r_MRegKernel (src/MotionOptimization.cu:163-241), fill_J_DepthKernel /
+ * fill_J_MRegKernel (:29-161), computeJTJAndJTrContrib* + sort/reduce_by_key + multiply* +
+ * fillJTJKernel / fillJTrKernel (:243-481, src/VolumeFusion.cu:504-646) and
+ * runInitIdentityKernel (src/Helper.cu:37-50).  `warped` are the canonical vertices warped by
+ * `transforms`; graph_idx is the filtered K_reg-NN of each node.  Synchronises `stream`;
+ * returns AFX_ERR_SINGULAR when a diagonal block has no inverse.  The system is kept in the
+ * workspace (the counters are copied); afx_gn_export and afx_gn_solve read only the workspace. */
+int afx_gn_build(afx_gn* g, const float* canonical, const unsigned* n_points, const uint32_t* knn_idx,
+                 const float* knn_weights, const int* corr, const unsigned* n_corr, const float* frame_vertices,
+                 const float* frame_normals, const float* warped, const float* nodes, const float* transforms,
+                 const int* n_nodes, const uint32_t* graph_idx, float lambda_depth, float lambda_reg, void* stream);
+
+/* The built system in the reference's layout (any pointer may be NULL): jtj = dense
+ * (6 n)^2 float, row-major (symmetric), untouched diagonal blocks the identity; jtr = 6 n;
+ * r_depth = one residual per correspondence; r_reg = 3 per (node, K_reg slot).  n_nodes_host is
+ * the node count (the device counter's value). */
+int afx_gn_export(afx_gn* g, int n_nodes_host, float* jtj, float* jtr, float* r_depth, float* r_reg, void* stream);
+
+/* x = (J^T J)^-1 J^T r by block-Jacobi preconditioned conjugate gradients: `iterations` steps, or
+ * until |r| <= tol |b| when tol > 0 (replaces linearSolverLUStable, src/LinearSolver.cu:179-224).
+ * x: 6 * n_nodes_max floats, device. */
+int afx_gn_solve(afx_gn* g, float* x, int iterations, double tol, void* stream);
+
+/* runUpdateTransformsKernel (src/MotionOptimization.cu:483-506): T -= [[x_rot]x, x_t; 0]. */
+int afx_update_transforms(float* transforms, const float* x, const int* n_nodes, int n_nodes_max, void* stream);
+
+/* ------------------------------------------------------------------------------------
  * Whole-frame session: af::runVolumeFusion's per-frame loop (src/VolumeFusion.cu:223-769)
  * with all state (TSDF, motion graph, solver) resident on the device.
  * ------------------------------------------------------------------------------------ */

@@ -1,0 +1,90 @@
+"""The Gauss-Newton operators through the C ABI (afx_gn_*) against the CPU oracle, on one
+frame of the small non-rigid case with the reference's constants (K = 6 skinning, K_reg = 4)
+and with the workload's (K = 4, K_reg = 8): residuals and J^T J bit-exact, J^T r to rounding
+(the GPU sums rows in a fixed butterfly, the oracle in sequence), the PCG solution against the
+oracle's FP64 PCG, and the transform update bit-exact."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import pyoracle as O  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def cu(a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a))
+    return (t.to(dtype) if dtype is not None else t).cuda()
+
+
+def _system(k, kreg, frame=14):
+    from volumefusion_gb300 import configs, synth
+    cfg = configs.small_nonrigid(n_frames=30)
+    mm0, K = synth.capsule_pair_frame(12, width=cfg["width"], height=cfg["height"], fx=float(cfg["K"][0, 0]),
+                                      fy=float(cfg["K"][1, 1]), cx=float(cfg["K"][0, 2]), cy=float(cfg["K"][1, 2]))
+    mm1, _ = synth.capsule_pair_frame(frame, width=cfg["width"], height=cfg["height"], fx=float(cfg["K"][0, 0]),
+                                      fy=float(cfg["K"][1, 1]), cx=float(cfg["K"][0, 2]), cy=float(cfg["K"][1, 2]))
+    d0, v0, n0, c = O.frame_prep(mm0, K)
+    dims = np.asarray(cfg["dims"], np.int32)
+    size = np.asarray(cfg["volume_size"], np.float32)
+    vs = size / dims.astype(np.float32)
+    S = int(np.prod(dims))
+    t0, w0 = np.full(S, -1, np.float32), np.zeros(S, np.float32)
+    O.integrate_rigid(t0, w0, d0, cfg["delta"], dims, vs, size, np.eye(3), c, K)
+    mesh = O.translate(O.sort_unique(O.mc_pointcloud(t0, w0, dims, vs, size)), c)
+    nodes, radii, T = O.build_graph(mesh, k, cfg["graph_radius"])
+    rng = np.random.default_rng(11)
+    T = T.copy()
+    T[:, 12:15] += rng.normal(0, 0.003, (len(T), 3)).astype(np.float32)
+    midx, mdist = O.knn(nodes, mesh, k)
+    mw = O.warp_weights(radii, midx, mdist)
+    warped = O.warp(mesh, T, midx, mw)
+    d1, v1, n1, _ = O.frame_prep(mm1, K)
+    corr = O.correspondences(warped, K, d1, v1, cfg["corr_thresh"])
+    gidx, gdist = O.knn(nodes, nodes, kreg, exclude_closest=True)
+    gidx, gdist = O.filter_disconnected(gidx, gdist, radii)
+    return dict(mesh=mesh, nodes=nodes, T=T, midx=midx, mw=mw, warped=warped, v1=v1, n1=n1, corr=corr, gidx=gidx,
+                lam_d=np.float32(cfg["lambda_depth"]), lam_r=np.float32(cfg["lambda_reg"]))
+
+
+@pytest.mark.parametrize("k,kreg", [(6, 4), (4, 8)])
+def test_gauss_newton_operators_match_oracle(k, kreg):
+    from volumefusion_gb300 import af
+    s = _system(k, kreg)
+    n, m, nc = len(s["nodes"]), len(s["mesh"]), len(s["corr"])
+    assert n > 10 and nc > 100
+    # oracle
+    rd = O.residual_depth(s["corr"], s["warped"], s["v1"], s["n1"], s["lam_d"])
+    rr = O.residual_reg(s["nodes"], s["T"], s["gidx"], s["lam_r"])
+    A, b, _ = O.assemble(s["corr"], s["mesh"], s["midx"], s["mw"], s["n1"], s["lam_d"], s["nodes"], s["gidx"],
+                         s["lam_r"], rd, rr)
+    x_o, _ = O.pcg(A, b, 10)
+    # GPU
+    g = af.GaussNewtonSystem(m + 16, n + 8, k, kreg)
+    cnt = lambda v: cu(np.array([v], np.int32))  # noqa: E731
+    g.build(cu(s["mesh"]), cnt(m), cu(s["midx"].view(np.int32)), cu(s["mw"]), cu(s["corr"]), cnt(nc), cu(s["v1"]),
+            cu(s["n1"]), cu(s["warped"]), cu(s["nodes"]), cu(s["T"]), cnt(n), cu(s["gidx"].view(np.int32)),
+            s["lam_d"], s["lam_r"])
+    jtj, jtr, grd, grr = g.export(n, nc)
+    assert np.array_equal(grd.cpu().numpy(), rd)
+    assert np.array_equal(grr.cpu().numpy(), rr)
+    assert np.array_equal(jtj.cpu().numpy(), A)
+    jb = jtr.cpu().numpy()
+    assert np.abs(jb - b).max() <= 1e-5 * max(1.0, np.abs(b).max())
+    # The system is stiff (condition number ~5e6 here: the regulariser is a graph Laplacian), so
+    # FP32 and FP64 Krylov iterates part by up to ~kappa * eps.  Converged: the true residual
+    # |b - A x| / |b| reaches FP32 level and x is within a few percent of the exact FP64 solve.
+    A64, b64 = A.astype(np.float64), b.astype(np.float64)
+    x_exact = np.linalg.solve(A64, b64)
+    xc = g.solve(400, tol=1e-7)[:6 * n].cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(b64 - A64 @ xc) <= 1e-4 * np.linalg.norm(b64)
+    assert np.linalg.norm(xc - x_exact) <= 5e-2 * np.linalg.norm(x_exact)
+    # ten iterations (the workload's setting) against the oracle's FP64 PCG
+    x = g.solve(10)[:6 * n].cpu().numpy()
+    assert np.linalg.norm(x - x_o) <= 3e-2 * np.linalg.norm(x_o)
+    # transform update with the same x
+    Tg = cu(s["T"])
+    af.runUpdateTransformsKernel(Tg, cu(x), cnt(n))
+    assert np.array_equal(Tg.cpu().numpy(), O.update_transforms(s["T"], x))
+    g.close()

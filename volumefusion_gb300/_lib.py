@@ -71,6 +71,12 @@ SIGNATURES = {
     "afx_correspondences": (i32, [vp, vp, i64, vp, vp, i64, vp, vp, i32, i32, vp, f32, vp, sz, vp]),
     "afx_correspondences_workspace_size": (sz, [i64]),
     "afx_correspondences_static": (i32, [vp, vp, i64, vp, vp, i64, vp, vp, i32, i32, vp, f32, vp]),
+    "afx_gn_create": (i32, [i64, i32, i32, i32, C.POINTER(vp)]),
+    "afx_gn_destroy": (i32, [vp]),
+    "afx_gn_build": (i32, [vp] + [vp] * 13 + [f32, f32, vp]),
+    "afx_gn_export": (i32, [vp, i32, vp, vp, vp, vp, vp]),
+    "afx_gn_solve": (i32, [vp, vp, i32, C.c_double, vp]),
+    "afx_update_transforms": (i32, [vp, vp, vp, i32, vp]),
     "afx_fusion_default_params": (None, [C.POINTER(FusionParams)]),
     "afx_fusion_create": (i32, [C.POINTER(FusionParams), C.POINTER(vp)]),
     "afx_fusion_destroy": (i32, [vp]),

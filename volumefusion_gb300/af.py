@@ -228,3 +228,56 @@ def runCorrespondencePairsKernel(corrIdxs, corrIdxsSize, warpedMesh, warpedMeshS
     _sync(lib().afx_correspondences(_p(corrIdxs), _p(corrIdxsSize), corrIdxs.shape[0], _p(warpedMesh), None,
                                     int(warpedMeshSize), _f(kcol(K), 9), _p(depth), rows, cols, _p(frameMesh),
                                     thresholdDist, _p(ws), ws.numel(), _stream()), "runCorrespondencePairsKernel")
+
+
+# ---- include/af/MotionOptimization.cuh, src/LinearSolver.cu (the Gauss-Newton steps) ----
+
+class GaussNewtonSystem:
+    """The Gauss-Newton system of one motion-graph solve (src/VolumeFusion.cu:454-691): residuals,
+    J^T J and J^T r (block-sparse on the device; `export` gives the reference's dense layout) and
+    the block-Jacobi PCG solve that replaces linearSolverLUStable."""
+
+    def __init__(self, n_points_max, n_nodes_max, k, kreg):
+        h = C.c_void_p()
+        check(lib().afx_gn_create(int(n_points_max), int(n_nodes_max), int(k), int(kreg), C.byref(h)), "afx_gn_create")
+        self.h = h
+        self.n_nodes_max = int(n_nodes_max)
+        self.kreg = int(kreg)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().afx_gn_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def build(self, canonical, n_points, knn_idx, knn_weights, corr, n_corr, frame_vertices, frame_normals, warped,
+              nodes, transforms, n_nodes, graph_idx, lambda_depth, lambda_reg):
+        _sync(lib().afx_gn_build(self.h, _p(canonical), _p(n_points), _p(knn_idx), _p(knn_weights), _p(corr),
+                                 _p(n_corr), _p(frame_vertices), _p(frame_normals), _p(warped), _p(nodes),
+                                 _p(transforms), _p(n_nodes), _p(graph_idx), float(lambda_depth), float(lambda_reg),
+                                 _stream()), "afx_gn_build")
+
+    def export(self, n_nodes, n_corr):
+        """(jtj (6n, 6n), jtr (6n,), r_depth (n_corr,), r_reg (n * kreg * 3,)) as CUDA tensors."""
+        dim = 6 * int(n_nodes)
+        jtj = torch.empty((dim, dim), dtype=torch.float32, device="cuda")
+        jtr = torch.empty(dim, dtype=torch.float32, device="cuda")
+        rd = torch.empty(max(int(n_corr), 1), dtype=torch.float32, device="cuda")
+        rr = torch.empty(max(int(n_nodes) * self.kreg * 3, 1), dtype=torch.float32, device="cuda")
+        _sync(lib().afx_gn_export(self.h, int(n_nodes), _p(jtj), _p(jtr), _p(rd), _p(rr), _stream()), "afx_gn_export")
+        return jtj, jtr, rd[:int(n_corr)], rr[:int(n_nodes) * self.kreg * 3]
+
+    def solve(self, iterations=10, tol=0.0):
+        x = torch.zeros(6 * self.n_nodes_max, dtype=torch.float32, device="cuda")
+        _sync(lib().afx_gn_solve(self.h, _p(x), int(iterations), float(tol), _stream()), "afx_gn_solve")
+        return x
+
+
+def runUpdateTransformsKernel(transforms, x, n_nodes):
+    _sync(lib().afx_update_transforms(_p(transforms), _p(x), _p(n_nodes), transforms.shape[0], _stream()),
+          "runUpdateTransformsKernel")

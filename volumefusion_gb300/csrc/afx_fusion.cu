@@ -413,7 +413,7 @@ static int extract_frame_mesh(afx_fusion* f, cudaStream_t st) {
     const bool mesh = f->p.extract_mesh != 0;
     return mc_fused_impl(f->tsdf, f->weights, f->vol, 0.f, f->points_buf[next], f->npoints_buf[next], f->p.mesh_capacity,
                          mesh ? f->mverts : nullptr, mesh ? f->nmverts : nullptr, f->p.triangle_capacity * 3,
-                         mesh ? f->mfaces : nullptr, mesh ? f->nmfaces : nullptr, f->p.triangle_capacity, st);
+                         mesh ? f->mfaces : nullptr, mesh ? f->nmfaces : nullptr, f->p.triangle_capacity, st, f->error);
 }
 
 int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {

@@ -15,6 +15,7 @@
 // products and FP64 6x6 block inverses.
 #include <cfloat>
 #include <cstring>
+#include <new>
 
 #include "afx_gn.h"
 
@@ -669,10 +670,9 @@ constexpr int kDsMaxCta = 16;
 
 struct DsLayout {
     float* z;       // [kDsNodes * 6] full copy
+    float* pf;      // [kDsNodes * 6] full copy of the search direction (each CTA forms it)
     float* x;       // [kDsNpc * 6] own slices
     float* r;
-    float* p;
-    float* ap;
     float* minv;    // [kDsNpc * 36]
     float* blk;     // [kDsBlocks * 36]
     int* col;       // [kDsBlocks] neighbour node of each block
@@ -681,7 +681,7 @@ struct DsLayout {
     int* misc;      // [4]
 };
 
-constexpr size_t kDsSmem = sizeof(float) * ((size_t)kDsNodes * 6 + 4 * kDsNpc * 6 + kDsNpc * 36 + (size_t)kDsBlocks * 36) +
+constexpr size_t kDsSmem = sizeof(float) * ((size_t)kDsNodes * 12 + 2 * kDsNpc * 6 + kDsNpc * 36 + (size_t)kDsBlocks * 36) +
                            sizeof(int) * (kDsBlocks + kDsNpc + 1 + 4) + sizeof(double) * 2 * kDsMaxCta * 4 + 64;
 
 AFX_D DsLayout ds_layout(void* base) {
@@ -691,13 +691,11 @@ AFX_D DsLayout ds_layout(void* base) {
     float* f = reinterpret_cast<float*>(dp + 2 * kDsMaxCta * 4);
     d.z = f;
     f += kDsNodes * 6;
+    d.pf = f;
+    f += kDsNodes * 6;
     d.x = f;
     f += kDsNpc * 6;
     d.r = f;
-    f += kDsNpc * 6;
-    d.p = f;
-    f += kDsNpc * 6;
-    d.ap = f;
     f += kDsNpc * 6;
     d.minv = f;
     f += kDsNpc * 36;
@@ -852,26 +850,22 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
     const double bnorm2 = d2[1];
     float beta = 0.f;
     for (int it = 0; it < L.pcg_iters; ++it) {
+        // p = z (first iteration) or z + beta p, formed for all nodes by every CTA from its copies
+        for (int i = threadIdx.x; i < n * 6; i += blockDim.x) d.pf[i] = it ? d.z[i] + beta * d.pf[i] : d.z[i];
+        __syncthreads();
         double pap[1] = {0.0};
+        float api = 0.f, pi = 0.f;
         if (act) {
             const int r0 = d.rowptr[li], r1 = d.rowptr[li + 1];
-            float acc = 0.f;
             for (int bk = r0; bk < r1; ++bk) {
                 const float* B = d.blk + bk * 36 + ei * 6;
-                const float* x = d.z + d.col[bk] * 6;
+                const float* x = d.pf + d.col[bk] * 6;
                 float s = 0.f;
 #pragma unroll
                 for (int j = 0; j < 6; ++j) s = s + B[j] * x[j];
-                acc = acc + s;
+                api = api + s;
             }
-            const float zi = d.z[(long)gnode * 6 + ei];
-            float pi = zi, api = acc;
-            if (it) {
-                pi = zi + beta * d.p[o];
-                api = acc + beta * d.ap[o];
-            }
-            d.p[o] = pi;
-            d.ap[o] = api;
+            pi = d.pf[(long)gnode * 6 + ei];
             pap[0] += (double)pi * (double)api;
         }
         ds_sum<1>(pap, d, cs, ph, live);
@@ -880,8 +874,8 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
         double q2[2] = {0.0, 0.0};
         float rv = 0.f;
         if (act) {
-            d.x[o] = d.x[o] + alpha * d.p[o];
-            rv = d.r[o] - alpha * d.ap[o];
+            d.x[o] = d.x[o] + alpha * pi;
+            rv = d.r[o] - alpha * api;
             d.r[o] = rv;
         }
         float zi = 0.f;
@@ -903,7 +897,7 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
     // T_pending -= [[x_rot]x, x_t; 0] for the own nodes (updateTransformsKernel,
     // src/MotionOptimization.cu:483-498); x also to global memory for inspection
     __syncthreads();
-    for (int t = threadIdx.x; t < own * 16; t += blockDim.x) {
+    for (int t = threadIdx.x; L.T_pending && t < own * 16; t += blockDim.x) {
         const int l = t >> 4, e = t & 15;
         const float* u = d.x + l * 6;
         float U;
@@ -925,6 +919,225 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
     for (int t = threadIdx.x; t < own * 6; t += blockDim.x) __stcg(b.x + (long)start * 6 + t, d.x[t]);
 }
 
+// ---- phases of the Gauss-Newton loop (all CTAs of the cluster unless stated) ----
+
+// Residuals (fill_r_DepthKernel / fill_r_MRegKernel, src/MotionOptimization.cu:163-227) with
+// the transforms T; partial FP64 energies of this thread (runSquareKernel + reductions,
+// src/VolumeFusion.cu:575-588).
+AFX_D void gn_residuals(const GnArgs& a, const float* warped, const float* T, int n, long ncorr, long gt, long gstride,
+                        double (&e2)[2]) {
+    const GnBuffers& b = a.b;
+    const long nreg = (long)n * a.kreg;
+    for (long c = gt; c < ncorr; c += gstride) {
+        const long v = a.corr[2 * c], px = a.corr[2 * c + 1];
+        const float* f = a.frame + 3 * px;
+        float d[3] = {__ldcg(warped + 3 * v) - f[0], __ldcg(warped + 3 * v + 1) - f[1], __ldcg(warped + 3 * v + 2) - f[2]};
+        const float r = a.lam_d * dot3(a.normals + 3 * px, d);
+        __stcg(b.rdepth + c, r);
+        e2[0] += (double)(r * r);
+    }
+    for (long t = gt; t < nreg; t += gstride) {
+        const int i = (int)(t / a.kreg);
+        const uint32_t nb = a.gidx[t];
+        float* rr = b.rreg + 3 * t;
+        if (nb >= (uint32_t)n) {
+            __stcg(rr, 0.f);
+            __stcg(rr + 1, 0.f);
+            __stcg(rr + 2, 0.f);
+            continue;
+        }
+        float Ti[16], Tn[16], tc[3], tn[3];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            Ti[e] = __ldcg(T + 16 * (long)i + e);
+            Tn[e] = __ldcg(T + 16 * (long)nb + e);
+        }
+        mat4_point(Ti, a.nodes + 3 * (long)i, tc);
+        mat4_point(Tn, a.nodes + 3 * (long)i, tn);
+        for (int ax = 0; ax < 3; ++ax) {
+            const float r = (tc[ax] - tn[ax]) * a.lam_r;
+            __stcg(rr + ax, r);
+            e2[1] += (double)(r * r);
+        }
+    }
+}
+
+// J^T r of every node into b.jtr (one node per warp).
+AFX_D void gn_jtr(const GnArgs& a, int n, int gw, int nw) {
+    const int lane = threadIdx.x & 31;
+    for (int node = gw; node < n; node += nw) {
+        float jv[6];
+        jtr_node(a, node, n, jv);
+        if (lane < 6) {
+            float ji = jv[0];
+#pragma unroll
+            for (int q = 1; q < 6; ++q)
+                if (lane == q) ji = jv[q];
+            __stcg(a.b.jtr + (long)node * 6 + lane, ji);
+        }
+    }
+}
+
+// PCG with the vectors in global memory (graphs above the shared-memory limit); J^T r from
+// b.jtr, solution in b.x.  Same recurrences and arithmetic as pcg_ds.
+AFX_D void pcg_global(const LoopArgs& L, int n, ClusterSums& cs) {
+    const GnBuffers& b = L.g.b;
+    const unsigned rank = cluster_rank(), ncta = cluster_size();
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int gw = (int)rank * kLoopWarps + w, nw = (int)ncta * kLoopWarps;
+    const int grp = lane / 6, ei = lane - 6 * grp;
+    const bool glane = lane < 30;
+    const int gstep = nw * 5;
+    // x = 0, r = b, z = M^-1 r; rz = r.z, bb = b.b
+    double d2[2] = {0.0, 0.0};
+    for (int base = gw * 5; base < n; base += gstep) {  // warp-uniform trip count
+        const int node = base + grp;
+        const bool act = glane && node < n;
+        const long o = (long)node * 6 + ei;
+        const float ji = act ? __ldcg(b.jtr + o) : 0.f;
+        float zi = 0.f;
+        const float* Mi = b.minv + (long)(act ? node : 0) * 36 + ei * 6;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const float rq = __shfl_sync(0xffffffffu, ji, glane ? grp * 6 + q : q);
+            if (act) zi = zi + Mi[q] * rq;
+        }
+        if (act) {
+            __stcg(b.x + o, 0.f);
+            __stcg(b.r + o, ji);
+            __stcg(b.z + o, zi);
+            d2[0] += (double)ji * (double)zi;
+            d2[1] += (double)ji * (double)ji;
+        }
+    }
+    cluster_sum<2>(d2, cs);
+    // six lanes per node (entry i = lane % 6 of node group lane / 6, five groups per warp)
+    double rz = d2[0];
+    const double bnorm2 = d2[1];
+    float beta = 0.f;
+    for (int it = 0; it < L.pcg_iters; ++it) {
+        // p = z (first iteration) or z + beta p for the own entries, then A p once all are written
+        for (int base = gw * 5; base < n; base += gstep) {
+            const int node = base + grp;
+            if (glane && node < n) {
+                const long o = (long)node * 6 + ei;
+                const float zi = __ldcg(b.z + o);
+                __stcg(b.p + o, it ? zi + beta * __ldcg(b.p + o) : zi);
+            }
+        }
+        cluster_barrier();
+        double pap[1] = {0.0};
+        if (glane)
+            for (int node = gw * 5 + grp; node < n; node += gstep) {
+                const long o = (long)node * 6 + ei;
+                const float api = spmv_entry(b, node, ei, b.p);
+                __stcg(b.ap + o, api);
+                pap[0] += (double)__ldcg(b.p + o) * (double)api;
+            }
+        cluster_sum<1>(pap, cs);
+        if (pap[0] == 0.0 || !(pap[0] == pap[0])) break;
+        const float alpha = (float)(rz / pap[0]);
+        // x += alpha p; r -= alpha A p; z = M^-1 r; r.z, r.r
+        double q2[2] = {0.0, 0.0};
+        for (int base = gw * 5; base < n; base += gstep) {
+            const int node = base + grp;
+            const bool act = glane && node < n;
+            const long o = (long)node * 6 + ei;
+            float rv = 0.f;
+            if (act) {
+                __stcg(b.x + o, __ldcg(b.x + o) + alpha * __ldcg(b.p + o));
+                rv = __ldcg(b.r + o) - alpha * __ldcg(b.ap + o);
+                __stcg(b.r + o, rv);
+            }
+            float zi = 0.f;
+            const float* Mi = b.minv + (long)(act ? node : 0) * 36 + ei * 6;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) {
+                const float rq = __shfl_sync(0xffffffffu, rv, glane ? grp * 6 + q : q);
+                if (act) zi = zi + Mi[q] * rq;
+            }
+            if (act) {
+                __stcg(b.z + o, zi);
+                q2[0] += (double)rv * (double)zi;
+                q2[1] += (double)rv * (double)rv;
+            }
+        }
+        cluster_sum<2>(q2, cs);
+        beta = (float)(q2[0] / rz);
+        rz = q2[0];
+        if (L.tol > 0 && q2[1] <= L.tol * L.tol * bnorm2) break;
+    }
+}
+
+// T -= [[x_rot]x, x_t; 0] for nodes [lo, hi) with x in global memory (updateTransformsKernel,
+// src/MotionOptimization.cu:483-498); entry e of node i by thread (i - lo) * 16 + e.
+AFX_D void update_transforms_range(float* T, const float* x, int lo, int hi, long t0, long tstride) {
+    for (long t = t0; t < (long)(hi - lo) * 16; t += tstride) {
+        const long node = lo + t / 16;
+        const int e = (int)(t & 15);
+        const float* u = x + node * 6;
+        float U;
+        switch (e) {
+            case 1: U = __ldcg(u + 2); break;
+            case 2: U = -__ldcg(u + 1); break;
+            case 4: U = -__ldcg(u + 2); break;
+            case 6: U = __ldcg(u + 0); break;
+            case 8: U = __ldcg(u + 1); break;
+            case 9: U = -__ldcg(u + 0); break;
+            case 12: U = __ldcg(u + 3); break;
+            case 13: U = __ldcg(u + 4); break;
+            case 14: U = __ldcg(u + 5); break;
+            default: U = 0.f;
+        }
+        float* Te = T + node * 16 + e;
+        __stcg(Te, __ldcg(Te) - U);
+    }
+}
+
+// Canonical vertices warped by T (warpKernel, src/ComputeCorrespondence.cu:13-30).
+AFX_D void gn_rewarp(const GnArgs& a, const float* points, float* warped, const float* T, long m, long gt,
+                     long gstride) {
+    for (long i = gt; i < m; i += gstride) {
+        const float p[3] = {points[3 * i], points[3 * i + 1], points[3 * i + 2]};
+        bool zero = true;
+        for (int j = 0; j < a.k; ++j)
+            if (!(fabsf(a.mw[i * a.k + j]) <= 1e-5f)) zero = false;
+        float acc[3] = {p[0], p[1], p[2]};
+        if (!zero) {
+            acc[0] = acc[1] = acc[2] = 0.f;
+            for (int j = 0; j < a.k; ++j) {
+                const uint32_t nb = a.midx[i * a.k + j];
+                if (nb == AFX_INVALID_INDEX) continue;
+                float Tn[16], o[3];
+#pragma unroll
+                for (int e = 0; e < 16; ++e) Tn[e] = __ldcg(T + 16 * (long)nb + e);
+                mat4_point(Tn, p, o);
+                const float wj = a.mw[i * a.k + j];
+                acc[0] = acc[0] + wj * o[0];
+                acc[1] = acc[1] + wj * o[1];
+                acc[2] = acc[2] + wj * o[2];
+            }
+        }
+        __stcg(warped + 3 * i, acc[0]);
+        __stcg(warped + 3 * i + 1, acc[1]);
+        __stcg(warped + 3 * i + 2, acc[2]);
+    }
+}
+
+// One solve from b.jtr: x in b.x (and in the own slices of the shared-memory layout); with
+// L.T_pending set, T_pending -= [x] as well.  Ends with a cluster barrier.
+AFX_D void gn_solve(const LoopArgs& L, int n, bool ds, const DsLayout& dsl, ClusterSums& cs, int& ds_ph, long gt,
+                    long gstride) {
+    if (ds) {
+        pcg_ds(L, n, dsl, cs, ds_ph);
+    } else {
+        pcg_global(L, n, cs);
+        cluster_barrier();  // x complete
+        if (L.T_pending) update_transforms_range(L.T_pending, L.g.b.x, 0, n, gt, gstride);
+    }
+    cluster_barrier();
+}
+
 __global__ void __launch_bounds__(kLoopThreads, 1) gn_loop_kernel(LoopArgs L) {
     const GnArgs& a = L.g;
     const GnBuffers& b = a.b;
@@ -933,13 +1146,12 @@ __global__ void __launch_bounds__(kLoopThreads, 1) gn_loop_kernel(LoopArgs L) {
     if (threadIdx.x == 0) cs.phase = 0;
     __syncthreads();
     const unsigned rank = cluster_rank(), ncta = cluster_size();
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int w = threadIdx.x >> 5;
     const long gt = (long)rank * kLoopThreads + threadIdx.x, gstride = (long)ncta * kLoopThreads;
     const int gw = (int)rank * kLoopWarps + w, nw = (int)ncta * kLoopWarps;
     const bool leader = rank == 0 && threadIdx.x == 0;
     const int n = min(*a.n_nodes, a.n_max);
     const long ncorr = min((long)*a.corr_count, a.c_max);
-    const long nreg = (long)n * a.kreg;
     const long m = min((long)*a.mesh_count, a.m_max);
     GnState* s = b.state;
     double e_prev = s->e_prev;
@@ -949,42 +1161,8 @@ __global__ void __launch_bounds__(kLoopThreads, 1) gn_loop_kernel(LoopArgs L) {
     int ds_ph = 0;
     const bool ds = !done && n > 0 && (n + (int)ncta - 1) / (int)ncta <= kDsNpc && ds_stage(b, n, dsl, cs, ds_ph);
     for (int iter = 0; iter < L.gn_iters && !done; ++iter) {
-        // ---- residuals and energies (fill_r_DepthKernel / fill_r_MRegKernel + runSquareKernel,
-        //      src/MotionOptimization.cu:163-227, src/VolumeFusion.cu:575-588), FP64 sums
         double e2[2] = {0.0, 0.0};
-        for (long c = gt; c < ncorr; c += gstride) {
-            long v = a.corr[2 * c], px = a.corr[2 * c + 1];
-            const float* f = a.frame + 3 * px;
-            float d[3] = {__ldcg(L.warped + 3 * v) - f[0], __ldcg(L.warped + 3 * v + 1) - f[1],
-                          __ldcg(L.warped + 3 * v + 2) - f[2]};
-            float r = a.lam_d * dot3(a.normals + 3 * px, d);
-            __stcg(b.rdepth + c, r);
-            e2[0] += (double)(r * r);
-        }
-        for (long t = gt; t < nreg; t += gstride) {
-            int i = (int)(t / a.kreg);
-            uint32_t nb = a.gidx[t];
-            float* rr = b.rreg + 3 * t;
-            if (nb >= (uint32_t)n) {
-                __stcg(rr, 0.f);
-                __stcg(rr + 1, 0.f);
-                __stcg(rr + 2, 0.f);
-                continue;
-            }
-            float Ti[16], Tn[16], tc[3], tn[3];
-#pragma unroll
-            for (int e = 0; e < 16; ++e) {
-                Ti[e] = __ldcg(L.T_pending + 16 * (long)i + e);
-                Tn[e] = __ldcg(L.T_pending + 16 * (long)nb + e);
-            }
-            mat4_point(Ti, a.nodes + 3 * (long)i, tc);
-            mat4_point(Tn, a.nodes + 3 * (long)i, tn);
-            for (int ax = 0; ax < 3; ++ax) {
-                float r = (tc[ax] - tn[ax]) * a.lam_r;
-                __stcg(rr + ax, r);
-                e2[1] += (double)(r * r);
-            }
-        }
+        gn_residuals(a, L.warped, L.T_pending, n, ncorr, gt, gstride, e2);
         cluster_sum<2>(e2, cs);
         // ---- energy test and commit decision (src/VolumeFusion.cu:589-598)
         const double e = e2[0] + e2[1];
@@ -1007,150 +1185,31 @@ __global__ void __launch_bounds__(kLoopThreads, 1) gn_loop_kernel(LoopArgs L) {
         }
         if (commit)
             for (long t = gt; t < (long)n * 16; t += gstride) L.T_committed[t] = __ldcg(L.T_pending + t);
-        if (ds) {
-            // ---- J^T r over the cluster, one node per warp; then the solve in CTA 0
-            for (int node = gw; node < n; node += nw) {
-                float jv[6];
-                jtr_node(a, node, n, jv);
-                if (lane < 6) {
-                    float ji = jv[0];
-#pragma unroll
-                    for (int q = 1; q < 6; ++q)
-                        if (lane == q) ji = jv[q];
-                    __stcg(b.jtr + (long)node * 6 + lane, ji);
-                }
-            }
-            cluster_barrier();
-            pcg_ds(L, n, dsl, cs, ds_ph);
-            cluster_barrier();
-        } else {
-        // ---- J^T r (one node per warp), then x = 0, r = b, z = M^-1 r; rz = r.z, bb = b.b
-        double d2[2] = {0.0, 0.0};
-        for (int node = gw; node < n; node += nw) {
-            float jv[6];
-            jtr_node(a, node, n, jv);
-            if (lane < 6) {
-                const long o = (long)node * 6;
-                const float* Mi = b.minv + (long)node * 36 + lane * 6;
-                float zi = 0.f;
-#pragma unroll
-                for (int q = 0; q < 6; ++q) zi = zi + Mi[q] * jv[q];
-                float ji = jv[0];
-#pragma unroll
-                for (int q = 1; q < 6; ++q)
-                    if (lane == q) ji = jv[q];
-                b.jtr[o + lane] = ji;
-                __stcg(b.x + o + lane, 0.f);
-                __stcg(b.r + o + lane, ji);
-                __stcg(b.z + o + lane, zi);
-                d2[0] += (double)ji * (double)zi;
-                d2[1] += (double)ji * (double)ji;
-            }
-        }
-        cluster_sum<2>(d2, cs);
-        // ---- PCG, six lanes per node (entry i = lane % 6 of node group lane / 6, five groups per
-        // warp).  Pipelined recurrences: A p_k = A z_k + beta_k A p_{k-1} and
-        // p_k = z_k + beta_k p_{k-1}, so the SpMV reads z, complete at the barrier that gave beta_k.
-        const int grp = lane / 6, ei = lane - 6 * grp;
-        const bool glane = lane < 30;
-        const int g0 = gw * 5 + grp, gstep = nw * 5;
-        double rz = d2[0];
-        const double bnorm2 = d2[1];
-        float beta = 0.f;
-        for (int it = 0; it < L.pcg_iters; ++it) {
-            double pap[1] = {0.0};
-            if (glane)
-                for (int node = g0; node < n; node += gstep) {
-                    const long o = (long)node * 6 + ei;
-                    const float az = spmv_entry(b, node, ei, b.z);
-                    const float zi = __ldcg(b.z + o);
-                    float pi = zi, api = az;
-                    if (it) {
-                        pi = zi + beta * __ldcg(b.p + o);
-                        api = az + beta * __ldcg(b.ap + o);
-                    }
-                    __stcg(b.p + o, pi);
-                    __stcg(b.ap + o, api);
-                    pap[0] += (double)pi * (double)api;
-                }
-            cluster_sum<1>(pap, cs);
-            if (pap[0] == 0.0 || !(pap[0] == pap[0])) break;
-            const float alpha = (float)(rz / pap[0]);
-            // x += alpha p; r -= alpha A p; z = M^-1 r; r.z, r.r
-            double q2[2] = {0.0, 0.0};
-            for (int base = gw * 5; base < n; base += gstep) {  // warp-uniform trip count
-                const int node = base + grp;
-                const bool act = glane && node < n;
-                const long o = (long)node * 6 + ei;
-                float rv = 0.f;
-                if (act) {
-                    __stcg(b.x + o, __ldcg(b.x + o) + alpha * __ldcg(b.p + o));
-                    rv = __ldcg(b.r + o) - alpha * __ldcg(b.ap + o);
-                    __stcg(b.r + o, rv);
-                }
-                float zi = 0.f;
-                const float* Mi = b.minv + (long)(act ? node : 0) * 36 + ei * 6;
-#pragma unroll
-                for (int q = 0; q < 6; ++q) {
-                    const float rq = __shfl_sync(0xffffffffu, rv, glane ? grp * 6 + q : q);
-                    if (act) zi = zi + Mi[q] * rq;
-                }
-                if (act) {
-                    __stcg(b.z + o, zi);
-                    q2[0] += (double)rv * (double)zi;
-                    q2[1] += (double)rv * (double)rv;
-                }
-            }
-            cluster_sum<2>(q2, cs);
-            beta = (float)(q2[0] / rz);
-            rz = q2[0];
-            if (L.tol > 0 && q2[1] <= L.tol * L.tol * bnorm2) break;
-        }
-        cluster_barrier();  // x complete
-        // ---- T_pending -= [[x_rot]x, x_t; 0] (updateTransformsKernel, src/MotionOptimization.cu:483-498)
-        for (int node = gw; node < n; node += nw) {
-            if (lane < 16) {
-                float u[6];
-#pragma unroll
-                for (int q = 0; q < 6; ++q) u[q] = __ldcg(b.x + (long)node * 6 + q);
-                const float U[16] = {0.f, u[2], -u[1], 0.f, -u[2], 0.f, u[0], 0.f,
-                                     u[1], -u[0], 0.f, 0.f, u[3], u[4], u[5], 0.f};
-                float* T = L.T_pending + (long)node * 16 + lane;
-                __stcg(T, __ldcg(T) - U[lane]);
-            }
-        }
+        gn_jtr(a, n, gw, nw);
         cluster_barrier();
-        }
-        // ---- re-warp the canonical vertices with T_pending (warpKernel, src/ComputeCorrespondence.cu:13-30)
-        for (long i = gt; i < m; i += gstride) {
-            const float p[3] = {L.points[3 * i], L.points[3 * i + 1], L.points[3 * i + 2]};
-            bool zero = true;
-            for (int j = 0; j < a.k; ++j)
-                if (!(fabsf(a.mw[i * a.k + j]) <= 1e-5f)) zero = false;
-            float acc[3] = {p[0], p[1], p[2]};
-            if (!zero) {
-                acc[0] = acc[1] = acc[2] = 0.f;
-                for (int j = 0; j < a.k; ++j) {
-                    uint32_t nb = a.midx[i * a.k + j];
-                    if (nb == AFX_INVALID_INDEX) continue;
-                    float T[16], o[3];
-#pragma unroll
-                    for (int e = 0; e < 16; ++e) T[e] = __ldcg(L.T_pending + 16 * (long)nb + e);
-                    mat4_point(T, p, o);
-                    float wj = a.mw[i * a.k + j];
-                    acc[0] = acc[0] + wj * o[0];
-                    acc[1] = acc[1] + wj * o[1];
-                    acc[2] = acc[2] + wj * o[2];
-                }
-            }
-            __stcg(L.warped + 3 * i, acc[0]);
-            __stcg(L.warped + 3 * i + 1, acc[1]);
-            __stcg(L.warped + 3 * i + 2, acc[2]);
-        }
+        gn_solve(L, n, ds, dsl, cs, ds_ph, gt, gstride);
+        gn_rewarp(a, L.points, L.warped, L.T_pending, m, gt, gstride);
         cluster_barrier();
     }
     // no CTA leaves while another may still read its shared memory
     cluster_barrier();
+}
+
+// One PCG solve of a system assembled by afx_gn_build (J^T J blocks, inverses and J^T r in the
+// workspace); x in b.x.
+__global__ void __launch_bounds__(kLoopThreads, 1) gn_solve_kernel(LoopArgs L) {
+    const GnArgs& a = L.g;
+    __shared__ ClusterSums cs;
+    extern __shared__ double ds_smem[];
+    if (threadIdx.x == 0) cs.phase = 0;
+    __syncthreads();
+    const unsigned rank = cluster_rank(), ncta = cluster_size();
+    const long gt = (long)rank * kLoopThreads + threadIdx.x, gstride = (long)ncta * kLoopThreads;
+    const int n = min(*a.n_nodes, a.n_max);
+    const DsLayout dsl = ds_layout(ds_smem);
+    int ds_ph = 0;
+    const bool ds = n > 0 && (n + (int)ncta - 1) / (int)ncta <= kDsNpc && ds_stage(a.b, n, dsl, cs, ds_ph);
+    gn_solve(L, n, ds, dsl, cs, ds_ph, gt, gstride);
 }
 
 }  // namespace afx
@@ -1175,6 +1234,8 @@ static int gn_cluster_size() {
     if (!cached) {
         cudaFuncSetAttribute(gn_loop_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         cudaFuncSetAttribute(gn_loop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDsSmem);
+        cudaFuncSetAttribute(gn_solve_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(gn_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDsSmem);
         const int sizes[2] = {16, 8};
         for (int c : sizes) {
             cudaLaunchConfig_t cfg = {};
@@ -1297,7 +1358,8 @@ int gn_icp_setup(const GnArgs& a, float* T_pending, const float* T_committed, cu
     const GnBuffers& b = a.b;
     gn_state_reset_kernel<<<1, 1, 0, st>>>(b.state);
     AFX_LAUNCH_CHECK();
-    AFX_CUDA(cudaMemcpyAsync(T_pending, T_committed, (size_t)a.n_max * 64, cudaMemcpyDeviceToDevice, st));
+    if (T_pending)
+        AFX_CUDA(cudaMemcpyAsync(T_pending, T_committed, (size_t)a.n_max * 64, cudaMemcpyDeviceToDevice, st));
     const unsigned nb = (unsigned)((a.n_max + kGnWarps - 1) / kGnWarps);
     const int words = (a.n_max + 31) / 32;
     const size_t smem = (size_t)kGnWarps * words * 4;
@@ -1317,18 +1379,7 @@ int gn_icp_setup(const GnArgs& a, float* T_pending, const float* T_committed, cu
 // All Gauss-Newton iterations of one ICP iteration (src/VolumeFusion.cu:571-691): one launch
 // of gn_loop_kernel.  On return (stream order) T_committed holds the last accepted transforms,
 // T_pending the last update and `warped` the canonical vertices warped by T_pending.
-int gn_loop(const GnArgs& a, const float* points, float* warped, float* T_committed, float* T_pending, int gn_iters,
-            int pcg_iters, double tol, cudaStream_t st) {
-    if (gn_iters <= 0) return AFX_OK;
-    LoopArgs L;
-    L.g = a;
-    L.points = points;
-    L.warped = warped;
-    L.T_committed = T_committed;
-    L.T_pending = T_pending;
-    L.gn_iters = gn_iters;
-    L.pcg_iters = pcg_iters;
-    L.tol = tol;
+static int launch_cluster(void (*kernel)(LoopArgs), const LoopArgs& L, cudaStream_t st) {
     const int c = gn_cluster_size();
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(c);
@@ -1342,9 +1393,252 @@ int gn_loop(const GnArgs& a, const float* points, float* warped, float* T_commit
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    AFX_CUDA(cudaLaunchKernelEx(&cfg, gn_loop_kernel, L));
+    AFX_CUDA(cudaLaunchKernelEx(&cfg, kernel, L));
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
 
+int gn_loop(const GnArgs& a, const float* points, float* warped, float* T_committed, float* T_pending, int gn_iters,
+            int pcg_iters, double tol, cudaStream_t st) {
+    if (gn_iters <= 0) return AFX_OK;
+    LoopArgs L;
+    L.g = a;
+    L.points = points;
+    L.warped = warped;
+    L.T_committed = T_committed;
+    L.T_pending = T_pending;
+    L.gn_iters = gn_iters;
+    L.pcg_iters = pcg_iters;
+    L.tol = tol;
+    return launch_cluster(gn_loop_kernel, L, st);
+}
+
 }  // namespace afx
+
+// ------------------------------------------------------------------------------------
+// Stand-alone Gauss-Newton operators: residuals, J^T J / J^T r (exported in the reference's dense
+// layout), the PCG solve and the transform update, for callers that drive the steps themselves.
+// ------------------------------------------------------------------------------------
+
+namespace afx {
+
+__global__ void gn_corr_of_vertex_kernel(const int* corr, const unsigned* n_corr, long c_max, int* cov) {
+    const long nc = min((long)*n_corr, c_max);
+    AFX_GRID_STRIDE(c, nc) cov[corr[2 * c]] = (int)c;
+}
+
+__global__ void __launch_bounds__(256) gn_residual_kernel(GnArgs a, const float* warped, const float* T) {
+    const int n = min(*a.n_nodes, a.n_max);
+    const long ncorr = min((long)*a.corr_count, a.c_max);
+    double e2[2] = {0.0, 0.0};
+    gn_residuals(a, warped, T, n, ncorr, blockIdx.x * (long)blockDim.x + threadIdx.x, (long)gridDim.x * blockDim.x, e2);
+}
+
+__global__ void __launch_bounds__(256) gn_jtr_kernel(GnArgs a) {
+    const int n = min(*a.n_nodes, a.n_max);
+    const int gw = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5);
+    gn_jtr(a, n, gw, (int)((gridDim.x * (long)blockDim.x) >> 5));
+}
+
+// Dense (6 n_host)^2 J^T J: diagonal blocks, upper blocks and their transposes (the layout
+// fillJTJKernel writes over runInitIdentityKernel's identity).
+__global__ void gn_dense_kernel(GnArgs a, int n_host, float* jtj) {
+    const int n = min(min(*a.n_nodes, a.n_max), n_host);
+    const long ld = 6L * n_host;
+    const int lane = threadIdx.x & 31;
+    for (long node = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5; node < n;
+         node += (gridDim.x * (long)blockDim.x) >> 5) {
+        for (int e = lane; e < 36; e += 32) {
+            const int i = e / 6, j = e % 6;
+            jtj[(node * 6 + i) * ld + node * 6 + j] = a.b.diag[node * 36 + e];
+        }
+        const int cnt = a.b.nbr_cnt[node];
+        for (int u = 0; u < cnt; ++u) {
+            const long other = a.b.nbr[node * kMaxNbr + u];
+            if (other <= node) continue;
+            const float* B = a.b.blocks + (node * kMaxNbr + u) * 36;
+            for (int e = lane; e < 36; e += 32) {
+                const int i = e / 6, j = e % 6;
+                jtj[(node * 6 + i) * ld + other * 6 + j] = B[e];
+                jtj[(other * 6 + j) * ld + node * 6 + i] = B[e];
+            }
+        }
+    }
+}
+
+__global__ void gn_copy_residuals_kernel(GnArgs a, float* r_depth, float* r_reg) {
+    const int n = min(*a.n_nodes, a.n_max);
+    const long ncorr = min((long)*a.corr_count, a.c_max);
+    const long nreg = (long)n * a.kreg * 3;
+    AFX_GRID_STRIDE(t, ncorr + nreg) {
+        if (t < ncorr) {
+            if (r_depth) r_depth[t] = __ldcg(a.b.rdepth + t);
+        } else if (r_reg) {
+            r_reg[t - ncorr] = __ldcg(a.b.rreg + (t - ncorr));
+        }
+    }
+}
+
+__global__ void update_transforms_kernel(float* T, const float* x, const int* n_nodes, int n_max) {
+    const int n = min(*n_nodes, n_max);
+    update_transforms_range(T, x, 0, n, blockIdx.x * (long)blockDim.x + threadIdx.x, (long)gridDim.x * blockDim.x);
+}
+
+}  // namespace afx
+
+struct afx_gn {
+    long m_max;
+    int n_max, k, kreg;
+    void* arena;
+    afx::GnBuffers b;
+    int* cov;
+    int* error;
+    unsigned* counts;  // copies of the caller's counters at build time: points, correspondences, nodes
+    afx::GnArgs last;
+    bool built;
+};
+
+using namespace afx;
+
+extern "C" {
+
+int afx_gn_create(long n_points_max, int n_nodes_max, int k, int kreg, afx_gn** out) {
+    if (!out || n_points_max < 1 || n_nodes_max < 1 || k < 1 || k > 8 || kreg < 1 || kreg > 8)
+        return AFX_ERR_INVALID_ARGUMENT;
+    afx_gn* g = new (std::nothrow) afx_gn();
+    if (!g) return AFX_ERR_NO_MEMORY;
+    g->m_max = n_points_max;
+    g->n_max = n_nodes_max;
+    g->k = k;
+    g->kreg = kreg;
+    const size_t ws = gn_workspace_size(n_points_max, n_nodes_max, k, kreg);
+    const size_t bytes = ws + al((size_t)n_points_max * 4) + 512;
+    if (cudaMalloc(&g->arena, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        delete g;
+        return AFX_ERR_NO_MEMORY;
+    }
+    gn_carve(g->arena, ws, n_points_max, n_nodes_max, k, kreg, &g->b);
+    g->cov = reinterpret_cast<int*>(static_cast<char*>(g->arena) + ws);
+    g->error = reinterpret_cast<int*>(static_cast<char*>(g->arena) + ws + al((size_t)n_points_max * 4));
+    g->counts = reinterpret_cast<unsigned*>(static_cast<char*>(g->arena) + ws + al((size_t)n_points_max * 4) + 256);
+    if (cudaMemset(g->error, 0, 4) != cudaSuccess) {
+        cudaFree(g->arena);
+        delete g;
+        return note_cuda_error(cudaGetLastError());
+    }
+    g->built = false;
+    *out = g;
+    return AFX_OK;
+}
+
+int afx_gn_destroy(afx_gn* g) {
+    if (!g) return AFX_ERR_INVALID_ARGUMENT;
+    cudaDeviceSynchronize();
+    cudaError_t e = cudaFree(g->arena);
+    delete g;
+    return note_cuda_error(e);
+}
+
+int afx_gn_build(afx_gn* g, const float* canonical, const unsigned* n_points, const uint32_t* knn_idx,
+                 const float* knn_weights, const int* corr, const unsigned* n_corr, const float* frame_vertices,
+                 const float* frame_normals, const float* warped, const float* nodes, const float* transforms,
+                 const int* n_nodes, const uint32_t* graph_idx, float lambda_depth, float lambda_reg, void* stream) {
+    if (!g || !canonical || !n_points || !knn_idx || !knn_weights || !corr || !n_corr || !frame_vertices ||
+        !frame_normals || !warped || !nodes || !transforms || !n_nodes || !graph_idx)
+        return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    // later calls use these copies, not the caller's counters
+    AFX_CUDA(cudaMemcpyAsync(g->counts, n_points, 4, cudaMemcpyDeviceToDevice, st));
+    AFX_CUDA(cudaMemcpyAsync(g->counts + 1, n_corr, 4, cudaMemcpyDeviceToDevice, st));
+    AFX_CUDA(cudaMemcpyAsync(g->counts + 2, n_nodes, 4, cudaMemcpyDeviceToDevice, st));
+    n_points = g->counts;
+    n_corr = g->counts + 1;
+    n_nodes = reinterpret_cast<const int*>(g->counts + 2);
+    GnArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.mesh = canonical;
+    a.mesh_count = n_points;
+    a.m_max = g->m_max;
+    a.midx = knn_idx;
+    a.mw = knn_weights;
+    a.k = g->k;
+    a.normals = frame_normals;
+    a.frame = frame_vertices;
+    a.corr = corr;
+    a.corr_count = n_corr;
+    a.c_max = g->m_max;
+    a.corr_of_vertex = g->cov;
+    a.nodes = nodes;
+    a.n_nodes = n_nodes;
+    a.n_max = g->n_max;
+    a.gidx = graph_idx;
+    a.kreg = g->kreg;
+    a.lam_d = lambda_depth;
+    a.lam_r = lambda_reg;
+    a.b = g->b;
+    a.error = g->error;
+    AFX_CUDA(cudaMemsetAsync(g->error, 0, 4, st));
+    AFX_CUDA(cudaMemsetAsync(g->cov, 0xff, (size_t)g->m_max * 4, st));
+    gn_corr_of_vertex_kernel<<<grid_for(g->m_max, 256), 256, 0, st>>>(corr, n_corr, g->m_max, g->cov);
+    AFX_LAUNCH_CHECK();
+    int rc = gn_frame_setup(a, st);
+    if (rc) return rc;
+    rc = gn_icp_setup(a, nullptr, nullptr, st);
+    if (rc) return rc;
+    gn_residual_kernel<<<grid_for(g->m_max + (long)g->n_max * g->kreg, 256), 256, 0, st>>>(a, warped, transforms);
+    AFX_LAUNCH_CHECK();
+    gn_jtr_kernel<<<grid_for((long)g->n_max * 32, 256), 256, 0, st>>>(a);
+    AFX_LAUNCH_CHECK();
+    g->last = a;
+    g->built = true;
+    int err = 0;
+    AFX_CUDA(cudaMemcpyAsync(&err, g->error, 4, cudaMemcpyDeviceToHost, st));
+    AFX_CUDA(cudaStreamSynchronize(st));
+    if (err & ERRF_SINGULAR) return AFX_ERR_SINGULAR;
+    if (err & ERRF_CAPACITY) return AFX_ERR_CAPACITY;
+    return AFX_OK;
+}
+
+int afx_gn_export(afx_gn* g, int n_nodes_host, float* jtj, float* jtr, float* r_depth, float* r_reg, void* stream) {
+    if (!g || !g->built || n_nodes_host < 0 || n_nodes_host > g->n_max) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    const long dim = 6L * n_nodes_host;
+    if (jtj && dim > 0) {
+        AFX_CUDA(cudaMemsetAsync(jtj, 0, (size_t)dim * dim * 4, st));
+        gn_dense_kernel<<<grid_for((long)n_nodes_host * 32, 256), 256, 0, st>>>(g->last, n_nodes_host, jtj);
+        AFX_LAUNCH_CHECK();
+    }
+    if (jtr && dim > 0) AFX_CUDA(cudaMemcpyAsync(jtr, g->b.jtr, (size_t)dim * 4, cudaMemcpyDeviceToDevice, st));
+    if (r_depth || r_reg) {
+        gn_copy_residuals_kernel<<<grid_for(g->m_max + (long)g->n_max * g->kreg * 3, 256), 256, 0, st>>>(g->last, r_depth,
+                                                                                                          r_reg);
+        AFX_LAUNCH_CHECK();
+    }
+    return AFX_OK;
+}
+
+int afx_gn_solve(afx_gn* g, float* x, int iterations, double tol, void* stream) {
+    if (!g || !g->built || !x || iterations < 0) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    LoopArgs L;
+    std::memset(&L, 0, sizeof(L));
+    L.g = g->last;
+    L.pcg_iters = iterations;
+    L.tol = tol;
+    int rc = launch_cluster(gn_solve_kernel, L, st);
+    if (rc) return rc;
+    AFX_CUDA(cudaMemcpyAsync(x, g->b.x, (size_t)g->n_max * 6 * 4, cudaMemcpyDeviceToDevice, st));
+    return AFX_OK;
+}
+
+int afx_update_transforms(float* transforms, const float* x, const int* n_nodes, int n_nodes_max, void* stream) {
+    if (!transforms || !x || !n_nodes || n_nodes_max < 0) return AFX_ERR_INVALID_ARGUMENT;
+    if (n_nodes_max == 0) return AFX_OK;
+    update_transforms_kernel<<<grid_for((long)n_nodes_max * 16, 256), 256, 0, as_stream(stream)>>>(transforms, x, n_nodes,
+                                                                                                  n_nodes_max);
+    AFX_LAUNCH_CHECK();
+    return AFX_OK;
+}
+
+}  // extern "C"

@@ -32,7 +32,7 @@ size_t sort_unique_workspace_size(long n_max);
 int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, cudaStream_t st);
 int mc_fused_impl(const float* tsdf, const float* weights, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
-                  unsigned* face_count, long face_cap, cudaStream_t st);
+                  unsigned* face_count, long face_cap, cudaStream_t st, int* error = nullptr);
 int translate_impl(float* pts, const unsigned* count, long n_max, const float* t, cudaStream_t st);
 // pts += sign * t_dev (t_dev in device memory); dst may differ from src
 int translate_dev_impl(float* dst, const float* src, const unsigned* count, long n_max, const float* t_dev, float sign,

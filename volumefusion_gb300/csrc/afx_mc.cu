@@ -6,9 +6,12 @@
 // Case index, edge interpolation and triangulation follow src/MarchingCubes.cu:294-420
 // (corner bit c set when tsdf > iso, cubes skipped when any corner weight is 0, cubes
 // x,y,z < dim-2).  The triangulation table is the reference's (packed re-encoding).
+#include <cuda.h>
+
 #include <cstring>
 
 #include "afx_internal.h"
+#include "afx_tma.h"
 
 namespace afx {
 
@@ -56,6 +59,7 @@ struct McArgs {
     unsigned* vert_count;
     long face_cap;
     int* faces;
+    int* error;  // TMA path: set on a tile-load timeout
 };
 
 // getVertex + interpolate (src/MarchingCubes.cu:294-336)
@@ -106,6 +110,65 @@ AFX_D unsigned warp_append(unsigned* counter, unsigned n) {
     if (lane == 31 && total) base = atomicAdd(counter, total);
     base = __shfl_sync(0xffffffffu, base, 31);
     return base + x - n;
+}
+
+// Vertices and triangles of one cube (all lanes of the warp call this together: the appends are
+// warp-aggregated).  Emits the point-cloud vertices (marchingCubesMeshKernel) and/or the
+// triangles (marchingCubesFullKernel).
+template <bool kPoints, bool kMesh>
+AFX_D void mc_emit(const float* __restrict__ tsdf, const McArgs& a, int x, int y, int z, int ci, bool active) {
+    const unsigned et = active ? c_edge_table[ci] : 0u;
+    float ep[12][3];
+    if (active) {
+#pragma unroll
+        for (int e = 0; e < 12; ++e)
+            if (et & (1u << e)) edge_vertex(tsdf, a.vol, x, y, z, e, a.iso, ep[e]);
+    }
+    if (kPoints) {
+        unsigned n = __popc(et);
+        unsigned pos = warp_append(a.point_count, n);
+        if (active)
+            for (int e = 0; e < 12; ++e)
+                if (et & (1u << e)) {
+                    if (pos < a.point_cap) {
+                        float* o = a.points + 3 * (long)pos;
+                        o[0] = ep[e][0]; o[1] = ep[e][1]; o[2] = ep[e][2];
+                    }
+                    ++pos;
+                }
+    }
+    if (kMesh) {
+        uint64_t tri = active ? c_tri_table[ci] : 0xFull;
+        unsigned nt = 0;
+        for (int s = 0; s < 15; s += 3) {
+            int e0 = (int)((tri >> (4 * s)) & 0xF);
+            if (e0 == 0xF) break;
+            int e1 = (int)((tri >> (4 * (s + 1))) & 0xF), e2 = (int)((tri >> (4 * (s + 2))) & 0xF);
+            if (vne(ep[e0], ep[e1]) && vne(ep[e0], ep[e2]) && vne(ep[e1], ep[e2])) ++nt;
+        }
+        unsigned f = warp_append(a.face_count, nt);
+        for (int s = 0; s < 15; s += 3) {
+            int e0 = (int)((tri >> (4 * s)) & 0xF);
+            if (e0 == 0xF) break;
+            int e1 = (int)((tri >> (4 * (s + 1))) & 0xF), e2 = (int)((tri >> (4 * (s + 2))) & 0xF);
+            if (!(vne(ep[e0], ep[e1]) && vne(ep[e0], ep[e2]) && vne(ep[e1], ep[e2]))) continue;
+            if (f < a.face_cap) {
+                float* o = a.verts + 9 * (long)f;
+                const int es[3] = {e0, e1, e2};
+#pragma unroll
+                for (int t = 0; t < 3; ++t) {
+                    o[3 * t] = ep[es[t]][0];
+                    o[3 * t + 1] = ep[es[t]][1];
+                    o[3 * t + 2] = ep[es[t]][2];
+                }
+                int* fo = a.faces + 3 * (long)f;
+                fo[0] = (int)(3 * f);
+                fo[1] = (int)(3 * f + 1);
+                fo[2] = (int)(3 * f + 2);
+            }
+            ++f;
+        }
+    }
 }
 
 // A CTA covers a 32 x 8 patch of cube columns and a run of kMcZ cubes along z; each thread
@@ -164,58 +227,103 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_kernel(const float* __restrict
         }
         const bool active = ci != 0 && ci != 255;
         if (!__any_sync(0xffffffffu, active)) continue;
-        const unsigned et = active ? c_edge_table[ci] : 0u;
-        float ep[12][3];
-        if (active) {
+        mc_emit<kPoints, kMesh>(tsdf, a, x, y, z, ci, active);
+    }
+}
+
+// Same cubes as mc_kernel, with the CTA's whole brick of corner values -- 40 x 9 x (kMcZ + 1)
+// floats of TSDF and of weights, x padded to a 16-byte multiple -- brought into shared memory by
+// two TMA tile loads on one mbarrier, so the march reads no global memory for inactive cubes.
+constexpr int kMcTX = 40;  // box width in floats (>= kMcX + 1, 160 B)
+// each brick starts on a 128-byte boundary (TMA destination alignment), plus slack to align the base
+constexpr size_t kMcBrickBytes = ((size_t)kMcTX * (kMcY + 1) * (kMcZ + 1) * sizeof(float) + 127) / 128 * 128;
+constexpr size_t kMcTmaSmem = 2 * kMcBrickBytes + 128;
+
+AFX_D uint32_t mc_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+template <bool kPoints, bool kMesh>
+__global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_constant__ CUtensorMap map_t,
+                                                            const __grid_constant__ CUtensorMap map_w,
+                                                            const float* __restrict__ tsdf, McArgs a) {
+    extern __shared__ __align__(128) unsigned char mc_raw[];
+    __shared__ alignas(8) unsigned long long mbar;
+    constexpr int kSlice = kMcTX * (kMcY + 1);
+    const uint32_t pad = (128u - (mc_smem_u32(mc_raw) & 127u)) & 127u;
+    float* st = reinterpret_cast<float*>(mc_raw + pad);
+    float* sw = reinterpret_cast<float*>(mc_raw + pad + kMcBrickBytes);
+    const int tid = threadIdx.y * kMcX + threadIdx.x;
+    const int x0 = blockIdx.x * kMcX, y0 = blockIdx.y * kMcY, z0 = blockIdx.z * kMcZ;
+    if (((mc_smem_u32(st) | mc_smem_u32(sw)) & 127u) != 0u) {  // never expected: refuse rather than fault
+        if (tid == 0 && a.error) atomicOr(a.error, ERRF_TMA);
+        return;
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mc_smem_u32(&mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const unsigned bytes = (unsigned)(2 * kSlice * (kMcZ + 1) * sizeof(float));
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mc_smem_u32(&mbar)), "r"(bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+            "[%5];" ::"r"(mc_smem_u32(st)),
+            "l"(&map_t), "r"(x0), "r"(y0), "r"(z0), "r"(mc_smem_u32(&mbar))
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+            "[%5];" ::"r"(mc_smem_u32(sw)),
+            "l"(&map_w), "r"(x0), "r"(y0), "r"(z0), "r"(mc_smem_u32(&mbar))
+            : "memory");
+    }
+    // bounded wait for the brick (phase 0); the give-up decision is uniform across the CTA
+    bool done = false;
+    for (int it = 0; it < (1 << 22) && !done; ++it) {
+        uint32_t ok;
+        asm volatile(
+            "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+            : "=r"(ok)
+            : "r"(mc_smem_u32(&mbar))
+            : "memory");
+        done = ok != 0;
+    }
+    if (__syncthreads_or(!done)) {
+        if (tid == 0 && a.error) atomicOr(a.error, ERRF_TMA | ERRF_TIMEOUT);
+        // the copies may still land: wait for them (bounded) before the CTA's shared memory goes
+        for (int it = 0; it < (1 << 22); ++it) {
+            uint32_t ok;
+            asm volatile(
+                "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+                : "=r"(ok)
+                : "r"(mc_smem_u32(&mbar))
+                : "memory");
+            if (ok) break;
+        }
+        return;
+    }
+    const int nx = a.vol.dims[0] - 2, ny = a.vol.dims[1] - 2, nz = a.vol.dims[2] - 2;
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+    const int z1 = min(z0 + kMcZ, nz);
+    const bool col = x < nx && y < ny;
+    const int o00 = threadIdx.y * kMcTX + threadIdx.x;  // (x, y) within a slice
+    for (int z = z0; z < z1; ++z) {
+        const int s0 = (z - z0) * kSlice + o00, s1 = s0 + kSlice;
+        int ci = 0;
+        if (col) {
+            // corners (src/MarchingCubes.cu:338-379): c0 (1,1,0) c1 (1,0,0) c2 (0,0,0) c3 (0,1,0), c4..c7 one slice up
+            const int off[8] = {s0 + kMcTX + 1, s0 + 1, s0, s0 + kMcTX, s1 + kMcTX + 1, s1 + 1, s1, s1 + kMcTX};
+            bool any_zero = false;
 #pragma unroll
-            for (int e = 0; e < 12; ++e)
-                if (et & (1u << e)) edge_vertex(tsdf, a.vol, x, y, z, e, a.iso, ep[e]);
-        }
-        if (kPoints) {
-            unsigned n = __popc(et);
-            unsigned pos = warp_append(a.point_count, n);
-            if (active)
-                for (int e = 0; e < 12; ++e)
-                    if (et & (1u << e)) {
-                        if (pos < a.point_cap) {
-                            float* o = a.points + 3 * (long)pos;
-                            o[0] = ep[e][0]; o[1] = ep[e][1]; o[2] = ep[e][2];
-                        }
-                        ++pos;
-                    }
-        }
-        if (kMesh) {
-            uint64_t tri = active ? c_tri_table[ci] : 0xFull;
-            unsigned nt = 0;
-            for (int s = 0; s < 15; s += 3) {
-                int e0 = (int)((tri >> (4 * s)) & 0xF);
-                if (e0 == 0xF) break;
-                int e1 = (int)((tri >> (4 * (s + 1))) & 0xF), e2 = (int)((tri >> (4 * (s + 2))) & 0xF);
-                if (vne(ep[e0], ep[e1]) && vne(ep[e0], ep[e2]) && vne(ep[e1], ep[e2])) ++nt;
-            }
-            unsigned f = warp_append(a.face_count, nt);
-            for (int s = 0; s < 15; s += 3) {
-                int e0 = (int)((tri >> (4 * s)) & 0xF);
-                if (e0 == 0xF) break;
-                int e1 = (int)((tri >> (4 * (s + 1))) & 0xF), e2 = (int)((tri >> (4 * (s + 2))) & 0xF);
-                if (!(vne(ep[e0], ep[e1]) && vne(ep[e0], ep[e2]) && vne(ep[e1], ep[e2]))) continue;
-                if (f < a.face_cap) {
-                    float* o = a.verts + 9 * (long)f;
-                    const int es[3] = {e0, e1, e2};
+            for (int c = 0; c < 8; ++c) any_zero |= (sw[off[c]] == 0.0f);
+            if (!any_zero)
 #pragma unroll
-                    for (int t = 0; t < 3; ++t) {
-                        o[3 * t] = ep[es[t]][0];
-                        o[3 * t + 1] = ep[es[t]][1];
-                        o[3 * t + 2] = ep[es[t]][2];
-                    }
-                    int* fo = a.faces + 3 * (long)f;
-                    fo[0] = (int)(3 * f);
-                    fo[1] = (int)(3 * f + 1);
-                    fo[2] = (int)(3 * f + 2);
-                }
-                ++f;
-            }
+                for (int c = 0; c < 8; ++c)
+                    if (st[off[c]] > a.iso) ci |= 1 << c;
         }
+        const bool active = ci != 0 && ci != 255;
+        if (!__any_sync(0xffffffffu, active)) continue;
+        mc_emit<kPoints, kMesh>(tsdf, a, x, y, z, ci, active);
     }
 }
 
@@ -223,9 +331,25 @@ __global__ void mc_vert_count_kernel(const unsigned* face_count, unsigned* vert_
     *vert_count = 3u * *face_count;
 }
 
+// 3-D tiled map over a float volume; the box is one CTA's brick of corner values.
+static bool make_volume_map(CUtensorMap* map, const float* base, const Volume& vol) {
+    if ((vol.dims[0] * sizeof(float)) % 16 != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)vol.dims[0], (cuuint64_t)vol.dims[1], (cuuint64_t)vol.dims[2]};
+    cuuint64_t strides[2] = {(cuuint64_t)vol.dims[0] * sizeof(float),
+                             (cuuint64_t)vol.dims[0] * vol.dims[1] * sizeof(float)};
+    cuuint32_t box[3] = {(cuuint32_t)kMcTX, (cuuint32_t)(kMcY + 1), (cuuint32_t)(kMcZ + 1)};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 int mc_fused_impl(const float* tsdf, const float* weights, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
-                  unsigned* face_count, long face_cap, cudaStream_t st) {
+                  unsigned* face_count, long face_cap, cudaStream_t st, int* error) {
     int rc = upload_tables();
     if (rc) return rc;
     McArgs a;
@@ -239,16 +363,32 @@ int mc_fused_impl(const float* tsdf, const float* weights, const Volume& vol, fl
     a.vert_count = vert_count;
     a.face_cap = face_cap < vert_cap / 3 ? face_cap : vert_cap / 3;
     a.faces = faces;
+    a.error = error;
     const long ncubes = (long)(vol.dims[0] - 2) * (vol.dims[1] - 2) * (vol.dims[2] - 2);
     if (ncubes <= 0) return AFX_OK;
     const dim3 grid((unsigned)((vol.dims[0] - 2 + kMcX - 1) / kMcX), (unsigned)((vol.dims[1] - 2 + kMcY - 1) / kMcY),
                     (unsigned)((vol.dims[2] - 2 + kMcZ - 1) / kMcZ));
     const dim3 block(kMcX, kMcY);
     const bool P = points != nullptr, M = verts != nullptr;
-    if (P && M) mc_kernel<true, true><<<grid, block, 0, st>>>(tsdf, weights, a);
-    else if (P) mc_kernel<true, false><<<grid, block, 0, st>>>(tsdf, weights, a);
-    else if (M) mc_kernel<false, true><<<grid, block, 0, st>>>(tsdf, weights, a);
-    else return AFX_OK;
+    if (!P && !M) return AFX_OK;
+    // TMA bricks where the caller can receive a load-timeout report and the map encodes
+    CUtensorMap mt, mw;
+    if (error && make_volume_map(&mt, tsdf, vol) && make_volume_map(&mw, weights, vol)) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(mc_tma_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMcTmaSmem);
+            cudaFuncSetAttribute(mc_tma_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMcTmaSmem);
+            cudaFuncSetAttribute(mc_tma_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMcTmaSmem);
+            attr = true;
+        }
+        if (P && M) mc_tma_kernel<true, true><<<grid, block, kMcTmaSmem, st>>>(mt, mw, tsdf, a);
+        else if (P) mc_tma_kernel<true, false><<<grid, block, kMcTmaSmem, st>>>(mt, mw, tsdf, a);
+        else mc_tma_kernel<false, true><<<grid, block, kMcTmaSmem, st>>>(mt, mw, tsdf, a);
+    } else {
+        if (P && M) mc_kernel<true, true><<<grid, block, 0, st>>>(tsdf, weights, a);
+        else if (P) mc_kernel<true, false><<<grid, block, 0, st>>>(tsdf, weights, a);
+        else mc_kernel<false, true><<<grid, block, 0, st>>>(tsdf, weights, a);
+    }
     AFX_LAUNCH_CHECK();
     if (M && vert_count) {
         mc_vert_count_kernel<<<1, 1, 0, st>>>(face_count, vert_count);

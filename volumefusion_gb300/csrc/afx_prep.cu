@@ -9,6 +9,7 @@
 #include <cstring>
 
 #include "afx_common.cuh"
+#include "afx_tma.h"
 
 namespace afx {
 
@@ -377,11 +378,7 @@ __global__ void remove_without_normals_kernel(const float* normals, float* V, fl
 
 // ---- TMA descriptor ----
 
-typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
-                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
-                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-static EncodeTiledFn encode_fn() {
+EncodeTiledFn encode_fn() {
     static EncodeTiledFn fn = nullptr;
     static bool tried = false;
     if (!tried) {
