@@ -75,15 +75,16 @@ AFX_D void edge_vertex(const float* __restrict__ tsdf, const Volume& vol, int x,
     float p0[3], p1[3];
     voxel_to_world(x1, y1, z1, vol.vs, vol.half, p0);
     voxel_to_world(x2, y2, z2, vol.vs, vol.half, p1);
-    if ((double)fabsf(iso - t0) < 1e-7) {
+    // (double)v < 1e-7 is v < 1e-7f for every float v: 1e-7f is the smallest float >= 1e-7
+    if (fabsf(iso - t0) < 1e-7f) {
         o[0] = p0[0]; o[1] = p0[1]; o[2] = p0[2];
         return;
     }
-    if ((double)fabsf(iso - t1) < 1e-7) {
+    if (fabsf(iso - t1) < 1e-7f) {
         o[0] = p1[0]; o[1] = p1[1]; o[2] = p1[2];
         return;
     }
-    if ((double)fabsf(t0 - t1) < 1e-7) {
+    if (fabsf(t0 - t1) < 1e-7f) {
         o[0] = p0[0]; o[1] = p0[1]; o[2] = p0[2];
         return;
     }
@@ -247,6 +248,8 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_consta
                                                             const float* __restrict__ tsdf, McArgs a) {
     extern __shared__ __align__(128) unsigned char mc_raw[];
     __shared__ alignas(8) unsigned long long mbar;
+    __shared__ unsigned q[kMcX * kMcY * kMcZ];  // surface cubes of this CTA: ci | x << 8 | y << 13 | z << 16
+    __shared__ unsigned q_n;
     constexpr int kSlice = kMcTX * (kMcY + 1);
     const uint32_t pad = (128u - (mc_smem_u32(mc_raw) & 127u)) & 127u;
     float* st = reinterpret_cast<float*>(mc_raw + pad);
@@ -260,6 +263,7 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_consta
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mc_smem_u32(&mbar)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        q_n = 0;
     }
     __syncthreads();
     if (tid == 0) {
@@ -322,8 +326,28 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_consta
                     if (st[off[c]] > a.iso) ci |= 1 << c;
         }
         const bool active = ci != 0 && ci != 255;
-        if (!__any_sync(0xffffffffu, active)) continue;
-        mc_emit<kPoints, kMesh>(tsdf, a, x, y, z, ci, active);
+        // queue the surface cubes (warp-aggregated), processed densely below
+        const unsigned bal = __ballot_sync(0xffffffffu, active);
+        if (bal) {
+            const int lane = threadIdx.x & 31;  // blockDim.x == 32: a warp is one row of x
+            unsigned base = 0;
+            if (lane == 0) base = atomicAdd(&q_n, (unsigned)__popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (active)
+                q[base + __popc(bal & ((1u << lane) - 1))] =
+                    (unsigned)ci | ((unsigned)threadIdx.x << 8) | ((unsigned)threadIdx.y << 13) | ((unsigned)(z - z0) << 16);
+        }
+    }
+    __syncthreads();
+    // edge vertices and triangles of the queued cubes, one per thread: the FP64 interpolation
+    // then runs with full warps instead of one or two surface lanes per warp
+    const unsigned nq = q_n;
+    for (unsigned r0 = 0; r0 < nq; r0 += kMcX * kMcY) {
+        const unsigned qi = r0 + tid;
+        const bool act = qi < nq;
+        const unsigned e = act ? q[qi] : 0u;
+        mc_emit<kPoints, kMesh>(tsdf, a, x0 + (int)((e >> 8) & 31u), y0 + (int)((e >> 13) & 7u),
+                                z0 + (int)((e >> 16) & 15u), (int)(e & 255u), act);
     }
 }
 
