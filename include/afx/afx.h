@@ -348,6 +348,14 @@ int afx_fusion_set_transforms(afx_fusion* f, const float* transforms_host, int n
 /* Number of kernels the library launched since the session was created. */
 long afx_fusion_kernel_launches(const afx_fusion* f);
 
+/* Replay non-rigid frames from CUDA graphs (default on): from the fourth frame of a sequence the
+ * frame's kernels are launched as one graph, captured on first use (one per buffer parity); the
+ * input is copied into the session's own buffer first.  Off: every kernel is launched one by
+ * one.  Results are the same either way.  Stage timing always launches one by one. */
+int afx_fusion_set_graphs(afx_fusion* f, int on);
+/* Number of frame graphs captured so far (0 while graphs are off or capture fell back). */
+int afx_fusion_graph_count(const afx_fusion* f);
+
 /* Per-stage GPU timing (CUDA events around each stage, like the reference's TimeMap).
  * Stages: 0 prep, 1 rigid integration, 2 point-cloud sort/unique, 3 graph build, 4 KNN +
  * weights, 5 Gauss-Newton structure, 6 Gauss-Newton iterations, 7 voxel support,

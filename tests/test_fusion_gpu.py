@@ -84,6 +84,29 @@ def test_session_is_deterministic():
         assert np.array_equal(a, b)
 
 
+def test_graph_replay_equals_eager_launches():
+    """Frames replayed from captured CUDA graphs give the same bits as kernels launched one by one."""
+    from volumefusion_gb300 import configs
+    cfg = configs.small_nonrigid(n_frames=8)
+    frames = configs.small_frames(cfg)
+    outs = []
+    for graphs in (True, False):
+        s = _session(cfg)
+        s.set_graphs(graphs)
+        for mm in frames:
+            s.process(mm)
+        st = s.stats()
+        assert st["error"] == 0, st
+        t, w = s.tsdf()
+        _, _, T = s.graph()
+        outs.append((t.cpu().numpy(), w.cpu().numpy(), T.cpu().numpy(), st["frame"], st["n_nodes"]))
+        assert (s.graph_count() > 0) == graphs
+        s.close()
+    for a, b in zip(outs[0], outs[1]):
+        assert np.array_equal(a, b)
+    assert outs[0][3] == len(frames) - 1
+
+
 def test_capsule_sequence_256_runs_clean():
     from volumefusion_gb300 import configs
     cfg = configs.nonrigid_capsules_256(n_frames=30)

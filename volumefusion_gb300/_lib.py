@@ -77,6 +77,8 @@ SIGNATURES = {
     "afx_gn_export": (i32, [vp, i32, vp, vp, vp, vp, vp]),
     "afx_gn_solve": (i32, [vp, vp, i32, C.c_double, vp]),
     "afx_update_transforms": (i32, [vp, vp, vp, i32, vp]),
+    "afx_fusion_set_graphs": (i32, [vp, i32]),
+    "afx_fusion_graph_count": (i32, [vp]),
     "afx_fusion_default_params": (None, [C.POINTER(FusionParams)]),
     "afx_fusion_create": (i32, [C.POINTER(FusionParams), C.POINTER(vp)]),
     "afx_fusion_destroy": (i32, [vp]),

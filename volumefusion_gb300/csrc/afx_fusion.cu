@@ -115,6 +115,14 @@ struct afx_fusion {
     float* points_buf[2];
     unsigned* npoints_buf[2];
     unsigned* mesh_used;   // canonical point count used by the last frame
+    int* frame_dev;        // frame index on the device (written into the statistics)
+    // non-rigid frames replayed from CUDA graphs, one per (graph built or not, buffer parity),
+    // captured on first use; per-stage timing runs eagerly instead
+    bool graphs = true;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    long glaunches[2][2] = {{0, 0}, {0, 0}};  // kernels in each captured frame
+    long replayed = 0;                        // kernels launched by graph replays
 };
 
 namespace afx {
@@ -140,10 +148,11 @@ __global__ void frame_begin_kernel(unsigned* epoch, unsigned* ncorr, int* error,
     *nmfaces = 0;
 }
 
-__global__ void stats_kernel(FrameStats* s, int frame, const int* n_nodes, const int* n_old, const unsigned* npoints,
+__global__ void stats_kernel(FrameStats* s, int* frame, const int* n_nodes, const int* n_old, const unsigned* npoints,
                              const unsigned* ncorr, const GnState* gn, const unsigned* nv, const unsigned* nf,
                              const int* error, int nonrigid) {
-    s->frame = frame;
+    s->frame = *frame;
+    *frame = *frame + 1;
     s->n_nodes = *n_nodes;
     s->new_nodes = nonrigid ? *n_nodes - *n_old : 0;
     s->mesh_points = *npoints;
@@ -276,7 +285,7 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     add(M * 12); add(M * 8); add(64); add(M * 4);
     add(p.triangle_capacity * 36); add(p.triangle_capacity * 12); add(64); add(64);
     add(nbricks * 512 * sizeof(WarpedVoxel)); add(nbricks * 512);
-    add(sizeof(FrameStats));
+    add(sizeof(FrameStats)); add(64);
     add(f->ws_sort_bytes); add(f->ws_graph_bytes); add(f->ws_corr_bytes); add(f->ws_support_bytes); add(f->ws_gn_bytes);
     f->arena_bytes = sz + 4096;
     cudaError_t e = cudaMalloc(&f->arena, f->arena_bytes);
@@ -334,6 +343,7 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     f->wvox = (WarpedVoxel*)take(nbricks * 512 * sizeof(WarpedVoxel));
     f->wcount = (unsigned char*)take(nbricks * 512);
     f->stats = (FrameStats*)take(sizeof(FrameStats));
+    f->frame_dev = (int*)take(64);
     f->ws_sort = take(f->ws_sort_bytes);
     f->ws_graph = take(f->ws_graph_bytes);
     f->ws_corr = take(f->ws_corr_bytes);
@@ -368,6 +378,10 @@ int afx_fusion_destroy(afx_fusion* f) {
     cudaDeviceSynchronize();
     for (auto& m : f->marks) cudaEventDestroy(m.second);
     for (auto e : f->ev_pool) cudaEventDestroy(e);
+    for (auto& row : f->gexec)
+        for (auto& g : row)
+            if (g) cudaGraphExecDestroy(g);
+    if (f->cap_stream) cudaStreamDestroy(f->cap_stream);
     cudaError_t e = cudaFree(f->arena);
     delete f;
     return note_cuda_error(e);
@@ -395,6 +409,7 @@ int afx_fusion_reset(afx_fusion* f, void* stream) {
     f->cur = 0;
     f->points = f->points_buf[0];
     f->npoints = f->npoints_buf[0];
+    AFX_CUDA(cudaMemsetAsync(f->frame_dev, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->n_nodes, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->n_old, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->ncorr, 0, 64, st));
@@ -405,10 +420,10 @@ int afx_fusion_reset(afx_fusion* f, void* stream) {
     return AFX_OK;
 }
 
-static int extract_frame_mesh(afx_fusion* f, cudaStream_t st) {
+static int extract_frame_mesh(afx_fusion* f, int cur, cudaStream_t st) {
     // canonical point cloud for the next frame (runMarchingCubesMeshKernel on the volume the next
     // frame starts from) and, if asked, the output mesh (runMarchingCubesFullKernel), in one pass
-    const int next = f->cur ^ 1;
+    const int next = cur ^ 1;
     AFX_CUDA(cudaMemsetAsync(f->npoints_buf[next], 0, 4, st));
     const bool mesh = f->p.extract_mesh != 0;
     return mc_fused_impl(f->tsdf, f->weights, f->vol, 0.f, f->points_buf[next], f->npoints_buf[next], f->p.mesh_capacity,
@@ -416,10 +431,11 @@ static int extract_frame_mesh(afx_fusion* f, cudaStream_t st) {
                          mesh ? f->mfaces : nullptr, mesh ? f->nmfaces : nullptr, f->p.triangle_capacity, st, f->error);
 }
 
-int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
-    if (!f || !depth_mm) return AFX_ERR_INVALID_ARGUMENT;
+// Everything a frame does on the device, in stream order on `st`; host state is not changed.
+// Non-rigid frames use the point-cloud buffer `cur` (the parity after the toggle) and build the
+// graph when `build`.
+static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t st, int cur, bool build) {
     const afx_fusion_params& p = f->p;
-    cudaStream_t st = as_stream(stream);
     int rc;
     static const float I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     frame_begin_kernel<<<1, 1, 0, st>>>(f->epoch, f->ncorr, f->error, f->nmverts, f->nmfaces);
@@ -446,34 +462,32 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
                                   st, f->centroid0);
         if (rc) return rc;
         stage_mark(f, ST_MC, st);
-        rc = extract_frame_mesh(f, st);
+        rc = extract_frame_mesh(f, cur, st);
         if (rc) return rc;
         stage_mark(f, -1, st);
-        stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame, f->n_nodes, f->n_old, f->mesh_used, f->ncorr, f->gn.state,
+        stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame_dev, f->n_nodes, f->n_old, f->mesh_used, f->ncorr, f->gn.state,
                                       f->nmverts, f->nmfaces, f->error, 0);
         AFX_LAUNCH_CHECK();
-        f->frame++;
         return AFX_OK;
     }
     const long M = p.mesh_capacity;
     const int N = p.node_capacity;
     // canonical point cloud: sort + unique, then + frame-0 centroid (src/VolumeFusion.cu:382-389)
     stage_mark(f, ST_SORT, st);
-    f->cur ^= 1;
-    f->points = f->points_buf[f->cur];
-    f->npoints = f->npoints_buf[f->cur];
-    rc = sort_unique_impl(f->points, f->npoints, M, f->ws_sort, f->ws_sort_bytes, st);
+    float* points = f->points_buf[cur];
+    unsigned* npoints = f->npoints_buf[cur];
+    rc = sort_unique_impl(points, npoints, M, f->ws_sort, f->ws_sort_bytes, st);
     if (rc) return rc;
-    AFX_CUDA(cudaMemcpyAsync(f->mesh_used, f->npoints, 4, cudaMemcpyDeviceToDevice, st));
+    AFX_CUDA(cudaMemcpyAsync(f->mesh_used, npoints, 4, cudaMemcpyDeviceToDevice, st));
     if (rc) return rc;
-    rc = translate_dev_impl(f->points, f->points, f->npoints, M, f->centroid0, 1.f, st);
+    rc = translate_dev_impl(points, points, npoints, M, f->centroid0, 1.f, st);
     if (rc) return rc;
     // motion graph (src/VolumeFusion.cu:394-404)
     stage_mark(f, ST_GRAPH, st);
     record_n_old_kernel<<<1, 1, 0, st>>>(f->n_nodes, f->n_old);
     AFX_LAUNCH_CHECK();
-    if (f->frame == 1 || p.update_graph) {
-        rc = build_graph_impl(f->nodes_host, f->radii, f->T, f->n_nodes, N, f->points, f->npoints, M, p.graph_radius,
+    if (build) {
+        rc = build_graph_impl(f->nodes_host, f->radii, f->T, f->n_nodes, N, points, npoints, M, p.graph_radius,
                               f->ws_graph, f->ws_graph_bytes, f->error, st);
         if (rc) return rc;
         copy_new_nodes_kernel<<<blocks_for(N, 256), 256, 0, st>>>(f->nodes_dev, f->nodes_host, f->n_old, f->n_nodes, N);
@@ -481,19 +495,19 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
     }
     // KNN and weights (src/VolumeFusion.cu:410-424)
     stage_mark(f, ST_KNN, st);
-    rc = knn_impl(f->midx, f->mdist, f->nodes_host, f->n_nodes, N, f->points, f->npoints, M, p.knn, 0, st);
+    rc = knn_impl(f->midx, f->mdist, f->nodes_host, f->n_nodes, N, points, npoints, M, p.knn, 0, st);
     if (rc) return rc;
     rc = knn_impl(f->gidx, f->gdist, f->nodes_host, f->n_nodes, N, f->nodes_host,
                   reinterpret_cast<const unsigned*>(f->n_nodes), N, p.kreg, 1, st);
     if (rc) return rc;
     rc = afx_filter_disconnected(f->gidx, f->gdist, f->n_nodes, N, p.kreg, f->radii, st);
     if (rc) return rc;
-    rc = warp_weights_impl(f->mw, f->radii, f->midx, f->mdist, f->npoints, M, p.knn, f->n_nodes, st);
+    rc = warp_weights_impl(f->mw, f->radii, f->midx, f->mdist, npoints, M, p.knn, f->n_nodes, st);
     if (rc) return rc;
     GnArgs g;
     std::memset(&g, 0, sizeof(g));
-    g.mesh = f->points;
-    g.mesh_count = f->npoints;
+    g.mesh = points;
+    g.mesh_count = npoints;
     g.m_max = M;
     g.midx = f->midx;
     g.mw = f->mw;
@@ -520,15 +534,15 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
     const double tol = p.solver == 2 ? p.pcg_tol : 0.0;
     for (int icp = 0; icp < p.icp_iterations; ++icp) {
         // warp with the committed transforms, then projective correspondences (src/VolumeFusion.cu:439-447)
-        rc = warp_impl(f->warped, f->points, f->T, f->midx, f->mw, f->npoints, M, p.knn, st);
+        rc = warp_impl(f->warped, points, f->T, f->midx, f->mw, npoints, M, p.knn, st);
         if (rc) return rc;
-        rc = correspondences_impl(f->corr, f->ncorr, M, f->warped, f->npoints, M, p.K, f->depth, p.height, p.width,
+        rc = correspondences_impl(f->corr, f->ncorr, M, f->warped, npoints, M, p.K, f->depth, p.height, p.width,
                                   f->verts, p.corr_thresh, f->corr_of_vertex, f->ws_corr, f->ws_corr_bytes, st);
         if (rc) return rc;
         rc = gn_icp_setup(g, f->Tp, f->T, st);
         if (rc) return rc;
         stage_mark(f, ST_GN_LOOP, st);
-        rc = gn_loop(g, f->points, f->warped, f->T, f->Tp, p.gn_iterations, p.pcg_iterations, tol, st);
+        rc = gn_loop(g, points, f->warped, f->T, f->Tp, p.gn_iterations, p.pcg_iterations, tol, st);
         if (rc) return rc;
     }
     // voxel support, warp, collisions and warped integration (src/VolumeFusion.cu:702-741)
@@ -586,12 +600,67 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
         if (rc) return rc;
     }
     stage_mark(f, ST_MC, st);
-    rc = extract_frame_mesh(f, st);
+    rc = extract_frame_mesh(f, cur, st);
     if (rc) return rc;
     stage_mark(f, -1, st);
-    stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame, f->n_nodes, f->n_old, f->mesh_used, f->ncorr, f->gn.state,
+    stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame_dev, f->n_nodes, f->n_old, f->mesh_used, f->ncorr, f->gn.state,
                                   f->nmverts, f->nmfaces, f->error, 1);
     AFX_LAUNCH_CHECK();
+    return AFX_OK;
+}
+
+// Capture the non-rigid frame for (build, cur) into a CUDA graph on a private stream.
+static int capture_frame(afx_fusion* f, int cur, bool build) {
+    if (!f->cap_stream) AFX_CUDA(cudaStreamCreateWithFlags(&f->cap_stream, cudaStreamNonBlocking));
+    const long l0 = launches_total();
+    AFX_CUDA(cudaStreamBeginCapture(f->cap_stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue_frame(f, f->depth_mm, f->cap_stream, cur, build);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(f->cap_stream, &graph);
+    if (rc || e != cudaSuccess || !graph) {
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();
+        return rc ? rc : AFX_ERR_CUDA;
+    }
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ie != cudaSuccess) return note_cuda_error(ie);
+    f->gexec[build][cur] = exec;
+    f->glaunches[build][cur] = launches_total() - l0;
+    return AFX_OK;
+}
+
+int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
+    if (!f || !depth_mm) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    if (f->frame == 0) {
+        const int rc = enqueue_frame(f, depth_mm, st, f->cur, false);
+        if (rc) return rc;
+        f->frame++;
+        return AFX_OK;
+    }
+    const int cur = f->cur ^ 1;
+    const bool build = f->frame == 1 || f->p.update_graph;
+    // frames 1 and 2 run eagerly (first-use set-up of the kernels happens there); later frames
+    // replay a captured graph that reads the frame from the session's own input buffer
+    bool replay = f->graphs && !f->timing && f->frame >= 3;
+    if (replay && !f->gexec[build][cur] && capture_frame(f, cur, build) != AFX_OK) {
+        f->graphs = false;  // capture failed: keep launching one by one
+        replay = false;
+    }
+    if (replay) {
+        if (depth_mm != f->depth_mm)
+            AFX_CUDA(cudaMemcpyAsync(f->depth_mm, depth_mm, (size_t)f->P * 2, cudaMemcpyDeviceToDevice, st));
+        AFX_CUDA(cudaGraphLaunch(f->gexec[build][cur], st));
+        f->replayed += f->glaunches[build][cur];
+    } else {
+        const int rc = enqueue_frame(f, depth_mm, st, cur, build);
+        if (rc) return rc;
+    }
+    f->cur = cur;
+    f->points = f->points_buf[cur];
+    f->npoints = f->npoints_buf[cur];
     f->frame++;
     return AFX_OK;
 }
@@ -678,7 +747,23 @@ int afx_fusion_set_transforms(afx_fusion* f, const float* transforms_host, int n
     return AFX_OK;
 }
 
-long afx_fusion_kernel_launches(const afx_fusion* f) { return f ? launches_total() - f->launches_at_create : 0; }
+long afx_fusion_kernel_launches(const afx_fusion* f) {
+    return f ? launches_total() - f->launches_at_create + f->replayed : 0;
+}
+
+int afx_fusion_set_graphs(afx_fusion* f, int on) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    f->graphs = on != 0;
+    return AFX_OK;
+}
+
+int afx_fusion_graph_count(const afx_fusion* f) {
+    if (!f) return 0;
+    int c = 0;
+    for (auto& row : f->gexec)
+        for (auto& g : row) c += g != nullptr;
+    return f->graphs ? c : 0;
+}
 
 int afx_fusion_set_timing(afx_fusion* f, int on) {
     if (!f) return AFX_ERR_INVALID_ARGUMENT;

@@ -135,6 +135,13 @@ class FusionSession:
     STAGES = ("prep", "rigid_integrate", "sort_unique", "graph", "knn", "gn_setup", "gn_loop", "voxel_support",
               "voxel_warp", "warped_integrate", "marching_cubes")
 
+    def set_graphs(self, on=True):
+        """Replay non-rigid frames from CUDA graphs (default) or launch kernels one by one."""
+        check(lib().afx_fusion_set_graphs(self.h, int(bool(on))), "afx_fusion_set_graphs")
+
+    def graph_count(self):
+        return lib().afx_fusion_graph_count(self.h)
+
     def set_timing(self, on=True):
         check(lib().afx_fusion_set_timing(self.h, int(on)), "afx_fusion_set_timing")
 
