@@ -310,6 +310,10 @@ typedef struct afx_fusion_params {
 
 typedef struct afx_fusion afx_fusion;
 
+/* Device bytes afx_fusion_create would allocate for these parameters (0 if they are invalid);
+ * used for admission by memory budget. */
+size_t afx_fusion_memory_bytes(const afx_fusion_params* params);
+
 typedef struct afx_frame_stats {
     int frame;
     int n_nodes;
@@ -334,6 +338,9 @@ int afx_fusion_reset(afx_fusion* f, void* stream);
 int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream);
 /* Same, from host memory: copies the frame to the device on `stream` first. */
 int afx_fusion_process_host(afx_fusion* f, const uint16_t* depth_mm_host, void* stream);
+/* Enqueue a copy of the last frame's statistics into host memory (pinned for an asynchronous
+ * copy); the values are there once `stream` has passed this point. */
+int afx_fusion_stats_async(afx_fusion* f, afx_frame_stats* out_host, void* stream);
 /* Copy the last frame's statistics to host memory (synchronises `stream`). */
 int afx_fusion_stats(afx_fusion* f, afx_frame_stats* out, void* stream);
 /* Device views of the session state (valid until destroy). */
@@ -364,6 +371,37 @@ int afx_fusion_graph_count(const afx_fusion* f);
  * ms[0..n) and returns the number of stages; reset != 0 starts a new accumulation. */
 int afx_fusion_set_timing(afx_fusion* f, int on);
 int afx_fusion_stage_times(afx_fusion* f, double* ms, int n, int reset);
+
+/* ------------------------------------------------------------------------------------
+ * Serving many depth streams on one GPU (no counterpart in the reference, which fuses one
+ * recorded sequence per process).  Sessions are admitted while their device bytes
+ * (afx_fusion_memory_bytes) fit the budget; each has its own stream, so frames of different
+ * sessions overlap on the device; frames of one session run in order.  Not thread-safe
+ * across servers sharing a session; calls on one server are serialised internally.
+ * ------------------------------------------------------------------------------------ */
+typedef struct afx_server afx_server;
+
+typedef struct afx_server_result {
+    int session_id;
+    uint64_t tag;        /* the caller's tag from afx_server_submit */
+    double latency_ms;   /* afx_server_submit to the completion seen by afx_server_poll */
+    afx_frame_stats stats;
+} afx_server_result;
+
+int afx_server_create(size_t memory_budget_bytes, int max_sessions, afx_server** out);
+int afx_server_destroy(afx_server* s);
+/* AFX_ERR_NO_MEMORY: the budget (or max_sessions) does not admit the session now. */
+int afx_server_open(afx_server* s, const afx_fusion_params* params, int* session_id);
+/* Closes once the session's frames in flight are done; its memory returns to the budget. */
+int afx_server_close(afx_server* s, int session_id);
+/* Queue one frame (host uint16 mm, copied before return).  AFX_ERR_CAPACITY: the session has
+ * 4 frames in flight; poll and retry. */
+int afx_server_submit(afx_server* s, int session_id, const uint16_t* depth_mm_host, uint64_t tag);
+/* Up to max_results finished frames, oldest first per session. */
+int afx_server_poll(afx_server* s, afx_server_result* out, int max_results, int* n_results);
+/* The session's afx_fusion (for its volume, graph, mesh); NULL if unknown. */
+afx_fusion* afx_server_session(afx_server* s, int session_id);
+int afx_server_usage(afx_server* s, size_t* used_bytes, int* sessions, long* denied);
 
 /* Stream-ordered device-to-device copy (helper for bindings that hold raw device views). */
 int afx_copy_device(void* dst, const void* src, size_t bytes, void* stream);

@@ -37,6 +37,10 @@ class FrameStats(C.Structure):
                 ("mesh_vertices", C.c_uint), ("mesh_faces", C.c_uint), ("error", i32)]
 
 
+class ServerResult(C.Structure):
+    _fields_ = [("session_id", i32), ("tag", C.c_uint64), ("latency_ms", f64), ("stats", FrameStats)]
+
+
 SIGNATURES = {
     "afx_status_string": (C.c_char_p, [i32]),
     "afx_version": (i32, []),
@@ -80,6 +84,16 @@ SIGNATURES = {
     "afx_fusion_set_graphs": (i32, [vp, i32]),
     "afx_fusion_graph_count": (i32, [vp]),
     "afx_fusion_default_params": (None, [C.POINTER(FusionParams)]),
+    "afx_fusion_memory_bytes": (sz, [C.POINTER(FusionParams)]),
+    "afx_fusion_stats_async": (i32, [vp, vp, vp]),
+    "afx_server_create": (i32, [sz, i32, C.POINTER(vp)]),
+    "afx_server_destroy": (i32, [vp]),
+    "afx_server_open": (i32, [vp, C.POINTER(FusionParams), C.POINTER(i32)]),
+    "afx_server_close": (i32, [vp, i32]),
+    "afx_server_submit": (i32, [vp, i32, vp, C.c_uint64]),
+    "afx_server_poll": (i32, [vp, vp, i32, C.POINTER(i32)]),
+    "afx_server_session": (vp, [vp, i32]),
+    "afx_server_usage": (i32, [vp, C.POINTER(sz), C.POINTER(i32), C.POINTER(C.c_long)]),
     "afx_fusion_create": (i32, [C.POINTER(FusionParams), C.POINTER(vp)]),
     "afx_fusion_destroy": (i32, [vp]),
     "afx_fusion_reset": (i32, [vp, vp]),

@@ -89,3 +89,67 @@ def small_frames(cfg, frames=None):
 
 def voxel_size(cfg):
     return np.array(cfg["volume_size"], np.float32) / np.array(cfg["dims"], np.float32)
+
+
+# ---- many concurrent sessions (the batched and served workloads) ----
+
+_VOLUMES = ((128, 0.008), (192, 0.006), (256, 0.004), (384, 0.003))  # cube edge ~1.0-1.15 m
+_CAMERAS = ((320, 288, 252.0), (640, 576, 504.0))
+SCENES = ("sphere", "torus", "capsule")
+
+
+def session_config(dims, voxel, width, height, focal, graph_radius, scene, seed):
+    """One served session: a seeded scene at one of the workload's volume and camera sizes."""
+    cfg = _base()
+    K = synth.intrinsics(focal, focal, width / 2.0, height / 2.0)
+    cfg.update(name="%s_%d" % (scene, dims), width=width, height=height, K=K, dims=(dims, dims, dims),
+               volume_size=(dims * voxel,) * 3, delta=max(0.016, 4 * voxel), graph_radius=graph_radius, knn=4, kreg=8,
+               icp_iterations=1, gn_iterations=5, lambda_reg=math.sqrt(200.0), n_frames=30, scene=scene, seed=seed,
+               node_cap=8192, mesh_cap=1_000_000, triangle_cap=1_000_000)
+    return cfg
+
+
+def session_mix(count, seed=0):
+    """`count` session configurations drawn from the batched/served workload: volumes from
+    {128, 192, 256, 384}^3, 320x288 or 640x576 depth, sphere / torus / bending capsules, graph
+    radius 20-35 mm (a few hundred to a few thousand nodes), each with its own seed."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        dims, voxel = _VOLUMES[rng.integers(len(_VOLUMES))]
+        w, h, f = _CAMERAS[rng.integers(len(_CAMERAS))]
+        scene = SCENES[rng.integers(len(SCENES))]
+        if scene == "torus":  # traced scene: the small camera keeps frame synthesis cheap
+            w, h, f = _CAMERAS[0]
+        out.append(session_config(dims, voxel, w, h, f, float(rng.uniform(0.020, 0.035)), scene, int(rng.integers(1 << 30))))
+    return out
+
+
+_FRAME_CACHE = {}
+
+
+def scene_frames(cfg, n_unique=None):
+    """Frames of a session's scene (cached per scene and camera).  Torus sequences have 10 unique
+    frames, played forward and back by scene_frame()."""
+    key = (cfg["scene"], cfg["width"], cfg["height"])
+    if key not in _FRAME_CACHE:
+        n = cfg.get("n_frames", 30)
+        K = cfg["K"]
+        kw = dict(width=cfg["width"], height=cfg["height"], fx=float(K[0, 0]), fy=float(K[1, 1]), cx=float(K[0, 2]),
+                  cy=float(K[1, 2]))
+        if cfg["scene"] == "sphere":
+            frames = [synth.moving_sphere_frame(i, n_frames=n, **kw)[0] for i in range(n)]
+        elif cfg["scene"] == "torus":
+            frames = [synth.torus_frame(i, n_frames=10, **kw)[0] for i in range(n_unique or 10)]
+        else:
+            frames = [synth.capsule_pair_frame(i, n_frames=n, **kw)[0] for i in range(n)]
+        _FRAME_CACHE[key] = frames
+    return _FRAME_CACHE[key]
+
+
+def scene_frame(cfg, i):
+    frames = scene_frames(cfg)
+    m = len(frames)
+    period = max(2 * (m - 1), 1)
+    r = i % period
+    return frames[r if r < m else period - r]

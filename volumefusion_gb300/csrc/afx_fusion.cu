@@ -249,16 +249,8 @@ void afx_fusion_default_params(afx_fusion_params* p) {
     p->triangle_capacity = 4000000;
 }
 
-int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
-    if (!params || !out) return AFX_ERR_INVALID_ARGUMENT;
-    const afx_fusion_params& p = *params;
-    if (p.width < 3 || p.height < 3 || p.dims[0] < 3 || p.dims[1] < 3 || p.dims[2] < 3 || p.knn < 1 || p.knn > 8 ||
-        p.kreg < 1 || p.kreg > 8 || p.node_capacity < 1 || p.mesh_capacity < 1 || p.triangle_capacity < 1 ||
-        !(p.graph_radius > 0.f) || p.icp_iterations < 0 || p.gn_iterations < 0 || p.pcg_iterations < 0)
-        return AFX_ERR_INVALID_ARGUMENT;
-    afx_fusion* f = new (std::nothrow) afx_fusion();
-    if (!f) return AFX_ERR_NO_MEMORY;
-    f->p = p;
+// Sizes of every buffer of a session with these parameters (no allocation).
+static void session_layout(const afx_fusion_params& p, afx_fusion* f) {
     float vs[3];
     for (int c = 0; c < 3; ++c) vs[c] = p.volume_size[c] / (float)p.dims[c];
     f->vol = make_volume(p.dims, vs, p.volume_size);
@@ -288,6 +280,33 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     add(sizeof(FrameStats)); add(64);
     add(f->ws_sort_bytes); add(f->ws_graph_bytes); add(f->ws_corr_bytes); add(f->ws_support_bytes); add(f->ws_gn_bytes);
     f->arena_bytes = sz + 4096;
+}
+
+static bool params_valid(const afx_fusion_params& p) {
+    return !(p.width < 3 || p.height < 3 || p.dims[0] < 3 || p.dims[1] < 3 || p.dims[2] < 3 || p.knn < 1 ||
+             p.knn > 8 || p.kreg < 1 || p.kreg > 8 || p.node_capacity < 1 || p.mesh_capacity < 1 ||
+             p.triangle_capacity < 1 || !(p.graph_radius > 0.f) || p.icp_iterations < 0 || p.gn_iterations < 0 ||
+             p.pcg_iterations < 0);
+}
+
+size_t afx_fusion_memory_bytes(const afx_fusion_params* params) {
+    if (!params || !params_valid(*params)) return 0;
+    afx_fusion tmp;
+    tmp.p = *params;
+    session_layout(*params, &tmp);
+    return tmp.arena_bytes;
+}
+
+int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
+    if (!params || !out) return AFX_ERR_INVALID_ARGUMENT;
+    const afx_fusion_params& p = *params;
+    if (!params_valid(p)) return AFX_ERR_INVALID_ARGUMENT;
+    afx_fusion* f = new (std::nothrow) afx_fusion();
+    if (!f) return AFX_ERR_NO_MEMORY;
+    f->p = p;
+    session_layout(p, f);
+    const long M = p.mesh_capacity, N = p.node_capacity, S = f->S, Pp = f->P;
+    const long nbricks = brick_count_total(f->vol);
     cudaError_t e = cudaMalloc(&f->arena, f->arena_bytes);
     if (e != cudaSuccess) {
         note_cuda_error(e);
@@ -362,7 +381,7 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
         delete f;
         return rc;
     }
-    e = cudaDeviceSynchronize();
+    e = cudaStreamSynchronize(nullptr);  // the reset above; other streams' work is not waited for
     if (e != cudaSuccess) {
         note_cuda_error(e);
         cudaFree(f->arena);
@@ -670,6 +689,14 @@ int afx_fusion_process_host(afx_fusion* f, const uint16_t* depth_mm_host, void* 
     cudaStream_t st = as_stream(stream);
     AFX_CUDA(cudaMemcpyAsync(f->depth_mm, depth_mm_host, f->P * 2, cudaMemcpyHostToDevice, st));
     return afx_fusion_process(f, f->depth_mm, stream);
+}
+
+static_assert(sizeof(FrameStats) == sizeof(afx_frame_stats), "statistics layouts differ");
+
+int afx_fusion_stats_async(afx_fusion* f, afx_frame_stats* out_host, void* stream) {
+    if (!f || !out_host) return AFX_ERR_INVALID_ARGUMENT;
+    AFX_CUDA(cudaMemcpyAsync(out_host, f->stats, sizeof(FrameStats), cudaMemcpyDeviceToHost, as_stream(stream)));
+    return AFX_OK;
 }
 
 int afx_fusion_stats(afx_fusion* f, afx_frame_stats* out, void* stream) {

@@ -49,9 +49,22 @@ class FusionSession:
         self.stream = stream
         self.S = int(np.prod(cfg["dims"]))
 
+    @classmethod
+    def attach(cls, handle, cfg, stream=None):
+        """View of a session owned elsewhere (e.g. by a Server); close() leaves it alone."""
+        obj = cls.__new__(cls)
+        obj.cfg = cfg
+        obj.params = params_from_config(cfg)
+        obj.h = C.c_void_p(handle)
+        obj.stream = stream
+        obj.S = int(np.prod(cfg["dims"]))
+        obj._owned = False
+        return obj
+
     def close(self):
         if getattr(self, "h", None):
-            lib().afx_fusion_destroy(self.h)
+            if getattr(self, "_owned", True):
+                lib().afx_fusion_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -128,3 +128,54 @@ def capsule_pair_sequence(n_frames=30, **kw):
         mm, K = capsule_pair_frame(f, n_frames=n_frames, **kw)
         frames.append(mm)
     return np.stack(frames), K
+
+
+def _rot(axis, angle):
+    axis = np.asarray(axis, dtype=np.float64)
+    axis = axis / np.linalg.norm(axis)
+    x, y, z = axis
+    c, s = math.cos(angle), math.sin(angle)
+    C1 = 1.0 - c
+    return np.array([[c + x * x * C1, x * y * C1 - z * s, x * z * C1 + y * s],
+                     [y * x * C1 + z * s, c + y * y * C1, y * z * C1 - x * s],
+                     [z * x * C1 - y * s, z * y * C1 + x * s, c + z * z * C1]])
+
+
+def _hit_torus(d, center, R_world, R, r, t0=0.2, t1=2.0, iters=96):
+    """Nearest ray parameter on a torus (major R, minor r; axis = R_world[:, 2]) by sphere tracing
+    its distance function; inf on a miss."""
+    n = d.shape[:-1]
+    dn = d / np.linalg.norm(d, axis=-1, keepdims=True)
+    t = np.full(n, t0)
+    alive = np.ones(n, dtype=bool)
+    for _ in range(iters):
+        p = dn * t[..., None] - center
+        q = p @ R_world  # torus frame
+        k = np.sqrt(q[..., 0] ** 2 + q[..., 1] ** 2) - R
+        dist = np.sqrt(k * k + q[..., 2] ** 2) - r
+        t = np.where(alive, t + dist, t)
+        alive &= (dist > 1e-6) & (t < t1)
+    hit = ~alive & (t < t1)
+    scale = np.linalg.norm(d, axis=-1)
+    return np.where(hit, t / scale, np.inf)
+
+
+def torus_frame(frame, n_frames=30, width=320, height=288, fx=252.0, fy=252.0, cx=160.0, cy=144.0, major=0.16,
+                minor=0.05, center=(0.0, 0.0, 0.8), tilt_deg=55.0, spin_deg=40.0, seed=0):
+    """Frame `frame` of a torus tilted towards the camera and spinning about its axis."""
+    K = intrinsics(fx, fy, cx, cy)
+    d = _rays(width, height, K)
+    a = math.radians(spin_deg) * (frame / max(n_frames - 1, 1))
+    Rw = _rot((1.0, 0.0, 0.0), math.radians(tilt_deg)) @ _rot((0.0, 0.0, 1.0), a)
+    t = _hit_torus(d, np.asarray(center, dtype=np.float64), Rw, major, minor)
+    return _to_mm(t, seed, frame), K
+
+
+def moving_sphere_frame(frame, n_frames=30, width=320, height=288, fx=252.0, fy=252.0, cx=160.0, cy=144.0,
+                        radius=0.15, start=(-0.05, 0.0, 0.75), stop=(0.05, 0.02, 0.8), seed=0):
+    """Frame `frame` of a sphere translating from `start` to `stop` over the sequence."""
+    K = intrinsics(fx, fy, cx, cy)
+    d = _rays(width, height, K)
+    u = frame / max(n_frames - 1, 1)
+    c = (1.0 - u) * np.asarray(start, dtype=np.float64) + u * np.asarray(stop, dtype=np.float64)
+    return _to_mm(_hit_sphere(d, c, radius), seed, frame), K
