@@ -41,6 +41,7 @@ def parse():
     ap.add_argument("--clip", type=int, default=N_FRAMES, help="frames of the sequence per step")
     ap.add_argument("--no-dense-graph", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--served-streams", type=int, default=64)
     ap.add_argument("--served-seconds", type=float, default=4.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -412,6 +413,36 @@ def main():
                  "n_nodes_last_frame": dst["n_nodes"], "correspondences_last_frame": dst["correspondences"],
                  "stage_ms_per_frame": dstage}
 
+    # ---- precision form: the sequence at 512^3 / 2 mm, FP16 values + uint16 weights vs FP32 ----
+    precision = None
+    if not args.no_precision:
+        from volumefusion_gb300.serve import session_bytes
+        precision = {"workload": "capsule pair, 30 frames, 512^3 @ 2 mm, 6.5 mm graph radius"}
+        for prec in ("fp16", "fp32"):
+            pcfg = dict(configs.precision_capsules_512(n_frames=N_FRAMES), precision=prec)
+            sp = FusionSession(pcfg, stream=stream)
+            run_device(sp, 1)
+            barrier()
+            psteps = max(1, min(2, args.steps))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            run_device(sp, psteps)
+            e1.record(stream)
+            barrier()
+            pms = reduce_max(e0.elapsed_time(e1))
+            sp.set_timing(True)
+            sp.stage_times(reset=True)
+            run_device(sp, 1)
+            barrier()
+            pstage = {k: v / clip for k, v in sp.stage_times(reset=True).items()}
+            sp.set_timing(False)
+            pst = sp.stats(check_errors=False)
+            sp.close()
+            torch.cuda.empty_cache()
+            precision[prec] = {"value": world * psteps * clip / (pms / 1000.0), "unit": "frames/s",
+                               "session_bytes": session_bytes(pcfg), "n_nodes_last_frame": pst["n_nodes"],
+                               "error": pst["error"], "stage_ms_per_frame": pstage}
+
     served = None
     if not args.no_served:
         served = served_arm(args, rank)
@@ -461,6 +492,7 @@ def main():
             "last_frame_stats": {k: st[k] for k in ("n_nodes", "mesh_points", "correspondences", "gn_iterations_done",
                                                 "mesh_faces", "error")},
             "dense_graph": dense,
+            "precision": precision,
             "served": served,
             "roofline": roof,
             "cpu_baseline": cpu,

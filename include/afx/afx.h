@@ -306,7 +306,12 @@ typedef struct afx_fusion_params {
     int node_capacity;
     long mesh_capacity;          /* canonical point cloud capacity */
     long triangle_capacity;
+    int precision;               /* AFX_PRECISION_FP32 (the reference's DeviceTsdf<float>) or
+                                    AFX_PRECISION_FP16: FP16 TSDF values + uint16 weights, 4 B/voxel */
 } afx_fusion_params;
+
+#define AFX_PRECISION_FP32 0
+#define AFX_PRECISION_FP16 1
 
 typedef struct afx_fusion afx_fusion;
 
@@ -344,7 +349,10 @@ int afx_fusion_stats_async(afx_fusion* f, afx_frame_stats* out_host, void* strea
 /* Copy the last frame's statistics to host memory (synchronises `stream`). */
 int afx_fusion_stats(afx_fusion* f, afx_frame_stats* out, void* stream);
 /* Device views of the session state (valid until destroy). */
-int afx_fusion_tsdf(afx_fusion* f, float** tsdf, float** weights);
+int afx_fusion_tsdf(afx_fusion* f, float** tsdf, float** weights);  /* FP32 sessions; else AFX_ERR_UNSUPPORTED */
+/* Device view of the volume in either storage format: FP32 values + FP32 weights, or (precision
+ * form) IEEE FP16 values + uint16 weights; *precision says which. */
+int afx_fusion_volume(afx_fusion* f, void** tsdf, void** weights, int* precision);
 int afx_fusion_graph(afx_fusion* f, float** nodes, float** radii, float** transforms, int** n_nodes);
 int afx_fusion_centroid(afx_fusion* f, float** centroid);
 int afx_fusion_point_cloud(afx_fusion* f, float** points, unsigned** count);

@@ -12,6 +12,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
+LIB64_PATH = os.path.join(HERE, "liboracle64.so")
 
 f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
 f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
@@ -47,7 +48,8 @@ def lib():
             "vfo_frame_prep": (None, [u16p, C.c_int, C.c_int, f32p, C.c_float, C.c_int, C.c_int, C.c_double,
                                       C.c_double, C.c_float, C.c_float, C.c_float, f32p, f32p, f32p, f32p]),
             "vfo_integrate_rigid": (None, [f32p, f32p, f32p, C.c_int, C.c_int, C.c_float, i32p, f32p, f32p, f32p,
-                                           f32p, f32p]),
+                                           f32p, f32p, C.c_int]),
+            "vfo_round_half": (C.c_float, [C.c_float]),
             "vfo_mc_pointcloud": (C.c_long, [f32p, f32p, i32p, f32p, f32p, C.c_float, f32p, C.c_long]),
             "vfo_sort_unique_vec3": (C.c_long, [f32p, C.c_long]),
             "vfo_mc_full": (C.c_long, [f32p, f32p, i32p, f32p, f32p, C.c_float, f32p, C.c_long, i32p, C.c_long,
@@ -74,7 +76,7 @@ def lib():
             "vfo_warp_tsdf": (None, [f32p, f32p, u32p, f32p, i32p, C.c_long, C.c_int]),
             "vfo_count_collisions": (None, [i32p, f32p, i32p, f32p, f32p, i32p, f32p, f32p]),
             "vfo_integrate_warped": (None, [f32p, f32p, f32p, i32p, i32p, f32p, C.c_int, C.c_int, C.c_float, f32p,
-                                            f32p, i32p, f32p, f32p, f32p]),
+                                            f32p, i32p, f32p, f32p, f32p, C.c_int]),
             "vfo_fusion_create": (C.c_void_p, [C.c_void_p]),
             "vfo_fusion_destroy": (None, [C.c_void_p]),
             "vfo_fusion_process": (C.c_int, [C.c_void_p, u16p]),
@@ -98,6 +100,45 @@ def lib():
             fn.argtypes = args
         _lib = L
     return _lib
+
+
+_lib64 = None
+
+
+def lib64():
+    """The FP64 oracle: the same restatement evaluated in binary64 (whole-frame driver only)."""
+    global _lib64
+    if _lib64 is None:
+        if not os.path.exists(LIB64_PATH):
+            build()
+        L = C.CDLL(LIB64_PATH)
+        vp = C.c_void_p
+        sig = {
+            "vfo_fusion_create": (vp, [vp]),
+            "vfo_fusion_destroy": (None, [vp]),
+            "vfo_fusion_process": (C.c_int, [vp, u16p]),
+            "vfo_fusion_num_nodes": (C.c_int, [vp]),
+            "vfo_fusion_mesh_size": (C.c_long, [vp]),
+            "vfo_fusion_num_corr": (C.c_long, [vp]),
+            "vfo_fusion_gn_done": (C.c_int, [vp]),
+            "vfo_fusion_energy": (C.c_double, [vp]),
+            "vfo_fusion_tsdf": (vp, [vp]),
+            "vfo_fusion_weights": (vp, [vp]),
+            "vfo_fusion_nodes": (vp, [vp]),
+            "vfo_fusion_transforms": (vp, [vp]),
+            "vfo_fusion_centroid": (vp, [vp]),
+            "vfo_fusion_mesh": (vp, [vp]),
+            "vfo_fusion_set_transforms": (None, [vp, f64p, C.c_int]),
+            "vfo_fusion_set_tsdf": (None, [vp, f64p, f64p]),
+            "vfo_mc_pointcloud": (C.c_long, [f64p, f64p, i32p, f64p, f64p, C.c_double, f64p, C.c_long]),
+            "vfo_sort_unique_vec3": (C.c_long, [f64p, C.c_long]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib64 = L
+    return _lib64
 
 
 def _f32(a):
@@ -170,10 +211,10 @@ def frame_prep(mm, K, depth_threshold=1.2, bilateral=1, r=2, sigma_i=0.03, sigma
     return depth, verts, nrm, cen
 
 
-def integrate_rigid(tsdf, weights, depth, delta, dims, voxel_size, volume_size, R, t, K):
+def integrate_rigid(tsdf, weights, depth, delta, dims, voxel_size, volume_size, R, t, K, half=False):
     h, w = depth.shape
     lib().vfo_integrate_rigid(tsdf, weights, _f32(depth), w, h, delta, _i32(dims), _f32(voxel_size),
-                              _f32(volume_size), kcol(R), _f32(t), kcol(K))
+                              _f32(volume_size), kcol(R), _f32(t), kcol(K), int(half))
 
 
 def mc_pointcloud(tsdf, weights, dims, voxel_size, volume_size, iso=0.0, cap=None):
@@ -353,10 +394,29 @@ def count_collisions(verts, kcount, voxel_size, volume_size, dims, Rinv, t):
 
 
 def integrate_warped(tsdf, weights, verts, collisions, kcount, depth, delta, voxel_size, volume_size, dims, Rinv, t,
-                     K):
+                     K, half=False):
     h, w = depth.shape
     lib().vfo_integrate_warped(tsdf, weights, _f32(verts), _i32(collisions), _i32(kcount), _f32(depth), w, h, delta,
-                               _f32(voxel_size), _f32(volume_size), _i32(dims), kcol(Rinv), _f32(t), kcol(K))
+                               _f32(voxel_size), _f32(volume_size), _i32(dims), kcol(Rinv), _f32(t), kcol(K), int(half))
+
+
+def round_half(x):
+    """Nearest binary16 values of a float32 array (ties to even), as float32."""
+    x = np.asarray(x, dtype=np.float32)
+    return np.array([lib().vfo_round_half(float(v)) for v in x.ravel()], dtype=np.float32).reshape(x.shape)
+
+
+def mc_pointcloud64(tsdf, weights, dims, voxel_size, volume_size, iso=0.0):
+    """Sorted unique marching-cubes point cloud of a volume, evaluated in binary64 (FP64 oracle)."""
+    L = lib64()
+    cap = max(1, int(np.prod(dims)) * 3)
+    out = np.zeros(3 * cap, np.float64)
+    n = L.vfo_mc_pointcloud(np.ascontiguousarray(tsdf, np.float64).ravel(),
+                            np.ascontiguousarray(weights, np.float64).ravel(), _i32(dims),
+                            np.ascontiguousarray(voxel_size, np.float64), np.ascontiguousarray(volume_size, np.float64),
+                            float(iso), out, cap)
+    n = L.vfo_sort_unique_vec3(out, min(n, cap))
+    return out[:3 * n].reshape(-1, 3)
 
 
 class VfoParams(C.Structure):
@@ -368,13 +428,16 @@ class VfoParams(C.Structure):
                 ("icp_iterations", C.c_int), ("gn_iterations", C.c_int), ("lambda_depth", C.c_float),
                 ("lambda_reg", C.c_float), ("energy_min_step", C.c_float), ("corr_thresh", C.c_float),
                 ("solver", C.c_int), ("pcg_iterations", C.c_int), ("pcg_tol", C.c_double), ("integrate", C.c_int),
-                ("node_cap", C.c_int), ("mesh_cap", C.c_long)]
+                ("node_cap", C.c_int), ("mesh_cap", C.c_long), ("precision", C.c_int)]
 
 
 class Fusion:
-    """Whole-sequence oracle driver (af::runVolumeFusion's per-frame loop) over in-memory frames."""
+    """Whole-sequence oracle driver (af::runVolumeFusion's per-frame loop) over in-memory frames.
+    fp64=True runs the binary64 build (liboracle64.so); arrays then come back as float64."""
 
-    def __init__(self, cfg):
+    def __init__(self, cfg, fp64=False):
+        self._L = lib64() if fp64 else lib()
+        self._ct, self._dt = (C.c_double, np.float64) if fp64 else (C.c_float, np.float32)
         p = VfoParams()
         p.width, p.height = cfg["width"], cfg["height"]
         p.K[:] = list(kcol(cfg["K"]))
@@ -387,68 +450,72 @@ class Fusion:
                     "solver", "pcg_iterations", "integrate", "node_cap", "mesh_cap"):
             setattr(p, key, int(cfg[key]))
         p.pcg_tol = float(cfg.get("pcg_tol", 0.0))
+        p.precision = {"fp32": 0, "fp16": 1}[cfg.get("precision", "fp32")]
         self.cfg = cfg
         self._p = p
-        self.h = lib().vfo_fusion_create(C.byref(p))
+        self.h = self._L.vfo_fusion_create(C.byref(p))
         self.S = int(np.prod(cfg["dims"]))
 
     def close(self):
         if self.h:
-            lib().vfo_fusion_destroy(self.h)
+            self._L.vfo_fusion_destroy(self.h)
             self.h = None
 
     def __del__(self):
         self.close()
 
     def process(self, mm):
-        st = lib().vfo_fusion_process(self.h, np.ascontiguousarray(mm, np.uint16))
+        st = self._L.vfo_fusion_process(self.h, np.ascontiguousarray(mm, np.uint16))
         if st:
             raise RuntimeError("oracle frame failed with status %d" % st)
 
-    def _arr(self, ptr, n, dtype=np.float32):
-        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_float)), shape=(n,)).astype(dtype).copy()
+    def _arr(self, ptr, n):
+        if n == 0:
+            return np.zeros(0, self._dt)
+        return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(self._ct)), shape=(n,)).copy()
 
     @property
     def num_nodes(self):
-        return lib().vfo_fusion_num_nodes(self.h)
+        return self._L.vfo_fusion_num_nodes(self.h)
 
     @property
     def mesh_size(self):
-        return lib().vfo_fusion_mesh_size(self.h)
+        return self._L.vfo_fusion_mesh_size(self.h)
 
     @property
     def num_corr(self):
-        return lib().vfo_fusion_num_corr(self.h)
+        return self._L.vfo_fusion_num_corr(self.h)
 
     @property
     def gn_done(self):
-        return lib().vfo_fusion_gn_done(self.h)
+        return self._L.vfo_fusion_gn_done(self.h)
 
     @property
     def energy(self):
-        return lib().vfo_fusion_energy(self.h)
+        return self._L.vfo_fusion_energy(self.h)
 
     def tsdf(self):
-        return self._arr(lib().vfo_fusion_tsdf(self.h), self.S)
+        return self._arr(self._L.vfo_fusion_tsdf(self.h), self.S)
 
     def weights(self):
-        return self._arr(lib().vfo_fusion_weights(self.h), self.S)
+        return self._arr(self._L.vfo_fusion_weights(self.h), self.S)
 
     def nodes(self):
-        return self._arr(lib().vfo_fusion_nodes(self.h), 3 * self.num_nodes).reshape(-1, 3)
+        return self._arr(self._L.vfo_fusion_nodes(self.h), 3 * self.num_nodes).reshape(-1, 3)
 
     def transforms(self):
-        return self._arr(lib().vfo_fusion_transforms(self.h), 16 * self.num_nodes).reshape(-1, 16)
+        return self._arr(self._L.vfo_fusion_transforms(self.h), 16 * self.num_nodes).reshape(-1, 16)
 
     def centroid(self):
-        return self._arr(lib().vfo_fusion_centroid(self.h), 3)
+        return self._arr(self._L.vfo_fusion_centroid(self.h), 3)
 
     def mesh(self):
-        return self._arr(lib().vfo_fusion_mesh(self.h), 3 * self.mesh_size).reshape(-1, 3)
+        return self._arr(self._L.vfo_fusion_mesh(self.h), 3 * self.mesh_size).reshape(-1, 3)
 
     def set_transforms(self, T):
-        T = _f32(T).reshape(-1, 16)
-        lib().vfo_fusion_set_transforms(self.h, T, len(T))
+        T = np.ascontiguousarray(T, dtype=self._dt).reshape(-1, 16)
+        self._L.vfo_fusion_set_transforms(self.h, T, len(T))
 
     def set_tsdf(self, tsdf, weights):
-        lib().vfo_fusion_set_tsdf(self.h, _f32(tsdf).ravel(), _f32(weights).ravel())
+        self._L.vfo_fusion_set_tsdf(self.h, np.ascontiguousarray(tsdf, dtype=self._dt).ravel(),
+                                  np.ascontiguousarray(weights, dtype=self._dt).ravel())

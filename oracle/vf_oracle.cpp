@@ -16,10 +16,18 @@
 #include <omp.h>
 #endif
 
+// The arithmetic type of the restatement: float (the reference's binary32, bit for bit) or, for
+// the FP64 oracle build (-DVFO_REAL=double, liboracle64.so), double throughout.
+typedef VFO_REAL real;
+
 namespace {
 
-const float kFltMax = std::numeric_limits<float>::max();
-const float kInf = std::numeric_limits<float>::infinity();
+// the reference pads KNN distances with FLT_MAX in either build
+const real kFltMax = (real)std::numeric_limits<float>::max();
+const real kInf = std::numeric_limits<real>::infinity();
+
+// exp of the reference's skinning weights: the oracle's own binary32 exp, or exp in binary64
+inline real vexp(real x);
 
 inline float bits_to_float(uint32_t u) {
     float f;
@@ -28,62 +36,89 @@ inline float bits_to_float(uint32_t u) {
 }
 
 // ---- Eigen-order vector arithmetic (measured on the vendored Eigen 3.3.90) ----
-inline float dot3(const float* a, const float* b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
-inline float sqnorm3(const float* a) { return a[0] * a[0] + (a[1] * a[1] + a[2] * a[2]); }
-inline float norm3(const float* a) { return std::sqrt(sqnorm3(a)); }
+inline real dot3(const real* a, const real* b) { return a[0] * b[0] + (a[1] * b[1] + a[2] * b[2]); }
+inline real sqnorm3(const real* a) { return a[0] * a[0] + (a[1] * a[1] + a[2] * a[2]); }
+inline real norm3(const real* a) { return std::sqrt(sqnorm3(a)); }
 // Mat3f (column-major) * Vec3f, row i = R(i,0)x + (R(i,1)y + R(i,2)z)
-inline void mat3_vec3(const float* R, const float* p, float* o) {
+inline void mat3_vec3(const real* R, const real* p, real* o) {
     for (int i = 0; i < 3; ++i) o[i] = R[i] * p[0] + (R[3 + i] * p[1] + R[6 + i] * p[2]);
 }
 // (Mat4f (column-major) * [p;1]).head(3), row i = ((T(i,0)x + T(i,1)y) + T(i,2)z) + T(i,3)
-inline void mat4_point(const float* T, const float* p, float* o) {
+inline void mat4_point(const real* T, const real* p, real* o) {
     for (int i = 0; i < 3; ++i) o[i] = ((T[i] * p[0] + T[4 + i] * p[1]) + T[8 + i] * p[2]) + T[12 + i];
 }
 // nanoflann L2_Simple_Adaptor::evalMetric (third_party nanoflann.hpp:432-440): ((0+d0^2)+d1^2)+d2^2
-inline float l2sq_nanoflann(const float* q, const float* p) {
-    float d0 = q[0] - p[0], d1 = q[1] - p[1], d2 = q[2] - p[2];
+inline real l2sq_nanoflann(const real* q, const real* p) {
+    real d0 = q[0] - p[0], d1 = q[1] - p[1], d2 = q[2] - p[2];
     return (d0 * d0 + d1 * d1) + d2 * d2;
 }
 
 // voxelToWorld (src/TSDFIntegration.cu:6-8, src/TSDFWarp.cu:8-10, src/MarchingCubes.cu:315-318)
-inline void voxel_to_world(int x, int y, int z, const float* vs, const float* size, float* o) {
-    o[0] = (float)x * vs[0] - size[0] * 0.5f;
-    o[1] = (float)y * vs[1] - size[1] * 0.5f;
-    o[2] = (float)z * vs[2] - size[2] * 0.5f;
+inline void voxel_to_world(int x, int y, int z, const real* vs, const real* size, real* o) {
+    o[0] = (real)x * vs[0] - size[0] * 0.5f;
+    o[1] = (real)y * vs[1] - size[1] * 0.5f;
+    o[2] = (real)z * vs[2] - size[2] * 0.5f;
 }
 // worldToVoxel (src/TSDFIntegration.cu:10-14, src/TSDFWarp.cu:11-15)
-inline void world_to_voxel(const float* p, const float* vs, const float* size, int* v) {
+inline void world_to_voxel(const real* p, const real* vs, const real* size, int* v) {
     for (int c = 0; c < 3; ++c) {
-        float inv = (float)(1.0 / (double)vs[c]);
-        float f = (p[c] + 0.5f * size[c]) * inv;
+        real inv = (real)(1.0 / (double)vs[c]);
+        real f = (p[c] + 0.5f * size[c]) * inv;
         v[c] = vfo_f2i_rz(f);
     }
 }
 
+// The binary16 value nearest to x (ties to even), as a real: IEEE 754 rounding of the significand
+// to the binary16 spacing of x's binade (2^(e-10) for normal binary16 values, 2^-24 below 2^-14).
+// |x| stays far below the binary16 maximum here (TSDF values lie in [-1, 1]).
+extern "C" float vfo_round_half(float x) {
+    uint32_t u;
+    std::memcpy(&u, &x, 4);
+    const uint32_t sign = u & 0x80000000u, a = u & 0x7fffffffu;
+    const int e = (int)(a >> 23) - 127;
+    if (a == 0 || e < -40) {  // zero, binary32 subnormals and anything below half the smallest step
+        float z = 0.f;
+        if (sign) z = -z;
+        return z;
+    }
+    const uint32_t m = (a & 0x7fffffu) | 0x800000u;  // 24-bit significand, value m * 2^(e-23)
+    const int k = (e > -14 ? e : -14) - 10;          // exponent of the binary16 spacing
+    const int r = k - (e - 23);                      // significand bits below that spacing (13..)
+    uint32_t q = r >= 32 ? 0u : (m >> r);
+    if (r < 32) {
+        const uint32_t rem = m & ((1u << r) - 1u), half = 1u << (r - 1);
+        if (rem > half || (rem == half && (q & 1u))) ++q;
+    }
+    float y = std::ldexp((float)q, k);
+    return sign ? -y : y;
+}
+
 // updateTsdf (src/TSDFIntegration.cu:16-67), K column-major
-inline void update_tsdf(float* tsdf, float* weights, const float* p, long idx, const float* depth, int W, int H,
-                        float delta, const float* K) {
+inline void update_tsdf(real* tsdf, real* weights, const real* p, long idx, const real* depth, int W, int H,
+                        real delta, const real* K, int half) {
     if (p[2] < 1.e-4f) return;
-    float zInv = 1.0f / p[2];
-    float uf = (K[0] * p[0]) * zInv + K[6];
-    float vf = (K[4] * p[1]) * zInv + K[7];
+    real zInv = 1.0f / p[2];
+    real uf = (K[0] * p[0]) * zInv + K[6];
+    real vf = (K[4] * p[1]) * zInv + K[7];
     int u = vfo_f2i_rz(uf + 0.5f);
     int v = vfo_f2i_rz(vf + 0.5f);
     if (u < 0 || u >= W || v < 0 || v >= H) return;
-    float D = depth[(long)v * W + u];
+    real D = depth[(long)v * W + u];
     if (std::isinf(D) || D < 1.e-4f) return;
-    float sdf = p[2] - D;
+    real sdf = p[2] - D;
     if (sdf > delta) return;
-    float tnew = (sdf < -delta) ? -1.0f : sdf / delta;
-    float wnew = 1.0f;
-    float wold = weights[idx];
-    float told = tsdf[idx];
-    tsdf[idx] = (told * wold + tnew * wnew) / (wold + wnew);
-    weights[idx] = std::min(wold + wnew, 15.0f);
+    real tnew = (sdf < -delta) ? -1.0f : sdf / delta;
+    real wnew = 1.0f;
+    real wold = weights[idx];
+    real told = tsdf[idx];
+    const real t = (told * wold + tnew * wnew) / (wold + wnew);
+    // precision form: the value is stored as FP16 (weights are integer counts, exact either way)
+    tsdf[idx] = half ? (real)vfo_round_half((float)t) : t;
+    weights[idx] = std::min(wold + wnew, (real)15.0f);
 }
 
 struct Cand {
-    float key;  // squared distance (graph KNN) or distance (voxel KNN)
+    real key;  // squared distance (graph KNN) or distance (voxel KNN)
     uint32_t idx;
 };
 inline bool cand_less(const Cand& a, const Cand& b) { return a.key < b.key || (a.key == b.key && a.idx < b.idx); }
@@ -116,12 +151,12 @@ int edge_table(int cube) {
 }
 
 struct McCtx {
-    const float* tsdf;
-    const float* w;
+    const real* tsdf;
+    const real* w;
     int X, Y, Z;
-    const float* vs;
-    const float* size;
-    float iso;
+    const real* vs;
+    const real* size;
+    real iso;
     long at(int x, int y, int z) const { return (long)z * X * Y + (long)y * X + x; }
     // computeLutIndex (src/MarchingCubes.cu:338-379)
     int cube_index(int x, int y, int z) const {
@@ -135,26 +170,26 @@ struct McCtx {
         return idx;
     }
     // getVertex + interpolate (src/MarchingCubes.cu:294-336)
-    void vertex(int x, int y, int z, int e, float* o) const {
+    void vertex(int x, int y, int z, int e, real* o) const {
         const int* ca = kCorner[kEdge[e][0]];
         const int* cb = kCorner[kEdge[e][1]];
         int x1 = x + ca[0], y1 = y + ca[1], z1 = z + ca[2];
         int x2 = x + cb[0], y2 = y + cb[1], z2 = z + cb[2];
-        float t0 = tsdf[at(x1, y1, z1)], t1 = tsdf[at(x2, y2, z2)];
-        float p0[3], p1[3];
+        real t0 = tsdf[at(x1, y1, z1)], t1 = tsdf[at(x2, y2, z2)];
+        real p0[3], p1[3];
         voxel_to_world(x1, y1, z1, vs, size, p0);
         voxel_to_world(x2, y2, z2, vs, size, p1);
-        if ((double)std::fabs(iso - t0) < 1e-7) { std::memcpy(o, p0, 12); return; }
-        if ((double)std::fabs(iso - t1) < 1e-7) { std::memcpy(o, p1, 12); return; }
-        if ((double)std::fabs(t0 - t1) < 1e-7) { std::memcpy(o, p0, 12); return; }
+        if ((double)std::fabs(iso - t0) < 1e-7) { std::memcpy(o, p0, 3 * sizeof(real)); return; }
+        if ((double)std::fabs(iso - t1) < 1e-7) { std::memcpy(o, p1, 3 * sizeof(real)); return; }
+        if ((double)std::fabs(t0 - t1) < 1e-7) { std::memcpy(o, p0, 3 * sizeof(real)); return; }
         double mu = (double)((iso - t0) / (t1 - t0));
         if (mu > 1.0) mu = 1.0;
         else if (mu < 0) mu = 0.0;
-        for (int c = 0; c < 3; ++c) o[c] = (float)((double)p0[c] + mu * (double)(p1[c] - p0[c]));
+        for (int c = 0; c < 3; ++c) o[c] = (real)((double)p0[c] + mu * (double)(p1[c] - p0[c]));
     }
 };
 
-inline bool vec3_less(const float* a, const float* b) {
+inline bool vec3_less(const real* a, const real* b) {
     if (a[0] < b[0]) return true;
     if (b[0] < a[0]) return false;
     if (a[1] < b[1]) return true;
@@ -163,7 +198,7 @@ inline bool vec3_less(const float* a, const float* b) {
 }
 
 struct P3 {
-    float v[3];
+    real v[3];
 };
 
 }  // namespace
@@ -198,71 +233,80 @@ float vfo_expf(float x) {
     return (p * s1) * s2;
 }
 
-// float -> int conversion with CUDA's cvt.rzi.s32.f32 semantics (truncate, saturate, NaN -> 0),
-// which is what static_cast<int>(float) does in the reference's device code.
-int vfo_f2i_rz(float x) {
+}  // extern "C"
+namespace {
+inline real vexp(real x) {
+    if (sizeof(real) == sizeof(float)) return (real)vfo_expf((float)x);
+    return (real)std::exp((double)x);
+}
+}  // namespace
+extern "C" {
+
+// real -> int conversion with CUDA's cvt.rzi.s32.f32 semantics (truncate, saturate, NaN -> 0),
+// which is what static_cast<int>(real) does in the reference's device code.
+int vfo_f2i_rz(real x) {
     if (x != x) return 0;
     if (x >= 2147483648.0f) return 2147483647;
     if (x <= -2147483648.0f) return (int)(-2147483647 - 1);
     return (int)x;
 }
 
-void vfo_depth_from_mm(const uint16_t* mm, long n, float* out) {
+void vfo_depth_from_mm(const uint16_t* mm, long n, real* out) {
     // cv::Mat::convertTo(CV_32FC1, 1/1000) after cv::imread (src/dataset.cpp:188)
-    for (long i = 0; i < n; ++i) out[i] = (float)mm[i] * 0.001f;
+    for (long i = 0; i < n; ++i) out[i] = (real)mm[i] * 0.001f;
 }
 
-void vfo_filter_depth(float* depth, long n, float threshold) {
+void vfo_filter_depth(real* depth, long n, real threshold) {
     // filterDepthKernel (src/VertexManipulation.cu:6-15), fill value +inf
     for (long i = 0; i < n; ++i) {
-        float v = depth[i];
+        real v = depth[i];
         if (v > threshold || v < 1.e-4f || std::isnan(v)) depth[i] = kInf;
     }
 }
 
 // updateGaussian16 (src/BilateralFilter.cu:12-50)
-static void bilateral_tables(int r, double sd, float* g2d, int* clr) {
-    float g[64];
+static void bilateral_tables(int r, double sd, real* g2d, int* clr) {
+    real g[64];
     for (int i = 0; i < 2 * r + 1; i++) {
-        float x = (float)(i - r);
-        g[i] = expf((float)((double)(-(x * x)) / (2 * sd * sd)));
+        real x = (real)(i - r);
+        g[i] = expf((real)((double)(-(x * x)) / (2 * sd * sd)));
     }
     int index = 0;
     for (int dy = -r; dy <= r; dy++)
         for (int dx = -r; dx <= r; dx++) g2d[index++] = g[dy + r] * g[dx + r];
-    float fc[31];
-    for (int i = 0; i <= 30; i++) fc[i] = (float)std::exp(-(std::pow(i / 10.0, 2)) / (2));
+    real fc[31];
+    for (int i = 0; i <= 30; i++) fc[i] = (real)std::exp(-(std::pow(i / 10.0, 2)) / (2));
     for (int i = 0; i <= 30; i++) clr[i] = (int)(fc[i] / fc[30]);
 }
 
-void vfo_bilateral(float* out, const float* in, int h, int w, int r, double sI, double sS, float thr) {
+void vfo_bilateral(real* out, const real* in, int h, int w, int r, double sI, double sS, real thr) {
     // gpuFilterTextureOpmShared (src/BilateralFilter.cu:52-127): clamp-to-edge tile, loop a (x) outer, b (y) inner
-    std::vector<float> g2d((2 * r + 1) * (2 * r + 1));
+    std::vector<real> g2d((2 * r + 1) * (2 * r + 1));
     int clr[31];
     bilateral_tables(r, sS, g2d.data(), clr);
-    const float normFactor = (float)(30 / (3 * sI));
+    const real normFactor = (real)(30 / (3 * sI));
     const int kd = 2 * r + 1;
 #pragma omp parallel for schedule(static)
     for (int y = 0; y < h; ++y) {
         for (int x = 0; x < w; ++x) {
-            float centre = in[(long)y * w + x];
+            real centre = in[(long)y * w + x];
             if (std::isinf(centre)) {
                 out[(long)y * w + x] = kInf;
                 continue;
             }
-            float iF = 0, wP = 0;
+            real iF = 0, wP = 0;
             int ig = 0;
             for (int a = 0; a < kd; ++a) {
                 for (int b = 0; b < kd; ++b, ++ig) {
                     int xx = std::min(std::max(x + a - r, 0), w - 1);
                     int yy = std::min(std::max(y + b - r, 0), h - 1);
-                    float cur = in[(long)yy * w + xx];
+                    real cur = in[(long)yy * w + xx];
                     if (std::isinf(cur)) continue;
-                    float diff = std::fabs(centre - cur);
+                    real diff = std::fabs(centre - cur);
                     if (diff > thr) continue;
                     int x0 = vfo_f2i_rz(std::fabs(diff * normFactor));
                     if (x0 > 30 || x0 < 0) x0 = 30;
-                    float wt = g2d[ig] * (float)clr[x0];
+                    real wt = g2d[ig] * (real)clr[x0];
                     iF += cur * wt;
                     wP += wt;
                 }
@@ -272,56 +316,56 @@ void vfo_bilateral(float* out, const float* in, int h, int w, int r, double sI, 
     }
 }
 
-void vfo_depth_to_mesh(float* mesh, const float* depth, int width, int height, const float* K) {
+void vfo_depth_to_mesh(real* mesh, const real* depth, int width, int height, const real* K) {
     // depthToMeshKernel (src/VertexManipulation.cu:43-63)
-    const float fxi = 1.0f / K[0], fyi = 1.0f / K[4];
+    const real fxi = 1.0f / K[0], fyi = 1.0f / K[4];
     for (int y = 0; y < height; ++y)
         for (int x = 0; x < width; ++x) {
             long id = (long)y * width + x;
-            float d = depth[id];
-            float* m = mesh + 3 * id;
+            real d = depth[id];
+            real* m = mesh + 3 * id;
             if (std::isinf(d) || d < 1.e-4f) {
                 m[0] = m[1] = m[2] = 0.f;
                 continue;
             }
-            float x0 = ((float)x - K[6]) * fxi;
-            float y0 = ((float)y - K[7]) * fyi;
+            real x0 = ((real)x - K[6]) * fxi;
+            real y0 = ((real)y - K[7]) * fyi;
             m[0] = x0 * d;
             m[1] = y0 * d;
             m[2] = d;
         }
 }
 
-void vfo_normals(float* normals, const float* V, int h, int w, float a_lo, float a_hi) {
+void vfo_normals(real* normals, const real* V, int h, int w, real a_lo, real a_hi) {
     // depthVerticesNormalsKernel (src/VertexManipulation.cu:147-207); border pixels get a zero normal
-    std::memset(normals, 0, sizeof(float) * 3 * (size_t)w * h);
+    std::memset(normals, 0, sizeof(real) * 3 * (size_t)w * h);
 #pragma omp parallel for schedule(static)
     for (int y = 1; y < h - 1; ++y) {
         for (int x = 1; x < w - 1; ++x) {
             long id = (long)y * w + x;
-            float* n = normals + 3 * id;
+            real* n = normals + 3 * id;
             if (V[3 * id + 2] < 1.e-4f) continue;
-            const float* xl = V + 3 * (id - 1);
-            const float* xr = V + 3 * (id + 1);
-            const float* yt = V + 3 * (id - w);
-            const float* yb = V + 3 * (id + w);
+            const real* xl = V + 3 * (id - 1);
+            const real* xr = V + 3 * (id + 1);
+            const real* yt = V + 3 * (id - w);
+            const real* yb = V + 3 * (id + w);
             if (xr[2] < 1.e-4f || xl[2] < 1.e-4f || yb[2] < 1.e-4f || yt[2] < 1.e-4f) continue;
-            float dX[3] = {xr[0] - xl[0], xr[1] - xl[1], xr[2] - xl[2]};
-            float dY[3] = {yb[0] - yt[0], yb[1] - yt[1], yb[2] - yt[2]};
-            float nx = std::sqrt(dX[0] * dX[0] + dX[1] * dX[1]);
-            float ny = std::sqrt(dY[0] * dY[0] + dY[1] * dY[1]);
-            float gX[3] = {dX[0] / nx, dX[1] / nx, dX[2] / nx};
-            float gY[3] = {dY[0] / ny, dY[1] / ny, dY[2] / ny};
-            float c[3] = {gY[1] * gX[2] - gY[2] * gX[1], gY[2] * gX[0] - gY[0] * gX[2], gY[0] * gX[1] - gY[1] * gX[0]};
-            float s = sqnorm3(c);
+            real dX[3] = {xr[0] - xl[0], xr[1] - xl[1], xr[2] - xl[2]};
+            real dY[3] = {yb[0] - yt[0], yb[1] - yt[1], yb[2] - yt[2]};
+            real nx = std::sqrt(dX[0] * dX[0] + dX[1] * dX[1]);
+            real ny = std::sqrt(dY[0] * dY[0] + dY[1] * dY[1]);
+            real gX[3] = {dX[0] / nx, dX[1] / nx, dX[2] / nx};
+            real gY[3] = {dY[0] / ny, dY[1] / ny, dY[2] / ny};
+            real c[3] = {gY[1] * gX[2] - gY[2] * gX[1], gY[2] * gX[0] - gY[0] * gX[2], gY[0] * gX[1] - gY[1] * gX[0]};
+            real s = sqnorm3(c);
             if (s > 0.f) {
-                float q = std::sqrt(s);
+                real q = std::sqrt(s);
                 c[0] /= q;
                 c[1] /= q;
                 c[2] /= q;
             }
-            float dot = 0.f * c[0] + (0.f * c[1] + 1.f * c[2]);
-            float angle = (float)std::acos((double)dot);
+            real dot = 0.f * c[0] + (0.f * c[1] + 1.f * c[2]);
+            real angle = (real)std::acos((double)dot);
             if (angle > a_lo && angle < a_hi) continue;
             n[0] = c[0];
             n[1] = c[1];
@@ -330,12 +374,12 @@ void vfo_normals(float* normals, const float* V, int h, int w, float a_lo, float
     }
 }
 
-void vfo_remove_without_normals(const float* normals, float* V, float* depth, int h, int w) {
+void vfo_remove_without_normals(const real* normals, real* V, real* depth, int h, int w) {
     // removeDepthWithoutNormalsKernel (src/VertexManipulation.cu:223-236), isZero(1e-4)
     for (int y = 1; y < h - 1; ++y)
         for (int x = 1; x < w - 1; ++x) {
             long id = (long)y * w + x;
-            const float* n = normals + 3 * id;
+            const real* n = normals + 3 * id;
             if (std::fabs(n[0]) <= 1.e-4f && std::fabs(n[1]) <= 1.e-4f && std::fabs(n[2]) <= 1.e-4f) {
                 V[3 * id] = V[3 * id + 1] = V[3 * id + 2] = 0.f;
                 depth[id] = kInf;
@@ -343,7 +387,7 @@ void vfo_remove_without_normals(const float* normals, float* V, float* depth, in
         }
 }
 
-void vfo_centroid(const float* V, long n, float out[3]) {
+void vfo_centroid(const real* V, long n, real out[3]) {
     // Sum of all vertices / count of z > 1e-4 (src/VolumeFusion.cu:217-219).  The sum is taken in
     // 2^-32 fixed point so that it does not depend on summation order.
     long long s[3] = {0, 0, 0};
@@ -352,18 +396,18 @@ void vfo_centroid(const float* V, long n, float out[3]) {
         for (int c = 0; c < 3; ++c) s[c] += std::llrint((double)V[3 * i + c] * 4294967296.0);
         if (V[3 * i + 2] > 1.e-4f) ++cnt;
     }
-    for (int c = 0; c < 3; ++c) out[c] = (float)(((double)s[c] / 4294967296.0) / (double)cnt);
+    for (int c = 0; c < 3; ++c) out[c] = (real)(((double)s[c] / 4294967296.0) / (double)cnt);
 }
 
-void vfo_frame_prep(const uint16_t* mm, int width, int height, const float* K, float depth_threshold, int bilateral,
-                    int r, double sigma_i, double sigma_s, float thr, float angle_lo, float angle_hi, float* depth,
-                    float* vertices, float* normals, float centroid[3]) {
+void vfo_frame_prep(const uint16_t* mm, int width, int height, const real* K, real depth_threshold, int bilateral,
+                    int r, double sigma_i, double sigma_s, real thr, real angle_lo, real angle_hi, real* depth,
+                    real* vertices, real* normals, real centroid[3]) {
     // af::loadProcessFrame (src/VolumeFusion.cu:184-220)
     long n = (long)width * height;
     vfo_depth_from_mm(mm, n, depth);
     vfo_filter_depth(depth, n, depth_threshold);
     if (bilateral) {
-        std::vector<float> tmp(depth, depth + n);
+        std::vector<real> tmp(depth, depth + n);
         vfo_bilateral(depth, tmp.data(), height, width, r, sigma_i, sigma_s, thr);
     }
     vfo_depth_to_mesh(vertices, depth, width, height, K);
@@ -372,22 +416,22 @@ void vfo_frame_prep(const uint16_t* mm, int width, int height, const float* K, f
     vfo_centroid(vertices, n, centroid);
 }
 
-void vfo_integrate_rigid(float* tsdf, float* weights, const float* depth, int width, int height, float delta,
-                         const int dims[3], const float vs[3], const float size[3], const float R[9], const float t[3],
-                         const float K[9]) {
+void vfo_integrate_rigid(real* tsdf, real* weights, const real* depth, int width, int height, real delta,
+                         const int dims[3], const real vs[3], const real size[3], const real R[9], const real t[3],
+                         const real K[9], int half) {
     // integrateTSDFFromFrameKernel (src/TSDFIntegration.cu:69-96)
     const int X = dims[0], Y = dims[1], Z = dims[2];
 #pragma omp parallel for schedule(static)
     for (int z = 0; z < Z; ++z)
         for (int y = 0; y < Y; ++y)
             for (int x = 0; x < X; ++x) {
-                float p[3], q[3];
+                real p[3], q[3];
                 voxel_to_world(x, y, z, vs, size, p);
                 mat3_vec3(R, p, q);
                 q[0] = q[0] + t[0];
                 q[1] = q[1] + t[1];
                 q[2] = q[2] + t[2];
-                update_tsdf(tsdf, weights, q, (long)z * X * Y + (long)y * X + x, depth, width, height, delta, K);
+                update_tsdf(tsdf, weights, q, (long)z * X * Y + (long)y * X + x, depth, width, height, delta, K, half);
             }
 }
 
@@ -408,8 +452,8 @@ static void mc_slab(const McCtx& m, int z, std::vector<P3>& out) {
         }
 }
 
-long vfo_mc_pointcloud(const float* tsdf, const float* weights, const int dims[3], const float vs[3],
-                       const float size[3], float iso, float* out, long cap) {
+long vfo_mc_pointcloud(const real* tsdf, const real* weights, const int dims[3], const real vs[3],
+                       const real size[3], real iso, real* out, long cap) {
     // marchingCubesMeshKernel (src/MarchingCubes.cu:422-508), cubes x,y,z < dim-2, z/y/x loop order
     McCtx m{tsdf, weights, dims[0], dims[1], dims[2], vs, size, iso};
     int nz = std::max(dims[2] - 2, 0);
@@ -419,35 +463,35 @@ long vfo_mc_pointcloud(const float* tsdf, const float* weights, const int dims[3
     long n = 0;
     for (auto& s : slabs) {
         for (auto& p : s) {
-            if (n < cap) std::memcpy(out + 3 * n, p.v, 12);
+            if (n < cap) std::memcpy(out + 3 * n, p.v, 3 * sizeof(real));
             ++n;
         }
     }
     return n;
 }
 
-long vfo_sort_unique_vec3(float* pts, long n) {
+long vfo_sort_unique_vec3(real* pts, long n) {
     // thrust::sort + thrust::unique with the lexicographic operator< (include/af/eigen_extension.cuh:15-25)
     std::vector<P3> v(n);
-    std::memcpy(v.data(), pts, 12 * n);
+    std::memcpy(v.data(), pts, 3 * sizeof(real) * n);
     std::sort(v.begin(), v.end(), [](const P3& a, const P3& b) { return vec3_less(a.v, b.v); });
     long m = 0;
     for (long i = 0; i < n; ++i) {
         if (m > 0 && v[i].v[0] == v[m - 1].v[0] && v[i].v[1] == v[m - 1].v[1] && v[i].v[2] == v[m - 1].v[2]) continue;
         v[m++] = v[i];
     }
-    std::memcpy(pts, v.data(), 12 * m);
+    std::memcpy(pts, v.data(), 3 * sizeof(real) * m);
     return m;
 }
 
-void vfo_translate(float* pts, long n, const float t[3]) {
+void vfo_translate(real* pts, long n, const real t[3]) {
     // translateKernel (src/VertexManipulation.cu:73-79)
     for (long i = 0; i < n; ++i)
         for (int c = 0; c < 3; ++c) pts[3 * i + c] = pts[3 * i + c] + t[c];
 }
 
-long vfo_mc_full(const float* tsdf, const float* weights, const int dims[3], const float vs[3], const float size[3],
-                 float iso, float* verts, long vcap, int* faces, long fcap, long* nfaces) {
+long vfo_mc_full(const real* tsdf, const real* weights, const int dims[3], const real vs[3], const real size[3],
+                 real iso, real* verts, long vcap, int* faces, long fcap, long* nfaces) {
     // marchingCubesFullKernel + computeTriangles (src/MarchingCubes.cu:393-420, 526-682), cube order z/y/x
     McCtx m{tsdf, weights, dims[0], dims[1], dims[2], vs, size, iso};
     int nz = std::max(dims[2] - 2, 0);
@@ -459,7 +503,7 @@ long vfo_mc_full(const float* tsdf, const float* weights, const int dims[3], con
                 int ci = m.cube_index(x, y, z);
                 if (ci == 0 || ci == 255) continue;
                 int et = edge_table(ci);
-                float ep[12][3];
+                real ep[12][3];
                 for (int e = 0; e < 12; ++e)
                     if (et & (1 << e)) m.vertex(x, y, z, e, ep[e]);
                 uint64_t tri = kTriTable[ci];
@@ -467,13 +511,13 @@ long vfo_mc_full(const float* tsdf, const float* weights, const int dims[3], con
                     int e0 = (int)((tri >> (4 * s)) & 0xF);
                     if (e0 == 0xF) break;
                     int e1 = (int)((tri >> (4 * (s + 1))) & 0xF), e2 = (int)((tri >> (4 * (s + 2))) & 0xF);
-                    const float *p1 = ep[e0], *p2 = ep[e1], *p3 = ep[e2];
-                    auto ne = [](const float* a, const float* b) { return a[0] != b[0] || a[1] != b[1] || a[2] != b[2]; };
+                    const real *p1 = ep[e0], *p2 = ep[e1], *p3 = ep[e2];
+                    auto ne = [](const real* a, const real* b) { return a[0] != b[0] || a[1] != b[1] || a[2] != b[2]; };
                     if (ne(p1, p2) && ne(p1, p3) && ne(p2, p3)) {
                         P3 a, b, c;
-                        std::memcpy(a.v, p1, 12);
-                        std::memcpy(b.v, p2, 12);
-                        std::memcpy(c.v, p3, 12);
+                        std::memcpy(a.v, p1, 3 * sizeof(real));
+                        std::memcpy(b.v, p2, 3 * sizeof(real));
+                        std::memcpy(c.v, p3, 3 * sizeof(real));
                         slabs[z].push_back(a);
                         slabs[z].push_back(b);
                         slabs[z].push_back(c);
@@ -484,7 +528,7 @@ long vfo_mc_full(const float* tsdf, const float* weights, const int dims[3], con
     long nv = 0;
     for (auto& s : slabs)
         for (auto& p : s) {
-            if (nv < vcap) std::memcpy(verts + 3 * nv, p.v, 12);
+            if (nv < vcap) std::memcpy(verts + 3 * nv, p.v, 3 * sizeof(real));
             ++nv;
         }
     long nf = nv / 3;
@@ -499,27 +543,27 @@ long vfo_mc_full(const float* tsdf, const float* weights, const int dims[3], con
 
 // ---- motion graph ----
 
-static int knn_query(const float* nodes, int n, const float* q, int k, Cand* out) {
+static int knn_query(const real* nodes, int n, const real* q, int k, Cand* out) {
     int cnt = 0;
     for (int j = 0; j < n; ++j) topk_insert(out, cnt, k, Cand{l2sq_nanoflann(q, nodes + 3 * j), (uint32_t)j});
     return cnt;
 }
 
-int vfo_build_graph(float* nodes, float* radii, float* T, int n, int cap, const float* mesh, long m, int knn,
-                    float radius) {
+int vfo_build_graph(real* nodes, real* radii, real* T, int n, int cap, const real* mesh, long m, int knn,
+                    real radius) {
     // af::buildGraph (src/GraphBuilder.cpp:12-50) with MotionGraph::knnSearch (src/MotionGraph.cpp:43-60)
-    static const float I4[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+    static const real I4[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
     if (m == 0) return n;
     if (n == 0) {
         if (cap < 1) return -1;
-        std::memcpy(nodes, mesh, 12);
+        std::memcpy(nodes, mesh, 3 * sizeof(real));
         radii[0] = radius;
-        std::memcpy(T, I4, 64);
+        std::memcpy(T, I4, 16 * sizeof(real));
         n = 1;
     }
     std::vector<Cand> c(knn);
     for (long i = 0; i < m; ++i) {
-        const float* q = mesh + 3 * i;
+        const real* q = mesh + 3 * i;
         int cnt = knn_query(nodes, n, q, knn, c.data());
         bool supported = false;
         for (int j = 0; j < cnt; ++j)
@@ -529,20 +573,20 @@ int vfo_build_graph(float* nodes, float* radii, float* T, int n, int cap, const 
             }
         if (supported) continue;
         if (n >= cap) return -1;
-        float d0 = std::sqrt(c[0].key);
-        float factor = d0 / (0.f + d0);
-        const float* Tn = T + 16 * c[0].idx;
-        float* Tnew = T + 16 * n;
+        real d0 = std::sqrt(c[0].key);
+        real factor = d0 / (0.f + d0);
+        const real* Tn = T + 16 * c[0].idx;
+        real* Tnew = T + 16 * n;
         for (int e = 0; e < 16; ++e) Tnew[e] = 0.f + Tn[e] * factor;
-        std::memcpy(nodes + 3 * n, q, 12);
+        std::memcpy(nodes + 3 * n, q, 3 * sizeof(real));
         radii[n] = radius;
         ++n;
     }
     return n;
 }
 
-void vfo_knn(const float* nodes, int n, const float* pts, long m, int k, int exclude_closest, uint32_t* idx,
-             float* dist) {
+void vfo_knn(const real* nodes, int n, const real* pts, long m, int k, int exclude_closest, uint32_t* idx,
+             real* dist) {
     // af::getKnnData<K> + MotionGraph::knnSearch<K> (include/af/GraphBuilder.h:118-130, include/af/MotionGraph.h:50-70).
     // Exact K nearest by nanoflann's squared distance; equal distances are ordered by node index.
     const int kk = k + (exclude_closest ? 1 : 0);
@@ -564,7 +608,7 @@ void vfo_knn(const float* nodes, int n, const float* pts, long m, int k, int exc
     }
 }
 
-void vfo_filter_disconnected(uint32_t* idx, float* dist, int n, int k, const float* radii) {
+void vfo_filter_disconnected(uint32_t* idx, real* dist, int n, int k, const real* radii) {
     // af::filterDisconnected<K> (include/af/GraphBuilder.h:132-146)
     for (int i = 0; i < n; ++i)
         for (int j = 0; j < k; ++j) {
@@ -576,19 +620,19 @@ void vfo_filter_disconnected(uint32_t* idx, float* dist, int n, int k, const flo
         }
 }
 
-void vfo_warp_weights(float* w, const float* radii, const uint32_t* idx, const float* dist, long m, int k,
+void vfo_warp_weights(real* w, const real* radii, const uint32_t* idx, const real* dist, long m, int k,
                       int n_nodes) {
     // computeWarpWeightsKernel + weight() (src/VertexManipulation.cu:105-132): cut off at d >= radius
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < m; ++i) {
-        float s = 0;
-        float* wi = w + i * k;
+        real s = 0;
+        real* wi = w + i * k;
         for (int j = 0; j < k; ++j) {
             uint32_t nb = idx[i * k + j];
-            float wj = 0.f;
+            real wj = 0.f;
             if (nb < (uint32_t)n_nodes) {
-                float r = radii[nb], d = dist[i * k + j];
-                wj = (d >= r) ? 0.f : vfo_expf(-(d * d) / (2.0f * (r * r)));
+                real r = radii[nb], d = dist[i * k + j];
+                wj = (d >= r) ? 0.f : vexp(-(d * d) / (2.0f * (r * r)));
             }
             wi[j] = wj;
             s += wj;
@@ -598,44 +642,44 @@ void vfo_warp_weights(float* w, const float* radii, const uint32_t* idx, const f
     }
 }
 
-void vfo_warp(float* out, const float* pts, long m, const float* T, const uint32_t* idx, const float* w, int k) {
+void vfo_warp(real* out, const real* pts, long m, const real* T, const uint32_t* idx, const real* w, int k) {
     // warpKernel (src/ComputeCorrespondence.cu:5-30): identity when all weights are zero (isZero, 1e-5)
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < m; ++i) {
-        const float* p = pts + 3 * i;
-        const float* wi = w + i * k;
+        const real* p = pts + 3 * i;
+        const real* wi = w + i * k;
         bool zero = true;
         for (int j = 0; j < k; ++j)
             if (!(std::fabs(wi[j]) <= 1e-5f)) zero = false;
-        float acc[3] = {0.f, 0.f, 0.f};
+        real acc[3] = {0.f, 0.f, 0.f};
         if (zero) {
-            std::memcpy(acc, p, 12);
+            std::memcpy(acc, p, 3 * sizeof(real));
         } else {
             for (int j = 0; j < k; ++j) {
                 uint32_t nb = idx[i * k + j];
                 if (nb == VFO_INVALID_IDX) continue;
-                float q[3];
+                real q[3];
                 mat4_point(T + 16 * (size_t)nb, p, q);
                 for (int c = 0; c < 3; ++c) acc[c] = acc[c] + wi[j] * q[c];
             }
         }
-        std::memcpy(out + 3 * i, acc, 12);
+        std::memcpy(out + 3 * i, acc, 3 * sizeof(real));
     }
 }
 
-long vfo_correspondences(int* corr, long cap, const float* warped, long m, const float* K, const float* depth,
-                         int rows, int cols, const float* frame_mesh, float thr) {
+long vfo_correspondences(int* corr, long cap, const real* warped, long m, const real* K, const real* depth,
+                         int rows, int cols, const real* frame_mesh, real thr) {
     // correspondencePairsKernel (src/ComputeCorrespondence.cu:45-81), output ordered by vertex index
     long n = 0;
     for (long i = 0; i < m; ++i) {
-        const float* v = warped + 3 * i;
-        float y0 = v[1] / v[2];
-        float x0 = v[0] / v[2];
+        const real* v = warped + 3 * i;
+        real y0 = v[1] / v[2];
+        real x0 = v[0] / v[2];
         int y = vfo_f2i_rz(y0 * K[4] + K[7]);
         int x = vfo_f2i_rz(x0 * K[0] + K[6]);
         if (y < 0 || x < 0 || y >= rows || x >= cols) continue;
         long px = (long)y * cols + x;
-        float d[3] = {frame_mesh[3 * px] - v[0], frame_mesh[3 * px + 1] - v[1], frame_mesh[3 * px + 2] - v[2]};
+        real d[3] = {frame_mesh[3 * px] - v[0], frame_mesh[3 * px + 1] - v[1], frame_mesh[3 * px + 2] - v[2]};
         if (norm3(d) > thr) continue;
         if (depth[px] > 1.e-4f) {
             if (n < cap) {
@@ -650,28 +694,28 @@ long vfo_correspondences(int* corr, long cap, const float* warped, long m, const
 
 // ---- Gauss-Newton ----
 
-void vfo_residual_depth(float* r, const int* corr, long c, const float* warped, const float* frame_mesh,
-                        const float* normals, float lambda) {
+void vfo_residual_depth(real* r, const int* corr, long c, const real* warped, const real* frame_mesh,
+                        const real* normals, real lambda) {
     // fill_r_DepthKernel (src/MotionOptimization.cu:163-181)
     for (long i = 0; i < c; ++i) {
-        const float* v = warped + 3 * (long)corr[2 * i];
-        const float* f = frame_mesh + 3 * (long)corr[2 * i + 1];
-        const float* n = normals + 3 * (long)corr[2 * i + 1];
-        float d[3] = {v[0] - f[0], v[1] - f[1], v[2] - f[2]};
+        const real* v = warped + 3 * (long)corr[2 * i];
+        const real* f = frame_mesh + 3 * (long)corr[2 * i + 1];
+        const real* n = normals + 3 * (long)corr[2 * i + 1];
+        real d[3] = {v[0] - f[0], v[1] - f[1], v[2] - f[2]};
         r[i] = lambda * dot3(n, d);
     }
 }
 
-void vfo_residual_reg(float* r, const float* nodes, const float* T, int n, const uint32_t* gidx, int kreg,
-                      float lambda) {
+void vfo_residual_reg(real* r, const real* nodes, const real* T, int n, const uint32_t* gidx, int kreg,
+                      real lambda) {
     // fill_r_MRegKernel (src/MotionOptimization.cu:198-227); rows of invalid slots are left untouched (zero)
     for (int i = 0; i < n; ++i) {
-        float tc[3];
+        real tc[3];
         mat4_point(T + 16 * (size_t)i, nodes + 3 * i, tc);
         for (int k = 0; k < kreg; ++k) {
             uint32_t nb = gidx[i * kreg + k];
             if (nb >= (uint32_t)n) continue;
-            float tn[3];
+            real tn[3];
             mat4_point(T + 16 * (size_t)nb, nodes + 3 * i, tn);
             long row = ((long)i * kreg + k) * 3;
             for (int a = 0; a < 3; ++a) r[row + a] = (tc[a] - tn[a]) * lambda;
@@ -679,7 +723,7 @@ void vfo_residual_reg(float* r, const float* nodes, const float* T, int n, const
     }
 }
 
-double vfo_energy(const float* r, long n) {
+double vfo_energy(const real* r, long n) {
     // runSquareKernel + thrust::reduce (src/VolumeFusion.cu:585-588), accumulated in FP64
     double e = 0;
     for (long i = 0; i < n; ++i) e += (double)(r[i] * r[i]);
@@ -687,44 +731,44 @@ double vfo_energy(const float* r, long n) {
 }
 
 // d(T p)/d xi rows for the additive update (gradOfTransfVertex, src/MotionOptimization.cu:10-26)
-static void grad_rows(const float* p, float G[3][6]) {
-    const float Gv[3][6] = {{0, p[2], -p[1], 1, 0, 0}, {-p[2], 0, p[0], 0, 1, 0}, {p[1], -p[0], 0, 0, 0, 1}};
+static void grad_rows(const real* p, real G[3][6]) {
+    const real Gv[3][6] = {{0, p[2], -p[1], 1, 0, 0}, {-p[2], 0, p[0], 0, 1, 0}, {p[1], -p[0], 0, 0, 0, 1}};
     std::memcpy(G, Gv, sizeof(Gv));
 }
 
-int vfo_assemble(double* jtj_dense, float* jtj_blocks, float* jtr, const int* corr, long c, const float* canon,
-                 const uint32_t* midx, const float* mw, int k, const float* normals, float lambda_d,
-                 const float* nodes, int n, const uint32_t* gidx, int kreg, float lambda_r, const float* r_depth,
-                 const float* r_reg) {
+int vfo_assemble(double* jtj_dense, real* jtj_blocks, real* jtr, const int* corr, long c, const real* canon,
+                 const uint32_t* midx, const real* mw, int k, const real* normals, real lambda_d,
+                 const real* nodes, int n, const uint32_t* gidx, int kreg, real lambda_r, const real* r_depth,
+                 const real* r_reg) {
     // J^T J and J^T r as assembled by runFill_J_*, runComputeJTJAndJTrContrib*, runMultiply*, reduce_by_key
     // and runFillJTJKernel/runFillJTrKernel (src/MotionOptimization.cu:29-481, src/VolumeFusion.cu:469-646).
     // Per block the contributions are summed in binary32 in the order: depth rows by ascending
     // correspondence, then regularisation rows by ascending row.  Diagonal blocks that receive no
     // contribution keep the identity written by runInitIdentityKernel.  jtj_blocks (optional) is
-    // the dense (6n)^2 float matrix, row-major; jtj_dense (optional) is the same in double.
+    // the dense (6n)^2 real matrix, row-major; jtj_dense (optional) is the same in double.
     const long dim = 6L * n;
-    std::vector<float> A((size_t)dim * dim, 0.f);
+    std::vector<real> A((size_t)dim * dim, 0.f);
     std::vector<char> touched((size_t)n * n, 0);
-    std::vector<float> b((size_t)dim, 0.f);
-    auto add_block = [&](int a, int bb, const float* Ja, const float* Jb) {
+    std::vector<real> b((size_t)dim, 0.f);
+    auto add_block = [&](int a, int bb, const real* Ja, const real* Jb) {
         touched[(size_t)a * n + bb] = 1;
         for (int i = 0; i < 6; ++i)
             for (int j = 0; j < 6; ++j) {
-                float& e = A[(size_t)(6 * a + i) * dim + 6 * bb + j];
+                real& e = A[(size_t)(6 * a + i) * dim + 6 * bb + j];
                 e = e + Ja[i] * Jb[j];
             }
     };
     for (long ci = 0; ci < c; ++ci) {
         int vi = corr[2 * ci], pi = corr[2 * ci + 1];
-        const float* nrm = normals + 3 * (long)pi;
-        float G[3][6];
+        const real* nrm = normals + 3 * (long)pi;
+        real G[3][6];
         grad_rows(canon + 3 * (long)vi, G);
-        float J[32][6];
+        real J[32][6];
         for (int s = 0; s < k; ++s) {
-            float wgt = mw[(long)vi * k + s];
+            real wgt = mw[(long)vi * k + s];
             for (int q = 0; q < 6; ++q) J[s][q] = 0.f;
             if (wgt < 1.e-4f) continue;
-            float nw[3] = {nrm[0] * wgt, nrm[1] * wgt, nrm[2] * wgt};
+            real nw[3] = {nrm[0] * wgt, nrm[1] * wgt, nrm[2] * wgt};
             for (int q = 0; q < 6; ++q) J[s][q] = (nw[0] * G[0][q] + (nw[1] * G[1][q] + nw[2] * G[2][q])) * lambda_d;
         }
         for (int s = 0; s < k; ++s) {
@@ -740,14 +784,14 @@ int vfo_assemble(double* jtj_dense, float* jtj_blocks, float* jtr, const int* co
         }
     }
     for (int i = 0; i < n; ++i) {
-        float G[3][6];
+        real G[3][6];
         grad_rows(nodes + 3 * i, G);
         for (int kk = 0; kk < kreg; ++kk) {
             uint32_t nb = gidx[i * kreg + kk];
             if (nb >= (uint32_t)n) continue;
             for (int ax = 0; ax < 3; ++ax) {
                 long row = ((long)i * kreg + kk) * 3 + ax;
-                float g[6], gn[6];
+                real g[6], gn[6];
                 for (int q = 0; q < 6; ++q) {
                     g[q] = G[ax][q] * lambda_r;
                     gn[q] = -g[q];
@@ -776,14 +820,14 @@ int vfo_assemble(double* jtj_dense, float* jtj_blocks, float* jtr, const int* co
                     A[(size_t)(6 * bb + i) * dim + 6 * a + j] = A[(size_t)(6 * a + j) * dim + 6 * bb + i];
         }
     }
-    if (jtj_blocks) std::memcpy(jtj_blocks, A.data(), sizeof(float) * A.size());
+    if (jtj_blocks) std::memcpy(jtj_blocks, A.data(), sizeof(real) * A.size());
     if (jtj_dense)
         for (size_t i = 0; i < A.size(); ++i) jtj_dense[i] = (double)A[i];
-    if (jtr) std::memcpy(jtr, b.data(), sizeof(float) * b.size());
+    if (jtr) std::memcpy(jtr, b.data(), sizeof(real) * b.size());
     return empty;
 }
 
-int vfo_solve_dense(const double* A, const float* b, int dim, double* x) {
+int vfo_solve_dense(const double* A, const real* b, int dim, double* x) {
     // FP64 Cholesky in place of the reference's FP32 cuSOLVER LU (src/LinearSolver.cu:179-224)
     std::vector<double> L((size_t)dim * dim, 0.0);
     for (int j = 0; j < dim; ++j) {
@@ -836,7 +880,7 @@ static bool inv6(const double* M, double* Minv) {
     return true;
 }
 
-int vfo_pcg(const double* A, const float* b, int n, int iters, double tol, double* x, int* iters_done) {
+int vfo_pcg(const double* A, const real* b, int n, int iters, double tol, double* x, int* iters_done) {
     // Block-Jacobi preconditioned conjugate gradients in FP64 (reference point for the GPU solver)
     const int dim = 6 * n;
     std::vector<double> Minv((size_t)n * 36), r(dim), z(dim), p(dim), Ap(dim);
@@ -894,20 +938,20 @@ int vfo_pcg(const double* A, const float* b, int n, int iters, double tol, doubl
     return 0;
 }
 
-void vfo_update_transforms(float* T, const float* x, int n) {
+void vfo_update_transforms(real* T, const real* x, int n) {
     // updateTransformsKernel (src/MotionOptimization.cu:483-498): T <- T - [[xi_rot]x, xi_t; 0 0 0 0]
     for (int i = 0; i < n; ++i) {
-        const float* u = x + 6 * i;
-        float* t = T + 16 * (size_t)i;
-        const float U[16] = {0, u[2], -u[1], 0, -u[2], 0, u[0], 0, u[1], -u[0], 0, 0, u[3], u[4], u[5], 0};  // column-major
+        const real* u = x + 6 * i;
+        real* t = T + 16 * (size_t)i;
+        const real U[16] = {0, u[2], -u[1], 0, -u[2], 0, u[0], 0, u[1], -u[0], 0, 0, u[3], u[4], u[5], 0};  // column-major
         for (int e = 0; e < 16; ++e) t[e] = t[e] - U[e];
     }
 }
 
 // ---- voxel warp and warped integration ----
 
-void vfo_tsdf_knn(uint32_t* kidx, float* kdist, int* kcount, const float* nodes, const float* radii, int n,
-                  const float vs[3], const float size[3], const int dims[3], const int per_node[3], int k) {
+void vfo_tsdf_knn(uint32_t* kidx, real* kdist, int* kcount, const real* nodes, const real* radii, int n,
+                  const real vs[3], const real size[3], const int dims[3], const int per_node[3], int k) {
     // tsdfKNNGraph (src/TSDFWarp.cu:23-68).  Support: voxels of the node's cube within 2*radius.
     // Slot rule: the K nearest supporting nodes, ordered by (distance, node index); the reference
     // keeps the first K to arrive, so the two agree whenever a voxel has at most K supporters.
@@ -916,7 +960,7 @@ void vfo_tsdf_knn(uint32_t* kidx, float* kdist, int* kcount, const float* nodes,
     std::vector<int> tot(S, 0);
     std::vector<Cand> best((size_t)S * k);
     for (int j = 0; j < n; ++j) {
-        const float* nd = nodes + 3 * j;
+        const real* nd = nodes + 3 * j;
         int nv[3];
         world_to_voxel(nd, vs, size, nv);
         for (int oz = 0; oz < per_node[2]; ++oz)
@@ -925,10 +969,10 @@ void vfo_tsdf_knn(uint32_t* kidx, float* kdist, int* kcount, const float* nodes,
                     int v[3] = {nv[0] - (per_node[0] - 1) / 2 + ox, nv[1] - (per_node[1] - 1) / 2 + oy,
                                 nv[2] - (per_node[2] - 1) / 2 + oz};
                     if (v[0] < 0 || v[1] < 0 || v[2] < 0 || v[0] >= X || v[1] >= Y || v[2] >= Z) continue;
-                    float tp[3];
+                    real tp[3];
                     voxel_to_world(v[0], v[1], v[2], vs, size, tp);
-                    float d3[3] = {tp[0] - nd[0], tp[1] - nd[1], tp[2] - nd[2]};
-                    float dist = norm3(d3);
+                    real d3[3] = {tp[0] - nd[0], tp[1] - nd[1], tp[2] - nd[2]};
+                    real dist = norm3(d3);
                     if (dist > radii[j] * 2.0f) continue;
                     long id = (long)v[2] * X * Y + (long)v[1] * X + v[0];
                     int cnt = std::min(tot[id], k);
@@ -951,19 +995,19 @@ void vfo_tsdf_knn(uint32_t* kidx, float* kdist, int* kcount, const float* nodes,
     }
 }
 
-void vfo_tsdf_weights(float* kw, const float* radii, const uint32_t* kidx, const float* kdist, const int* kcount,
+void vfo_tsdf_weights(real* kw, const real* radii, const uint32_t* kidx, const real* kdist, const int* kcount,
                       long s, int k) {
     // computeTsdfWarpWeightsKernel (src/TSDFWarp.cu:88-116): no distance cut-off; zero for empty voxels
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < s; ++i) {
-        float* w = kw + i * k;
+        real* w = kw + i * k;
         for (int j = 0; j < k; ++j) w[j] = 0.f;
         int cnt = kcount[i];
         if (!cnt) continue;
-        float sum = 0;
+        real sum = 0;
         for (int j = 0; j < cnt; ++j) {
-            float r = radii[kidx[i * k + j]], d = kdist[i * k + j];
-            w[j] = vfo_expf(-(d * d) / (2.0f * (r * r)));
+            real r = radii[kidx[i * k + j]], d = kdist[i * k + j];
+            w[j] = vexp(-(d * d) / (2.0f * (r * r)));
             sum += w[j];
         }
         if (sum != 0.f)
@@ -971,7 +1015,7 @@ void vfo_tsdf_weights(float* kw, const float* radii, const uint32_t* kidx, const
     }
 }
 
-void vfo_tsdf_vertices(float* verts, const float vs[3], const float size[3], const int dims[3]) {
+void vfo_tsdf_vertices(real* verts, const real vs[3], const real size[3], const int dims[3]) {
     // generateTsdfVerticesKernel (src/TSDFWarp.cu:131-145)
     const int X = dims[0], Y = dims[1], Z = dims[2];
 #pragma omp parallel for schedule(static)
@@ -980,34 +1024,34 @@ void vfo_tsdf_vertices(float* verts, const float vs[3], const float size[3], con
             for (int x = 0; x < X; ++x) voxel_to_world(x, y, z, vs, size, verts + 3 * ((long)z * X * Y + (long)y * X + x));
 }
 
-void vfo_warp_tsdf(float* verts, const float* T, const uint32_t* kidx, const float* kw, const int* kcount, long s,
+void vfo_warp_tsdf(real* verts, const real* T, const uint32_t* kidx, const real* kw, const int* kcount, long s,
                    int k) {
     // warpTsdfKernel (src/TSDFWarp.cu:158-190)
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < s; ++i) {
         int cnt = kcount[i];
         if (!cnt) continue;
-        const float* w = kw + i * k;
+        const real* w = kw + i * k;
         bool zero = true;
         for (int j = 0; j < k; ++j)
             if (!(std::fabs(w[j]) <= 1e-5f)) zero = false;
         if (zero) continue;
-        float p[3];
-        std::memcpy(p, verts + 3 * i, 12);
-        float acc[3] = {0.f, 0.f, 0.f};
+        real p[3];
+        std::memcpy(p, verts + 3 * i, 3 * sizeof(real));
+        real acc[3] = {0.f, 0.f, 0.f};
         for (int j = 0; j < cnt; ++j) {
-            float q[3];
+            real q[3];
             mat4_point(T + 16 * (size_t)kidx[i * k + j], p, q);
             for (int c = 0; c < 3; ++c) acc[c] = acc[c] + w[j] * q[c];
         }
-        std::memcpy(verts + 3 * i, acc, 12);
+        std::memcpy(verts + 3 * i, acc, 3 * sizeof(real));
     }
 }
 
-static bool warped_target(const float* wp, const float* vs, const float* size, const int* dims, const float* Rinv,
-                          const float* t, long* target) {
-    float d[3] = {wp[0] - t[0], wp[1] - t[1], wp[2] - t[2]};
-    float o[3];
+static bool warped_target(const real* wp, const real* vs, const real* size, const int* dims, const real* Rinv,
+                          const real* t, long* target) {
+    real d[3] = {wp[0] - t[0], wp[1] - t[1], wp[2] - t[2]};
+    real o[3];
     mat3_vec3(Rinv, d, o);
     int v[3];
     world_to_voxel(o, vs, size, v);
@@ -1016,8 +1060,8 @@ static bool warped_target(const float* wp, const float* vs, const float* size, c
     return true;
 }
 
-void vfo_count_collisions(int* counts, const float* verts, const int* kcount, const float vs[3], const float size[3],
-                          const int dims[3], const float Rinv[9], const float t[3]) {
+void vfo_count_collisions(int* counts, const real* verts, const int* kcount, const real vs[3], const real size[3],
+                          const int dims[3], const real Rinv[9], const real t[3]) {
     // countCollisionsPerVoxelKernel (src/TSDFIntegration.cu:252-283)
     const long S = (long)dims[0] * dims[1] * dims[2];
 #pragma omp parallel for schedule(static)
@@ -1030,10 +1074,10 @@ void vfo_count_collisions(int* counts, const float* verts, const int* kcount, co
     }
 }
 
-void vfo_integrate_warped(float* tsdf, float* weights, const float* verts, const int* collisions, const int* kcount,
-                          const float* depth, int width, int height, float delta, const float vs[3],
-                          const float size[3], const int dims[3], const float Rinv[9], const float t[3],
-                          const float K[9]) {
+void vfo_integrate_warped(real* tsdf, real* weights, const real* verts, const int* collisions, const int* kcount,
+                          const real* depth, int width, int height, real delta, const real vs[3],
+                          const real size[3], const int dims[3], const real Rinv[9], const real t[3],
+                          const real K[9], int half) {
     // integrateWarpedTSDFFromFrameKernel (src/TSDFIntegration.cu:173-226)
     const long S = (long)dims[0] * dims[1] * dims[2];
 #pragma omp parallel for schedule(static)
@@ -1042,7 +1086,7 @@ void vfo_integrate_warped(float* tsdf, float* weights, const float* verts, const
         long tg;
         if (!warped_target(verts + 3 * i, vs, size, dims, Rinv, t, &tg)) continue;
         if (collisions[tg] > 1) continue;
-        update_tsdf(tsdf, weights, verts + 3 * i, i, depth, width, height, delta, K);
+        update_tsdf(tsdf, weights, verts + 3 * i, i, depth, width, height, delta, K, half);
     }
 }
 
@@ -1053,14 +1097,15 @@ void vfo_integrate_warped(float* tsdf, float* weights, const float* verts, const
 struct vfo_fusion {
     vfo_params p;
     long S = 0, P = 0;
-    float vs[3] = {0, 0, 0};
+    real vs[3] = {0, 0, 0};
+    real K[9], vsize[3];  // f->K and f->vsize in the arithmetic type
     int frame = 0;
-    std::vector<float> tsdf, weights;
-    std::vector<float> depth, verts, normals;
-    float c0[3] = {0, 0, 0};
+    std::vector<real> tsdf, weights;
+    std::vector<real> depth, verts, normals;
+    real c0[3] = {0, 0, 0};
     int n = 0;
-    std::vector<float> nodes_host, nodes_dev, radii, T;
-    std::vector<float> mesh, mesh_out;
+    std::vector<real> nodes_host, nodes_dev, radii, T;
+    std::vector<real> mesh, mesh_out;
     long m = 0, mesh_out_n = 0, ncorr = 0;
     int gn_done = 0;
     double energy = 0;
@@ -1073,7 +1118,9 @@ vfo_fusion* vfo_fusion_create(const vfo_params* p) {
     f->p = *p;
     f->S = (long)p->dims[0] * p->dims[1] * p->dims[2];
     f->P = (long)p->width * p->height;
-    for (int c = 0; c < 3; ++c) f->vs[c] = p->volume_size[c] / (float)p->dims[c];
+    for (int c = 0; c < 3; ++c) f->vs[c] = (real)p->volume_size[c] / (real)p->dims[c];
+    for (int c = 0; c < 9; ++c) f->K[c] = (real)p->K[c];
+    for (int c = 0; c < 3; ++c) f->vsize[c] = (real)p->volume_size[c];
     f->tsdf.assign(f->S, -1.f);
     f->weights.assign(f->S, 0.f);
     f->depth.resize(f->P);
@@ -1091,21 +1138,21 @@ void vfo_fusion_destroy(vfo_fusion* f) { delete f; }
 int vfo_fusion_process(vfo_fusion* f, const uint16_t* depth_mm) {
     // af::runVolumeFusion per-frame loop (src/VolumeFusion.cu:327-769)
     const vfo_params& p = f->p;
-    static const float I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    float cen[3];
-    vfo_frame_prep(depth_mm, p.width, p.height, p.K, p.depth_threshold, p.bilateral, p.bilateral_r, p.sigma_i,
+    static const real I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    real cen[3];
+    vfo_frame_prep(depth_mm, p.width, p.height, f->K, p.depth_threshold, p.bilateral, p.bilateral_r, p.sigma_i,
                    p.sigma_s, p.bilateral_thr, p.angle_lo, p.angle_hi, f->depth.data(), f->verts.data(),
                    f->normals.data(), cen);
     if (f->frame == 0) {
-        std::memcpy(f->c0, cen, 12);
+        std::memcpy(f->c0, cen, 3 * sizeof(real));
         vfo_integrate_rigid(f->tsdf.data(), f->weights.data(), f->depth.data(), p.width, p.height, p.delta, p.dims,
-                            f->vs, p.volume_size, I3, f->c0, p.K);
+                            f->vs, f->vsize, I3, f->c0, f->K, p.precision);
         f->frame++;
         return 0;
     }
     // canonical point cloud: MC point cloud, sort + unique, translate by the frame-0 centroid (:372-389)
     f->mesh.resize(3 * (size_t)p.mesh_cap);
-    long raw = vfo_mc_pointcloud(f->tsdf.data(), f->weights.data(), p.dims, f->vs, p.volume_size, 0.f,
+    long raw = vfo_mc_pointcloud(f->tsdf.data(), f->weights.data(), p.dims, f->vs, f->vsize, 0.f,
                                  f->mesh.data(), p.mesh_cap);
     if (raw > p.mesh_cap) return -2;
     f->m = vfo_sort_unique_vec3(f->mesh.data(), raw);
@@ -1120,29 +1167,29 @@ int vfo_fusion_process(vfo_fusion* f, const uint16_t* depth_mm) {
         f->n = nn;
     }
     const int n = f->n;
-    std::memcpy(f->nodes_dev.data() + 3 * n_old, f->nodes_host.data() + 3 * n_old, 12 * (size_t)(n - n_old));
+    std::memcpy(f->nodes_dev.data() + 3 * n_old, f->nodes_host.data() + 3 * n_old, 3 * sizeof(real) * (size_t)(n - n_old));
     // KNN (:410-419)
     std::vector<uint32_t> midx((size_t)m * p.knn), gidx((size_t)n * p.kreg);
-    std::vector<float> mdist((size_t)m * p.knn), gdist((size_t)n * p.kreg), mw((size_t)m * p.knn);
+    std::vector<real> mdist((size_t)m * p.knn), gdist((size_t)n * p.kreg), mw((size_t)m * p.knn);
     vfo_knn(f->nodes_host.data(), n, f->mesh.data(), m, p.knn, 0, midx.data(), mdist.data());
     vfo_knn(f->nodes_host.data(), n, f->nodes_host.data(), n, p.kreg, 1, gidx.data(), gdist.data());
     vfo_filter_disconnected(gidx.data(), gdist.data(), n, p.kreg, f->radii.data());
     vfo_warp_weights(mw.data(), f->radii.data(), midx.data(), mdist.data(), m, p.knn, n);
-    std::vector<float> warped(3 * (size_t)m);
+    std::vector<real> warped(3 * (size_t)m);
     vfo_warp(warped.data(), f->mesh.data(), m, f->T.data(), midx.data(), mw.data(), p.knn);
     // ICP / Gauss-Newton (:434-691)
-    std::vector<float> pending(f->T.size());
+    std::vector<real> pending(f->T.size());
     f->gn_done = 0;
     for (int icp = 0; icp < p.icp_iterations; ++icp) {
         vfo_warp(warped.data(), f->mesh.data(), m, f->T.data(), midx.data(), mw.data(), p.knn);
         std::vector<int> corr(2 * (size_t)m);
-        long c = vfo_correspondences(corr.data(), m, warped.data(), m, p.K, f->depth.data(), p.height, p.width,
+        long c = vfo_correspondences(corr.data(), m, warped.data(), m, f->K, f->depth.data(), p.height, p.width,
                                      f->verts.data(), p.corr_thresh);
         f->ncorr = c;
         const long jreg = (long)n * p.kreg * 3;
-        std::vector<float> rd(c), rr(jreg);
+        std::vector<real> rd(c), rr(jreg);
         std::vector<double> A((size_t)36 * n * n);
-        std::vector<float> b(6 * (size_t)n), xf(6 * (size_t)n);
+        std::vector<real> b(6 * (size_t)n), xf(6 * (size_t)n);
         std::vector<double> x(6 * (size_t)n);
         std::copy(f->T.begin(), f->T.begin() + 16 * (size_t)n, pending.begin());
         double E = (double)kFltMax;
@@ -1163,7 +1210,7 @@ int vfo_fusion_process(vfo_fusion* f, const uint16_t* depth_mm) {
             if (p.solver == 0) st = vfo_solve_dense(A.data(), b.data(), 6 * n, x.data());
             else st = vfo_pcg(A.data(), b.data(), n, p.pcg_iterations, p.pcg_tol, x.data(), nullptr);
             if (st) return -4;
-            for (int i = 0; i < 6 * n; ++i) xf[i] = (float)x[i];
+            for (int i = 0; i < 6 * n; ++i) xf[i] = (real)x[i];
             vfo_update_transforms(pending.data(), xf.data(), n);
             vfo_warp(warped.data(), f->mesh.data(), m, pending.data(), midx.data(), mw.data(), p.knn);
             f->gn_done = gn + 1;
@@ -1172,23 +1219,23 @@ int vfo_fusion_process(vfo_fusion* f, const uint16_t* depth_mm) {
     // voxel KNN, warp and warped integration (:702-741)
     int per[3];
     for (int c = 0; c < 3; ++c) per[c] = 2 * (vfo_f2i_rz(p.graph_radius / f->vs[c]) + 1) + 1;
-    const float negc[3] = {-f->c0[0], -f->c0[1], -f->c0[2]};
+    const real negc[3] = {-f->c0[0], -f->c0[1], -f->c0[2]};
     vfo_translate(f->nodes_dev.data(), n, negc);
     const long S = f->S;
     std::vector<uint32_t> kidx((size_t)S * p.knn);
-    std::vector<float> kdist((size_t)S * p.knn), kw((size_t)S * p.knn), tv(3 * (size_t)S);
+    std::vector<real> kdist((size_t)S * p.knn), kw((size_t)S * p.knn), tv(3 * (size_t)S);
     std::vector<int> kcount(S), coll(S, 0);
     vfo_tsdf_knn(kidx.data(), kdist.data(), kcount.data(), f->nodes_dev.data(), f->radii.data(), n, f->vs,
-                 p.volume_size, p.dims, per, p.knn);
+                 f->vsize, p.dims, per, p.knn);
     vfo_tsdf_weights(kw.data(), f->radii.data(), kidx.data(), kdist.data(), kcount.data(), S, p.knn);
-    vfo_tsdf_vertices(tv.data(), f->vs, p.volume_size, p.dims);
+    vfo_tsdf_vertices(tv.data(), f->vs, f->vsize, p.dims);
     vfo_translate(f->nodes_dev.data(), n, f->c0);
     vfo_translate(tv.data(), S, f->c0);
     vfo_warp_tsdf(tv.data(), f->T.data(), kidx.data(), kw.data(), kcount.data(), S, p.knn);
-    vfo_count_collisions(coll.data(), tv.data(), kcount.data(), f->vs, p.volume_size, p.dims, I3, f->c0);
+    vfo_count_collisions(coll.data(), tv.data(), kcount.data(), f->vs, f->vsize, p.dims, I3, f->c0);
     if (p.integrate)
         vfo_integrate_warped(f->tsdf.data(), f->weights.data(), tv.data(), coll.data(), kcount.data(), f->depth.data(),
-                             p.width, p.height, p.delta, f->vs, p.volume_size, p.dims, I3, f->c0, p.K);
+                             p.width, p.height, p.delta, f->vs, f->vsize, p.dims, I3, f->c0, f->K, p.precision);
     f->frame++;
     return 0;
 }
@@ -1198,19 +1245,19 @@ long vfo_fusion_mesh_size(const vfo_fusion* f) { return f->m; }
 long vfo_fusion_num_corr(const vfo_fusion* f) { return f->ncorr; }
 int vfo_fusion_gn_done(const vfo_fusion* f) { return f->gn_done; }
 double vfo_fusion_energy(const vfo_fusion* f) { return f->energy; }
-const float* vfo_fusion_tsdf(const vfo_fusion* f) { return f->tsdf.data(); }
-const float* vfo_fusion_weights(const vfo_fusion* f) { return f->weights.data(); }
-const float* vfo_fusion_nodes(const vfo_fusion* f) { return f->nodes_host.data(); }
-const float* vfo_fusion_transforms(const vfo_fusion* f) { return f->T.data(); }
-const float* vfo_fusion_centroid(const vfo_fusion* f) { return f->c0; }
-const float* vfo_fusion_mesh(const vfo_fusion* f) { return f->mesh.data(); }
-void vfo_fusion_set_transforms(vfo_fusion* f, const float* T, int n) {
-    std::memcpy(f->T.data(), T, 64 * (size_t)std::min(n, f->n));
+const real* vfo_fusion_tsdf(const vfo_fusion* f) { return f->tsdf.data(); }
+const real* vfo_fusion_weights(const vfo_fusion* f) { return f->weights.data(); }
+const real* vfo_fusion_nodes(const vfo_fusion* f) { return f->nodes_host.data(); }
+const real* vfo_fusion_transforms(const vfo_fusion* f) { return f->T.data(); }
+const real* vfo_fusion_centroid(const vfo_fusion* f) { return f->c0; }
+const real* vfo_fusion_mesh(const vfo_fusion* f) { return f->mesh.data(); }
+void vfo_fusion_set_transforms(vfo_fusion* f, const real* T, int n) {
+    std::memcpy(f->T.data(), T, 16 * sizeof(real) * (size_t)std::min(n, f->n));
 }
 
-void vfo_fusion_set_tsdf(vfo_fusion* f, const float* tsdf, const float* weights) {
-    std::memcpy(f->tsdf.data(), tsdf, sizeof(float) * f->S);
-    std::memcpy(f->weights.data(), weights, sizeof(float) * f->S);
+void vfo_fusion_set_tsdf(vfo_fusion* f, const real* tsdf, const real* weights) {
+    std::memcpy(f->tsdf.data(), tsdf, sizeof(real) * f->S);
+    std::memcpy(f->weights.data(), weights, sizeof(real) * f->S);
 }
 
 }  // extern "C"

@@ -27,74 +27,84 @@ extern "C" {
 
 #define VFO_INVALID_IDX 0xFFFFFFFFu
 
+/* VFO_REAL is float in liboracle.so (the binary32 restatement) and double in liboracle64.so (the
+ * same algorithm evaluated in binary64: the FP64 oracle the precision form's error is stated
+ * against).  vfo_params and vfo_expf / vfo_round_half stay binary32 in both. */
+#ifndef VFO_REAL
+#define VFO_REAL float
+#endif
+
 float vfo_expf(float x);
-int vfo_f2i_rz(float x);
+int vfo_f2i_rz(VFO_REAL x);
 
 /* ---- frame preparation (src/VertexManipulation.cu, src/BilateralFilter.cu) ---- */
-void vfo_depth_from_mm(const uint16_t* mm, long n, float* out);
-void vfo_filter_depth(float* depth, long n, float threshold);
-void vfo_bilateral(float* out, const float* in, int height, int width, int r, double sigma_i, double sigma_s, float thr);
-void vfo_depth_to_mesh(float* mesh, const float* depth, int width, int height, const float K[9]);
-void vfo_normals(float* normals, const float* vertices, int height, int width, float angle_lo, float angle_hi);
-void vfo_remove_without_normals(const float* normals, float* vertices, float* depth, int height, int width);
-void vfo_centroid(const float* vertices, long n, float out[3]);
-void vfo_frame_prep(const uint16_t* mm, int width, int height, const float K[9], float depth_threshold, int bilateral,
-                    int r, double sigma_i, double sigma_s, float thr, float angle_lo, float angle_hi,
-                    float* depth, float* vertices, float* normals, float centroid[3]);
+void vfo_depth_from_mm(const uint16_t* mm, long n, VFO_REAL* out);
+void vfo_filter_depth(VFO_REAL* depth, long n, VFO_REAL threshold);
+void vfo_bilateral(VFO_REAL* out, const VFO_REAL* in, int height, int width, int r, double sigma_i, double sigma_s, VFO_REAL thr);
+void vfo_depth_to_mesh(VFO_REAL* mesh, const VFO_REAL* depth, int width, int height, const VFO_REAL K[9]);
+void vfo_normals(VFO_REAL* normals, const VFO_REAL* vertices, int height, int width, VFO_REAL angle_lo, VFO_REAL angle_hi);
+void vfo_remove_without_normals(const VFO_REAL* normals, VFO_REAL* vertices, VFO_REAL* depth, int height, int width);
+void vfo_centroid(const VFO_REAL* vertices, long n, VFO_REAL out[3]);
+void vfo_frame_prep(const uint16_t* mm, int width, int height, const VFO_REAL K[9], VFO_REAL depth_threshold, int bilateral,
+                    int r, double sigma_i, double sigma_s, VFO_REAL thr, VFO_REAL angle_lo, VFO_REAL angle_hi,
+                    VFO_REAL* depth, VFO_REAL* vertices, VFO_REAL* normals, VFO_REAL centroid[3]);
 
-/* ---- TSDF integration (src/TSDFIntegration.cu) ---- */
-void vfo_integrate_rigid(float* tsdf, float* weights, const float* depth, int width, int height, float delta,
-                         const int dims[3], const float voxel_size[3], const float volume_size[3], const float R[9],
-                         const float t[3], const float K[9]);
+/* ---- TSDF integration (src/TSDFIntegration.cu) ----
+ * half != 0: the precision form's storage -- each updated value is rounded to the nearest binary16
+ * (ties to even) as it is stored; values read are then always binary16 values. */
+float vfo_round_half(float x);
+void vfo_integrate_rigid(VFO_REAL* tsdf, VFO_REAL* weights, const VFO_REAL* depth, int width, int height, VFO_REAL delta,
+                         const int dims[3], const VFO_REAL voxel_size[3], const VFO_REAL volume_size[3], const VFO_REAL R[9],
+                         const VFO_REAL t[3], const VFO_REAL K[9], int half);
 
 /* ---- marching cubes (src/MarchingCubes.cu / .cpp) ---- */
-long vfo_mc_pointcloud(const float* tsdf, const float* weights, const int dims[3], const float voxel_size[3],
-                       const float volume_size[3], float iso, float* out, long cap);
-long vfo_sort_unique_vec3(float* pts, long n);
-long vfo_mc_full(const float* tsdf, const float* weights, const int dims[3], const float voxel_size[3],
-                 const float volume_size[3], float iso, float* verts, long vcap, int* faces, long fcap, long* nfaces);
-void vfo_translate(float* pts, long n, const float t[3]);
+long vfo_mc_pointcloud(const VFO_REAL* tsdf, const VFO_REAL* weights, const int dims[3], const VFO_REAL voxel_size[3],
+                       const VFO_REAL volume_size[3], VFO_REAL iso, VFO_REAL* out, long cap);
+long vfo_sort_unique_vec3(VFO_REAL* pts, long n);
+long vfo_mc_full(const VFO_REAL* tsdf, const VFO_REAL* weights, const int dims[3], const VFO_REAL voxel_size[3],
+                 const VFO_REAL volume_size[3], VFO_REAL iso, VFO_REAL* verts, long vcap, int* faces, long fcap, long* nfaces);
+void vfo_translate(VFO_REAL* pts, long n, const VFO_REAL t[3]);
 
 /* ---- motion graph (src/GraphBuilder.cpp, src/MotionGraph.cpp, include/af/GraphBuilder.h) ---- */
-int vfo_build_graph(float* nodes, float* radii, float* transforms, int n_nodes, int cap, const float* mesh, long m,
-                    int knn, float radius);
-void vfo_knn(const float* nodes, int n_nodes, const float* pts, long m, int k, int exclude_closest, uint32_t* idx,
-             float* dist);
-void vfo_filter_disconnected(uint32_t* idx, float* dist, int n_nodes, int k, const float* radii);
-void vfo_warp_weights(float* w, const float* radii, const uint32_t* idx, const float* dist, long m, int k, int n_nodes);
-void vfo_warp(float* out, const float* pts, long m, const float* transforms, const uint32_t* idx, const float* w, int k);
+int vfo_build_graph(VFO_REAL* nodes, VFO_REAL* radii, VFO_REAL* transforms, int n_nodes, int cap, const VFO_REAL* mesh, long m,
+                    int knn, VFO_REAL radius);
+void vfo_knn(const VFO_REAL* nodes, int n_nodes, const VFO_REAL* pts, long m, int k, int exclude_closest, uint32_t* idx,
+             VFO_REAL* dist);
+void vfo_filter_disconnected(uint32_t* idx, VFO_REAL* dist, int n_nodes, int k, const VFO_REAL* radii);
+void vfo_warp_weights(VFO_REAL* w, const VFO_REAL* radii, const uint32_t* idx, const VFO_REAL* dist, long m, int k, int n_nodes);
+void vfo_warp(VFO_REAL* out, const VFO_REAL* pts, long m, const VFO_REAL* transforms, const uint32_t* idx, const VFO_REAL* w, int k);
 
 /* ---- projective correspondences (src/ComputeCorrespondence.cu) ---- */
-long vfo_correspondences(int* corr, long cap, const float* warped, long m, const float K[9], const float* depth,
-                         int rows, int cols, const float* frame_mesh, float thr);
+long vfo_correspondences(int* corr, long cap, const VFO_REAL* warped, long m, const VFO_REAL K[9], const VFO_REAL* depth,
+                         int rows, int cols, const VFO_REAL* frame_mesh, VFO_REAL thr);
 
 /* ---- Gauss-Newton (src/MotionOptimization.cu, src/VolumeFusion.cu:454-691) ---- */
-void vfo_residual_depth(float* r, const int* corr, long c, const float* warped, const float* frame_mesh,
-                        const float* normals, float lambda);
-void vfo_residual_reg(float* r, const float* nodes, const float* transforms, int n, const uint32_t* gidx, int kreg,
-                      float lambda);
-double vfo_energy(const float* r, long n);
-int vfo_assemble(double* jtj_dense, float* jtj_blocks, float* jtr, const int* corr, long c, const float* canon,
-                 const uint32_t* midx, const float* mw, int k, const float* normals, float lambda_d, const float* nodes,
-                 int n, const uint32_t* gidx, int kreg, float lambda_r, const float* r_depth, const float* r_reg);
-int vfo_solve_dense(const double* A, const float* b, int dim, double* x);
-int vfo_pcg(const double* A, const float* b, int n_nodes, int iters, double tol, double* x, int* iters_done);
-void vfo_update_transforms(float* transforms, const float* update, int n);
+void vfo_residual_depth(VFO_REAL* r, const int* corr, long c, const VFO_REAL* warped, const VFO_REAL* frame_mesh,
+                        const VFO_REAL* normals, VFO_REAL lambda);
+void vfo_residual_reg(VFO_REAL* r, const VFO_REAL* nodes, const VFO_REAL* transforms, int n, const uint32_t* gidx, int kreg,
+                      VFO_REAL lambda);
+double vfo_energy(const VFO_REAL* r, long n);
+int vfo_assemble(double* jtj_dense, VFO_REAL* jtj_blocks, VFO_REAL* jtr, const int* corr, long c, const VFO_REAL* canon,
+                 const uint32_t* midx, const VFO_REAL* mw, int k, const VFO_REAL* normals, VFO_REAL lambda_d, const VFO_REAL* nodes,
+                 int n, const uint32_t* gidx, int kreg, VFO_REAL lambda_r, const VFO_REAL* r_depth, const VFO_REAL* r_reg);
+int vfo_solve_dense(const double* A, const VFO_REAL* b, int dim, double* x);
+int vfo_pcg(const double* A, const VFO_REAL* b, int n_nodes, int iters, double tol, double* x, int* iters_done);
+void vfo_update_transforms(VFO_REAL* transforms, const VFO_REAL* update, int n);
 
 /* ---- voxel warp + warped integration (src/TSDFWarp.cu, src/TSDFIntegration.cu) ---- */
-void vfo_tsdf_knn(uint32_t* kidx, float* kdist, int* kcount, const float* nodes, const float* radii, int n,
-                  const float voxel_size[3], const float volume_size[3], const int dims[3], const int per_node[3], int k);
-void vfo_tsdf_weights(float* kw, const float* radii, const uint32_t* kidx, const float* kdist, const int* kcount,
+void vfo_tsdf_knn(uint32_t* kidx, VFO_REAL* kdist, int* kcount, const VFO_REAL* nodes, const VFO_REAL* radii, int n,
+                  const VFO_REAL voxel_size[3], const VFO_REAL volume_size[3], const int dims[3], const int per_node[3], int k);
+void vfo_tsdf_weights(VFO_REAL* kw, const VFO_REAL* radii, const uint32_t* kidx, const VFO_REAL* kdist, const int* kcount,
                       long s, int k);
-void vfo_tsdf_vertices(float* verts, const float voxel_size[3], const float volume_size[3], const int dims[3]);
-void vfo_warp_tsdf(float* verts, const float* transforms, const uint32_t* kidx, const float* kw, const int* kcount,
+void vfo_tsdf_vertices(VFO_REAL* verts, const VFO_REAL voxel_size[3], const VFO_REAL volume_size[3], const int dims[3]);
+void vfo_warp_tsdf(VFO_REAL* verts, const VFO_REAL* transforms, const uint32_t* kidx, const VFO_REAL* kw, const int* kcount,
                    long s, int k);
-void vfo_count_collisions(int* counts, const float* verts, const int* kcount, const float voxel_size[3],
-                          const float volume_size[3], const int dims[3], const float Rinv[9], const float t[3]);
-void vfo_integrate_warped(float* tsdf, float* weights, const float* verts, const int* collisions, const int* kcount,
-                          const float* depth, int width, int height, float delta, const float voxel_size[3],
-                          const float volume_size[3], const int dims[3], const float Rinv[9], const float t[3],
-                          const float K[9]);
+void vfo_count_collisions(int* counts, const VFO_REAL* verts, const int* kcount, const VFO_REAL voxel_size[3],
+                          const VFO_REAL volume_size[3], const int dims[3], const VFO_REAL Rinv[9], const VFO_REAL t[3]);
+void vfo_integrate_warped(VFO_REAL* tsdf, VFO_REAL* weights, const VFO_REAL* verts, const int* collisions, const int* kcount,
+                          const VFO_REAL* depth, int width, int height, VFO_REAL delta, const VFO_REAL voxel_size[3],
+                          const VFO_REAL volume_size[3], const int dims[3], const VFO_REAL Rinv[9], const VFO_REAL t[3],
+                          const VFO_REAL K[9], int half);
 
 /* ---- whole-frame driver mirroring af::runVolumeFusion's per-frame loop (src/VolumeFusion.cu:343-769) ---- */
 typedef struct vfo_params {
@@ -118,6 +128,7 @@ typedef struct vfo_params {
     int integrate;
     int node_cap;
     long mesh_cap;
+    int precision;    /* 0 = FP32 volume, 1 = FP16 values + integer weights (the precision form) */
 } vfo_params;
 
 typedef struct vfo_fusion vfo_fusion;
@@ -129,16 +140,16 @@ long vfo_fusion_mesh_size(const vfo_fusion* f);
 long vfo_fusion_num_corr(const vfo_fusion* f);
 int vfo_fusion_gn_done(const vfo_fusion* f);
 double vfo_fusion_energy(const vfo_fusion* f);
-const float* vfo_fusion_tsdf(const vfo_fusion* f);
-const float* vfo_fusion_weights(const vfo_fusion* f);
-const float* vfo_fusion_nodes(const vfo_fusion* f);
-const float* vfo_fusion_transforms(const vfo_fusion* f);
-const float* vfo_fusion_centroid(const vfo_fusion* f);
-const float* vfo_fusion_mesh(const vfo_fusion* f);
+const VFO_REAL* vfo_fusion_tsdf(const vfo_fusion* f);
+const VFO_REAL* vfo_fusion_weights(const vfo_fusion* f);
+const VFO_REAL* vfo_fusion_nodes(const vfo_fusion* f);
+const VFO_REAL* vfo_fusion_transforms(const vfo_fusion* f);
+const VFO_REAL* vfo_fusion_centroid(const vfo_fusion* f);
+const VFO_REAL* vfo_fusion_mesh(const vfo_fusion* f);
 /* Replace the committed node transforms (used to feed a GPU solution back for stage-wise parity). */
-void vfo_fusion_set_transforms(vfo_fusion* f, const float* transforms, int n);
+void vfo_fusion_set_transforms(vfo_fusion* f, const VFO_REAL* transforms, int n);
 /* Replace the volume (stage-wise parity: continue from the GPU's volume). */
-void vfo_fusion_set_tsdf(vfo_fusion* f, const float* tsdf, const float* weights);
+void vfo_fusion_set_tsdf(vfo_fusion* f, const VFO_REAL* tsdf, const VFO_REAL* weights);
 
 #ifdef __cplusplus
 }

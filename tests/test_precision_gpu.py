@@ -1,0 +1,184 @@
+"""Precision form: FP16 TSDF values with uint16 weights (4 B/voxel instead of 8), FP32 Jacobian and
+J^T J, FP64 PCG dot products and 6x6 block inverses.
+
+* parity: the GPU matches the oracle's FP16-storage emulation (every stored value rounded to the
+  nearest binary16, ties to even) exactly on the first frame and, frame by frame from a common
+  state, in the point cloud, graph and correspondences;
+* error statement: each frame is re-run from the session's own state by the FP64 oracle (the same
+  restatement compiled in binary64) and the TSDF values, warp parameters and mesh vertices are
+  compared, for the FP16 and the FP32 form side by side;
+* the 512^3 / 2 mm workload runs clean and stays within the FP16 bound of the FP32 form."""
+import json
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from oracle import pyoracle as O  # noqa: E402
+
+
+def _fp16(cfg):
+    return dict(cfg, precision="fp16")
+
+
+def _session(cfg):
+    from volumefusion_gb300.fusion import FusionSession
+    return FusionSession(cfg, extract_mesh=True)
+
+
+def test_precision_form_halves_voxel_bytes():
+    from volumefusion_gb300 import configs
+    from volumefusion_gb300.serve import session_bytes
+    cfg = configs.nonrigid_capsules_256()
+    S = int(np.prod(cfg["dims"]))
+    b32, b16 = session_bytes(cfg), session_bytes(_fp16(cfg))
+    assert b32 - b16 >= 4 * S - 4096  # two arrays of S values, 2 B saved each
+
+
+@pytest.mark.gpu
+def test_precision_first_frame_bit_exact():
+    from volumefusion_gb300 import configs
+    cfg = _fp16(configs.small_nonrigid(n_frames=2))
+    frames = configs.small_frames(cfg)
+    s = _session(cfg)
+    o = O.Fusion(cfg)
+    s.process(frames[0])
+    o.process(frames[0])
+    t16, w16, fmt = s.volume_raw()
+    assert fmt == "fp16" and t16.dtype == torch.float16
+    t, w = s.tsdf()
+    assert np.array_equal(w.cpu().numpy(), o.weights())
+    assert np.array_equal(t.cpu().numpy(), o.tsdf())
+    # values really are stored as binary16: widening is exact, so a round trip changes nothing
+    assert np.array_equal(O.round_half(o.tsdf()[:4096]), o.tsdf()[:4096])
+    s.close()
+
+
+@pytest.mark.gpu
+def test_precision_form_tracks_fp16_oracle():
+    from volumefusion_gb300 import configs
+    cfg = _fp16(configs.small_nonrigid(n_frames=6))
+    frames = configs.small_frames(cfg)
+    s = _session(cfg)
+    o = O.Fusion(cfg)
+    for i, mm in enumerate(frames):
+        s.process(mm)
+        o.process(mm)
+        st = s.stats()
+        assert st["error"] == 0, st
+        t, w = s.tsdf()
+        t, w = t.cpu().numpy(), w.cpu().numpy()
+        if i == 0:
+            assert np.array_equal(t, o.tsdf()) and np.array_equal(w, o.weights())
+        else:
+            assert st["n_nodes"] == o.num_nodes and st["mesh_points"] == o.mesh_size, (i, st)
+            assert np.array_equal(s.point_cloud().cpu().numpy(), o.mesh())
+            nodes, _, T = s.graph()
+            assert np.array_equal(nodes.cpu().numpy(), o.nodes())
+            assert st["correspondences"] == o.num_corr
+            dT = np.abs(T.cpu().numpy() - o.transforms()).max()
+            assert dT < 1e-4, (i, dT)
+            ot, ow = o.tsdf(), o.weights()
+            bad = (t != ot) | (w != ow)  # storage rounding is exact; only a moved projection differs
+            assert bad.mean() < 1e-3, (i, int(bad.sum()))
+            o.set_transforms(T.cpu().numpy())
+        o.set_tsdf(t, w)
+    s.close()
+
+
+def _error_vs_fp64(cfg, frames):
+    """Per frame: the FP64 oracle re-runs the frame from the session's state at the end of the
+    previous frame; returns the TSDF, warp-parameter and mesh-vertex errors of the session."""
+    sp = pytest.importorskip("scipy.spatial")
+    from volumefusion_gb300 import configs
+    vs = configs.voxel_size(cfg).astype(np.float64)
+    size = np.array(cfg["volume_size"], np.float64)
+    s = _session(cfg)
+    ref = O.Fusion(cfg, fp64=True)
+    rows = []
+    for i, mm in enumerate(frames):
+        s.process(mm)
+        ref.process(mm)
+        assert s.stats()["error"] == 0
+        t, w = (x.cpu().numpy() for x in s.tsdf())
+        t64, w64 = ref.tsdf(), ref.weights()
+        same = (w == w64) & (w > 0)
+        e = np.abs(t[same].astype(np.float64) - t64[same])
+        row = {"frame": i, "tsdf_p50": float(np.median(e)), "tsdf_p99": float(np.percentile(e, 99)),
+               "tsdf_max": float(e.max()), "voxels_compared": int(same.sum()),
+               "voxels_update_differs": int((w != w64).sum())}
+        if i > 0:
+            _, _, T = s.graph()
+            T = T.cpu().numpy()
+            assert len(T) == ref.num_nodes
+            row["warp_max"] = float(np.abs(T.astype(np.float64) - ref.transforms()).max())
+            a = O.mc_pointcloud64(t, w, cfg["dims"], vs, size)
+            b = O.mc_pointcloud64(t64, w64, cfg["dims"], vs, size)
+            d, _ = sp.cKDTree(b).query(a)
+            d = d / vs[0]
+            row.update(mesh_p50_vox=float(np.median(d)), mesh_p99_vox=float(np.percentile(d, 99)),
+                       mesh_max_vox=float(d.max()))
+            ref.set_transforms(T)
+        ref.set_tsdf(t, w)
+        rows.append(row)
+    s.close()
+    return rows
+
+
+@pytest.mark.gpu
+def test_precision_form_error_against_fp64_oracle():
+    """Errors of one frame of arithmetic, FP16 storage vs FP32 storage, against binary64.  Most of
+    both comes from decisions binary64 takes differently (a projection landing on the other pixel,
+    a bilateral weight bucket, PCG in a different precision); the FP16 form stays within the FP32
+    form's own error plus the binary16 rounding of the stored values (<= 2^-11 per update)."""
+    from volumefusion_gb300 import configs
+    cfg = configs.small_nonrigid(n_frames=6)
+    frames = configs.small_frames(cfg)
+    r32 = _error_vs_fp64(cfg, frames)
+    r16 = _error_vs_fp64(_fp16(cfg), frames)
+    print("\nFP64_ERROR_REPORT " + json.dumps({"config": "small_nonrigid 64^3 @ 8 mm, 6 frames", "fp32": r32,
+                                                "fp16": r16}))
+    for a, b in zip(r32, r16):
+        assert b["tsdf_p50"] <= 5e-4 and b["tsdf_p99"] <= a["tsdf_p99"] + 5e-4, (a, b)
+        if b["frame"] > 0:
+            assert b["warp_max"] < 2e-3, b
+            assert b["mesh_p50_vox"] < 0.01 and b["mesh_p99_vox"] < 0.1, b
+
+
+@pytest.mark.gpu
+def test_precision_512_runs_clean_and_stays_near_fp32():
+    """The 512^3 / 2 mm capsule workload in FP16 and FP32 storage.  After the rigid first frame the
+    FP16 volume is exactly the FP32 volume rounded to binary16 (ties to even).  After six frames both
+    run clean with graphs of more than 1000 nodes; their graphs differ a little (the greedy node
+    selection over a point cloud from a rounded volume takes some decisions the other way), and
+    voxels updated alike agree within the binary16 rounding accumulated over the frames."""
+    from volumefusion_gb300 import configs
+    cfg16 = configs.precision_capsules_512()
+    cfg32 = dict(cfg16, precision="fp32")
+    frames = configs.capsule_frames(cfg16, frames=range(6))
+    s16, s32 = _session(cfg16), _session(cfg32)
+    for k, mm in enumerate(frames):
+        s16.process(mm)
+        s32.process(mm)
+        st16, st32 = s16.stats(), s32.stats()
+        assert st16["error"] == 0 and st32["error"] == 0, (st16, st32)
+        if k == 0:
+            t16, w16 = s16.tsdf()
+            t32, w32 = s32.tsdf()
+            assert torch.equal(w16, w32)
+            assert torch.equal(t16, t32.half().float())
+            del t16, w16, t32, w32
+    assert st16["n_nodes"] > 1000 and st32["n_nodes"] > 1000, (st16, st32)
+    assert abs(st16["n_nodes"] - st32["n_nodes"]) <= 0.1 * st32["n_nodes"], (st16, st32)
+    t16, w16 = s16.tsdf()
+    t32, w32 = s32.tsdf()
+    same = (w16 == w32) & (w16 > 0)
+    e = (t16[same] - t32[same]).abs()
+    frac = float(same.sum()) / float((w32 > 0).sum())
+    q = torch.quantile(e[torch.randperm(e.numel(), device=e.device)[:1 << 20]], torch.tensor([0.5, 0.99], device=e.device))
+    print("\nPRECISION_512 nodes fp16 %d fp32 %d; voxels updated alike %.4f; |fp16 - fp32| p50 %.2e p99 %.2e"
+          % (st16["n_nodes"], st32["n_nodes"], frac, float(q[0]), float(q[1])))
+    assert frac > 0.8 and float(q[0]) <= 5e-4, (frac, q)
+    s16.close()
+    s32.close()

@@ -28,7 +28,8 @@ class FusionParams(C.Structure):
                 ("graph_radius", f32), ("knn", i32), ("kreg", i32), ("update_graph", i32), ("icp_iterations", i32),
                 ("gn_iterations", i32), ("lambda_depth", f32), ("lambda_reg", f32), ("energy_min_step", f32),
                 ("corr_thresh", f32), ("solver", i32), ("pcg_iterations", i32), ("pcg_tol", f64), ("integrate", i32),
-                ("extract_mesh", i32), ("node_capacity", i32), ("mesh_capacity", i64), ("triangle_capacity", i64)]
+                ("extract_mesh", i32), ("node_capacity", i32), ("mesh_capacity", i64), ("triangle_capacity", i64),
+                ("precision", i32)]
 
 
 class FrameStats(C.Structure):
@@ -101,6 +102,7 @@ SIGNATURES = {
     "afx_fusion_process_host": (i32, [vp, vp, vp]),
     "afx_fusion_stats": (i32, [vp, C.POINTER(FrameStats), vp]),
     "afx_fusion_tsdf": (i32, [vp, C.POINTER(vp), C.POINTER(vp)]),
+    "afx_fusion_volume": (i32, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(i32)]),
     "afx_fusion_graph": (i32, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
     "afx_fusion_centroid": (i32, [vp, C.POINTER(vp)]),
     "afx_fusion_point_cloud": (i32, [vp, C.POINTER(vp), C.POINTER(vp)]),

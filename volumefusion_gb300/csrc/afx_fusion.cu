@@ -55,8 +55,9 @@ struct afx_fusion {
     // device buffers
     void* arena = nullptr;
     size_t arena_bytes = 0;
-    float* tsdf;
-    float* weights;
+    int fmt = kVoxF32;     // voxel storage: kVoxF32, or kVoxF16 (precision form)
+    void* tsdf;
+    void* weights;
     unsigned* coll;
     uint16_t* depth_mm;
     float* depth;
@@ -267,7 +268,9 @@ static void session_layout(const afx_fusion_params& p, afx_fusion* f) {
     f->ws_gn_bytes = gn_workspace_size(M, (int)N, p.knn, p.kreg);
     size_t sz = 0;
     auto add = [&](size_t n) { sz += al(n); };
-    add(S * 4); add(S * 4); add(S * 4);                  // tsdf weights coll
+    f->fmt = p.precision == AFX_PRECISION_FP16 ? kVoxF16 : kVoxF32;
+    const long vb = (long)vox_bytes(f->fmt);
+    add(S * vb); add(S * vb); add(S * 4);                // tsdf weights coll
     add(Pp * 2); add(Pp * 4); add(Pp * 12); add(Pp * 12);  // frame buffers
     add(64); add(64); add(64); add(64); add(64);          // centroids acc error epoch
     add(M * 12); add(64); add(M * 12); add(64); add(64);  // point-cloud double buffer + used count
@@ -286,7 +289,7 @@ static bool params_valid(const afx_fusion_params& p) {
     return !(p.width < 3 || p.height < 3 || p.dims[0] < 3 || p.dims[1] < 3 || p.dims[2] < 3 || p.knn < 1 ||
              p.knn > 8 || p.kreg < 1 || p.kreg > 8 || p.node_capacity < 1 || p.mesh_capacity < 1 ||
              p.triangle_capacity < 1 || !(p.graph_radius > 0.f) || p.icp_iterations < 0 || p.gn_iterations < 0 ||
-             p.pcg_iterations < 0);
+             p.pcg_iterations < 0 || (p.precision != AFX_PRECISION_FP32 && p.precision != AFX_PRECISION_FP16));
 }
 
 size_t afx_fusion_memory_bytes(const afx_fusion_params* params) {
@@ -319,8 +322,8 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
         q += al(n);
         return r;
     };
-    f->tsdf = (float*)take(S * 4);
-    f->weights = (float*)take(S * 4);
+    f->tsdf = take(S * vox_bytes(f->fmt));
+    f->weights = take(S * vox_bytes(f->fmt));
     f->coll = (unsigned*)take(S * 4);
     f->depth_mm = (uint16_t*)take(Pp * 2);
     f->depth = (float*)take(Pp * 4);
@@ -411,12 +414,21 @@ __global__ void fill_kernel(float* p, long n, float v) {
     if (i < n) p[i] = v;
 }
 
+__global__ void fill_u16_kernel(unsigned short* p, long n, unsigned short v) {
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
 int afx_fusion_reset(afx_fusion* f, void* stream) {
     if (!f) return AFX_ERR_INVALID_ARGUMENT;
     cudaStream_t st = as_stream(stream);
-    fill_kernel<<<blocks_for(f->S, 256), 256, 0, st>>>(f->tsdf, f->S, -1.f);  // DeviceTsdf::initDefault
+    // DeviceTsdf::initDefault: values -1, weights 0 (0xBC00 is -1 in FP16)
+    if (f->fmt == kVoxF16)
+        fill_u16_kernel<<<blocks_for(f->S, 256), 256, 0, st>>>(static_cast<unsigned short*>(f->tsdf), f->S, 0xBC00);
+    else
+        fill_kernel<<<blocks_for(f->S, 256), 256, 0, st>>>(static_cast<float*>(f->tsdf), f->S, -1.f);
     AFX_LAUNCH_CHECK();
-    AFX_CUDA(cudaMemsetAsync(f->weights, 0, f->S * 4, st));
+    AFX_CUDA(cudaMemsetAsync(f->weights, 0, f->S * vox_bytes(f->fmt), st));
     AFX_CUDA(cudaMemsetAsync(f->coll, 0, f->S * 4, st));
     AFX_CUDA(cudaMemsetAsync(f->centroid0, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->acc, 0, 64, st));
@@ -445,7 +457,7 @@ static int extract_frame_mesh(afx_fusion* f, int cur, cudaStream_t st) {
     const int next = cur ^ 1;
     AFX_CUDA(cudaMemsetAsync(f->npoints_buf[next], 0, 4, st));
     const bool mesh = f->p.extract_mesh != 0;
-    return mc_fused_impl(f->tsdf, f->weights, f->vol, 0.f, f->points_buf[next], f->npoints_buf[next], f->p.mesh_capacity,
+    return mc_fused_impl(f->tsdf, f->weights, f->fmt, f->vol, 0.f, f->points_buf[next], f->npoints_buf[next], f->p.mesh_capacity,
                          mesh ? f->mverts : nullptr, mesh ? f->nmverts : nullptr, f->p.triangle_capacity * 3,
                          mesh ? f->mfaces : nullptr, mesh ? f->nmfaces : nullptr, f->p.triangle_capacity, st, f->error);
 }
@@ -477,7 +489,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
     if (f->frame == 0) {
         stage_mark(f, ST_INTEGRATE_RIGID, st);
         // rigid integration at the frame-0 centroid (src/VolumeFusion.cu:334-336)
-        rc = integrate_rigid_impl(f->tsdf, f->weights, f->depth, p.width, p.height, p.delta, f->vol, I3, nullptr, p.K,
+        rc = integrate_rigid_impl(f->tsdf, f->weights, f->fmt, f->depth, p.width, p.height, p.delta, f->vol, I3, nullptr, p.K,
                                   st, f->centroid0);
         if (rc) return rc;
         stage_mark(f, ST_MC, st);
@@ -610,6 +622,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
         ia.epoch_dev = f->epoch;
         ia.tsdf = f->tsdf;
         ia.weights = f->weights;
+        ia.fmt = f->fmt;
         ia.depth = f->depth;
         ia.W = p.width;
         ia.H = p.height;
@@ -724,8 +737,17 @@ int afx_fusion_stats(afx_fusion* f, afx_frame_stats* out, void* stream) {
 
 int afx_fusion_tsdf(afx_fusion* f, float** tsdf, float** weights) {
     if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    if (f->fmt != kVoxF32) return AFX_ERR_UNSUPPORTED;  // FP16 sessions: afx_fusion_volume
+    if (tsdf) *tsdf = static_cast<float*>(f->tsdf);
+    if (weights) *weights = static_cast<float*>(f->weights);
+    return AFX_OK;
+}
+
+int afx_fusion_volume(afx_fusion* f, void** tsdf, void** weights, int* precision) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
     if (tsdf) *tsdf = f->tsdf;
     if (weights) *weights = f->weights;
+    if (precision) *precision = f->fmt == kVoxF16 ? AFX_PRECISION_FP16 : AFX_PRECISION_FP32;
     return AFX_OK;
 }
 

@@ -12,6 +12,7 @@
 // are touched.
 #include <cstring>
 
+#include "afx_store.cuh"
 #include "afx_voxel.h"
 
 namespace afx {
@@ -43,7 +44,8 @@ struct RigidArgs {
     int W, H;
 };
 
-__global__ void __launch_bounds__(256) integrate_rigid_x4_kernel(float* __restrict__ tsdf, float* __restrict__ weights,
+template <class TT, class WT>
+__global__ void __launch_bounds__(256) integrate_rigid_x4_kernel(TT* __restrict__ tsdf, WT* __restrict__ weights,
                                                                  const float* __restrict__ depth, RigidArgs a) {
     const int qx = blockIdx.x * blockDim.x + threadIdx.x;  // quad index along x
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -66,18 +68,16 @@ __global__ void __launch_bounds__(256) integrate_rigid_x4_kernel(float* __restri
     }
     if (!upd) return;
     const long base = ((long)z * Y + y) * X + qx * 4;
-    float4 t4 = *reinterpret_cast<const float4*>(tsdf + base);
-    float4 w4 = *reinterpret_cast<const float4*>(weights + base);
-    float* tv = reinterpret_cast<float*>(&t4);
-    float* wv = reinterpret_cast<float*>(&w4);
+    float tv[4], wv[4];
+    vox_get4(tsdf, weights, base, tv, wv);
 #pragma unroll
     for (int i = 0; i < 4; ++i)
         if (upd & (1u << i)) tsdf_blend(tv[i], wv[i], tn[i]);
-    *reinterpret_cast<float4*>(tsdf + base) = t4;
-    *reinterpret_cast<float4*>(weights + base) = w4;
+    vox_put4(tsdf, weights, base, tv, wv);
 }
 
-__global__ void integrate_rigid_kernel(float* tsdf, float* weights, const float* __restrict__ depth, RigidArgs a) {
+template <class TT, class WT>
+__global__ void integrate_rigid_kernel(TT* tsdf, WT* weights, const float* __restrict__ depth, RigidArgs a) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y, z = blockIdx.z;
     const int X = a.vol.dims[0], Y = a.vol.dims[1];
     if (x >= X || y >= Y) return;
@@ -89,14 +89,14 @@ __global__ void integrate_rigid_kernel(float* tsdf, float* weights, const float*
     q[2] = q[2] + (a.t_dev ? a.t_dev[2] : a.t[2]);
     if (!tsdf_update_value(q, depth, a.W, a.H, a.delta, a.K, &tn)) return;
     const long i = ((long)z * Y + y) * X + x;
-    float t = tsdf[i], w = weights[i];
+    float t = vox_get_t(tsdf, i), w = vox_get_w(weights, i);
     tsdf_blend(t, w, tn);
-    tsdf[i] = t;
-    weights[i] = w;
+    vox_put(tsdf, weights, i, t, w);
 }
 
-int integrate_rigid_impl(float* tsdf, float* weights, const float* depth, int W, int H, float delta, const Volume& vol,
-                         const float* R, const float* t, const float* K, cudaStream_t st, const float* t_dev) {
+int integrate_rigid_impl(void* tsdf, void* weights, int fmt, const float* depth, int W, int H, float delta,
+                         const Volume& vol, const float* R, const float* t, const float* K, cudaStream_t st,
+                         const float* t_dev) {
     RigidArgs a;
     a.vol = vol;
     for (int i = 0; i < 9; ++i) a.R[i] = R[i];
@@ -107,14 +107,18 @@ int integrate_rigid_impl(float* tsdf, float* weights, const float* depth, int W,
     a.W = W;
     a.H = H;
     const int X = vol.dims[0], Y = vol.dims[1], Z = vol.dims[2];
-    bool vec = (X % 4 == 0) && ((reinterpret_cast<uintptr_t>(tsdf) | reinterpret_cast<uintptr_t>(weights)) & 15) == 0;
-    if (vec) {
-        dim3 block(64, 4), grid((X / 4 + 63) / 64, (Y + 3) / 4, Z);
-        integrate_rigid_x4_kernel<<<grid, block, 0, st>>>(tsdf, weights, depth, a);
-    } else {
-        dim3 block(64, 4), grid((X + 63) / 64, (Y + 3) / 4, Z);
-        integrate_rigid_kernel<<<grid, block, 0, st>>>(tsdf, weights, depth, a);
-    }
+    const uintptr_t align = 4 * vox_bytes(fmt) - 1;  // four voxels per vector access
+    bool vec = (X % 4 == 0) && ((reinterpret_cast<uintptr_t>(tsdf) | reinterpret_cast<uintptr_t>(weights)) & align) == 0;
+    vox_dispatch(fmt, tsdf, weights, [&](auto* tp, auto* wp) {
+        if (vec) {
+            dim3 block(64, 4), grid((X / 4 + 63) / 64, (Y + 3) / 4, Z);
+            integrate_rigid_x4_kernel<<<grid, block, 0, st>>>(tp, wp, depth, a);
+        } else {
+            dim3 block(64, 4), grid((X + 63) / 64, (Y + 3) / 4, Z);
+            integrate_rigid_kernel<<<grid, block, 0, st>>>(tp, wp, depth, a);
+        }
+        return 0;
+    });
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
@@ -316,7 +320,10 @@ __global__ void __launch_bounds__(kBrickVox) brick_warp_kernel(WarpArgs a) {
 }
 
 // integrateWarpedTSDFFromFrameKernel (src/TSDFIntegration.cu:173-226) over the active bricks
+template <class TT, class WT>
 __global__ void __launch_bounds__(kBrickVox) brick_integrate_kernel(WarpedIntegrateArgs a) {
+    TT* __restrict__ tsdf = static_cast<TT*>(a.tsdf);
+    WT* __restrict__ weights = static_cast<WT*>(a.weights);
     const unsigned n_active = *a.n_active;
     for (unsigned slot = blockIdx.x; slot < n_active; slot += gridDim.x) [&] {
     const long local = (long)slot * kBrickVox + threadIdx.x;
@@ -331,10 +338,9 @@ __global__ void __launch_bounds__(kBrickVox) brick_integrate_kernel(WarpedIntegr
     const int x = bx * kBrick + threadIdx.x % kBrick, y = by * kBrick + (threadIdx.x / kBrick) % kBrick,
               z = bz * kBrick + threadIdx.x / (kBrick * kBrick);
     const long v = ((long)z * a.vol.dims[1] + y) * a.vol.dims[0] + x;
-    float t = a.tsdf[v], w = a.weights[v];
+    float t = vox_get_t(tsdf, v), w = vox_get_w(weights, v);
     tsdf_blend(t, w, tn);
-    a.tsdf[v] = t;
-    a.weights[v] = w;
+    vox_put(tsdf, weights, v, t, w);
     }();
 }
 
@@ -428,7 +434,8 @@ int launch_brick_warp(const WarpArgs& a, long max_active, cudaStream_t st) {
 
 int launch_brick_integrate(const WarpedIntegrateArgs& a, long max_active, cudaStream_t st) {
     if (max_active <= 0) return AFX_OK;
-    brick_integrate_kernel<<<brick_grid(max_active), kBrickVox, 0, st>>>(a);
+    if (a.fmt == kVoxF16) brick_integrate_kernel<__half, unsigned short><<<brick_grid(max_active), kBrickVox, 0, st>>>(a);
+    else brick_integrate_kernel<float, float><<<brick_grid(max_active), kBrickVox, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
@@ -568,7 +575,8 @@ int afx_integrate_tsdf(float* tsdf, float* weights, const float* depth, int widt
     if (!tsdf || !weights || !depth || !dims || !voxel_size || !volume_size || !rotate || !translate || !K)
         return AFX_ERR_INVALID_ARGUMENT;
     if (width <= 0 || height <= 0 || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return AFX_ERR_INVALID_ARGUMENT;
-    return integrate_rigid_impl(tsdf, weights, depth, width, height, delta, make_volume(dims, voxel_size, volume_size),
+    return integrate_rigid_impl(tsdf, weights, kVoxF32, depth, width, height, delta,
+                                make_volume(dims, voxel_size, volume_size),
                                 rotate, translate, K, as_stream(stream));
 }
 

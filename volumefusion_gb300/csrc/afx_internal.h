@@ -9,6 +9,11 @@
 
 namespace afx {
 
+// Voxel storage formats (afx_store.cuh): the reference's FP32 values + FP32 weights, or the
+// precision form's FP16 values + uint16 weights.
+enum { kVoxF32 = 0, kVoxF16 = 1 };
+inline size_t vox_bytes(int fmt) { return fmt == kVoxF16 ? 2 : 4; }  // per array and voxel
+
 // ---- scans (afx_scan.cu) ----
 // Exclusive prefix sum of n unsigned values; out may alias in.  If total != nullptr the
 // sum of all n values is written there (device).  Workspace: scan_workspace_size(n).
@@ -23,14 +28,15 @@ int frame_prep_impl(const uint16_t* mm, int width, int height, const afx_prep_pa
                     float* normals, float* centroid, unsigned long long* acc, int* error, cudaStream_t st);
 
 // ---- integration (afx_integrate.cu) ----
-int integrate_rigid_impl(float* tsdf, float* weights, const float* depth, int W, int H, float delta, const Volume& vol,
-                         const float* R, const float* t, const float* K, cudaStream_t st, const float* t_dev = nullptr);
+int integrate_rigid_impl(void* tsdf, void* weights, int fmt, const float* depth, int W, int H, float delta,
+                         const Volume& vol, const float* R, const float* t, const float* K, cudaStream_t st,
+                         const float* t_dev = nullptr);
 void rotation_inverse(const float* R, float* Rinv);
 
 // ---- marching cubes and sorting (afx_mc.cu) ----
 size_t sort_unique_workspace_size(long n_max);
 int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, cudaStream_t st);
-int mc_fused_impl(const float* tsdf, const float* weights, const Volume& vol, float iso, float* points,
+int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
                   unsigned* face_count, long face_cap, cudaStream_t st, int* error = nullptr);
 int translate_impl(float* pts, const unsigned* count, long n_max, const float* t, cudaStream_t st);

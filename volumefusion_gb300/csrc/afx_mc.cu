@@ -11,6 +11,7 @@
 #include <cstring>
 
 #include "afx_internal.h"
+#include "afx_store.cuh"
 #include "afx_tma.h"
 
 namespace afx {
@@ -63,15 +64,16 @@ struct McArgs {
 };
 
 // getVertex + interpolate (src/MarchingCubes.cu:294-336)
-AFX_D void edge_vertex(const float* __restrict__ tsdf, const Volume& vol, int x, int y, int z, int e, float iso,
+template <class TT>
+AFX_D void edge_vertex(const TT* __restrict__ tsdf, const Volume& vol, int x, int y, int z, int e, float iso,
                        float* o) {
     const int* ca = c_corner[c_edge[e][0]];
     const int* cb = c_corner[c_edge[e][1]];
     const int X = vol.dims[0], Y = vol.dims[1];
     int x1 = x + ca[0], y1 = y + ca[1], z1 = z + ca[2];
     int x2 = x + cb[0], y2 = y + cb[1], z2 = z + cb[2];
-    float t0 = __ldg(tsdf + ((long)z1 * Y + y1) * X + x1);
-    float t1 = __ldg(tsdf + ((long)z2 * Y + y2) * X + x2);
+    float t0 = vox_ld_t(tsdf, ((long)z1 * Y + y1) * X + x1);
+    float t1 = vox_ld_t(tsdf, ((long)z2 * Y + y2) * X + x2);
     float p0[3], p1[3];
     voxel_to_world(x1, y1, z1, vol.vs, vol.half, p0);
     voxel_to_world(x2, y2, z2, vol.vs, vol.half, p1);
@@ -116,8 +118,8 @@ AFX_D unsigned warp_append(unsigned* counter, unsigned n) {
 // Vertices and triangles of one cube (all lanes of the warp call this together: the appends are
 // warp-aggregated).  Emits the point-cloud vertices (marchingCubesMeshKernel) and/or the
 // triangles (marchingCubesFullKernel).
-template <bool kPoints, bool kMesh>
-AFX_D void mc_emit(const float* __restrict__ tsdf, const McArgs& a, int x, int y, int z, int ci, bool active) {
+template <bool kPoints, bool kMesh, class TT>
+AFX_D void mc_emit(const TT* __restrict__ tsdf, const McArgs& a, int x, int y, int z, int ci, bool active) {
     const unsigned et = active ? c_edge_table[ci] : 0u;
     float ep[12][3];
     if (active) {
@@ -181,21 +183,22 @@ AFX_D void mc_emit(const float* __restrict__ tsdf, const McArgs& a, int x, int y
 constexpr int kMcX = 32, kMcY = 8, kMcZ = 16;
 
 // tsdf/weight of the corners (x, y), (x+1, y), (x, y+1), (x+1, y+1) of slice z
-AFX_D void mc_slice(const float* __restrict__ tsdf, const float* __restrict__ w, long row0, long X, float t[4],
+template <class TT, class WT>
+AFX_D void mc_slice(const TT* __restrict__ tsdf, const WT* __restrict__ w, long row0, long X, float t[4],
                     float ww[4]) {
-    t[0] = __ldg(tsdf + row0);
-    t[1] = __ldg(tsdf + row0 + 1);
-    t[2] = __ldg(tsdf + row0 + X);
-    t[3] = __ldg(tsdf + row0 + X + 1);
-    ww[0] = __ldg(w + row0);
-    ww[1] = __ldg(w + row0 + 1);
-    ww[2] = __ldg(w + row0 + X);
-    ww[3] = __ldg(w + row0 + X + 1);
+    t[0] = vox_ld_t(tsdf, row0);
+    t[1] = vox_ld_t(tsdf, row0 + 1);
+    t[2] = vox_ld_t(tsdf, row0 + X);
+    t[3] = vox_ld_t(tsdf, row0 + X + 1);
+    ww[0] = vox_ld_w(w, row0);
+    ww[1] = vox_ld_w(w, row0 + 1);
+    ww[2] = vox_ld_w(w, row0 + X);
+    ww[3] = vox_ld_w(w, row0 + X + 1);
 }
 
-template <bool kPoints, bool kMesh>
-__global__ void __launch_bounds__(kMcX * kMcY) mc_kernel(const float* __restrict__ tsdf,
-                                                        const float* __restrict__ weights, McArgs a) {
+template <class TT, class WT, bool kPoints, bool kMesh>
+__global__ void __launch_bounds__(kMcX * kMcY) mc_kernel(const TT* __restrict__ tsdf,
+                                                        const WT* __restrict__ weights, McArgs a) {
     const int nx = a.vol.dims[0] - 2, ny = a.vol.dims[1] - 2, nz = a.vol.dims[2] - 2;
     const long X = a.vol.dims[0], XY = X * a.vol.dims[1];
     const int x = blockIdx.x * kMcX + threadIdx.x, y = blockIdx.y * kMcY + threadIdx.y;
@@ -233,27 +236,34 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_kernel(const float* __restrict
 }
 
 // Same cubes as mc_kernel, with the CTA's whole brick of corner values -- 40 x 9 x (kMcZ + 1)
-// floats of TSDF and of weights, x padded to a 16-byte multiple -- brought into shared memory by
+// elements of TSDF and of weights, x padded to a 16-byte multiple -- brought into shared memory by
 // two TMA tile loads on one mbarrier, so the march reads no global memory for inactive cubes.
-constexpr int kMcTX = 40;  // box width in floats (>= kMcX + 1, 160 B)
+constexpr int kMcTX = 40;  // box width in elements (>= kMcX + 1; 160 B in FP32, 80 B in FP16)
 // each brick starts on a 128-byte boundary (TMA destination alignment), plus slack to align the base
-constexpr size_t kMcBrickBytes = ((size_t)kMcTX * (kMcY + 1) * (kMcZ + 1) * sizeof(float) + 127) / 128 * 128;
-constexpr size_t kMcTmaSmem = 2 * kMcBrickBytes + 128;
+__host__ __device__ constexpr size_t mc_brick_bytes(size_t elem) { return ((size_t)kMcTX * (kMcY + 1) * (kMcZ + 1) * elem + 127) / 128 * 128; }
+__host__ __device__ constexpr size_t mc_tma_smem(size_t elem) { return 2 * mc_brick_bytes(elem) + 128; }
 
 AFX_D uint32_t mc_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-template <bool kPoints, bool kMesh>
+AFX_D float smem_t(const float* p, int i) { return p[i]; }
+AFX_D float smem_t(const __half* p, int i) { return __half2float(p[i]); }
+AFX_D bool smem_w_zero(const float* p, int i) { return p[i] == 0.0f; }
+AFX_D bool smem_w_zero(const unsigned short* p, int i) { return p[i] == 0; }
+
+template <class TT, class WT, bool kPoints, bool kMesh>
 __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_constant__ CUtensorMap map_t,
                                                             const __grid_constant__ CUtensorMap map_w,
-                                                            const float* __restrict__ tsdf, McArgs a) {
+                                                            const TT* __restrict__ tsdf, McArgs a) {
+    static_assert(sizeof(TT) == sizeof(WT), "value and weight bricks share one layout");
+    constexpr size_t kMcBrickBytes = mc_brick_bytes(sizeof(TT));
     extern __shared__ __align__(128) unsigned char mc_raw[];
     __shared__ alignas(8) unsigned long long mbar;
     __shared__ unsigned q[kMcX * kMcY * kMcZ];  // surface cubes of this CTA: ci | x << 8 | y << 13 | z << 16
     __shared__ unsigned q_n;
     constexpr int kSlice = kMcTX * (kMcY + 1);
     const uint32_t pad = (128u - (mc_smem_u32(mc_raw) & 127u)) & 127u;
-    float* st = reinterpret_cast<float*>(mc_raw + pad);
-    float* sw = reinterpret_cast<float*>(mc_raw + pad + kMcBrickBytes);
+    TT* st = reinterpret_cast<TT*>(mc_raw + pad);
+    WT* sw = reinterpret_cast<WT*>(mc_raw + pad + kMcBrickBytes);
     const int tid = threadIdx.y * kMcX + threadIdx.x;
     const int x0 = blockIdx.x * kMcX, y0 = blockIdx.y * kMcY, z0 = blockIdx.z * kMcZ;
     if (((mc_smem_u32(st) | mc_smem_u32(sw)) & 127u) != 0u) {  // never expected: refuse rather than fault
@@ -267,7 +277,7 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_consta
     }
     __syncthreads();
     if (tid == 0) {
-        const unsigned bytes = (unsigned)(2 * kSlice * (kMcZ + 1) * sizeof(float));
+        const unsigned bytes = (unsigned)(kSlice * (kMcZ + 1) * (sizeof(TT) + sizeof(WT)));
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mc_smem_u32(&mbar)), "r"(bytes)
                      : "memory");
         asm volatile(
@@ -319,11 +329,11 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_consta
             const int off[8] = {s0 + kMcTX + 1, s0 + 1, s0, s0 + kMcTX, s1 + kMcTX + 1, s1 + 1, s1, s1 + kMcTX};
             bool any_zero = false;
 #pragma unroll
-            for (int c = 0; c < 8; ++c) any_zero |= (sw[off[c]] == 0.0f);
+            for (int c = 0; c < 8; ++c) any_zero |= smem_w_zero(sw, off[c]);
             if (!any_zero)
 #pragma unroll
                 for (int c = 0; c < 8; ++c)
-                    if (st[off[c]] > a.iso) ci |= 1 << c;
+                    if (smem_t(st, off[c]) > a.iso) ci |= 1 << c;
         }
         const bool active = ci != 0 && ci != 255;
         // queue the surface cubes (warp-aggregated), processed densely below
@@ -355,23 +365,49 @@ __global__ void mc_vert_count_kernel(const unsigned* face_count, unsigned* vert_
     *vert_count = 3u * *face_count;
 }
 
-// 3-D tiled map over a float volume; the box is one CTA's brick of corner values.
-static bool make_volume_map(CUtensorMap* map, const float* base, const Volume& vol) {
-    if ((vol.dims[0] * sizeof(float)) % 16 != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
+// 3-D tiled map over one voxel array (element type `type`, `elem` bytes); the box is one CTA's
+// brick of corner values.
+static bool make_volume_map(CUtensorMap* map, const void* base, const Volume& vol, CUtensorMapDataType type,
+                            size_t elem) {
+    if ((vol.dims[0] * elem) % 16 != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
     cuuint64_t dims[3] = {(cuuint64_t)vol.dims[0], (cuuint64_t)vol.dims[1], (cuuint64_t)vol.dims[2]};
-    cuuint64_t strides[2] = {(cuuint64_t)vol.dims[0] * sizeof(float),
-                             (cuuint64_t)vol.dims[0] * vol.dims[1] * sizeof(float)};
+    cuuint64_t strides[2] = {(cuuint64_t)vol.dims[0] * elem, (cuuint64_t)vol.dims[0] * vol.dims[1] * elem};
     cuuint32_t box[3] = {(cuuint32_t)kMcTX, (cuuint32_t)(kMcY + 1), (cuuint32_t)(kMcZ + 1)};
     cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estr,
+    CUresult r = fn(map, type, 3, const_cast<void*>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS;
 }
 
-int mc_fused_impl(const float* tsdf, const float* weights, const Volume& vol, float iso, float* points,
+template <class TT, class WT, bool kPoints, bool kMesh>
+static void mc_launch(const TT* tsdf, const WT* weights, const McArgs& a, const CUtensorMap* mt, const CUtensorMap* mw,
+                      dim3 grid, dim3 block, cudaStream_t st) {
+    if (mt) {
+        constexpr int smem = (int)mc_tma_smem(sizeof(TT));
+        static bool attr = false;  // per instantiation: the dynamic shared memory opt-in
+        if (!attr) {
+            cudaFuncSetAttribute(mc_tma_kernel<TT, WT, kPoints, kMesh>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 smem);
+            attr = true;
+        }
+        mc_tma_kernel<TT, WT, kPoints, kMesh><<<grid, block, smem, st>>>(*mt, *mw, tsdf, a);
+    } else {
+        mc_kernel<TT, WT, kPoints, kMesh><<<grid, block, 0, st>>>(tsdf, weights, a);
+    }
+}
+
+template <class TT, class WT>
+static void mc_launch_any(const TT* tsdf, const WT* weights, const McArgs& a, const CUtensorMap* mt,
+                          const CUtensorMap* mw, bool P, bool M, dim3 grid, dim3 block, cudaStream_t st) {
+    if (P && M) mc_launch<TT, WT, true, true>(tsdf, weights, a, mt, mw, grid, block, st);
+    else if (P) mc_launch<TT, WT, true, false>(tsdf, weights, a, mt, mw, grid, block, st);
+    else mc_launch<TT, WT, false, true>(tsdf, weights, a, mt, mw, grid, block, st);
+}
+
+int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
                   unsigned* face_count, long face_cap, cudaStream_t st, int* error) {
     int rc = upload_tables();
@@ -395,24 +431,20 @@ int mc_fused_impl(const float* tsdf, const float* weights, const Volume& vol, fl
     const dim3 block(kMcX, kMcY);
     const bool P = points != nullptr, M = verts != nullptr;
     if (!P && !M) return AFX_OK;
-    // TMA bricks where the caller can receive a load-timeout report and the map encodes
+    // TMA bricks where the caller can receive a load-timeout report and the maps encode
     CUtensorMap mt, mw;
-    if (error && make_volume_map(&mt, tsdf, vol) && make_volume_map(&mw, weights, vol)) {
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(mc_tma_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMcTmaSmem);
-            cudaFuncSetAttribute(mc_tma_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMcTmaSmem);
-            cudaFuncSetAttribute(mc_tma_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMcTmaSmem);
-            attr = true;
-        }
-        if (P && M) mc_tma_kernel<true, true><<<grid, block, kMcTmaSmem, st>>>(mt, mw, tsdf, a);
-        else if (P) mc_tma_kernel<true, false><<<grid, block, kMcTmaSmem, st>>>(mt, mw, tsdf, a);
-        else mc_tma_kernel<false, true><<<grid, block, kMcTmaSmem, st>>>(mt, mw, tsdf, a);
-    } else {
-        if (P && M) mc_kernel<true, true><<<grid, block, 0, st>>>(tsdf, weights, a);
-        else if (P) mc_kernel<true, false><<<grid, block, 0, st>>>(tsdf, weights, a);
-        else mc_kernel<false, true><<<grid, block, 0, st>>>(tsdf, weights, a);
-    }
+    const bool f16 = fmt == kVoxF16;
+    const size_t elem = vox_bytes(fmt);
+    const bool tma = error && make_volume_map(&mt, tsdf, vol, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 :
+                                                                     CU_TENSOR_MAP_DATA_TYPE_FLOAT32, elem) &&
+                     make_volume_map(&mw, weights, vol, f16 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 :
+                                                              CU_TENSOR_MAP_DATA_TYPE_FLOAT32, elem);
+    if (f16)
+        mc_launch_any(static_cast<const __half*>(tsdf), static_cast<const unsigned short*>(weights), a,
+                      tma ? &mt : nullptr, tma ? &mw : nullptr, P, M, grid, block, st);
+    else
+        mc_launch_any(static_cast<const float*>(tsdf), static_cast<const float*>(weights), a, tma ? &mt : nullptr,
+                      tma ? &mw : nullptr, P, M, grid, block, st);
     AFX_LAUNCH_CHECK();
     if (M && vert_count) {
         mc_vert_count_kernel<<<1, 1, 0, st>>>(face_count, vert_count);
@@ -728,7 +760,7 @@ int afx_marching_cubes_points(float* points, unsigned* count, long capacity, con
                               const int dims[3], const float voxel_size[3], const float volume_size[3], float iso,
                               void* stream) {
     if (!points || !count || !tsdf || !weights || !dims || capacity < 0) return AFX_ERR_INVALID_ARGUMENT;
-    return mc_fused_impl(tsdf, weights, make_volume(dims, voxel_size, volume_size), iso, points, count, capacity,
+    return mc_fused_impl(tsdf, weights, kVoxF32, make_volume(dims, voxel_size, volume_size), iso, points, count, capacity,
                          nullptr, nullptr, 0, nullptr, nullptr, 0, as_stream(stream));
 }
 
@@ -738,7 +770,7 @@ int afx_marching_cubes_mesh(float* vertices, unsigned* vertex_count, long vertex
                             void* stream) {
     if (!vertices || !vertex_count || !faces || !face_count || !tsdf || !weights || !dims)
         return AFX_ERR_INVALID_ARGUMENT;
-    return mc_fused_impl(tsdf, weights, make_volume(dims, voxel_size, volume_size), iso, nullptr, nullptr, 0, vertices,
+    return mc_fused_impl(tsdf, weights, kVoxF32, make_volume(dims, voxel_size, volume_size), iso, nullptr, nullptr, 0, vertices,
                          vertex_count, vertex_capacity, faces, face_count, face_capacity, as_stream(stream));
 }
 
@@ -756,7 +788,7 @@ int afx_extract_point_cloud(float* points, unsigned* count, long capacity, const
     if (!points || !count || !tsdf || !weights || !dims) return AFX_ERR_INVALID_ARGUMENT;
     cudaStream_t st = as_stream(stream);
     AFX_CUDA(cudaMemsetAsync(count, 0, sizeof(unsigned), st));
-    int rc = mc_fused_impl(tsdf, weights, make_volume(dims, voxel_size, volume_size), iso, points, count, capacity,
+    int rc = mc_fused_impl(tsdf, weights, kVoxF32, make_volume(dims, voxel_size, volume_size), iso, points, count, capacity,
                            nullptr, nullptr, 0, nullptr, nullptr, 0, st);
     if (rc) return rc;
     return sort_unique_impl(points, count, capacity, workspace, workspace_bytes, st);

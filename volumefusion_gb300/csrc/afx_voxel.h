@@ -83,8 +83,9 @@ struct WarpedIntegrateArgs {
     const unsigned char* in_count;
     const unsigned* coll;
     const unsigned* epoch_dev;
-    float* tsdf;
-    float* weights;
+    void* tsdf;     // voxel storage of format fmt (kVoxF32 / kVoxF16)
+    void* weights;
+    int fmt;
     const float* depth;
     int W, H;
     float delta;

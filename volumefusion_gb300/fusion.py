@@ -34,6 +34,7 @@ def params_from_config(cfg, extract_mesh=True, triangle_capacity=None):
     p.pcg_tol = float(cfg.get("pcg_tol", 0.0))
     p.extract_mesh = int(extract_mesh)
     p.triangle_capacity = int(triangle_capacity or cfg.get("triangle_cap", 4_000_000))
+    p.precision = {"fp32": 0, "fp16": 1}[cfg.get("precision", "fp32")]
     return p
 
 
@@ -102,9 +103,23 @@ class FusionSession:
         return {f[0]: getattr(s, f[0]) for f in FrameStats._fields_}
 
     def tsdf(self):
-        t, w = C.c_void_p(), C.c_void_p()
-        lib().afx_fusion_tsdf(self.h, C.byref(t), C.byref(w))
-        return _wrap_device(t.value, self.S, torch.float32), _wrap_device(w.value, self.S, torch.float32)
+        """Copies of the volume as FP32 tensors (values, weights), whatever the storage format."""
+        t, w, prec = C.c_void_p(), C.c_void_p(), C.c_int(0)
+        check(lib().afx_fusion_volume(self.h, C.byref(t), C.byref(w), C.byref(prec)), "afx_fusion_volume")
+        if prec.value == 0:
+            return _wrap_device(t.value, self.S, torch.float32), _wrap_device(w.value, self.S, torch.float32)
+        # precision form: FP16 values widen exactly; uint16 weights are counts <= 15
+        return (_wrap_device(t.value, self.S, torch.float16).float(),
+                _wrap_device(w.value, self.S, torch.int16).float())
+
+    def volume_raw(self):
+        """The stored arrays as they are: (values, weights, precision) with FP16 / int16 (bit
+        pattern of uint16) tensors in the precision form."""
+        t, w, prec = C.c_void_p(), C.c_void_p(), C.c_int(0)
+        check(lib().afx_fusion_volume(self.h, C.byref(t), C.byref(w), C.byref(prec)), "afx_fusion_volume")
+        if prec.value == 0:
+            return _wrap_device(t.value, self.S, torch.float32), _wrap_device(w.value, self.S, torch.float32), "fp32"
+        return _wrap_device(t.value, self.S, torch.float16), _wrap_device(w.value, self.S, torch.int16), "fp16"
 
     def graph(self):
         nodes, radii, T, n = C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p()
