@@ -417,7 +417,7 @@ def main():
     precision = None
     if not args.no_precision:
         from volumefusion_gb300.serve import session_bytes
-        precision = {"workload": "capsule pair, 30 frames, 512^3 @ 2 mm, 6.5 mm graph radius"}
+        precision = {"workload": "capsule pair, 30 frames, 512^3 @ 2 mm, 9 mm graph radius"}
         for prec in ("fp16", "fp32"):
             pcfg = dict(configs.precision_capsules_512(n_frames=N_FRAMES), precision=prec)
             sp = FusionSession(pcfg, stream=stream)
