@@ -42,6 +42,7 @@ def parse():
     ap.add_argument("--no-dense-graph", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--served-streams", type=int, default=64)
     ap.add_argument("--served-seconds", type=float, default=4.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -176,6 +177,74 @@ def stage_bytes(cfg, st):
         "marching_cubes": 8.0 * S + 12.0 * st["mesh_points"] * 4 + 48.0 * st["mesh_faces"],
         "warped_integrate": 16.0 * A if A else None,
     }
+
+
+def batched_arm(args, stream, barrier, reduce_max, world):
+    """16 sessions of uneven size (the config-4 mix: volumes 128^3-384^3, 320x288 or 640x576,
+    sphere / torus / capsule) fusing 30-frame sequences: one afx_batch_process per frame of all
+    sessions (frames 3.. as one graph launch) against the plain drop-in running the same sessions
+    one after another; marching-cubes tiles chosen per session by the autotuner first."""
+    import torch
+    from volumefusion_gb300 import configs
+    from volumefusion_gb300.batch import Batch
+    from volumefusion_gb300.fusion import FusionSession
+
+    pool = configs.session_mix(16, seed=3)
+    nf = 30
+    frames = [[torch.from_numpy(configs.scene_frame(c, i).astype(np.int16)).cuda() for i in range(nf)] for c in pool]
+    sessions = [FusionSession(c, stream=stream) for c in pool]
+    batch = Batch(sessions)
+
+    def run_batch(steps):
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                for s in sessions:
+                    s.reset()
+                for i in range(nf):
+                    batch.process([frames[k][i] for k in range(len(sessions))], stream)
+
+    def run_plain(steps):
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                for k, s in enumerate(sessions):
+                    s.reset()
+                    for i in range(nf):
+                        s.process(frames[k][i])
+
+    run_batch(1)
+    barrier()
+    tiles = [s.autotune()[0] for s in sessions]  # on each session's last volume
+    run_batch(1)  # graphs captured again with the chosen tiles
+    barrier()
+    steps = max(1, min(3, args.steps))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0 = batch.graph_launches()
+    e0.record(stream)
+    run_batch(steps)
+    e1.record(stream)
+    barrier()
+    bms = reduce_max(e0.elapsed_time(e1))
+    glaunch = batch.graph_launches() - g0
+    st = batch.stats(stream)
+    run_plain(1)
+    barrier()
+    e0.record(stream)
+    run_plain(steps)
+    e1.record(stream)
+    barrier()
+    pms = reduce_max(e0.elapsed_time(e1))
+    total = steps * nf * len(sessions)
+    out = {"sessions": len(sessions), "volumes": sorted(int(c["dims"][0]) for c in pool),
+           "frames_per_session_step": nf, "frames_per_s": world * total / (bms / 1000.0),
+           "plain_frames_per_s": world * total / (pms / 1000.0), "graph_launches_per_step": glaunch // steps,
+           "mc_tiles": tiles, "errors": sum(int(x["error"] != 0) for x in st),
+           "nodes": [int(x["n_nodes"]) for x in st]}
+    out["batched_over_plain"] = out["frames_per_s"] / out["plain_frames_per_s"]
+    batch.close()
+    for s in sessions:
+        s.close()
+    torch.cuda.empty_cache()
+    return out
 
 
 def served_arm(args, rank):
@@ -443,6 +512,10 @@ def main():
                                "session_bytes": session_bytes(pcfg), "n_nodes_last_frame": pst["n_nodes"],
                                "error": pst["error"], "stage_ms_per_frame": pstage}
 
+    batched = None
+    if not args.no_batched:
+        batched = batched_arm(args, stream, barrier, reduce_max, world)
+
     served = None
     if not args.no_served:
         served = served_arm(args, rank)
@@ -493,6 +566,7 @@ def main():
                                                 "mesh_faces", "error")},
             "dense_graph": dense,
             "precision": precision,
+            "batched": batched,
             "served": served,
             "roofline": roof,
             "cpu_baseline": cpu,

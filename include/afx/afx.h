@@ -371,6 +371,22 @@ int afx_fusion_set_graphs(afx_fusion* f, int on);
 /* Number of frame graphs captured so far (0 while graphs are off or capture fell back). */
 int afx_fusion_graph_count(const afx_fusion* f);
 
+/* Marching-cubes tile of the session (no counterpart in the reference): AFX_MC_TILE_TMA16 (default:
+ * a CTA's brick of 32x8x16 cubes brought into shared memory by TMA), AFX_MC_TILE_TMA8,
+ * AFX_MC_TILE_TMA32 (8 or 32 cubes along z) or AFX_MC_TILE_COLUMN (column march from global memory).
+ * Results are the same with every tile (point and triangle sets; triangle order may differ).
+ * afx_fusion_autotune times each tile on the session's current volume (call it after a few
+ * frames), keeps the fastest and returns it in *tile (and the best time of each tile in ms[4] if
+ * given); it re-extracts the current frame's mesh and blocks on `stream`.  Changing the tile drops
+ * the captured frame graphs, which are captured again on next use. */
+#define AFX_MC_TILE_TMA16 0
+#define AFX_MC_TILE_TMA8 1
+#define AFX_MC_TILE_TMA32 2
+#define AFX_MC_TILE_COLUMN 3
+int afx_fusion_set_tile(afx_fusion* f, int tile);
+int afx_fusion_get_tile(const afx_fusion* f);
+int afx_fusion_autotune(afx_fusion* f, int* tile, float* ms, void* stream);
+
 /* Per-stage GPU timing (CUDA events around each stage, like the reference's TimeMap).
  * Stages: 0 prep, 1 rigid integration, 2 point-cloud sort/unique, 3 graph build, 4 KNN +
  * weights, 5 Gauss-Newton structure, 6 Gauss-Newton iterations, 7 voxel support,
@@ -410,6 +426,24 @@ int afx_server_poll(afx_server* s, afx_server_result* out, int max_results, int*
 /* The session's afx_fusion (for its volume, graph, mesh); NULL if unknown. */
 afx_fusion* afx_server_session(afx_server* s, int session_id);
 int afx_server_usage(afx_server* s, size_t* used_bytes, int* sessions, long* denied);
+
+/* ------------------------------------------------------------------------------------
+ * Batched form (no counterpart in the reference): one frame of every session of a batch in one
+ * graph launch.  Sessions keep their own state and results (the same as processing them one by
+ * one); from the fourth frame of a session's sequence its frame graph is a child of one parent
+ * graph per pattern of the sessions' states, with the frame copies and the statistics copies as
+ * graph nodes.  Sessions in their first frames run their kernels one by one on `stream` first.
+ * depth_mm[i] is session i's frame (device or pinned host memory, uint16 mm, not the session's own
+ * input buffer).  afx_batch_stats copies the statistics of the last processed frames (valid once
+ * `stream` has passed afx_batch_process).  The batch does not own the sessions.
+ * ------------------------------------------------------------------------------------ */
+typedef struct afx_batch afx_batch;
+int afx_batch_create(afx_fusion* const* sessions, int n, afx_batch** out);
+int afx_batch_destroy(afx_batch* b);
+int afx_batch_process(afx_batch* b, const uint16_t* const* depth_mm, void* stream);
+int afx_batch_stats(afx_batch* b, afx_frame_stats* out, int n);
+/* Parent-graph launches so far (one per afx_batch_process with a replayed session). */
+long afx_batch_graph_launches(const afx_batch* b);
 
 /* Stream-ordered device-to-device copy (helper for bindings that hold raw device views). */
 int afx_copy_device(void* dst, const void* src, size_t bytes, void* stream);

@@ -84,6 +84,14 @@ SIGNATURES = {
     "afx_update_transforms": (i32, [vp, vp, vp, i32, vp]),
     "afx_fusion_set_graphs": (i32, [vp, i32]),
     "afx_fusion_graph_count": (i32, [vp]),
+    "afx_fusion_set_tile": (i32, [vp, i32]),
+    "afx_fusion_get_tile": (i32, [vp]),
+    "afx_fusion_autotune": (i32, [vp, C.POINTER(i32), C.POINTER(C.c_float), vp]),
+    "afx_batch_create": (i32, [C.POINTER(vp), i32, C.POINTER(vp)]),
+    "afx_batch_destroy": (i32, [vp]),
+    "afx_batch_process": (i32, [vp, C.POINTER(vp), vp]),
+    "afx_batch_stats": (i32, [vp, vp, i32]),
+    "afx_batch_graph_launches": (C.c_long, [vp]),
     "afx_fusion_default_params": (None, [C.POINTER(FusionParams)]),
     "afx_fusion_memory_bytes": (sz, [C.POINTER(FusionParams)]),
     "afx_fusion_stats_async": (i32, [vp, vp, vp]),

@@ -9,7 +9,9 @@
 // point cloud and graph to the host every frame.
 #include <atomic>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <map>
 #include <new>
 #include <vector>
 
@@ -122,6 +124,9 @@ struct afx_fusion {
     bool graphs = true;
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    cudaGraph_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // kept for batch graphs
+    unsigned graph_epoch = 0;  // advanced whenever the captured graphs are dropped
+    int mc_tile = kMcTileTma16;  // marching-cubes tile (afx_fusion_autotune)
     long glaunches[2][2] = {{0, 0}, {0, 0}};  // kernels in each captured frame
     long replayed = 0;                        // kernels launched by graph replays
 };
@@ -395,14 +400,25 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     return AFX_OK;
 }
 
+// Forget the captured frame graphs (they are captured again on next use).
+static void drop_graphs(afx_fusion* f) {
+    for (int b = 0; b < 2; ++b)
+        for (int c = 0; c < 2; ++c) {
+            if (f->gexec[b][c]) cudaGraphExecDestroy(f->gexec[b][c]);
+            if (f->graph[b][c]) cudaGraphDestroy(f->graph[b][c]);
+            f->gexec[b][c] = nullptr;
+            f->graph[b][c] = nullptr;
+            f->glaunches[b][c] = 0;
+        }
+    ++f->graph_epoch;
+}
+
 int afx_fusion_destroy(afx_fusion* f) {
     if (!f) return AFX_ERR_INVALID_ARGUMENT;
     cudaDeviceSynchronize();
     for (auto& m : f->marks) cudaEventDestroy(m.second);
     for (auto e : f->ev_pool) cudaEventDestroy(e);
-    for (auto& row : f->gexec)
-        for (auto& g : row)
-            if (g) cudaGraphExecDestroy(g);
+    drop_graphs(f);
     if (f->cap_stream) cudaStreamDestroy(f->cap_stream);
     cudaError_t e = cudaFree(f->arena);
     delete f;
@@ -459,7 +475,8 @@ static int extract_frame_mesh(afx_fusion* f, int cur, cudaStream_t st) {
     const bool mesh = f->p.extract_mesh != 0;
     return mc_fused_impl(f->tsdf, f->weights, f->fmt, f->vol, 0.f, f->points_buf[next], f->npoints_buf[next], f->p.mesh_capacity,
                          mesh ? f->mverts : nullptr, mesh ? f->nmverts : nullptr, f->p.triangle_capacity * 3,
-                         mesh ? f->mfaces : nullptr, mesh ? f->nmfaces : nullptr, f->p.triangle_capacity, st, f->error);
+                         mesh ? f->mfaces : nullptr, mesh ? f->nmfaces : nullptr, f->p.triangle_capacity, st, f->error,
+                         f->mc_tile);
 }
 
 // Everything a frame does on the device, in stream order on `st`; host state is not changed.
@@ -656,9 +673,12 @@ static int capture_frame(afx_fusion* f, int cur, bool build) {
     }
     cudaGraphExec_t exec = nullptr;
     const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ie != cudaSuccess) return note_cuda_error(ie);
+    if (ie != cudaSuccess) {
+        cudaGraphDestroy(graph);
+        return note_cuda_error(ie);
+    }
     f->gexec[build][cur] = exec;
+    f->graph[build][cur] = graph;
     f->glaunches[build][cur] = launches_total() - l0;
     return AFX_OK;
 }
@@ -814,6 +834,59 @@ int afx_fusion_graph_count(const afx_fusion* f) {
     return f->graphs ? c : 0;
 }
 
+int afx_fusion_set_tile(afx_fusion* f, int tile) {
+    if (!f || tile < 0 || tile >= kMcTiles) return AFX_ERR_INVALID_ARGUMENT;
+    if (tile != f->mc_tile) {
+        AFX_CUDA(cudaDeviceSynchronize());  // graphs in flight may still use the old tile
+        drop_graphs(f);
+        f->mc_tile = tile;
+    }
+    return AFX_OK;
+}
+
+int afx_fusion_get_tile(const afx_fusion* f) { return f ? f->mc_tile : -1; }
+
+// Times every marching-cubes tile on the session's current volume (the extraction at the end of
+// a frame, re-run: the next frame's raw point cloud and the current mesh are written again with the
+// same contents, triangles possibly in another order) and keeps the fastest.  Blocks on `stream`.
+int afx_fusion_autotune(afx_fusion* f, int* tile_out, float* ms_out, void* stream) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    AFX_CUDA(cudaStreamSynchronize(st));
+    cudaEvent_t e0, e1;
+    AFX_CUDA(cudaEventCreate(&e0));
+    AFX_CUDA(cudaEventCreate(&e1));
+    const int saved = f->mc_tile;
+    int best = saved;
+    float best_ms = 1e30f;
+    int rc = AFX_OK;
+    for (int tile = 0; tile < kMcTiles && rc == AFX_OK; ++tile) {
+        f->mc_tile = tile;
+        float t_min = 1e30f;
+        for (int rep = 0; rep < 4 && rc == AFX_OK; ++rep) {  // the first run of a tile also sets it up
+            cudaEventRecord(e0, st);
+            rc = extract_frame_mesh(f, f->cur, st);
+            cudaEventRecord(e1, st);
+            if (cudaEventSynchronize(e1) != cudaSuccess) rc = AFX_ERR_CUDA;
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (rep > 0 && ms < t_min) t_min = ms;
+        }
+        if (ms_out) ms_out[tile] = t_min;
+        if (t_min < best_ms) {
+            best_ms = t_min;
+            best = tile;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    f->mc_tile = saved;
+    if (rc) return rc;
+    rc = afx_fusion_set_tile(f, best);
+    if (tile_out) *tile_out = best;
+    return rc;
+}
+
 int afx_fusion_set_timing(afx_fusion* f, int on) {
     if (!f) return AFX_ERR_INVALID_ARGUMENT;
     f->timing = on != 0;
@@ -846,3 +919,187 @@ int afx_copy_device(void* dst, const void* src, size_t bytes, void* stream) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------------
+// Batched form: one frame of every session of a batch with one graph launch.
+//
+// Each session keeps its own buffers, kernels and reduction orders (so its results are those it
+// has alone).  A session whose next frame is replayed (fourth frame of a sequence on) contributes
+// its captured frame graph as a child node of one parent graph, after a copy node that brings its
+// frame into the session's input buffer and before a copy node that brings its statistics to the
+// batch's pinned host array.  The children have no edges between them, so their kernels overlap on
+// the device.  Parent graphs are cached per pattern of (build mode, buffer parity, graph epoch)
+// of the sessions -- a batch that advances in step alternates between two -- and only the copy
+// sources change from call to call (executable-graph node updates, no re-instantiation).  Sessions
+// in their first frames run their kernels one by one on the caller's stream first.
+// ------------------------------------------------------------------------------------
+
+struct afx_batch {
+    std::vector<afx_fusion*> s;
+    afx_frame_stats* stats_host = nullptr;  // pinned, one per session
+    struct Exec {
+        cudaGraphExec_t exec = nullptr;
+        cudaGraph_t graph = nullptr;              // kept: node updates name its nodes
+        std::vector<int> members;                 // session indices in the graph
+        std::vector<cudaGraphNode_t> in_copy;     // frame copy node of each member
+    };
+    std::map<std::vector<long>, Exec> cache;
+    long graph_launches = 0;
+};
+
+namespace {
+
+// Failure of a graph-building call: reported on stderr when AFX_VERBOSE is set; the runtime's
+// last-error state is cleared so that later launches do not see it.
+int batch_fail(const char* what, cudaError_t e) {
+    if (std::getenv("AFX_VERBOSE")) std::fprintf(stderr, "afx_batch: %s: %s\n", what, cudaGetErrorString(e));
+    cudaGetLastError();
+    return note_cuda_error(e);
+}
+
+void batch_free(afx_batch* b) {
+    for (auto& kv : b->cache) {
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+        if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+    }
+    if (b->stats_host) cudaFreeHost(b->stats_host);
+    delete b;
+}
+
+// The parent graph for the members' (build, cur) variants.
+int batch_instantiate(afx_batch* b, const std::vector<int>& members, const std::vector<int>& build,
+                      const std::vector<int>& cur, const uint16_t* const* depth, afx_batch::Exec* out) {
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess) return batch_fail("cudaGraphCreate", e);
+    out->members = members;
+    out->in_copy.assign(members.size(), nullptr);
+    const char* what = nullptr;
+    for (size_t k = 0; k < members.size() && e == cudaSuccess; ++k) {
+        afx_fusion* f = b->s[members[k]];
+        cudaGraphNode_t cp = nullptr, child = nullptr, st = nullptr;
+        what = "frame copy node";
+        e = cudaGraphAddMemcpyNode1D(&cp, g, nullptr, 0, f->depth_mm, depth[members[k]], (size_t)f->P * 2,
+                                     cudaMemcpyDefault);
+        if (e == cudaSuccess) {
+            what = "child graph node";
+            e = cudaGraphAddChildGraphNode(&child, g, &cp, 1, f->graph[build[k]][cur[k]]);
+        }
+        if (e == cudaSuccess) {
+            what = "statistics copy node";
+            e = cudaGraphAddMemcpyNode1D(&st, g, &child, 1, b->stats_host + members[k], f->stats, sizeof(FrameStats),
+                                         cudaMemcpyDefault);
+        }
+        out->in_copy[k] = cp;
+    }
+    if (e == cudaSuccess) {
+        what = "instantiate";
+        e = cudaGraphInstantiate(&out->exec, g, 0);
+    }
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(g);
+        out->exec = nullptr;
+        return batch_fail(what, e);
+    }
+    out->graph = g;
+    return AFX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int afx_batch_create(afx_fusion* const* sessions, int n, afx_batch** out) {
+    if (!sessions || n < 1 || !out) return AFX_ERR_INVALID_ARGUMENT;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < i; ++j)
+            if (!sessions[i] || sessions[i] == sessions[j]) return AFX_ERR_INVALID_ARGUMENT;
+    afx_batch* b = new (std::nothrow) afx_batch();
+    if (!b) return AFX_ERR_NO_MEMORY;
+    b->s.assign(sessions, sessions + n);
+    const cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&b->stats_host), sizeof(afx_frame_stats) * n,
+                                        cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        batch_free(b);
+        return note_cuda_error(e);
+    }
+    std::memset(b->stats_host, 0, sizeof(afx_frame_stats) * n);
+    *out = b;
+    return AFX_OK;
+}
+
+int afx_batch_destroy(afx_batch* b) {
+    if (!b) return AFX_ERR_INVALID_ARGUMENT;
+    cudaDeviceSynchronize();
+    batch_free(b);
+    return AFX_OK;
+}
+
+int afx_batch_process(afx_batch* b, const uint16_t* const* depth_mm, void* stream) {
+    if (!b || !depth_mm) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    const int n = (int)b->s.size();
+    for (int i = 0; i < n; ++i)
+        if (!depth_mm[i] || depth_mm[i] == b->s[i]->depth_mm) return AFX_ERR_INVALID_ARGUMENT;
+    std::vector<int> members, build, cur;
+    std::vector<long> key;
+    for (int i = 0; i < n; ++i) {
+        afx_fusion* f = b->s[i];
+        const int c = f->cur ^ 1;
+        const bool bd = f->frame == 1 || f->p.update_graph;
+        bool replay = f->graphs && !f->timing && f->frame >= 3;
+        if (replay && !f->gexec[bd][c] && capture_frame(f, c, bd) != AFX_OK) {
+            f->graphs = false;
+            replay = false;
+        }
+        if (!replay) {  // first frames of a sequence (or graphs off): kernels one by one
+            int rc = afx_fusion_process(f, depth_mm[i], stream);
+            if (!rc) rc = afx_fusion_stats_async(f, b->stats_host + i, stream);
+            if (rc) return rc;
+            continue;
+        }
+        members.push_back(i);
+        build.push_back(bd);
+        cur.push_back(c);
+        key.push_back(((long)i << 40) | ((long)f->graph_epoch << 2) | (bd << 1) | c);
+    }
+    if (members.empty()) return AFX_OK;
+    auto it = b->cache.find(key);
+    if (it == b->cache.end()) {
+        afx_batch::Exec ex;
+        const int rc = batch_instantiate(b, members, build, cur, depth_mm, &ex);
+        if (rc) return rc;
+        it = b->cache.emplace(key, ex).first;
+    } else {
+        for (size_t k = 0; k < members.size(); ++k) {
+            afx_fusion* f = b->s[members[k]];
+            const cudaError_t e = cudaGraphExecMemcpyNodeSetParams1D(
+                it->second.exec, it->second.in_copy[k], f->depth_mm, depth_mm[members[k]], (size_t)f->P * 2,
+                cudaMemcpyDefault);
+            if (e != cudaSuccess) return batch_fail("frame copy update", e);
+        }
+    }
+    const cudaError_t le = cudaGraphLaunch(it->second.exec, st);
+    if (le != cudaSuccess) return batch_fail("launch", le);
+    ++b->graph_launches;
+    for (size_t k = 0; k < members.size(); ++k) {
+        afx_fusion* f = b->s[members[k]];
+        f->replayed += f->glaunches[build[k]][cur[k]];
+        f->cur = cur[k];
+        f->points = f->points_buf[cur[k]];
+        f->npoints = f->npoints_buf[cur[k]];
+        f->frame++;
+    }
+    return AFX_OK;
+}
+
+int afx_batch_stats(afx_batch* b, afx_frame_stats* out, int n) {
+    if (!b || !out || n < (int)b->s.size()) return AFX_ERR_INVALID_ARGUMENT;
+    std::memcpy(out, b->stats_host, sizeof(afx_frame_stats) * b->s.size());
+    return AFX_OK;
+}
+
+long afx_batch_graph_launches(const afx_batch* b) { return b ? b->graph_launches : 0; }
+
+}  // extern "C"
+

@@ -38,7 +38,10 @@ size_t sort_unique_workspace_size(long n_max);
 int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, cudaStream_t st);
 int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
-                  unsigned* face_count, long face_cap, cudaStream_t st, int* error = nullptr);
+                  unsigned* face_count, long face_cap, cudaStream_t st, int* error = nullptr, int tile = 0);
+// marching-cubes tiles (the session's autotuner picks one): TMA bricks of 16, 8 or 32 cubes along z,
+// or the column march from global memory
+enum { kMcTileTma16 = 0, kMcTileTma8 = 1, kMcTileTma32 = 2, kMcTileColumn = 3, kMcTiles = 4 };
 int translate_impl(float* pts, const unsigned* count, long n_max, const float* t, cudaStream_t st);
 // pts += sign * t_dev (t_dev in device memory); dst may differ from src
 int translate_dev_impl(float* dst, const float* src, const unsigned* count, long n_max, const float* t_dev, float sign,

@@ -235,13 +235,15 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_kernel(const TT* __restrict__ 
     }
 }
 
-// Same cubes as mc_kernel, with the CTA's whole brick of corner values -- 40 x 9 x (kMcZ + 1)
+// Same cubes as mc_kernel, with the CTA's whole brick of corner values -- 40 x 9 x (ZR + 1)
 // elements of TSDF and of weights, x padded to a 16-byte multiple -- brought into shared memory by
 // two TMA tile loads on one mbarrier, so the march reads no global memory for inactive cubes.
 constexpr int kMcTX = 40;  // box width in elements (>= kMcX + 1; 160 B in FP32, 80 B in FP16)
 // each brick starts on a 128-byte boundary (TMA destination alignment), plus slack to align the base
-__host__ __device__ constexpr size_t mc_brick_bytes(size_t elem) { return ((size_t)kMcTX * (kMcY + 1) * (kMcZ + 1) * elem + 127) / 128 * 128; }
-__host__ __device__ constexpr size_t mc_tma_smem(size_t elem) { return 2 * mc_brick_bytes(elem) + 128; }
+__host__ __device__ constexpr size_t mc_brick_bytes(size_t elem, int zr) {
+    return ((size_t)kMcTX * (kMcY + 1) * (zr + 1) * elem + 127) / 128 * 128;
+}
+__host__ __device__ constexpr size_t mc_tma_smem(size_t elem, int zr) { return 2 * mc_brick_bytes(elem, zr) + 128; }
 
 AFX_D uint32_t mc_smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -250,22 +252,24 @@ AFX_D float smem_t(const __half* p, int i) { return __half2float(p[i]); }
 AFX_D bool smem_w_zero(const float* p, int i) { return p[i] == 0.0f; }
 AFX_D bool smem_w_zero(const unsigned short* p, int i) { return p[i] == 0; }
 
-template <class TT, class WT, bool kPoints, bool kMesh>
+// ZR: cubes per CTA along z (the tile depth the autotuner chooses: 8, 16 or 32)
+template <class TT, class WT, bool kPoints, bool kMesh, int ZR>
 __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_constant__ CUtensorMap map_t,
                                                             const __grid_constant__ CUtensorMap map_w,
                                                             const TT* __restrict__ tsdf, McArgs a) {
     static_assert(sizeof(TT) == sizeof(WT), "value and weight bricks share one layout");
-    constexpr size_t kMcBrickBytes = mc_brick_bytes(sizeof(TT));
+    static_assert(ZR <= 64, "the queue entry keeps z in 6 bits");
+    constexpr size_t kMcBrickBytes = mc_brick_bytes(sizeof(TT), ZR);
     extern __shared__ __align__(128) unsigned char mc_raw[];
     __shared__ alignas(8) unsigned long long mbar;
-    __shared__ unsigned q[kMcX * kMcY * kMcZ];  // surface cubes of this CTA: ci | x << 8 | y << 13 | z << 16
+    __shared__ unsigned q[kMcX * kMcY * ZR];  // surface cubes of this CTA: ci | x << 8 | y << 13 | z << 16
     __shared__ unsigned q_n;
     constexpr int kSlice = kMcTX * (kMcY + 1);
     const uint32_t pad = (128u - (mc_smem_u32(mc_raw) & 127u)) & 127u;
     TT* st = reinterpret_cast<TT*>(mc_raw + pad);
     WT* sw = reinterpret_cast<WT*>(mc_raw + pad + kMcBrickBytes);
     const int tid = threadIdx.y * kMcX + threadIdx.x;
-    const int x0 = blockIdx.x * kMcX, y0 = blockIdx.y * kMcY, z0 = blockIdx.z * kMcZ;
+    const int x0 = blockIdx.x * kMcX, y0 = blockIdx.y * kMcY, z0 = blockIdx.z * ZR;
     if (((mc_smem_u32(st) | mc_smem_u32(sw)) & 127u) != 0u) {  // never expected: refuse rather than fault
         if (tid == 0 && a.error) atomicOr(a.error, ERRF_TMA);
         return;
@@ -277,7 +281,7 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_consta
     }
     __syncthreads();
     if (tid == 0) {
-        const unsigned bytes = (unsigned)(kSlice * (kMcZ + 1) * (sizeof(TT) + sizeof(WT)));
+        const unsigned bytes = (unsigned)(kSlice * (ZR + 1) * (sizeof(TT) + sizeof(WT)));
         asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mc_smem_u32(&mbar)), "r"(bytes)
                      : "memory");
         asm volatile(
@@ -318,7 +322,7 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_consta
     }
     const int nx = a.vol.dims[0] - 2, ny = a.vol.dims[1] - 2, nz = a.vol.dims[2] - 2;
     const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
-    const int z1 = min(z0 + kMcZ, nz);
+    const int z1 = min(z0 + ZR, nz);
     const bool col = x < nx && y < ny;
     const int o00 = threadIdx.y * kMcTX + threadIdx.x;  // (x, y) within a slice
     for (int z = z0; z < z1; ++z) {
@@ -357,7 +361,7 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_consta
         const bool act = qi < nq;
         const unsigned e = act ? q[qi] : 0u;
         mc_emit<kPoints, kMesh>(tsdf, a, x0 + (int)((e >> 8) & 31u), y0 + (int)((e >> 13) & 7u),
-                                z0 + (int)((e >> 16) & 15u), (int)(e & 255u), act);
+                                z0 + (int)((e >> 16) & 63u), (int)(e & 255u), act);
     }
 }
 
@@ -368,13 +372,13 @@ __global__ void mc_vert_count_kernel(const unsigned* face_count, unsigned* vert_
 // 3-D tiled map over one voxel array (element type `type`, `elem` bytes); the box is one CTA's
 // brick of corner values.
 static bool make_volume_map(CUtensorMap* map, const void* base, const Volume& vol, CUtensorMapDataType type,
-                            size_t elem) {
+                            size_t elem, int zr) {
     if ((vol.dims[0] * elem) % 16 != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0) return false;
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
     cuuint64_t dims[3] = {(cuuint64_t)vol.dims[0], (cuuint64_t)vol.dims[1], (cuuint64_t)vol.dims[2]};
     cuuint64_t strides[2] = {(cuuint64_t)vol.dims[0] * elem, (cuuint64_t)vol.dims[0] * vol.dims[1] * elem};
-    cuuint32_t box[3] = {(cuuint32_t)kMcTX, (cuuint32_t)(kMcY + 1), (cuuint32_t)(kMcZ + 1)};
+    cuuint32_t box[3] = {(cuuint32_t)kMcTX, (cuuint32_t)(kMcY + 1), (cuuint32_t)(zr + 1)};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = fn(map, type, 3, const_cast<void*>(base), dims, strides, box, estr,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -382,34 +386,51 @@ static bool make_volume_map(CUtensorMap* map, const void* base, const Volume& vo
     return r == CUDA_SUCCESS;
 }
 
+template <class TT, class WT, bool kPoints, bool kMesh, int ZR>
+static void mc_launch_tma(const TT* tsdf, const McArgs& a, const CUtensorMap* mt, const CUtensorMap* mw,
+                          cudaStream_t st) {
+    constexpr int smem = (int)mc_tma_smem(sizeof(TT), ZR);
+    static bool attr = false;  // per instantiation: the dynamic shared memory opt-in
+    if (!attr) {
+        cudaFuncSetAttribute(mc_tma_kernel<TT, WT, kPoints, kMesh, ZR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+        attr = true;
+    }
+    const dim3 grid((unsigned)((a.vol.dims[0] - 2 + kMcX - 1) / kMcX), (unsigned)((a.vol.dims[1] - 2 + kMcY - 1) / kMcY),
+                    (unsigned)((a.vol.dims[2] - 2 + ZR - 1) / ZR));
+    mc_tma_kernel<TT, WT, kPoints, kMesh, ZR><<<grid, dim3(kMcX, kMcY), smem, st>>>(*mt, *mw, tsdf, a);
+}
+
+// tile: kMcTileTma16 (default), kMcTileTma8, kMcTileTma32 (TMA bricks of that many cubes along z) or
+// kMcTileColumn (column march from global memory, 16 cubes along z).  mt/mw are the maps encoded for
+// that depth, or null (then the column march runs).
 template <class TT, class WT, bool kPoints, bool kMesh>
 static void mc_launch(const TT* tsdf, const WT* weights, const McArgs& a, const CUtensorMap* mt, const CUtensorMap* mw,
-                      dim3 grid, dim3 block, cudaStream_t st) {
-    if (mt) {
-        constexpr int smem = (int)mc_tma_smem(sizeof(TT));
-        static bool attr = false;  // per instantiation: the dynamic shared memory opt-in
-        if (!attr) {
-            cudaFuncSetAttribute(mc_tma_kernel<TT, WT, kPoints, kMesh>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 smem);
-            attr = true;
-        }
-        mc_tma_kernel<TT, WT, kPoints, kMesh><<<grid, block, smem, st>>>(*mt, *mw, tsdf, a);
+                      int tile, cudaStream_t st) {
+    if (mt && tile == kMcTileTma8) {
+        mc_launch_tma<TT, WT, kPoints, kMesh, 8>(tsdf, a, mt, mw, st);
+    } else if (mt && tile == kMcTileTma32) {
+        mc_launch_tma<TT, WT, kPoints, kMesh, 32>(tsdf, a, mt, mw, st);
+    } else if (mt) {
+        mc_launch_tma<TT, WT, kPoints, kMesh, 16>(tsdf, a, mt, mw, st);
     } else {
-        mc_kernel<TT, WT, kPoints, kMesh><<<grid, block, 0, st>>>(tsdf, weights, a);
+        const dim3 grid((unsigned)((a.vol.dims[0] - 2 + kMcX - 1) / kMcX),
+                        (unsigned)((a.vol.dims[1] - 2 + kMcY - 1) / kMcY), (unsigned)((a.vol.dims[2] - 2 + kMcZ - 1) / kMcZ));
+        mc_kernel<TT, WT, kPoints, kMesh><<<grid, dim3(kMcX, kMcY), 0, st>>>(tsdf, weights, a);
     }
 }
 
 template <class TT, class WT>
 static void mc_launch_any(const TT* tsdf, const WT* weights, const McArgs& a, const CUtensorMap* mt,
-                          const CUtensorMap* mw, bool P, bool M, dim3 grid, dim3 block, cudaStream_t st) {
-    if (P && M) mc_launch<TT, WT, true, true>(tsdf, weights, a, mt, mw, grid, block, st);
-    else if (P) mc_launch<TT, WT, true, false>(tsdf, weights, a, mt, mw, grid, block, st);
-    else mc_launch<TT, WT, false, true>(tsdf, weights, a, mt, mw, grid, block, st);
+                          const CUtensorMap* mw, bool P, bool M, int tile, cudaStream_t st) {
+    if (P && M) mc_launch<TT, WT, true, true>(tsdf, weights, a, mt, mw, tile, st);
+    else if (P) mc_launch<TT, WT, true, false>(tsdf, weights, a, mt, mw, tile, st);
+    else mc_launch<TT, WT, false, true>(tsdf, weights, a, mt, mw, tile, st);
 }
 
 int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
-                  unsigned* face_count, long face_cap, cudaStream_t st, int* error) {
+                  unsigned* face_count, long face_cap, cudaStream_t st, int* error, int tile) {
     int rc = upload_tables();
     if (rc) return rc;
     McArgs a;
@@ -426,25 +447,24 @@ int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& 
     a.error = error;
     const long ncubes = (long)(vol.dims[0] - 2) * (vol.dims[1] - 2) * (vol.dims[2] - 2);
     if (ncubes <= 0) return AFX_OK;
-    const dim3 grid((unsigned)((vol.dims[0] - 2 + kMcX - 1) / kMcX), (unsigned)((vol.dims[1] - 2 + kMcY - 1) / kMcY),
-                    (unsigned)((vol.dims[2] - 2 + kMcZ - 1) / kMcZ));
-    const dim3 block(kMcX, kMcY);
     const bool P = points != nullptr, M = verts != nullptr;
     if (!P && !M) return AFX_OK;
     // TMA bricks where the caller can receive a load-timeout report and the maps encode
     CUtensorMap mt, mw;
     const bool f16 = fmt == kVoxF16;
     const size_t elem = vox_bytes(fmt);
-    const bool tma = error && make_volume_map(&mt, tsdf, vol, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 :
-                                                                     CU_TENSOR_MAP_DATA_TYPE_FLOAT32, elem) &&
+    const int zr = tile == kMcTileTma8 ? 8 : tile == kMcTileTma32 ? 32 : 16;
+    const bool tma = error && tile != kMcTileColumn &&
+                     make_volume_map(&mt, tsdf, vol, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 :
+                                                           CU_TENSOR_MAP_DATA_TYPE_FLOAT32, elem, zr) &&
                      make_volume_map(&mw, weights, vol, f16 ? CU_TENSOR_MAP_DATA_TYPE_UINT16 :
-                                                              CU_TENSOR_MAP_DATA_TYPE_FLOAT32, elem);
+                                                              CU_TENSOR_MAP_DATA_TYPE_FLOAT32, elem, zr);
     if (f16)
         mc_launch_any(static_cast<const __half*>(tsdf), static_cast<const unsigned short*>(weights), a,
-                      tma ? &mt : nullptr, tma ? &mw : nullptr, P, M, grid, block, st);
+                      tma ? &mt : nullptr, tma ? &mw : nullptr, P, M, tile, st);
     else
         mc_launch_any(static_cast<const float*>(tsdf), static_cast<const float*>(weights), a, tma ? &mt : nullptr,
-                      tma ? &mw : nullptr, P, M, grid, block, st);
+                      tma ? &mw : nullptr, P, M, tile, st);
     AFX_LAUNCH_CHECK();
     if (M && vert_count) {
         mc_vert_count_kernel<<<1, 1, 0, st>>>(face_count, vert_count);

@@ -170,6 +170,19 @@ class FusionSession:
     def graph_count(self):
         return lib().afx_fusion_graph_count(self.h)
 
+    def set_tile(self, tile):
+        """Marching-cubes tile: 0 TMA 16 cubes along z (default), 1 TMA 8, 2 TMA 32, 3 column march."""
+        check(lib().afx_fusion_set_tile(self.h, int(tile)), "afx_fusion_set_tile")
+
+    def tile(self):
+        return lib().afx_fusion_get_tile(self.h)
+
+    def autotune(self):
+        """Time every marching-cubes tile on the current volume and keep the fastest: (tile, ms per tile)."""
+        t, ms = C.c_int(0), (C.c_float * 4)()
+        check(lib().afx_fusion_autotune(self.h, C.byref(t), ms, self._st()), "afx_fusion_autotune")
+        return t.value, list(ms)
+
     def set_timing(self, on=True):
         check(lib().afx_fusion_set_timing(self.h, int(on)), "afx_fusion_set_timing")
 
