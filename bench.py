@@ -167,6 +167,21 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def ncu_traffic(stage):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the stage's kernel from
+    the committed ncu summary of the same workload, or None."""
+    files = {"marching_cubes": "mc_tma_kernel_capsules256.md"}
+    if stage not in files:
+        return None
+    path = os.path.join(ROOT, "profiles", files[stage])
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("traffic_bytes_per_launch:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
 def stage_bytes(cfg, st):
     """Algorithmic bytes per frame of the stages with an exact HBM figure."""
     S = int(np.prod(cfg["dims"]))
@@ -532,7 +547,7 @@ def main():
     pick = dom if dom in algo else max(algo, key=lambda k: per_frame.get(k, 0.0))
     achieved = algo[pick] / (per_frame[pick] / 1000.0) / 1e9
     roof = {"bound": "hbm", "kernel": pick, "achieved": achieved, "peak": hbm, "unit": "GB/s",
-            "frac": achieved / hbm, "traffic": None,
+            "frac": achieved / hbm, "traffic": ncu_traffic(pick),
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"}
     if pick != dom:
         roof["note"] = "dominant stage is %s (%.3f ms/frame), latency-bound" % (dom, per_frame[dom])
