@@ -308,6 +308,8 @@ typedef struct afx_fusion_params {
     long triangle_capacity;
     int precision;               /* AFX_PRECISION_FP32 (the reference's DeviceTsdf<float>) or
                                     AFX_PRECISION_FP16: FP16 TSDF values + uint16 weights, 4 B/voxel */
+    int warp_mesh;               /* settings.isMeshWarped: warp the output mesh into the live frame
+                                    (details::warpMeshGPU, src/VolumeFusion.cu:75-110) */
 } afx_fusion_params;
 
 #define AFX_PRECISION_FP32 0
@@ -356,6 +358,9 @@ int afx_fusion_volume(afx_fusion* f, void** tsdf, void** weights, int* precision
 int afx_fusion_graph(afx_fusion* f, float** nodes, float** radii, float** transforms, int** n_nodes);
 int afx_fusion_centroid(afx_fusion* f, float** centroid);
 int afx_fusion_point_cloud(afx_fusion* f, float** points, unsigned** count);
+/* The frame's output mesh (runMarchingCubesFullKernel, src/VolumeFusion.cu:744-762): 3 vertices and
+ * one face per triangle, vertices translated by the frame-0 centroid and, with warp_mesh, warped
+ * into the live frame.  The canonical point cloud (afx_fusion_point_cloud) is not warped. */
 int afx_fusion_mesh(afx_fusion* f, float** vertices, unsigned** vertex_count, int** faces, unsigned** face_count);
 int afx_fusion_frame_views(afx_fusion* f, float** depth, float** vertices, float** normals);
 /* Overwrite the committed node transforms (host memory), e.g. to replay a trajectory. */

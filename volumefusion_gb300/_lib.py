@@ -29,7 +29,7 @@ class FusionParams(C.Structure):
                 ("gn_iterations", i32), ("lambda_depth", f32), ("lambda_reg", f32), ("energy_min_step", f32),
                 ("corr_thresh", f32), ("solver", i32), ("pcg_iterations", i32), ("pcg_tol", f64), ("integrate", i32),
                 ("extract_mesh", i32), ("node_capacity", i32), ("mesh_capacity", i64), ("triangle_capacity", i64),
-                ("precision", i32)]
+                ("precision", i32), ("warp_mesh", i32)]
 
 
 class FrameStats(C.Structure):

@@ -92,6 +92,9 @@ struct afx_fusion {
     float* mverts;
     int* mfaces;
     unsigned* nmverts;
+    uint32_t* vidx;        // output-mesh warp: KNN and weights per mesh vertex (warp_mesh only)
+    float* vdist;
+    float* vw;
     unsigned* nmfaces;
     WarpedVoxel* wvox;
     unsigned char* wcount;
@@ -284,6 +287,8 @@ static void session_layout(const afx_fusion_params& p, afx_fusion* f) {
     add(N * p.kreg * 4); add(N * p.kreg * 4);
     add(M * 12); add(M * 8); add(64); add(M * 4);
     add(p.triangle_capacity * 36); add(p.triangle_capacity * 12); add(64); add(64);
+    const long mesh_knn = p.warp_mesh ? p.triangle_capacity * 3 * p.knn * 4 : 0;  // output-mesh warp
+    add(mesh_knn); add(mesh_knn); add(mesh_knn);
     add(nbricks * 512 * sizeof(WarpedVoxel)); add(nbricks * 512);
     add(sizeof(FrameStats)); add(64);
     add(f->ws_sort_bytes); add(f->ws_graph_bytes); add(f->ws_corr_bytes); add(f->ws_support_bytes); add(f->ws_gn_bytes);
@@ -367,6 +372,10 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     f->mfaces = (int*)take(p.triangle_capacity * 12);
     f->nmverts = (unsigned*)take(64);
     f->nmfaces = (unsigned*)take(64);
+    const long mesh_knn = p.warp_mesh ? p.triangle_capacity * 3 * p.knn * 4 : 0;
+    f->vidx = (uint32_t*)take(mesh_knn);
+    f->vdist = (float*)take(mesh_knn);
+    f->vw = (float*)take(mesh_knn);
     f->wvox = (WarpedVoxel*)take(nbricks * 512 * sizeof(WarpedVoxel));
     f->wcount = (unsigned char*)take(nbricks * 512);
     f->stats = (FrameStats*)take(sizeof(FrameStats));
@@ -467,6 +476,24 @@ int afx_fusion_reset(afx_fusion* f, void* stream) {
     return AFX_OK;
 }
 
+// The output mesh of the frame, as the reference leaves it (src/VolumeFusion.cu:744-762): vertices
+// translated by the frame-0 centroid (runTranslateKernel) and, with warp_mesh (settings.isMeshWarped,
+// details::warpMeshGPU :75-110), warped into the live frame: the K nearest graph nodes of every
+// vertex (getKnnData over the host node positions), skinning weights with the d < r cut-off
+// (runComputeWarpWeightsKernel) and the blend of the committed transforms (runWarpKernel, in place).
+static int finish_output_mesh(afx_fusion* f, bool nonrigid, cudaStream_t st) {
+    const afx_fusion_params& p = f->p;
+    if (!p.extract_mesh) return AFX_OK;
+    const long vmax = p.triangle_capacity * 3;
+    int rc = translate_dev_impl(f->mverts, f->mverts, f->nmverts, vmax, f->centroid0, 1.f, st);
+    if (rc || !p.warp_mesh || !nonrigid) return rc;
+    rc = knn_impl(f->vidx, f->vdist, f->nodes_host, f->n_nodes, p.node_capacity, f->mverts, f->nmverts, vmax, p.knn, 0,
+                  st);
+    if (!rc) rc = warp_weights_impl(f->vw, f->radii, f->vidx, f->vdist, f->nmverts, vmax, p.knn, f->n_nodes, st);
+    if (!rc) rc = warp_impl(f->mverts, f->mverts, f->T, f->vidx, f->vw, f->nmverts, vmax, p.knn, st);
+    return rc;
+}
+
 static int extract_frame_mesh(afx_fusion* f, int cur, cudaStream_t st) {
     // canonical point cloud for the next frame (runMarchingCubesMeshKernel on the volume the next
     // frame starts from) and, if asked, the output mesh (runMarchingCubesFullKernel), in one pass
@@ -511,6 +538,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
         if (rc) return rc;
         stage_mark(f, ST_MC, st);
         rc = extract_frame_mesh(f, cur, st);
+        if (!rc) rc = finish_output_mesh(f, false, st);
         if (rc) return rc;
         stage_mark(f, -1, st);
         stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame_dev, f->n_nodes, f->n_old, f->mesh_used, f->ncorr, f->gn.state,
@@ -650,6 +678,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
     }
     stage_mark(f, ST_MC, st);
     rc = extract_frame_mesh(f, cur, st);
+    if (!rc) rc = finish_output_mesh(f, true, st);
     if (rc) return rc;
     stage_mark(f, -1, st);
     stats_kernel<<<1, 1, 0, st>>>(f->stats, f->frame_dev, f->n_nodes, f->n_old, f->mesh_used, f->ncorr, f->gn.state,

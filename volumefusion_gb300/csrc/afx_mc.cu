@@ -749,16 +749,15 @@ __global__ void translate_kernel(float* pts, const unsigned* count, long n_max, 
 
 __global__ void translate_dev_kernel(float* dst, const float* src, const unsigned* count, long n_max, const float* t,
                                      float sign) {
-    long n = count ? min((long)*count, n_max) : n_max;
-    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    for (int c = 0; c < 3; ++c) dst[3 * i + c] = src[3 * i + c] + sign * t[c];
+    const long n = count ? min((long)*count, n_max) : n_max;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        for (int c = 0; c < 3; ++c) dst[3 * i + c] = src[3 * i + c] + sign * t[c];
 }
 
 int translate_dev_impl(float* dst, const float* src, const unsigned* count, long n_max, const float* t_dev, float sign,
                        cudaStream_t st) {
     if (n_max <= 0) return AFX_OK;
-    translate_dev_kernel<<<blocks_for(n_max, 256), 256, 0, st>>>(dst, src, count, n_max, t_dev, sign);
+    translate_dev_kernel<<<grid_for(n_max, 256), 256, 0, st>>>(dst, src, count, n_max, t_dev, sign);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
