@@ -37,7 +37,8 @@ typedef enum afx_status {
     AFX_ERR_WORKSPACE = 5,       /* workspace too small */
     AFX_ERR_UNSUPPORTED = 6,     /* input outside what this implementation supports */
     AFX_ERR_TIMEOUT = 7,         /* a bounded device-side wait gave up */
-    AFX_ERR_NO_MEMORY = 8
+    AFX_ERR_NO_MEMORY = 8,
+    AFX_ERR_IO = 9               /* a file could not be opened, read or written */
 } afx_status;
 
 #define AFX_INVALID_INDEX 0xFFFFFFFFu
@@ -449,6 +450,29 @@ int afx_batch_process(afx_batch* b, const uint16_t* const* depth_mm, void* strea
 int afx_batch_stats(afx_batch* b, afx_frame_stats* out, int n);
 /* Parent-graph launches so far (one per afx_batch_process with a replayed session). */
 long afx_batch_graph_launches(const afx_batch* b);
+
+/* ------------------------------------------------------------------------------------
+ * On-disk formats of the reference (host arrays; the session helpers copy device state).
+ * afx_save_ply: Mesh::savePly (src/Mesh.cpp:23-64), ASCII PLY with float x y z + uchar rgb per
+ *   vertex (colors may be NULL: 0 0 0) and "3 a b c" faces; refuses an empty vertex list.
+ * afx_tsdf_save / afx_tsdf_load: TSDFVolume::save / load (src/TSDFVolume.cpp:315-361): int32 dims,
+ *   the volume size and voxel size (the 24 bytes the reference writes from m_size), float delta,
+ *   float tsdf[S], float weights[S], then colour arrays (written as 127 with colour weights 0;
+ *   ignored on load).  afx_tsdf_load reads the values and weights of a volume of n_voxels voxels.
+ * afx_fusion_save_volume / afx_fusion_load_volume: the session's volume in that format (FP16
+ *   sessions widen on save and round to nearest binary16 on load; weights must be integers 0..65535);
+ *   the loaded file must have the session's dims.  afx_fusion_save_mesh_ply: the frame's output
+ *   mesh.  All three synchronise `stream`.
+ * ------------------------------------------------------------------------------------ */
+int afx_save_ply(const char* path, const float* vertices, long n_vertices, const unsigned char* colors,
+                 const int* faces, long n_faces);
+int afx_tsdf_save(const char* path, const int dims[3], const float volume_size[3], const float voxel_size[3],
+                  float delta, const float* tsdf, const float* weights);
+int afx_tsdf_load_header(const char* path, int dims[3], float volume_size[3], float voxel_size[3], float* delta);
+int afx_tsdf_load(const char* path, float* tsdf, float* weights, long n_voxels);
+int afx_fusion_save_volume(afx_fusion* f, const char* path, void* stream);
+int afx_fusion_load_volume(afx_fusion* f, const char* path, void* stream);
+int afx_fusion_save_mesh_ply(afx_fusion* f, const char* path, void* stream);
 
 /* Stream-ordered device-to-device copy (helper for bindings that hold raw device views). */
 int afx_copy_device(void* dst, const void* src, size_t bytes, void* stream);

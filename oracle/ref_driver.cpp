@@ -157,4 +157,45 @@ void ref_warp(const float* nodes, const float* radii, const float* T, int n, con
         for (int c = 0; c < 3; ++c) out[3 * i + c] = W[i][c];
 }
 
+// Mesh::savePly (src/Mesh.cpp:23-64) of the given vertices (and colours, 0 if null) and faces.
+int ref_save_ply(const char* path, const float* v, long nv, const unsigned char* rgb, const int* faces, long nf) {
+    Mesh mesh;
+    for (long i = 0; i < nv; ++i) {
+        Vec3b c(rgb ? rgb[3 * i] : 0, rgb ? rgb[3 * i + 1] : 0, rgb ? rgb[3 * i + 2] : 0);
+        mesh.addVertex(Vec3f(v[3 * i], v[3 * i + 1], v[3 * i + 2]), c);
+    }
+    for (long i = 0; i < nf; ++i) mesh.faces().push_back(Vec3i(faces[3 * i], faces[3 * i + 1], faces[3 * i + 2]));
+    return mesh.savePly(path) ? 0 : 1;
+}
+
+// TSDFVolume::save (src/TSDFVolume.cpp:343-361) of a volume holding the given values and weights.
+int ref_tsdf_save(const char* path, const int* dims, const float* size, float delta, const float* tsdf,
+                  const float* weights) {
+    TSDFVolume vol(Vec3i(dims[0], dims[1], dims[2]), Vec3f(size[0], size[1], size[2]), Mat3f::Identity());
+    vol.setDelta(delta);
+    std::memcpy(vol.ptrTsdf(), tsdf, sizeof(float) * vol.gridSize());
+    std::memcpy(vol.ptrTsdfWeights(), weights, sizeof(float) * vol.gridSize());
+    return vol.save(path) ? 0 : 1;
+}
+
+// TSDFVolume::load (src/TSDFVolume.cpp:315-341): dims, size, voxel size and delta as loaded, and the
+// values and weights (cap voxels at most).
+long ref_tsdf_load(const char* path, int* dims, float* size, float* voxel_size, float* delta, float* tsdf,
+                   float* weights, long cap) {
+    TSDFVolume vol(Vec3i(1, 1, 1), Vec3f(1.f, 1.f, 1.f), Mat3f::Identity());
+    if (!vol.load(path)) return -1;
+    Vec3i d = vol.dimensions();
+    Vec3f sz = vol.size(), vs = vol.voxelSize();
+    for (int c = 0; c < 3; ++c) {
+        dims[c] = d[c];
+        size[c] = sz[c];
+        voxel_size[c] = vs[c];
+    }
+    *delta = vol.delta();
+    const long n = (long)vol.gridSize() < cap ? (long)vol.gridSize() : cap;
+    std::memcpy(tsdf, vol.ptrTsdf(), sizeof(float) * n);
+    std::memcpy(weights, vol.ptrTsdfWeights(), sizeof(float) * n);
+    return (long)vol.gridSize();
+}
+
 }  // extern "C"

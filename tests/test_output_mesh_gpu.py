@@ -49,3 +49,35 @@ def test_output_mesh_translated_and_warped():
     assert not np.array_equal(_tri_rows(v1), _tri_rows(v0))  # the graph has moved
     plain.close()
     warped.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_session_volume_and_mesh_files(tmp_path, precision):
+    """afx_fusion_save_volume writes the session's volume in TSDFVolume::save's format;
+    afx_fusion_load_volume brings it back into a fresh session unchanged (FP16 values round-trip
+    exactly through the widened file); afx_fusion_save_mesh_ply writes the frame's output mesh."""
+    from volumefusion_gb300 import configs, formats
+    from volumefusion_gb300.fusion import FusionSession
+    cfg = dict(configs.small_nonrigid(n_frames=3), precision=precision)
+    frames = configs.small_frames(cfg)
+    s = FusionSession(cfg)
+    for mm in frames:
+        s.process(mm)
+    t, w = (x.cpu().numpy() for x in s.tsdf())
+    path = tmp_path / "vol.tsdf"
+    s.save_volume(path)
+    t2, w2, dims, size, vs, delta = formats.load_tsdf(path)
+    assert np.array_equal(t2.ravel(), t) and np.array_equal(w2.ravel(), w)
+    assert list(dims) == list(cfg["dims"]) and np.array_equal(vs, configs.voxel_size(cfg))
+    assert delta == np.float32(cfg["delta"])
+    s2 = FusionSession(cfg)
+    s2.load_volume(path)
+    t3, w3 = (x.cpu().numpy() for x in s2.tsdf())
+    assert np.array_equal(t3, t) and np.array_equal(w3, w)
+    ply = tmp_path / "mesh.ply"
+    s.save_mesh_ply(ply)
+    v, f = s.mesh()
+    head = ply.read_text().split("end_header\n")[0]
+    assert "element vertex %d\n" % len(v) in head and "element face %d\n" % len(f) in head
+    s.close()
+    s2.close()

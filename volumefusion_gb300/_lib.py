@@ -119,6 +119,13 @@ SIGNATURES = {
     "afx_fusion_set_transforms": (i32, [vp, vp, i32, vp]),
     "afx_fusion_kernel_launches": (i64, [vp]),
     "afx_copy_device": (i32, [vp, vp, sz, vp]),
+    "afx_save_ply": (i32, [C.c_char_p, vp, C.c_long, vp, vp, C.c_long]),
+    "afx_tsdf_save": (i32, [C.c_char_p, vp, vp, vp, f32, vp, vp]),
+    "afx_tsdf_load_header": (i32, [C.c_char_p, vp, vp, vp, vp]),
+    "afx_tsdf_load": (i32, [C.c_char_p, vp, vp, C.c_long]),
+    "afx_fusion_save_volume": (i32, [vp, C.c_char_p, vp]),
+    "afx_fusion_load_volume": (i32, [vp, C.c_char_p, vp]),
+    "afx_fusion_save_mesh_ply": (i32, [vp, C.c_char_p, vp]),
     "afx_fusion_set_timing": (i32, [vp, i32]),
     "afx_fusion_stage_times": (i32, [vp, C.POINTER(f64), i32, i32]),
 }

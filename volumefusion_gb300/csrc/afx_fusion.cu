@@ -15,6 +15,8 @@
 #include <new>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "afx_gn.h"
 #include "afx_voxel.h"
 
@@ -213,6 +215,7 @@ const char* afx_status_string(int s) {
         case AFX_ERR_UNSUPPORTED: return "unsupported input";
         case AFX_ERR_TIMEOUT: return "device wait timed out";
         case AFX_ERR_NO_MEMORY: return "out of device memory";
+        case AFX_ERR_IO: return "file input/output failed";
     }
     return "unknown status";
 }
@@ -1132,3 +1135,78 @@ long afx_batch_graph_launches(const afx_batch* b) { return b ? b->graph_launches
 
 }  // extern "C"
 
+// ------------------------------------------------------------------------------------
+// Session volume and mesh to and from the reference's file formats (afx_io.cu)
+// ------------------------------------------------------------------------------------
+
+extern "C" {
+
+int afx_fusion_save_volume(afx_fusion* f, const char* path, void* stream) {
+    if (!f || !path) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    const size_t S = (size_t)f->S;
+    std::vector<float> t(S), w(S);
+    if (f->fmt == kVoxF16) {
+        std::vector<__half> th(S);
+        std::vector<unsigned short> wh(S);
+        AFX_CUDA(cudaMemcpyAsync(th.data(), f->tsdf, 2 * S, cudaMemcpyDeviceToHost, st));
+        AFX_CUDA(cudaMemcpyAsync(wh.data(), f->weights, 2 * S, cudaMemcpyDeviceToHost, st));
+        AFX_CUDA(cudaStreamSynchronize(st));
+        for (size_t i = 0; i < S; ++i) {
+            t[i] = __half2float(th[i]);  // exact widening
+            w[i] = (float)wh[i];
+        }
+    } else {
+        AFX_CUDA(cudaMemcpyAsync(t.data(), f->tsdf, 4 * S, cudaMemcpyDeviceToHost, st));
+        AFX_CUDA(cudaMemcpyAsync(w.data(), f->weights, 4 * S, cudaMemcpyDeviceToHost, st));
+        AFX_CUDA(cudaStreamSynchronize(st));
+    }
+    return afx_tsdf_save(path, f->p.dims, f->p.volume_size, f->vol.vs, f->p.delta, t.data(), w.data());
+}
+
+int afx_fusion_load_volume(afx_fusion* f, const char* path, void* stream) {
+    if (!f || !path) return AFX_ERR_INVALID_ARGUMENT;
+    int dims[3];
+    int rc = afx_tsdf_load_header(path, dims, nullptr, nullptr, nullptr);
+    if (rc) return rc;
+    if (dims[0] != f->p.dims[0] || dims[1] != f->p.dims[1] || dims[2] != f->p.dims[2]) return AFX_ERR_INVALID_ARGUMENT;
+    const size_t S = (size_t)f->S;
+    std::vector<float> t(S), w(S);
+    rc = afx_tsdf_load(path, t.data(), w.data(), (long)S);
+    if (rc) return rc;
+    cudaStream_t st = as_stream(stream);
+    if (f->fmt == kVoxF16) {
+        std::vector<__half> th(S);
+        std::vector<unsigned short> wh(S);
+        for (size_t i = 0; i < S; ++i) {
+            if (!(w[i] >= 0.f && w[i] <= 65535.f) || w[i] != (float)(unsigned short)w[i]) return AFX_ERR_UNSUPPORTED;
+            th[i] = __float2half_rn(t[i]);
+            wh[i] = (unsigned short)w[i];
+        }
+        AFX_CUDA(cudaMemcpyAsync(f->tsdf, th.data(), 2 * S, cudaMemcpyHostToDevice, st));
+        AFX_CUDA(cudaMemcpyAsync(f->weights, wh.data(), 2 * S, cudaMemcpyHostToDevice, st));
+    } else {
+        AFX_CUDA(cudaMemcpyAsync(f->tsdf, t.data(), 4 * S, cudaMemcpyHostToDevice, st));
+        AFX_CUDA(cudaMemcpyAsync(f->weights, w.data(), 4 * S, cudaMemcpyHostToDevice, st));
+    }
+    AFX_CUDA(cudaStreamSynchronize(st));
+    return AFX_OK;
+}
+
+int afx_fusion_save_mesh_ply(afx_fusion* f, const char* path, void* stream) {
+    if (!f || !path) return AFX_ERR_INVALID_ARGUMENT;
+    if (!f->p.extract_mesh) return AFX_ERR_UNSUPPORTED;
+    cudaStream_t st = as_stream(stream);
+    unsigned nf = 0;
+    AFX_CUDA(cudaMemcpyAsync(&nf, f->nmfaces, 4, cudaMemcpyDeviceToHost, st));
+    AFX_CUDA(cudaStreamSynchronize(st));
+    const long faces = nf < (unsigned long)f->p.triangle_capacity ? (long)nf : f->p.triangle_capacity;
+    std::vector<float> v(9 * (size_t)faces);
+    std::vector<int> fc(3 * (size_t)faces);
+    AFX_CUDA(cudaMemcpyAsync(v.data(), f->mverts, v.size() * 4, cudaMemcpyDeviceToHost, st));
+    AFX_CUDA(cudaMemcpyAsync(fc.data(), f->mfaces, fc.size() * 4, cudaMemcpyDeviceToHost, st));
+    AFX_CUDA(cudaStreamSynchronize(st));
+    return afx_save_ply(path, v.data(), 3 * faces, nullptr, fc.data(), faces);
+}
+
+}  // extern "C"

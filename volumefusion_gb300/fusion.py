@@ -171,6 +171,18 @@ class FusionSession:
     def graph_count(self):
         return lib().afx_fusion_graph_count(self.h)
 
+    def save_volume(self, path):
+        """The volume in TSDFVolume::save's file format (FP16 sessions are widened)."""
+        check(lib().afx_fusion_save_volume(self.h, str(path).encode(), self._st()), "afx_fusion_save_volume")
+
+    def load_volume(self, path):
+        """Replace the volume with a TSDFVolume file of the same dims."""
+        check(lib().afx_fusion_load_volume(self.h, str(path).encode(), self._st()), "afx_fusion_load_volume")
+
+    def save_mesh_ply(self, path):
+        """The frame's output mesh as Mesh::savePly writes it."""
+        check(lib().afx_fusion_save_mesh_ply(self.h, str(path).encode(), self._st()), "afx_fusion_save_mesh_ply")
+
     def set_tile(self, tile):
         """Marching-cubes tile: 0 TMA 16 cubes along z (default), 1 TMA 8, 2 TMA 32, 3 column march."""
         check(lib().afx_fusion_set_tile(self.h, int(tile)), "afx_fusion_set_tile")
