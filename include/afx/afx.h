@@ -452,6 +452,42 @@ int afx_batch_stats(afx_batch* b, afx_frame_stats* out, int n);
 long afx_batch_graph_launches(const afx_batch* b);
 
 /* ------------------------------------------------------------------------------------
+ * Rigid multi-camera reconstruction stream (af::startMeshReconstructionStream,
+ * src/MeshRecontructionStream.cu:115-206; settings in src/Settings.cpp).  Each frame: every
+ * camera's depth (uint16 mm, device) is converted, filtered (depth_threshold), bilateral-filtered
+ * when enabled, back-projected with its intrinsics and moved to world space by camera_to_world (the
+ * inverse of the reference's world2camera.txt, DeviceDepthImage::backProject); the clouds are
+ * concatenated in camera order (n_cameras * width * height points, invalid pixels included).  The
+ * volume is re-initialised and camera 0's filtered depth alone is integrated at `center` with
+ * `rotation` (the reference's DeviceTsdf::integrate of cameras[0]); the full marching-cubes mesh
+ * follows (3 vertices and a face per triangle, untranslated).  Lens undistortion is not applied:
+ * frames must already be undistorted.  Asynchronous on `stream`; outputs are device views.
+ * ------------------------------------------------------------------------------------ */
+#define AFX_MAX_CAMERAS 8
+typedef struct afx_rigid_stream_params {
+    int n_cameras;
+    int width, height;                          /* every camera's frame size */
+    float K[AFX_MAX_CAMERAS][9];                /* column-major intrinsics per camera */
+    float camera_to_world[AFX_MAX_CAMERAS][16]; /* column-major 4x4 per camera */
+    int dims[3];                                /* settings.tsdfDim */
+    float volume_size[3];                       /* settings.tsdfSize */
+    float delta;                                /* settings.tsdfDelta */
+    float center[3];                            /* settings.tsdfCenter */
+    float rotation[9];                          /* column-major, the rotation settings.tsdfRotation gives */
+    float depth_threshold;
+    int bilateral, bilateral_r;
+    float sigma_i, sigma_s, bilateral_thr;
+    long triangle_capacity;
+} afx_rigid_stream_params;
+typedef struct afx_rigid_stream afx_rigid_stream;
+void afx_rigid_stream_default_params(afx_rigid_stream_params* p);
+int afx_rigid_stream_create(const afx_rigid_stream_params* params, afx_rigid_stream** out);
+int afx_rigid_stream_destroy(afx_rigid_stream* s);
+int afx_rigid_stream_process(afx_rigid_stream* s, const uint16_t* const* depth_mm, void* stream);
+int afx_rigid_stream_outputs(afx_rigid_stream* s, float** cloud, long* cloud_points, float** vertices,
+                             unsigned** vertex_count, int** faces, unsigned** face_count, float** tsdf, float** weights);
+
+/* ------------------------------------------------------------------------------------
  * On-disk formats of the reference (host arrays; the session helpers copy device state).
  * afx_save_ply: Mesh::savePly (src/Mesh.cpp:23-64), ASCII PLY with float x y z + uchar rgb per
  *   vertex (colors may be NULL: 0 0 0) and "3 a b c" faces; refuses an empty vertex list.

@@ -52,6 +52,7 @@ def lib():
             "vfo_round_half": (C.c_float, [C.c_float]),
             "vfo_mc_pointcloud": (C.c_long, [f32p, f32p, i32p, f32p, f32p, C.c_float, f32p, C.c_long]),
             "vfo_sort_unique_vec3": (C.c_long, [f32p, C.c_long]),
+            "vfo_transform_points": (None, [f32p, C.c_long, f32p]),
             "vfo_mc_full": (C.c_long, [f32p, f32p, i32p, f32p, f32p, C.c_float, f32p, C.c_long, i32p, C.c_long,
                                        C.POINTER(C.c_long)]),
             "vfo_translate": (None, [f32p, C.c_long, f32p]),
@@ -241,6 +242,13 @@ def mc_full(tsdf, weights, dims, voxel_size, volume_size, iso=0.0, cap=None):
                            cap, faces, cap, C.byref(nf))
     assert nv <= cap
     return verts[:nv].copy(), faces[:nf.value].copy()
+
+
+def transform_points(pts, T):
+    """(T * [p; 1]).head(3) for every point; T (4, 4) column-major flattened or a (4, 4) matrix."""
+    p = _f32(pts).reshape(-1, 3).copy()
+    lib().vfo_transform_points(p, len(p), kcol(T) if np.shape(T) == (4, 4) else _f32(T))
+    return p
 
 
 def translate(pts, t):

@@ -484,6 +484,15 @@ long vfo_sort_unique_vec3(real* pts, long n) {
     return m;
 }
 
+void vfo_transform_points(real* pts, long n, const real T[16]) {
+    // transformKernel (src/VertexManipulation.cu:89-95): p <- (T * [p; 1]).head(3)
+    for (long i = 0; i < n; ++i) {
+        real q[3];
+        mat4_point(T, pts + 3 * i, q);
+        std::memcpy(pts + 3 * i, q, 3 * sizeof(real));
+    }
+}
+
 void vfo_translate(real* pts, long n, const real t[3]) {
     // translateKernel (src/VertexManipulation.cu:73-79)
     for (long i = 0; i < n; ++i)

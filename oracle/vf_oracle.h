@@ -64,6 +64,7 @@ long vfo_sort_unique_vec3(VFO_REAL* pts, long n);
 long vfo_mc_full(const VFO_REAL* tsdf, const VFO_REAL* weights, const int dims[3], const VFO_REAL voxel_size[3],
                  const VFO_REAL volume_size[3], VFO_REAL iso, VFO_REAL* verts, long vcap, int* faces, long fcap, long* nfaces);
 void vfo_translate(VFO_REAL* pts, long n, const VFO_REAL t[3]);
+void vfo_transform_points(VFO_REAL* pts, long n, const VFO_REAL T[16]);
 
 /* ---- motion graph (src/GraphBuilder.cpp, src/MotionGraph.cpp, include/af/GraphBuilder.h) ---- */
 int vfo_build_graph(VFO_REAL* nodes, VFO_REAL* radii, VFO_REAL* transforms, int n_nodes, int cap, const VFO_REAL* mesh, long m,

@@ -119,6 +119,12 @@ SIGNATURES = {
     "afx_fusion_set_transforms": (i32, [vp, vp, i32, vp]),
     "afx_fusion_kernel_launches": (i64, [vp]),
     "afx_copy_device": (i32, [vp, vp, sz, vp]),
+    "afx_rigid_stream_default_params": (None, [vp]),
+    "afx_rigid_stream_create": (i32, [vp, C.POINTER(vp)]),
+    "afx_rigid_stream_destroy": (i32, [vp]),
+    "afx_rigid_stream_process": (i32, [vp, C.POINTER(vp), vp]),
+    "afx_rigid_stream_outputs": (i32, [vp, C.POINTER(vp), C.POINTER(C.c_long), C.POINTER(vp), C.POINTER(vp),
+                                       C.POINTER(vp), C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
     "afx_save_ply": (i32, [C.c_char_p, vp, C.c_long, vp, vp, C.c_long]),
     "afx_tsdf_save": (i32, [C.c_char_p, vp, vp, vp, f32, vp, vp]),
     "afx_tsdf_load_header": (i32, [C.c_char_p, vp, vp, vp, vp]),
@@ -131,6 +137,17 @@ SIGNATURES = {
 }
 
 _lib = None
+
+
+MAX_CAMERAS = 8
+
+
+class RigidStreamParams(C.Structure):
+    _fields_ = [("n_cameras", i32), ("width", i32), ("height", i32), ("K", (f32 * 9) * MAX_CAMERAS),
+                ("camera_to_world", (f32 * 16) * MAX_CAMERAS), ("dims", i32 * 3), ("volume_size", f32 * 3),
+                ("delta", f32), ("center", f32 * 3), ("rotation", f32 * 9), ("depth_threshold", f32),
+                ("bilateral", i32), ("bilateral_r", i32), ("sigma_i", f32), ("sigma_s", f32), ("bilateral_thr", f32),
+                ("triangle_capacity", i64)]
 
 
 class AfxError(RuntimeError):
