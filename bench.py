@@ -43,6 +43,7 @@ def parse():
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-rigid-stream", action="store_true")
     ap.add_argument("--served-streams", type=int, default=64)
     ap.add_argument("--served-seconds", type=float, default=4.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -192,6 +193,88 @@ def stage_bytes(cfg, st):
         "marching_cubes": 8.0 * S + 12.0 * st["mesh_points"] * 4 + 48.0 * st["mesh_faces"],
         "warped_integrate": 16.0 * A if A else None,
     }
+
+
+def rigid_stream_arm(args, stream, barrier, reduce_max, world, hbm):
+    """The rigid multi-camera stream at the reference's default volume (400^3 over 1 m, rotated
+    45/-45/0 degrees): 3 cameras of 640x576 capsule frames, 30 frames per step; and the fused
+    initialise + integrate kernel timed alone on that volume (8 B per voxel written)."""
+    import ctypes as C
+
+    import torch
+    from volumefusion_gb300 import configs
+    from volumefusion_gb300._lib import check, lib
+    from volumefusion_gb300.rigid_stream import RigidStream
+
+    cfg = configs.nonrigid_capsules_256(n_frames=N_FRAMES)
+    frames = [torch.from_numpy(f.astype(np.int16)).cuda() for f in configs.capsule_frames(cfg)]
+    K = np.asarray(cfg["K"], np.float32)
+
+    def rot(axis, deg):
+        a = np.radians(deg)
+        c, s_ = np.cos(a), np.sin(a)
+        return {"x": np.array([[1, 0, 0], [0, c, -s_], [0, s_, c]]), "y": np.array([[c, 0, s_], [0, 1, 0], [-s_, 0, c]]),
+                "z": np.array([[c, -s_, 0], [s_, c, 0], [0, 0, 1]])}[axis]
+
+    def pose(R, t):
+        T = np.eye(4)
+        T[:3, :3], T[:3, 3] = R, t
+        return T
+
+    c2w = [np.eye(4), pose(rot("y", 20), [0.15, 0.0, 0.05]), pose(rot("x", -15), [0.0, -0.1, 0.02])]
+    mm0 = frames[0].cpu().numpy().astype(np.float64)
+    v, u = np.nonzero(mm0 > 0)
+    z = mm0[v, u] / 1000.0
+    center = [float(np.mean((u - K[0, 2]) * z / K[0, 0])), float(np.mean((v - K[1, 2]) * z / K[1, 1])), float(np.mean(z))]
+    R = (rot("x", 45) @ rot("y", -45)).astype(np.float32)  # settings.tsdfRotation default (45, -45, 0)
+    dims, size = (400, 400, 400), (1.0, 1.0, 1.0)
+    rs = RigidStream([K] * 3, c2w, cfg["width"], cfg["height"], dims, size, 0.016, center, R, stream=stream)
+    nf = N_FRAMES
+
+    def run(steps):
+        with torch.cuda.stream(stream):
+            for _ in range(steps):
+                for i in range(nf):
+                    rs.process([frames[i], frames[(i + 10) % nf], frames[(i + 20) % nf]])
+
+    run(1)
+    barrier()
+    steps = max(1, min(3, args.steps))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    run(steps)
+    e1.record(stream)
+    barrier()
+    fps = world * steps * nf / (reduce_max(e0.elapsed_time(e1)) / 1000.0)
+    _, verts, _, _, _ = rs.outputs()
+    rs.close()
+    # the fused initialise + integrate kernel alone, on a volume of the same size
+    S = int(np.prod(dims))
+    tsdf = torch.empty(S, device="cuda")
+    weights = torch.empty(S, device="cuda")
+    depth = (frames[0].float() * 0.001).contiguous()
+    f = lambda a: (C.c_float * len(a))(*[float(x) for x in a])  # noqa: E731
+    col = lambda m: f(np.asarray(m, np.float64).T.ravel())  # noqa: E731
+    args_c = (C.c_void_p(tsdf.data_ptr()), C.c_void_p(weights.data_ptr()), C.c_void_p(depth.data_ptr()),
+              cfg["width"], cfg["height"], C.c_float(0.016), (C.c_int * 3)(*dims), f([s_ / d for s_, d in zip(size, dims)]),
+              f(size), col(R), f(center), col(K), C.c_void_p(stream.cuda_stream))
+    for _ in range(3):
+        check(lib().afx_integrate_tsdf_fresh(*args_c), "afx_integrate_tsdf_fresh")
+    reps = 20
+    barrier()
+    e0.record(stream)
+    for _ in range(reps):
+        check(lib().afx_integrate_tsdf_fresh(*args_c), "afx_integrate_tsdf_fresh")
+    e1.record(stream)
+    barrier()
+    ms = e0.elapsed_time(e1) / reps
+    gbs = 8.0 * S / (ms / 1000.0) / 1e9
+    del tsdf, weights
+    torch.cuda.empty_cache()
+    return {"cameras": 3, "volume": "400^3 over 1 m, rotated (45, -45, 0) deg", "frames_per_s": fps,
+            "mesh_vertices_last_frame": int(verts.shape[0]),
+            "fresh_integration": {"ms": ms, "bytes": 8 * S, "achieved_gbs": gbs, "peak_gbs": hbm, "frac": gbs / hbm,
+                                  "note": "write-only: 8 B per voxel; outputs (512 MB) larger than L2"}}
 
 
 def batched_arm(args, stream, barrier, reduce_max, world):
@@ -527,6 +610,12 @@ def main():
                                "session_bytes": session_bytes(pcfg), "n_nodes_last_frame": pst["n_nodes"],
                                "error": pst["error"], "stage_ms_per_frame": pstage}
 
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    hbm_peak = json.load(open(peaks_path)).get("hbm_gbs", 6800.0) if os.path.exists(peaks_path) else 6800.0
+    rigid = None
+    if not args.no_rigid_stream:
+        rigid = rigid_stream_arm(args, stream, barrier, reduce_max, world, hbm_peak)
+
     batched = None
     if not args.no_batched:
         batched = batched_arm(args, stream, barrier, reduce_max, world)
@@ -582,6 +671,7 @@ def main():
             "dense_graph": dense,
             "precision": precision,
             "batched": batched,
+            "rigid_stream": rigid,
             "served": served,
             "roofline": roof,
             "cpu_baseline": cpu,

@@ -451,6 +451,14 @@ int afx_batch_stats(afx_batch* b, afx_frame_stats* out, int n);
 /* Parent-graph launches so far (one per afx_batch_process with a replayed session). */
 long afx_batch_graph_launches(const afx_batch* b);
 
+/* DeviceTsdf::initDefault followed by runIntegrateTSDFFromFrameKernel (include/af/DeviceTsdf.cuh:26-35),
+ * in one write-only pass over the volume (8 B per voxel written): the same values and weights as
+ * initialising the volume and integrating the frame.  Needs dims[0] % 4 == 0 and 16-byte aligned
+ * arrays (AFX_ERR_UNSUPPORTED otherwise). */
+int afx_integrate_tsdf_fresh(float* tsdf, float* weights, const float* depth, int width, int height, float delta,
+                             const int dims[3], const float voxel_size[3], const float volume_size[3],
+                             const float rotate[9], const float translate[3], const float K[9], void* stream);
+
 /* ------------------------------------------------------------------------------------
  * Rigid multi-camera reconstruction stream (af::startMeshReconstructionStream,
  * src/MeshRecontructionStream.cu:115-206; settings in src/Settings.cpp).  Each frame: every

@@ -76,3 +76,35 @@ def test_rigid_stream_matches_oracle():
         assert np.array_equal(_tri_rows(verts), _tri_rows(ev))
         assert np.array_equal(faces.ravel(), np.arange(len(verts), dtype=np.int32))
     st.close()
+
+
+def test_fresh_integration_equals_initialise_then_integrate():
+    """afx_integrate_tsdf_fresh (one write-only pass) gives the values and weights of
+    DeviceTsdf::initDefault followed by runIntegrateTSDFFromFrameKernel, at a rotated pose."""
+    import ctypes as C
+
+    from volumefusion_gb300 import af, configs
+    from volumefusion_gb300._lib import check, lib
+    cfg, [mm] = configs.rigid_sphere_128()
+    depth, _, _, cen = O.frame_prep(mm, cfg["K"])
+    d = torch.from_numpy(depth).cuda()
+    dims, size = cfg["dims"], cfg["volume_size"]
+    vs = configs.voxel_size(cfg)
+    R = _rot("y", 12).astype(np.float32)
+    S = int(np.prod(dims))
+    t1 = torch.full((S,), -1.0, device="cuda")
+    w1 = torch.zeros(S, device="cuda")
+    af.runIntegrateTSDFFromFrameKernel(t1, w1, d, (cfg["width"], cfg["height"]), cfg["delta"], dims, vs, size, R, cen,
+                                       cfg["K"])
+    t2 = torch.full((S,), 7.0, device="cuda")  # garbage: every voxel must be written
+    w2 = torch.full((S,), 7.0, device="cuda")
+    f = lambda a: (C.c_float * len(a))(*[float(x) for x in a])  # noqa: E731
+    col = lambda m: f(np.asarray(m, np.float64).T.ravel())  # noqa: E731
+    check(lib().afx_integrate_tsdf_fresh(C.c_void_p(t2.data_ptr()), C.c_void_p(w2.data_ptr()), C.c_void_p(d.data_ptr()),
+                                         cfg["width"], cfg["height"], C.c_float(cfg["delta"]),
+                                         (C.c_int * 3)(*dims), f(vs), f(size), col(R), f(cen), col(cfg["K"]),
+                                         C.c_void_p(torch.cuda.current_stream().cuda_stream)), "fresh")
+    torch.cuda.synchronize()
+    assert int((w1 > 0).sum()) > 1000
+    assert torch.equal(t1.view(torch.int32), t2.view(torch.int32))  # bit for bit, signed zeros included
+    assert torch.equal(w1.view(torch.int32), w2.view(torch.int32))

@@ -119,6 +119,7 @@ SIGNATURES = {
     "afx_fusion_set_transforms": (i32, [vp, vp, i32, vp]),
     "afx_fusion_kernel_launches": (i64, [vp]),
     "afx_copy_device": (i32, [vp, vp, sz, vp]),
+    "afx_integrate_tsdf_fresh": (i32, [vp, vp, vp, i32, i32, f32, vp, vp, vp, vp, vp, vp, vp]),
     "afx_rigid_stream_default_params": (None, [vp]),
     "afx_rigid_stream_create": (i32, [vp, C.POINTER(vp)]),
     "afx_rigid_stream_destroy": (i32, [vp]),

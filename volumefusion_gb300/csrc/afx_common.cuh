@@ -156,7 +156,11 @@ AFX_D bool tsdf_update_value(const float* p, const float* depth, int W, int H, f
     if (isinf(D) || D < 1.e-4f) return false;
     float sdf = p[2] - D;
     if (sdf > delta) return false;
-    *tnew = (sdf < -delta) ? -1.0f : sdf / delta;
+    if (sdf < -delta) {  // behind the truncation band: no division (most voxels that update)
+        *tnew = -1.0f;
+        return true;
+    }
+    *tnew = sdf / delta;
     return true;
 }
 

@@ -94,6 +94,57 @@ __global__ void integrate_rigid_kernel(TT* tsdf, WT* weights, const float* __res
     vox_put(tsdf, weights, i, t, w);
 }
 
+// DeviceTsdf::initDefault followed by integrateTSDFFromFrameKernel, in one pass that only writes: a
+// freshly initialised voxel (-1, weight 0) that is updated becomes ((-1 * 0) + t * 1) / (0 + 1) = t
+// with weight min(0 + 1, 15) = 1 -- exactly, since -0 + t = t and t / 1 = t -- and every other voxel
+// stays (-1, 0).  8 B per voxel written instead of 8 written + 16 read and written.
+// Threads run over the quads of a z slice in memory order (a slice is contiguous), so no lane idles
+// whatever X is.  The blend of a fresh voxel is written out as its result (t, 1): the division by
+// (0 + 1) and the products by 0 and 1 change nothing.
+__global__ void __launch_bounds__(256) integrate_fresh_x4_kernel(float* __restrict__ tsdf, float* __restrict__ weights,
+                                                                 const float* __restrict__ depth, RigidArgs a) {
+    const int X = a.vol.dims[0], Y = a.vol.dims[1];
+    const int qx_n = X >> 2;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;  // quad within the slice
+    if (j >= qx_n * Y) return;
+    const int y = j / qx_n, qx = j - y * qx_n, z = blockIdx.y;
+    float tv[4], wv[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float p[3], q[3], tn;
+        voxel_to_world(qx * 4 + i, y, z, a.vol.vs, a.vol.half, p);
+        mat3_vec3(a.R, p, q);
+        q[0] = q[0] + a.t[0];
+        q[1] = q[1] + a.t[1];
+        q[2] = q[2] + a.t[2];
+        const bool upd = tsdf_update_value(q, depth, a.W, a.H, a.delta, a.K, &tn);
+        tv[i] = upd ? tn : -1.f;
+        wv[i] = upd ? 1.f : 0.f;
+    }
+    vox_put4(tsdf, weights, ((long)z * Y + y) * X + qx * 4, tv, wv);
+}
+
+int integrate_fresh_impl(float* tsdf, float* weights, const float* depth, int W, int H, float delta, const Volume& vol,
+                         const float* R, const float* t, const float* K, cudaStream_t st) {
+    const int X = vol.dims[0], Y = vol.dims[1], Z = vol.dims[2];
+    const bool vec = (X % 4 == 0) && ((reinterpret_cast<uintptr_t>(tsdf) | reinterpret_cast<uintptr_t>(weights)) & 15) == 0;
+    if (!vec) return AFX_ERR_UNSUPPORTED;  // callers fall back to initialise + integrate
+    RigidArgs a;
+    a.vol = vol;
+    for (int i = 0; i < 9; ++i) a.R[i] = R[i];
+    for (int i = 0; i < 3; ++i) a.t[i] = t[i];
+    a.t_dev = nullptr;
+    a.K = make_intrinsics(K);
+    a.delta = delta;
+    a.W = W;
+    a.H = H;
+    const long quads = (long)(X / 4) * Y;
+    dim3 grid((unsigned)((quads + 255) / 256), (unsigned)Z);
+    integrate_fresh_x4_kernel<<<grid, 256, 0, st>>>(tsdf, weights, depth, a);
+    AFX_LAUNCH_CHECK();
+    return AFX_OK;
+}
+
 int integrate_rigid_impl(void* tsdf, void* weights, int fmt, const float* depth, int W, int H, float delta,
                          const Volume& vol, const float* R, const float* t, const float* K, cudaStream_t st,
                          const float* t_dev) {
@@ -577,6 +628,16 @@ int afx_integrate_tsdf(float* tsdf, float* weights, const float* depth, int widt
     if (width <= 0 || height <= 0 || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return AFX_ERR_INVALID_ARGUMENT;
     return integrate_rigid_impl(tsdf, weights, kVoxF32, depth, width, height, delta,
                                 make_volume(dims, voxel_size, volume_size),
+                                rotate, translate, K, as_stream(stream));
+}
+
+int afx_integrate_tsdf_fresh(float* tsdf, float* weights, const float* depth, int width, int height, float delta,
+                             const int dims[3], const float voxel_size[3], const float volume_size[3],
+                             const float rotate[9], const float translate[3], const float K[9], void* stream) {
+    if (!tsdf || !weights || !depth || !dims || !voxel_size || !volume_size || !rotate || !translate || !K)
+        return AFX_ERR_INVALID_ARGUMENT;
+    if (width <= 0 || height <= 0 || dims[0] <= 0 || dims[1] <= 0 || dims[2] <= 0) return AFX_ERR_INVALID_ARGUMENT;
+    return integrate_fresh_impl(tsdf, weights, depth, width, height, delta, make_volume(dims, voxel_size, volume_size),
                                 rotate, translate, K, as_stream(stream));
 }
 

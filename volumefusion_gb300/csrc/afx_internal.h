@@ -31,6 +31,10 @@ int frame_prep_impl(const uint16_t* mm, int width, int height, const afx_prep_pa
 int integrate_rigid_impl(void* tsdf, void* weights, int fmt, const float* depth, int W, int H, float delta,
                          const Volume& vol, const float* R, const float* t, const float* K, cudaStream_t st,
                          const float* t_dev = nullptr);
+// initialise (-1, 0) + rigid integration in one write-only pass (FP32 volumes, X % 4 == 0, 16-byte
+// aligned arrays; AFX_ERR_UNSUPPORTED otherwise)
+int integrate_fresh_impl(float* tsdf, float* weights, const float* depth, int W, int H, float delta, const Volume& vol,
+                         const float* R, const float* t, const float* K, cudaStream_t st);
 void rotation_inverse(const float* R, float* Rinv);
 
 // ---- marching cubes and sorting (afx_mc.cu) ----

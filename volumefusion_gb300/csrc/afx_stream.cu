@@ -166,10 +166,16 @@ int afx_rigid_stream_process(afx_rigid_stream* s, const uint16_t* const* depth_m
         transform_points_kernel<<<grid_for(P, 256), 256, 0, st>>>(cloud, P, T);
         AFX_LAUNCH_CHECK();
     }
-    stream_init_kernel<<<grid_for(s->S, 256), 256, 0, st>>>(s->tsdf, s->weights, s->S, s->counts);
-    AFX_LAUNCH_CHECK();
-    int rc = integrate_rigid_impl(s->tsdf, s->weights, kVoxF32, s->depth, p.width, p.height, p.delta, s->vol, p.rotation,
+    // DeviceTsdf::initDefault + integrate(cameras[0]): one write-only pass where the layout allows
+    AFX_CUDA(cudaMemsetAsync(s->counts, 0, 8, st));
+    int rc = integrate_fresh_impl(s->tsdf, s->weights, s->depth, p.width, p.height, p.delta, s->vol, p.rotation,
                                   p.center, p.K[0], st);
+    if (rc == AFX_ERR_UNSUPPORTED) {
+        stream_init_kernel<<<grid_for(s->S, 256), 256, 0, st>>>(s->tsdf, s->weights, s->S, s->counts);
+        AFX_LAUNCH_CHECK();
+        rc = integrate_rigid_impl(s->tsdf, s->weights, kVoxF32, s->depth, p.width, p.height, p.delta, s->vol,
+                                  p.rotation, p.center, p.K[0], st);
+    }
     if (rc) return rc;
     const long T = p.triangle_capacity;
     rc = mc_fused_impl(s->tsdf, s->weights, kVoxF32, s->vol, 0.f, nullptr, nullptr, 0, s->verts, s->counts + 1, T * 3,
