@@ -169,6 +169,14 @@ int afx_marching_cubes_mesh(float* vertices, unsigned* vertex_count, long vertex
 int afx_sort_unique_points(float* points, unsigned* count, long n_max, void* workspace, size_t workspace_bytes,
                            void* stream);
 size_t afx_sort_unique_points_workspace_size(long n_max);
+/* The same sort + unique for a marching-cubes point cloud of a volume (every x within the volume):
+ * points are bucketed by voxel column, each column sorted in shared memory, and the unique points
+ * compacted in order; a column of more than 8192 points falls back to the general sort on the
+ * device.  Results are identical to afx_sort_unique_points. */
+size_t afx_sort_unique_volume_points_workspace_size(long n_max, const int dims[3]);
+int afx_sort_unique_volume_points(float* points, unsigned* count, long n_max, const int dims[3],
+                                  const float voxel_size[3], const float volume_size[3], void* workspace,
+                                  size_t workspace_bytes, void* stream);
 
 /* DeviceTsdf::extractPointCloud (include/af/DeviceTsdf.cuh:34-42): marching-cubes points,
  * then sort + unique. */

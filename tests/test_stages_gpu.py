@@ -255,3 +255,62 @@ def test_voxel_warp_and_warped_integration_bit_exact(af, frames):
                                                  size, dims, np.eye(3), c, K)
         assert np.array_equal(host(tg), t1)
         assert np.array_equal(host(wg), w1)
+
+
+def _sort_dev(pts, fn, *extra):
+    import ctypes as C
+
+    from volumefusion_gb300._lib import check, lib
+    n = len(pts)
+    p = torch.from_numpy(np.ascontiguousarray(pts, np.float32).ravel()).cuda()
+    cnt = torch.tensor([n], dtype=torch.int32, device="cuda")
+    if fn == "general":
+        wsb = lib().afx_sort_unique_points_workspace_size(n)
+    else:
+        wsb = lib().afx_sort_unique_volume_points_workspace_size(n, extra[0])
+    ws = torch.empty(int(wsb), dtype=torch.uint8, device="cuda")
+    st = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if fn == "general":
+        check(lib().afx_sort_unique_points(C.c_void_p(p.data_ptr()), C.c_void_p(cnt.data_ptr()), n,
+                                           C.c_void_p(ws.data_ptr()), int(wsb), st), "sort")
+    else:
+        check(lib().afx_sort_unique_volume_points(C.c_void_p(p.data_ptr()), C.c_void_p(cnt.data_ptr()), n, *extra,
+                                                  C.c_void_p(ws.data_ptr()), int(wsb), st), "sort")
+    m = int(cnt.item())
+    return p[:3 * m].view(-1, 3).cpu().numpy()
+
+
+def test_volume_sort_equals_general_sort():
+    """The column-bucket sort + unique of a marching-cubes cloud gives the general sort's result bit
+    for bit: on a real cloud, with +0/-0 twins, and with one column too large for shared memory (the
+    device falls back to the general sort)."""
+    import ctypes as C
+
+    from volumefusion_gb300 import configs
+    cfg, [mm] = configs.rigid_sphere_128()
+    depth, _, _, cen = O.frame_prep(mm, cfg["K"])
+    vs = configs.voxel_size(cfg)
+    S = int(np.prod(cfg["dims"]))
+    t = np.full(S, -1.0, np.float32)
+    w = np.zeros(S, np.float32)
+    O.integrate_rigid(t, w, depth, cfg["delta"], cfg["dims"], vs, cfg["volume_size"], np.eye(3), cen, cfg["K"])
+    raw = O.mc_pointcloud(t, w, cfg["dims"], vs, cfg["volume_size"])
+    rng = np.random.default_rng(4)
+    twins = raw[rng.integers(0, len(raw), 200)].copy()
+    twins[:, 0] = 0.0
+    neg = twins.copy()
+    neg[:, 0] = -0.0
+    half = np.float32(cfg["volume_size"][0]) / 2
+    column = np.stack([np.full(12000, -half + np.float32(40.5) * vs[0], np.float32),
+                       (rng.integers(0, 100, 12000) * vs[1] - half).astype(np.float32),
+                       (rng.integers(0, 100, 12000) * vs[2] - half).astype(np.float32)], axis=1)
+    dims = (C.c_int * 3)(*cfg["dims"])
+    f3 = lambda a: (C.c_float * 3)(*[float(x) for x in a])  # noqa: E731
+    extra = (dims, f3(vs), f3(cfg["volume_size"]))
+    for case in (raw, np.concatenate([raw, neg, twins, raw[:500]]), np.concatenate([raw, column])):
+        case = case[rng.permutation(len(case))]
+        a = _sort_dev(case, "general")
+        b = _sort_dev(case, "volume", *extra)
+        assert a.shape == b.shape and len(a) > 0
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    assert np.array_equal(_sort_dev(raw, "volume", *extra), O.sort_unique(raw))

@@ -65,6 +65,8 @@ SIGNATURES = {
     "afx_marching_cubes_mesh": (i32, [vp, vp, i64, vp, vp, i64, vp, vp, vp, vp, vp, f32, vp]),
     "afx_sort_unique_points": (i32, [vp, vp, i64, vp, sz, vp]),
     "afx_sort_unique_points_workspace_size": (sz, [i64]),
+    "afx_sort_unique_volume_points_workspace_size": (sz, [i64, vp]),
+    "afx_sort_unique_volume_points": (i32, [vp, vp, i64, vp, vp, vp, vp, sz, vp]),
     "afx_extract_point_cloud": (i32, [vp, vp, i64, vp, vp, vp, vp, vp, f32, vp, sz, vp]),
     "afx_translate": (i32, [vp, vp, i64, vp, vp]),
     "afx_build_graph": (i32, [vp, vp, vp, vp, i32, vp, vp, i64, i32, f32, vp, sz, vp]),

@@ -23,6 +23,7 @@ enum : int {
     ERRF_SINGULAR = 4,
     ERRF_UNSUPPORTED = 8,
     ERRF_TMA = 16,
+    ERRF_INDEX = 32,  // an index failed a bounds check; the access was skipped
 };
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }

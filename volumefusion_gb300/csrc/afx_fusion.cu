@@ -272,7 +272,7 @@ static void session_layout(const afx_fusion_params& p, afx_fusion* f) {
     for (int c = 0; c < 3; ++c) f->per[c] = 2 * ((int)(p.graph_radius / vs[c]) + 1) + 1;
     const long M = p.mesh_capacity, N = p.node_capacity, S = f->S, Pp = f->P;
     const long nbricks = brick_count_total(f->vol);
-    f->ws_sort_bytes = sort_unique_workspace_size(M);
+    f->ws_sort_bytes = sort_unique_volume_workspace_size(M, p.dims[0] + 1);
     f->ws_graph_bytes = build_graph_ws(M);
     f->ws_corr_bytes = corr_ws(M);
     f->ws_support_bytes = support_workspace_size(f->vol, (int)N, f->per);
@@ -555,7 +555,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
     stage_mark(f, ST_SORT, st);
     float* points = f->points_buf[cur];
     unsigned* npoints = f->npoints_buf[cur];
-    rc = sort_unique_impl(points, npoints, M, f->ws_sort, f->ws_sort_bytes, st);
+    rc = sort_unique_volume_impl(points, npoints, M, f->ws_sort, f->ws_sort_bytes, f->vol, st, f->error);
     if (rc) return rc;
     AFX_CUDA(cudaMemcpyAsync(f->mesh_used, npoints, 4, cudaMemcpyDeviceToDevice, st));
     if (rc) return rc;
@@ -783,7 +783,7 @@ int afx_fusion_stats(afx_fusion* f, afx_frame_stats* out, void* stream) {
     if (s.error & ERRF_TIMEOUT) return AFX_ERR_TIMEOUT;
     if (s.error & ERRF_SINGULAR) return AFX_ERR_SINGULAR;
     if (s.error & ERRF_UNSUPPORTED) return AFX_ERR_UNSUPPORTED;
-    if (s.error & ERRF_CAPACITY) return AFX_ERR_CAPACITY;
+    if (s.error & (ERRF_CAPACITY | ERRF_INDEX)) return AFX_ERR_CAPACITY;
     return AFX_OK;
 }
 

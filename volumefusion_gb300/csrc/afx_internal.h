@@ -40,6 +40,10 @@ void rotation_inverse(const float* R, float* Rinv);
 // ---- marching cubes and sorting (afx_mc.cu) ----
 size_t sort_unique_workspace_size(long n_max);
 int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, cudaStream_t st);
+// The same result for a marching-cubes cloud of `vol` (x within the volume), by voxel-column buckets.
+size_t sort_unique_volume_workspace_size(long n_max, int nb);
+int sort_unique_volume_impl(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, const Volume& vol,
+                            cudaStream_t st, int* error = nullptr);
 int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
                   unsigned* face_count, long face_cap, cudaStream_t st, int* error = nullptr, int tile = 0);

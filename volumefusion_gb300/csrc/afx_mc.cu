@@ -571,7 +571,7 @@ AFX_D void merge_chunk(const Key3* __restrict__ in, Key3* __restrict__ out, long
     for (int t = threadIdx.x; t < la + lb; t += blockDim.x) s[t] = t < la ? in[a0 + i0 + t] : in[b0 + j0 + (t - la)];
     __syncthreads();
     const int tot = la + lb;
-    const int per = kSortTile / kSortThreads;
+    const int per = kSortTile / blockDim.x;  // blockDim.x divides kSortTile
     const int q0 = threadIdx.x * per;
     if (q0 < tot) {
         int lo = max(0, q0 - lb), hi = min(q0, la);
@@ -738,6 +738,237 @@ int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t w
     return AFX_OK;
 }
 
+// ------------------------------------------------------------------------------------
+// Column-bucket sort + unique of a marching-cubes point cloud of a known volume.
+//
+// Every point of the cloud has x in [-half, half] of the volume, and b(x) = trunc((x + half) * inv)
+// (clamped) is monotone in x under IEEE rounding, so bucketing by voxel column keeps the
+// lexicographic order between buckets and puts equal points (-0 and +0 included) in one bucket.
+// Pipeline: count per bucket, scan, scatter (order within a bucket arbitrary), one CTA per bucket
+// sorting it and counting its unique points, scan of those counts, ordered compaction back into the
+// cloud.  A bucket of up to kBucketCap points is sorted in shared memory; a larger one (a surface
+// lying along one x column) is sorted as kBucketCap runs in shared memory that the same CTA then
+// merges (merge path) between the workspace's two key buffers.
+// ------------------------------------------------------------------------------------
+
+constexpr int kBucketCap = 8192;  // keys per bucket sorted in shared memory (96 KB)
+constexpr int kBucketThreads = 512;
+
+struct BucketArgs {
+    float half0, inv0;
+    int nb;
+};
+
+AFX_D int bucket_of(float x, const BucketArgs& a) {
+    const float u = (x + a.half0) * a.inv0;
+    const int b = u > 0.f ? f2i(u) : 0;
+    return b >= a.nb ? a.nb - 1 : b;
+}
+
+struct BucketWs {
+    unsigned* cnt;     // [nb]
+    unsigned* off;     // [nb + 1]
+    unsigned* cursor;  // [nb]
+    unsigned* ucnt;    // [nb]
+    unsigned* uoff;    // [nb + 1]
+};
+
+__global__ void bucket_count_kernel(const float* __restrict__ pts, const unsigned* count, long n_max, BucketArgs a,
+                                    unsigned* cnt) {
+    const long n = min((long)*count, n_max);
+    AFX_GRID_STRIDE(i, n) atomicAdd(cnt + bucket_of(pts[3 * i], a), 1u);
+}
+
+// Exclusive scan of n values by one CTA of 1024 threads (n up to a few thousand); out[n] = total, and
+// the total also goes to *total when given.
+__global__ void __launch_bounds__(1024) small_scan_kernel(const unsigned* in, int n, unsigned* out, unsigned* copy,
+                                                          unsigned* total) {
+    __shared__ unsigned part[1024];
+    const int per = (n + 1023) / 1024;
+    const int lo = threadIdx.x * per, hi = min(n, lo + per);
+    unsigned sum = 0;
+    for (int i = lo; i < hi; ++i) sum += in[i];
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {
+        const unsigned v = threadIdx.x >= o ? part[threadIdx.x - o] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    unsigned run = part[threadIdx.x] - sum;
+    for (int i = lo; i < hi; ++i) {
+        out[i] = run;
+        if (copy) copy[i] = run;
+        run += in[i];
+    }
+    if (threadIdx.x == 1023) {
+        out[n] = part[1023];
+        if (total) *total = part[1023];
+    }
+}
+
+__global__ void bucket_scatter_kernel(const float* __restrict__ pts, const unsigned* count, long n_max, BucketArgs a,
+                                      unsigned* cursor, Key3* keys, int* error) {
+    const long n = min((long)*count, n_max);
+    AFX_GRID_STRIDE(i, n) {
+        Key3 k;
+        k.k[0] = f2key(pts[3 * i]);
+        k.k[1] = f2key(pts[3 * i + 1]);
+        k.k[2] = f2key(pts[3 * i + 2]);
+        const unsigned pos = atomicAdd(cursor + bucket_of(pts[3 * i], a), 1u);
+        if (pos < (unsigned long)n) keys[pos] = k;
+        else if (error) atomicOr(error, ERRF_INDEX);
+    }
+}
+
+// Bitonic sort of m <= kBucketCap keys at g in shared memory (padded to a power of two with keys that
+// sort last), written back to g.
+AFX_D void bucket_bitonic(Key3* g, unsigned m, Key3* sk) {
+    unsigned P = 1;
+    while (P < m) P <<= 1;
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < P; i += blockDim.x) {
+        Key3 k;
+        if (i < m) k = g[i];
+        else k.k[0] = k.k[1] = k.k[2] = 0xffffffffu;
+        sk[i] = k;
+    }
+    __syncthreads();
+    for (unsigned size = 2; size <= P; size <<= 1)
+        for (unsigned stride = size >> 1; stride > 0; stride >>= 1) {
+            for (unsigned q = threadIdx.x; q < P / 2; q += blockDim.x) {
+                const unsigned i = 2 * stride * (q / stride) + (q % stride), j = i + stride;
+                const bool asc = (i & size) == 0;
+                const Key3 x = sk[i], y = sk[j];
+                if (key_less(y, x) == asc) {
+                    sk[i] = y;
+                    sk[j] = x;
+                }
+            }
+            __syncthreads();
+        }
+    for (unsigned i = threadIdx.x; i < m; i += blockDim.x) g[i] = sk[i];
+    __syncthreads();
+}
+
+// One CTA per bucket: sort it in place and count its unique points.
+__global__ void __launch_bounds__(kBucketThreads) bucket_sort_kernel(Key3* keys, Key3* tmp, const unsigned* off,
+                                                                   unsigned* ucnt, long n_max, int* error) {
+    extern __shared__ Key3 sk[];
+    __shared__ unsigned wsum[kBucketThreads / 32];
+    __shared__ long split[2];
+    const int b = blockIdx.x;
+    const unsigned lo = off[b], n = off[b + 1] - lo;
+    if (lo > off[b + 1] || (long)off[b + 1] > n_max) {  // the scan's offsets must stay within the keys
+        if (threadIdx.x == 0) {
+            ucnt[b] = 0;
+            if (error) atomicOr(error, ERRF_INDEX);
+        }
+        return;
+    }
+    if (n == 0) {
+        if (threadIdx.x == 0) ucnt[b] = 0;
+        return;
+    }
+    Key3* g = keys + lo;
+    for (unsigned r = 0; r < n; r += kBucketCap) bucket_bitonic(g + r, min((unsigned)kBucketCap, n - r), sk);
+    if (n > (unsigned)kBucketCap) {  // merge the sorted runs, ping-ponging through tmp
+        Key3* src = g;
+        Key3* dst = tmp + lo;
+        for (long L = kBucketCap; L < (long)n; L <<= 1) {
+            for (long o0 = 0; o0 < (long)n; o0 += kSortTile) merge_chunk(src, dst, n, L, o0, sk, split);
+            __syncthreads();
+            Key3* t = src;
+            src = dst;
+            dst = t;
+        }
+        if (src != g)
+            for (unsigned i = threadIdx.x; i < n; i += blockDim.x) g[i] = src[i];
+        __syncthreads();
+    }
+    unsigned c = 0;
+    for (unsigned i = threadIdx.x; i < n; i += blockDim.x) c += (i == 0 || !key_same_point(g[i - 1], g[i])) ? 1u : 0u;
+    c = warp_sum(c);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned t = 0;
+        for (int w = 0; w < kBucketThreads / 32; ++w) t += wsum[w];
+        ucnt[b] = t;
+    }
+}
+
+// One CTA per bucket: its unique points, in order, at the bucket's place in the output.
+__global__ void __launch_bounds__(kBucketThreads) bucket_compact_kernel(const Key3* keys, const unsigned* off,
+                                                                      const unsigned* uoff, float* pts, long n_max,
+                                                                      int* error) {
+    __shared__ unsigned wsum[kBucketThreads / 32];
+    const int b = blockIdx.x;
+    if (off[b] > off[b + 1] || (long)off[b + 1] > n_max || (long)uoff[b + 1] > n_max) {
+        if (threadIdx.x == 0 && error) atomicOr(error, ERRF_INDEX);
+        return;
+    }
+    const unsigned lo = off[b], n = off[b + 1] - lo;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned run = uoff[b];
+    for (unsigned r0 = 0; r0 < n; r0 += blockDim.x) {
+        const unsigned i = r0 + threadIdx.x;
+        const bool keep = i < n && (i == 0 || !key_same_point(keys[lo + i - 1], keys[lo + i]));
+        const unsigned bal = __ballot_sync(0xffffffffu, keep);
+        __syncthreads();
+        if (lane == 0) wsum[w] = __popc(bal);
+        __syncthreads();
+        unsigned before = 0, all = 0;
+        for (int k = 0; k < kBucketThreads / 32; ++k) {
+            const unsigned v = wsum[k];
+            if (k < w) before += v;
+            all += v;
+        }
+        if (keep) {
+            const Key3 k = keys[lo + i];
+            float* o = pts + 3 * (long)(run + before + __popc(bal & ((1u << lane) - 1)));
+            o[0] = key2f(k.k[0]);
+            o[1] = key2f(k.k[1]);
+            o[2] = key2f(k.k[2]);
+        }
+        run += all;
+    }
+}
+
+size_t sort_unique_volume_workspace_size(long n_max, int nb) {
+    return sort_unique_workspace_size(n_max) + al((size_t)(5 * (nb + 2) + 1) * 4);
+}
+
+int sort_unique_volume_impl(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, const Volume& vol,
+                            cudaStream_t st, int* error) {
+    if (n_max <= 0) return AFX_OK;
+    const int nb = vol.dims[0] + 1;
+    if (nb > 8 * 1024) return sort_unique_impl(pts, count, n_max, ws, ws_bytes, st);
+    if (!ws || ws_bytes < sort_unique_volume_workspace_size(n_max, nb)) return AFX_ERR_WORKSPACE;
+    const size_t base = sort_unique_workspace_size(n_max);
+    unsigned* u = reinterpret_cast<unsigned*>(static_cast<char*>(ws) + base);
+    BucketWs w{u, u + nb, u + 2 * nb + 1, u + 3 * nb + 1, u + 4 * nb + 1};
+    Key3* keys = reinterpret_cast<Key3*>(ws);  // the general sort's two key buffers
+    Key3* tmp = reinterpret_cast<Key3*>(static_cast<char*>(ws) + al(n_max * sizeof(Key3)));
+    BucketArgs a{vol.half[0], vol.inv[0], nb};
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(kBucketCap * sizeof(Key3)));
+        attr = true;
+    }
+    AFX_CUDA(cudaMemsetAsync(w.cnt, 0, nb * 4, st));
+    bucket_count_kernel<<<grid_for(n_max, 256), 256, 0, st>>>(pts, count, n_max, a, w.cnt);
+    small_scan_kernel<<<1, 1024, 0, st>>>(w.cnt, nb, w.off, w.cursor, nullptr);
+    bucket_scatter_kernel<<<grid_for(n_max, 256), 256, 0, st>>>(pts, count, n_max, a, w.cursor, keys, error);
+    bucket_sort_kernel<<<nb, kBucketThreads, kBucketCap * sizeof(Key3), st>>>(keys, tmp, w.off, w.ucnt, n_max, error);
+    small_scan_kernel<<<1, 1024, 0, st>>>(w.ucnt, nb, w.uoff, nullptr, count);
+    bucket_compact_kernel<<<nb, kBucketThreads, 0, st>>>(keys, w.off, w.uoff, pts, n_max, error);
+    AFX_LAUNCH_CHECK();
+    return AFX_OK;
+}
+
 __global__ void translate_kernel(float* pts, const unsigned* count, long n_max, float tx, float ty, float tz) {
     long n = count ? min((long)*count, n_max) : n_max;
     long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
@@ -799,6 +1030,20 @@ int afx_sort_unique_points(float* points, unsigned* count, long n_max, void* wor
                            void* stream) {
     if (!points || !count || n_max < 0) return AFX_ERR_INVALID_ARGUMENT;
     return sort_unique_impl(points, count, n_max, workspace, workspace_bytes, as_stream(stream));
+}
+
+size_t afx_sort_unique_volume_points_workspace_size(long n_max, const int dims[3]) {
+    if (!dims || dims[0] < 1) return 0;
+    return sort_unique_volume_workspace_size(n_max < 1 ? 1 : n_max, dims[0] + 1);
+}
+
+int afx_sort_unique_volume_points(float* points, unsigned* count, long n_max, const int dims[3],
+                                  const float voxel_size[3], const float volume_size[3], void* workspace,
+                                  size_t workspace_bytes, void* stream) {
+    if (!points || !count || n_max < 0 || !dims || !voxel_size || !volume_size || dims[0] < 1)
+        return AFX_ERR_INVALID_ARGUMENT;
+    return sort_unique_volume_impl(points, count, n_max, workspace, workspace_bytes,
+                                   make_volume(dims, voxel_size, volume_size), as_stream(stream), nullptr);
 }
 
 int afx_extract_point_cloud(float* points, unsigned* count, long capacity, const float* tsdf, const float* weights,
