@@ -1210,6 +1210,8 @@ __global__ void __launch_bounds__(kLoopThreads, 1) gn_solve_kernel(LoopArgs L) {
     int ds_ph = 0;
     const bool ds = n > 0 && (n + (int)ncta - 1) / (int)ncta <= kDsNpc && ds_stage(a.b, n, dsl, cs, ds_ph);
     gn_solve(L, n, ds, dsl, cs, ds_ph, gt, gstride);
+    // no CTA leaves while another may still read its shared memory
+    cluster_barrier();
 }
 
 }  // namespace afx

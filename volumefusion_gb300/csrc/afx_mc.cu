@@ -598,8 +598,10 @@ AFX_D bool key_same_point(const Key3& a, const Key3& b) {
 // consecutive points and an ordered compaction back into `pts`.  Phases are separated by the
 // hardware cluster barrier.
 __global__ void __launch_bounds__(kSortThreads, 1) sort_unique_kernel(float* pts, unsigned* count, long n_max,
-                                                                     Key3* buf0, Key3* buf1, unsigned* tile_cnt) {
+                                                                     Key3* buf0, Key3* buf1, unsigned* tile_cnt,
+                                                                     const unsigned* only_if) {
     __shared__ Key3 s[kSortTile];
+    if (only_if && *only_if == 0u) return;  // the column-bucket sort did the work
     __shared__ long split[2];
     __shared__ unsigned wsum[kSortThreads / 32];
     __shared__ unsigned s_base;
@@ -712,7 +714,15 @@ static int sort_cluster_size() {
     return cached;
 }
 
+static int sort_unique_cluster(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, cudaStream_t st,
+                               const unsigned* only_if);
+
 int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, cudaStream_t st) {
+    return sort_unique_cluster(pts, count, n_max, ws, ws_bytes, st, nullptr);
+}
+
+static int sort_unique_cluster(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, cudaStream_t st,
+                               const unsigned* only_if) {
     if (n_max <= 0) return AFX_OK;
     if (!ws || ws_bytes < sort_unique_workspace_size(n_max)) return AFX_ERR_WORKSPACE;
     char* p = static_cast<char*>(ws);
@@ -733,7 +743,7 @@ int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t w
     at[0].val.clusterDim.z = 1;
     cfg.attrs = at;
     cfg.numAttrs = 1;
-    AFX_CUDA(cudaLaunchKernelEx(&cfg, sort_unique_kernel, pts, count, n_max, buf0, buf1, tile_cnt));
+    AFX_CUDA(cudaLaunchKernelEx(&cfg, sort_unique_kernel, pts, count, n_max, buf0, buf1, tile_cnt, only_if));
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
@@ -745,10 +755,10 @@ int sort_unique_impl(float* pts, unsigned* count, long n_max, void* ws, size_t w
 // (clamped) is monotone in x under IEEE rounding, so bucketing by voxel column keeps the
 // lexicographic order between buckets and puts equal points (-0 and +0 included) in one bucket.
 // Pipeline: count per bucket, scan, scatter (order within a bucket arbitrary), one CTA per bucket
-// sorting it and counting its unique points, scan of those counts, ordered compaction back into the
-// cloud.  A bucket of up to kBucketCap points is sorted in shared memory; a larger one (a surface
-// lying along one x column) is sorted as kBucketCap runs in shared memory that the same CTA then
-// merges (merge path) between the workspace's two key buffers.
+// sorting it in shared memory and counting its unique points, scan of those counts, ordered
+// compaction back into the cloud.  A bucket larger than kBucketCap (a surface lying along one x
+// column) raises a flag on the device; the bucket kernels then stand down and the cluster sort above
+// runs instead, on the untouched cloud.
 // ------------------------------------------------------------------------------------
 
 constexpr int kBucketCap = 8192;  // keys per bucket sorted in shared memory (96 KB)
@@ -771,6 +781,7 @@ struct BucketWs {
     unsigned* cursor;  // [nb]
     unsigned* ucnt;    // [nb]
     unsigned* uoff;    // [nb + 1]
+    unsigned* overflow;
 };
 
 __global__ void bucket_count_kernel(const float* __restrict__ pts, const unsigned* count, long n_max, BucketArgs a,
@@ -779,15 +790,21 @@ __global__ void bucket_count_kernel(const float* __restrict__ pts, const unsigne
     AFX_GRID_STRIDE(i, n) atomicAdd(cnt + bucket_of(pts[3 * i], a), 1u);
 }
 
-// Exclusive scan of n values by one CTA of 1024 threads (n up to a few thousand); out[n] = total, and
-// the total also goes to *total when given.
+// Exclusive scan of n values by one CTA of 1024 threads (n up to a few thousand); out[n] = total.
+// With `overflow`, flags it when a value exceeds `cap`; with `total`, also writes the total there
+// unless *skip is set.
 __global__ void __launch_bounds__(1024) small_scan_kernel(const unsigned* in, int n, unsigned* out, unsigned* copy,
-                                                          unsigned* total) {
+                                                          unsigned cap, unsigned* overflow, unsigned* total,
+                                                          const unsigned* skip) {
     __shared__ unsigned part[1024];
     const int per = (n + 1023) / 1024;
     const int lo = threadIdx.x * per, hi = min(n, lo + per);
-    unsigned sum = 0;
-    for (int i = lo; i < hi; ++i) sum += in[i];
+    unsigned sum = 0, big = 0;
+    for (int i = lo; i < hi; ++i) {
+        sum += in[i];
+        big |= in[i] > cap;
+    }
+    if (overflow && __syncthreads_or(big) && threadIdx.x == 0) *overflow = 1u;
     part[threadIdx.x] = sum;
     __syncthreads();
     for (int o = 1; o < 1024; o <<= 1) {
@@ -804,12 +821,13 @@ __global__ void __launch_bounds__(1024) small_scan_kernel(const unsigned* in, in
     }
     if (threadIdx.x == 1023) {
         out[n] = part[1023];
-        if (total) *total = part[1023];
+        if (total && !(skip && *skip)) *total = part[1023];
     }
 }
 
 __global__ void bucket_scatter_kernel(const float* __restrict__ pts, const unsigned* count, long n_max, BucketArgs a,
-                                      unsigned* cursor, Key3* keys, int* error) {
+                                      unsigned* cursor, Key3* keys, const unsigned* overflow, int* error) {
+    if (*overflow) return;
     const long n = min((long)*count, n_max);
     AFX_GRID_STRIDE(i, n) {
         Key3 k;
@@ -852,15 +870,15 @@ AFX_D void bucket_bitonic(Key3* g, unsigned m, Key3* sk) {
     __syncthreads();
 }
 
-// One CTA per bucket: sort it in place and count its unique points.
-__global__ void __launch_bounds__(kBucketThreads) bucket_sort_kernel(Key3* keys, Key3* tmp, const unsigned* off,
-                                                                   unsigned* ucnt, long n_max, int* error) {
+// One CTA per bucket (at most kBucketCap points): sort it in place and count its unique points.
+__global__ void __launch_bounds__(kBucketThreads) bucket_sort_kernel(Key3* keys, const unsigned* off, unsigned* ucnt,
+                                                                   const unsigned* overflow, long n_max, int* error) {
     extern __shared__ Key3 sk[];
     __shared__ unsigned wsum[kBucketThreads / 32];
-    __shared__ long split[2];
+    if (*overflow) return;
     const int b = blockIdx.x;
     const unsigned lo = off[b], n = off[b + 1] - lo;
-    if (lo > off[b + 1] || (long)off[b + 1] > n_max) {  // the scan's offsets must stay within the keys
+    if (lo > off[b + 1] || (long)off[b + 1] > n_max || n > (unsigned)kBucketCap) {  // never expected: skip, flag
         if (threadIdx.x == 0) {
             ucnt[b] = 0;
             if (error) atomicOr(error, ERRF_INDEX);
@@ -872,21 +890,7 @@ __global__ void __launch_bounds__(kBucketThreads) bucket_sort_kernel(Key3* keys,
         return;
     }
     Key3* g = keys + lo;
-    for (unsigned r = 0; r < n; r += kBucketCap) bucket_bitonic(g + r, min((unsigned)kBucketCap, n - r), sk);
-    if (n > (unsigned)kBucketCap) {  // merge the sorted runs, ping-ponging through tmp
-        Key3* src = g;
-        Key3* dst = tmp + lo;
-        for (long L = kBucketCap; L < (long)n; L <<= 1) {
-            for (long o0 = 0; o0 < (long)n; o0 += kSortTile) merge_chunk(src, dst, n, L, o0, sk, split);
-            __syncthreads();
-            Key3* t = src;
-            src = dst;
-            dst = t;
-        }
-        if (src != g)
-            for (unsigned i = threadIdx.x; i < n; i += blockDim.x) g[i] = src[i];
-        __syncthreads();
-    }
+    bucket_bitonic(g, n, sk);
     unsigned c = 0;
     for (unsigned i = threadIdx.x; i < n; i += blockDim.x) c += (i == 0 || !key_same_point(g[i - 1], g[i])) ? 1u : 0u;
     c = warp_sum(c);
@@ -902,8 +906,9 @@ __global__ void __launch_bounds__(kBucketThreads) bucket_sort_kernel(Key3* keys,
 // One CTA per bucket: its unique points, in order, at the bucket's place in the output.
 __global__ void __launch_bounds__(kBucketThreads) bucket_compact_kernel(const Key3* keys, const unsigned* off,
                                                                       const unsigned* uoff, float* pts, long n_max,
-                                                                      int* error) {
+                                                                      const unsigned* overflow, int* error) {
     __shared__ unsigned wsum[kBucketThreads / 32];
+    if (*overflow) return;
     const int b = blockIdx.x;
     if (off[b] > off[b + 1] || (long)off[b + 1] > n_max || (long)uoff[b + 1] > n_max) {
         if (threadIdx.x == 0 && error) atomicOr(error, ERRF_INDEX);
@@ -948,9 +953,8 @@ int sort_unique_volume_impl(float* pts, unsigned* count, long n_max, void* ws, s
     if (!ws || ws_bytes < sort_unique_volume_workspace_size(n_max, nb)) return AFX_ERR_WORKSPACE;
     const size_t base = sort_unique_workspace_size(n_max);
     unsigned* u = reinterpret_cast<unsigned*>(static_cast<char*>(ws) + base);
-    BucketWs w{u, u + nb, u + 2 * nb + 1, u + 3 * nb + 1, u + 4 * nb + 1};
-    Key3* keys = reinterpret_cast<Key3*>(ws);  // the general sort's two key buffers
-    Key3* tmp = reinterpret_cast<Key3*>(static_cast<char*>(ws) + al(n_max * sizeof(Key3)));
+    BucketWs w{u, u + nb, u + 2 * nb + 1, u + 3 * nb + 1, u + 4 * nb + 1, u + 5 * nb + 2};
+    Key3* keys = reinterpret_cast<Key3*>(ws);  // the cluster sort's first buffer (it rebuilds it from the cloud)
     BucketArgs a{vol.half[0], vol.inv[0], nb};
     static bool attr = false;
     if (!attr) {
@@ -959,14 +963,17 @@ int sort_unique_volume_impl(float* pts, unsigned* count, long n_max, void* ws, s
         attr = true;
     }
     AFX_CUDA(cudaMemsetAsync(w.cnt, 0, nb * 4, st));
+    AFX_CUDA(cudaMemsetAsync(w.overflow, 0, 4, st));
     bucket_count_kernel<<<grid_for(n_max, 256), 256, 0, st>>>(pts, count, n_max, a, w.cnt);
-    small_scan_kernel<<<1, 1024, 0, st>>>(w.cnt, nb, w.off, w.cursor, nullptr);
-    bucket_scatter_kernel<<<grid_for(n_max, 256), 256, 0, st>>>(pts, count, n_max, a, w.cursor, keys, error);
-    bucket_sort_kernel<<<nb, kBucketThreads, kBucketCap * sizeof(Key3), st>>>(keys, tmp, w.off, w.ucnt, n_max, error);
-    small_scan_kernel<<<1, 1024, 0, st>>>(w.ucnt, nb, w.uoff, nullptr, count);
-    bucket_compact_kernel<<<nb, kBucketThreads, 0, st>>>(keys, w.off, w.uoff, pts, n_max, error);
+    small_scan_kernel<<<1, 1024, 0, st>>>(w.cnt, nb, w.off, w.cursor, kBucketCap, w.overflow, nullptr, nullptr);
+    bucket_scatter_kernel<<<grid_for(n_max, 256), 256, 0, st>>>(pts, count, n_max, a, w.cursor, keys, w.overflow,
+                                                                 error);
+    bucket_sort_kernel<<<nb, kBucketThreads, kBucketCap * sizeof(Key3), st>>>(keys, w.off, w.ucnt, w.overflow, n_max,
+                                                                              error);
+    small_scan_kernel<<<1, 1024, 0, st>>>(w.ucnt, nb, w.uoff, nullptr, 0xffffffffu, nullptr, count, w.overflow);
+    bucket_compact_kernel<<<nb, kBucketThreads, 0, st>>>(keys, w.off, w.uoff, pts, n_max, w.overflow, error);
     AFX_LAUNCH_CHECK();
-    return AFX_OK;
+    return sort_unique_cluster(pts, count, n_max, ws, ws_bytes, st, w.overflow);
 }
 
 __global__ void translate_kernel(float* pts, const unsigned* count, long n_max, float tx, float ty, float tz) {
