@@ -229,6 +229,16 @@ __global__ void __launch_bounds__(kTW * kTH) prep_kernel(const __grid_constant__
         }
         if (__syncthreads_or(!done)) {
             if (tid == 0) atomicOr(A.error, ERRF_TMA | ERRF_TIMEOUT);
+            // the copy may still land: wait for it (bounded) before the CTA's shared memory goes
+            for (int it = 0; it < (1 << 22); ++it) {
+                uint32_t ok;
+                asm volatile(
+                    "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0; selp.u32 %0, 1, 0, p; }"
+                    : "=r"(ok)
+                    : "r"(smem_u32(&mbar))
+                    : "memory");
+                if (ok) break;
+            }
             return;
         }
     } else {
