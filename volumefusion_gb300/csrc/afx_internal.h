@@ -48,8 +48,9 @@ int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& 
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
                   unsigned* face_count, long face_cap, cudaStream_t st, int* error = nullptr, int tile = 0);
 // marching-cubes tiles (the session's autotuner picks one): TMA bricks of 16, 8 or 32 cubes along z,
-// or the column march from global memory
-enum { kMcTileTma16 = 0, kMcTileTma8 = 1, kMcTileTma32 = 2, kMcTileColumn = 3, kMcTiles = 4 };
+// the column march from global memory, or a persistent grid with two stages of bricks 8 or 16 deep
+enum { kMcTileTma16 = 0, kMcTileTma8 = 1, kMcTileTma32 = 2, kMcTileColumn = 3, kMcTilePipe8 = 4, kMcTilePipe16 = 5,
+       kMcTiles = 6 };
 int translate_impl(float* pts, const unsigned* count, long n_max, const float* t, cudaStream_t st);
 // pts += sign * t_dev (t_dev in device memory); dst may differ from src
 int translate_dev_impl(float* dst, const float* src, const unsigned* count, long n_max, const float* t_dev, float sign,

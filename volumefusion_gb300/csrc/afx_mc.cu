@@ -365,6 +365,143 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_consta
     }
 }
 
+// The same cubes again, by a persistent grid: a CTA walks the tiles blockIdx.x, + gridDim.x, ...
+// with two stages of TMA-loaded bricks.  The load of tile k + 2 is issued as soon as tile k's
+// classification has read its stage, so loads overlap the FP64 edge interpolation and the appends
+// of the tiles before.  Every wait is bounded; on a timeout the CTA flags the error, waits (bounded)
+// for the loads it issued and leaves.
+AFX_D bool mc_wait(uint32_t bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t ok;
+        asm volatile("{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+                     : "=r"(ok)
+                     : "r"(bar), "r"(parity)
+                     : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+template <class TT, class WT, bool kPoints, bool kMesh, int ZR>
+__global__ void __launch_bounds__(kMcX * kMcY) mc_pipe_kernel(const __grid_constant__ CUtensorMap map_t,
+                                                             const __grid_constant__ CUtensorMap map_w,
+                                                             const TT* __restrict__ tsdf, McArgs a, int tx_n, int ty_n,
+                                                             int tz_n) {
+    static_assert(sizeof(TT) == sizeof(WT), "value and weight bricks share one layout");
+    static_assert(ZR <= 64, "the queue entry keeps z in 6 bits");
+    constexpr size_t kBrick = mc_brick_bytes(sizeof(TT), ZR);
+    constexpr int kSlice = kMcTX * (kMcY + 1);
+    constexpr unsigned kBytes = (unsigned)(kSlice * (ZR + 1) * (sizeof(TT) + sizeof(WT)));
+    extern __shared__ __align__(128) unsigned char mc_raw[];
+    __shared__ alignas(8) unsigned long long mbar[2];
+    __shared__ unsigned q[kMcX * kMcY * ZR];
+    __shared__ unsigned q_n;
+    const uint32_t pad = (128u - (mc_smem_u32(mc_raw) & 127u)) & 127u;
+    TT* st[2];
+    WT* sw[2];
+    for (int k = 0; k < 2; ++k) {
+        st[k] = reinterpret_cast<TT*>(mc_raw + pad + (2 * k) * kBrick);
+        sw[k] = reinterpret_cast<WT*>(mc_raw + pad + (2 * k + 1) * kBrick);
+    }
+    const int tid = threadIdx.y * kMcX + threadIdx.x;
+    const long nt = (long)tx_n * ty_n * tz_n;
+    if ((mc_smem_u32(st[0]) & 127u) != 0u) {  // never expected: refuse rather than fault
+        if (tid == 0 && a.error) atomicOr(a.error, ERRF_TMA);
+        return;
+    }
+    auto origin = [&](long t, int& x0, int& y0, int& z0) {
+        const int tx = (int)(t % tx_n), ty = (int)((t / tx_n) % ty_n), tz = (int)(t / ((long)tx_n * ty_n));
+        x0 = tx * kMcX;
+        y0 = ty * kMcY;
+        z0 = tz * ZR;
+    };
+    auto issue = [&](int s, long t) {  // one thread
+        int x0, y0, z0;
+        origin(t, x0, y0, z0);
+        const uint32_t bar = mc_smem_u32(&mbar[s]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(kBytes) : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+            "[%5];" ::"r"(mc_smem_u32(st[s])),
+            "l"(&map_t), "r"(x0), "r"(y0), "r"(z0), "r"(bar)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+            "[%5];" ::"r"(mc_smem_u32(sw[s])),
+            "l"(&map_w), "r"(x0), "r"(y0), "r"(z0), "r"(bar)
+            : "memory");
+    };
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mc_smem_u32(&mbar[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mc_smem_u32(&mbar[1])));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const long G = gridDim.x;
+    if (tid == 0) {
+        if ((long)blockIdx.x < nt) issue(0, blockIdx.x);
+        if ((long)blockIdx.x + G < nt) issue(1, blockIdx.x + G);
+    }
+    const int nx = a.vol.dims[0] - 2, ny = a.vol.dims[1] - 2, nz = a.vol.dims[2] - 2;
+    const int o00 = threadIdx.y * kMcTX + threadIdx.x;
+    int k = 0;
+    for (long t = blockIdx.x; t < nt; t += G, ++k) {
+        const int s = k & 1;
+        const uint32_t parity = (uint32_t)((k >> 1) & 1);
+        const bool ok = mc_wait(mc_smem_u32(&mbar[s]), parity);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0 && a.error) atomicOr(a.error, ERRF_TMA | ERRF_TIMEOUT);
+            // loads issued and not yet waited for: this tile's (stage s, if it timed out) and the next
+            mc_wait(mc_smem_u32(&mbar[s]), parity);
+            if (t + G < nt) mc_wait(mc_smem_u32(&mbar[s ^ 1]), (uint32_t)(((k + 1) >> 1) & 1));
+            return;
+        }
+        if (tid == 0) q_n = 0;
+        __syncthreads();
+        int x0, y0, z0;
+        origin(t, x0, y0, z0);
+        const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
+        const int z1 = min(z0 + ZR, nz);
+        const bool col = x < nx && y < ny;
+        for (int z = z0; z < z1; ++z) {
+            const int s0 = (z - z0) * kSlice + o00, s1 = s0 + kSlice;
+            int ci = 0;
+            if (col) {
+                const int off[8] = {s0 + kMcTX + 1, s0 + 1, s0, s0 + kMcTX, s1 + kMcTX + 1, s1 + 1, s1, s1 + kMcTX};
+                bool any_zero = false;
+#pragma unroll
+                for (int c = 0; c < 8; ++c) any_zero |= smem_w_zero(sw[s], off[c]);
+                if (!any_zero)
+#pragma unroll
+                    for (int c = 0; c < 8; ++c)
+                        if (smem_t(st[s], off[c]) > a.iso) ci |= 1 << c;
+            }
+            const bool active = ci != 0 && ci != 255;
+            const unsigned bal = __ballot_sync(0xffffffffu, active);
+            if (bal) {
+                const int lane = threadIdx.x & 31;
+                unsigned base = 0;
+                if (lane == 0) base = atomicAdd(&q_n, (unsigned)__popc(bal));
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (active)
+                    q[base + __popc(bal & ((1u << lane) - 1))] = (unsigned)ci | ((unsigned)threadIdx.x << 8) |
+                                                                 ((unsigned)threadIdx.y << 13) | ((unsigned)(z - z0) << 16);
+            }
+        }
+        __syncthreads();  // stage s has been read: it can take tile t + 2G
+        if (tid == 0 && t + 2 * G < nt) issue(s, t + 2 * G);
+        const unsigned nq = q_n;
+        for (unsigned r0 = 0; r0 < nq; r0 += kMcX * kMcY) {
+            const unsigned qi = r0 + tid;
+            const bool act = qi < nq;
+            const unsigned e = act ? q[qi] : 0u;
+            mc_emit<kPoints, kMesh>(tsdf, a, x0 + (int)((e >> 8) & 31u), y0 + (int)((e >> 13) & 7u),
+                                    z0 + (int)((e >> 16) & 63u), (int)(e & 255u), act);
+        }
+        __syncthreads();  // the queue is reused by the next tile
+    }
+}
+
 __global__ void mc_vert_count_kernel(const unsigned* face_count, unsigned* vert_count) {
     *vert_count = 3u * *face_count;
 }
@@ -401,13 +538,43 @@ static void mc_launch_tma(const TT* tsdf, const McArgs& a, const CUtensorMap* mt
     mc_tma_kernel<TT, WT, kPoints, kMesh, ZR><<<grid, dim3(kMcX, kMcY), smem, st>>>(*mt, *mw, tsdf, a);
 }
 
-// tile: kMcTileTma16 (default), kMcTileTma8, kMcTileTma32 (TMA bricks of that many cubes along z) or
+template <class TT, class WT, bool kPoints, bool kMesh, int ZR>
+static void mc_launch_pipe(const TT* tsdf, const McArgs& a, const CUtensorMap* mt, const CUtensorMap* mw,
+                           cudaStream_t st) {
+    constexpr int smem = (int)(4 * mc_brick_bytes(sizeof(TT), ZR) + 128);
+    static int per_sm = 0, sms = 0;  // per instantiation: opt-in and resident CTAs per SM
+    if (!per_sm) {
+        cudaFuncSetAttribute(mc_pipe_kernel<TT, WT, kPoints, kMesh, ZR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_pipe_kernel<TT, WT, kPoints, kMesh, ZR>, kMcX * kMcY,
+                                                      smem);
+        if (per_sm < 1) per_sm = 1;
+        if (sms < 1) sms = 1;
+        cudaGetLastError();
+    }
+    const int tx = (a.vol.dims[0] - 2 + kMcX - 1) / kMcX, ty = (a.vol.dims[1] - 2 + kMcY - 1) / kMcY,
+              tz = (a.vol.dims[2] - 2 + ZR - 1) / ZR;
+    const long nt = (long)tx * ty * tz;
+    const long grid = nt < (long)sms * per_sm ? nt : (long)sms * per_sm;
+    mc_pipe_kernel<TT, WT, kPoints, kMesh, ZR><<<(unsigned)grid, dim3(kMcX, kMcY), smem, st>>>(*mt, *mw, tsdf, a, tx,
+                                                                                              ty, tz);
+}
+
+// tile: kMcTileTma16 (default), kMcTileTma8, kMcTileTma32 (TMA bricks of that many cubes along z),
+// kMcTilePipe8 / kMcTilePipe16 (persistent grid with two stages of bricks 8 or 16 cubes deep) or
 // kMcTileColumn (column march from global memory, 16 cubes along z).  mt/mw are the maps encoded for
 // that depth, or null (then the column march runs).
 template <class TT, class WT, bool kPoints, bool kMesh>
 static void mc_launch(const TT* tsdf, const WT* weights, const McArgs& a, const CUtensorMap* mt, const CUtensorMap* mw,
                       int tile, cudaStream_t st) {
-    if (mt && tile == kMcTileTma8) {
+    if (mt && tile == kMcTilePipe8) {
+        mc_launch_pipe<TT, WT, kPoints, kMesh, 8>(tsdf, a, mt, mw, st);
+    } else if (mt && tile == kMcTilePipe16) {
+        mc_launch_pipe<TT, WT, kPoints, kMesh, 16>(tsdf, a, mt, mw, st);
+    } else if (mt && tile == kMcTileTma8) {
         mc_launch_tma<TT, WT, kPoints, kMesh, 8>(tsdf, a, mt, mw, st);
     } else if (mt && tile == kMcTileTma32) {
         mc_launch_tma<TT, WT, kPoints, kMesh, 32>(tsdf, a, mt, mw, st);
@@ -453,7 +620,7 @@ int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& 
     CUtensorMap mt, mw;
     const bool f16 = fmt == kVoxF16;
     const size_t elem = vox_bytes(fmt);
-    const int zr = tile == kMcTileTma8 ? 8 : tile == kMcTileTma32 ? 32 : 16;
+    const int zr = (tile == kMcTileTma8 || tile == kMcTilePipe8) ? 8 : tile == kMcTileTma32 ? 32 : 16;
     const bool tma = error && tile != kMcTileColumn &&
                      make_volume_map(&mt, tsdf, vol, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 :
                                                            CU_TENSOR_MAP_DATA_TYPE_FLOAT32, elem, zr) &&

@@ -184,7 +184,8 @@ class FusionSession:
         check(lib().afx_fusion_save_mesh_ply(self.h, str(path).encode(), self._st()), "afx_fusion_save_mesh_ply")
 
     def set_tile(self, tile):
-        """Marching-cubes tile: 0 TMA 16 cubes along z (default), 1 TMA 8, 2 TMA 32, 3 column march."""
+        """Marching-cubes tile: 0 TMA 16 cubes along z (default), 1 TMA 8, 2 TMA 32, 3 column march,
+        4 / 5 persistent two-stage TMA 8 / 16."""
         check(lib().afx_fusion_set_tile(self.h, int(tile)), "afx_fusion_set_tile")
 
     def tile(self):
@@ -192,7 +193,7 @@ class FusionSession:
 
     def autotune(self):
         """Time every marching-cubes tile on the current volume and keep the fastest: (tile, ms per tile)."""
-        t, ms = C.c_int(0), (C.c_float * 4)()
+        t, ms = C.c_int(0), (C.c_float * 6)()
         check(lib().afx_fusion_autotune(self.h, C.byref(t), ms, self._st()), "afx_fusion_autotune")
         return t.value, list(ms)
 
