@@ -667,6 +667,7 @@ def main():
             torch.cuda.empty_cache()
             precision[prec] = {"value": world * psteps * clip / (pms / 1000.0), "unit": "frames/s",
                                "session_bytes": session_bytes(pcfg), "n_nodes_last_frame": pst["n_nodes"],
+                               "mesh_points_last_frame": pst["mesh_points"],
                                "error": pst["error"], "stage_ms_per_frame": pstage,
                                "mc_tile": ptile, "mc_tile_ms": [round(x, 4) for x in ptile_ms]}
 
