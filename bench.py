@@ -123,7 +123,7 @@ REF_FRAMES_PER_STEP = 4
 
 
 def run_reference(args):
-    """The reference's CPU path (its oracle port; see DESIGN) on the host cores.  A step is a
+    """The reference's CPU path (the oracle's restatement of it) on the host cores.  A step is a
     bounded sample of the workload: the first REF_FRAMES_PER_STEP frames of the sequence from
     an empty volume (frame 0 rigid, then non-rigid frames)."""
     rank = int(os.environ.get("RANK", "0"))

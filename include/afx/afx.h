@@ -238,7 +238,8 @@ size_t afx_correspondences_workspace_size(long n_points_max);
  * point has no counterpart in the reference.  Scratch is a fixed device array of the
  * library sized for AFX_CORR_STATIC_MAX_POINTS vertices (about 3 MiB); n_points_max above
  * that returns AFX_ERR_CAPACITY before any work.  The first call on each device looks up
- * the array's address (make that first call before any stream capture).  All calls on a
+ * the array's address, and so does the first call after a device reset (make that first
+ * call before any stream capture).  All calls on a
  * device share the one array: calls that overlap in time (other streams, other host
  * threads) race and must be ordered by the caller.  Results equal afx_correspondences. */
 #define AFX_CORR_STATIC_MAX_POINTS 262144L

@@ -65,7 +65,9 @@ def write(words, path, comment):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VF_REFERENCE", "")
+    if not ref:
+        sys.exit("usage: gen_mc_tables.py <reference tree>  (or set VF_REFERENCE)")
     words = pack(parse_tri_table(ref))
     write(words, os.path.join(ROOT, "volumefusion_gb300", "csrc", "mc_tables.inc"),
           "Triangulation per case equals the reference's (src/MarchingCubes.cpp:35).")

@@ -86,7 +86,9 @@ def write_if_changed(dst, text):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VF_REFERENCE", "")
+    if not ref:
+        sys.exit("usage: build_emu.py <reference tree>  (or set VF_REFERENCE)")
     os.makedirs(os.path.join(GEN, "include", "af"), exist_ok=True)
     for h in HEADERS:
         write_if_changed(os.path.join(GEN, "include", "af", h),

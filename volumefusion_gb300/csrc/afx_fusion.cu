@@ -15,9 +15,11 @@
 #include <new>
 #include <vector>
 
+#include <cuda.h>
 #include <cuda_fp16.h>
 
 #include "afx_gn.h"
+#include "afx_host.h"
 #include "afx_voxel.h"
 
 namespace afx {
@@ -33,6 +35,32 @@ int note_cuda_error(cudaError_t e) {
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 long launches_total() { return g_launches.load(std::memory_order_relaxed); }
 
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = reinterpret_cast<CtxGetCurrentFn>(p);
+        p = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = reinterpret_cast<CtxGetIdFn>(p);
+        cudaGetLastError();
+    });
+    if (!get_current || !get_id) return 0;
+    CUcontext c = nullptr;
+    if (get_current(&c) != CUDA_SUCCESS || !c) return 0;
+    unsigned long long id = 0;
+    return get_id(c, &id) == CUDA_SUCCESS ? id : 0;
+}
+
 struct FrameStats {
     int frame;
     int n_nodes;
@@ -43,6 +71,44 @@ struct FrameStats {
     double energy;
     unsigned mesh_vertices, mesh_faces;
     int error;
+};
+
+// The streams an object has enqueued work on, each with an event recorded after its latest work
+// there, so that tearing the object down waits for its own work only (not the whole device).
+struct WorkMarks {
+    std::vector<std::pair<cudaStream_t, cudaEvent_t>> marks;
+    bool lost = false;  // an event could not be created: teardown waits for the device instead
+
+    // Called after enqueueing work on `st` (never while `st` is capturing).
+    void note(cudaStream_t st) {
+        for (auto& m : marks)
+            if (m.first == st) {
+                if (cudaEventRecord(m.second, st) != cudaSuccess) lost = true;
+                return;
+            }
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventRecord(e, st) != cudaSuccess) {
+            if (e) cudaEventDestroy(e);
+            cudaGetLastError();
+            lost = true;
+            return;
+        }
+        marks.push_back({st, e});
+    }
+    // Waits for every marked piece of work, then forgets the marks.
+    cudaError_t wait_and_clear() {
+        cudaError_t r = cudaSuccess;
+        if (lost) r = cudaDeviceSynchronize();
+        for (auto& m : marks) {
+            const cudaError_t e = cudaEventSynchronize(m.second);
+            if (r == cudaSuccess) r = e;
+            cudaEventDestroy(m.second);
+        }
+        marks.clear();
+        lost = false;
+        return r;
+    }
 };
 
 }  // namespace afx
@@ -134,6 +200,7 @@ struct afx_fusion {
     int mc_tile = kMcTileTma16;  // marching-cubes tile (afx_fusion_autotune)
     long glaunches[2][2] = {{0, 0}, {0, 0}};  // kernels in each captured frame
     long replayed = 0;                        // kernels launched by graph replays
+    WorkMarks work;                           // streams holding this session's work (destroy waits on them)
 };
 
 namespace afx {
@@ -395,18 +462,21 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
         return AFX_ERR_WORKSPACE;
     }
     f->launches_at_create = launches_total();
-    int rc = afx_fusion_reset(f, nullptr);
+    // The whole arena is cleared, so no buffer starts with the bytes of an earlier allocation,
+    // then the volume and counters are set; on a private non-blocking stream, so that creating a
+    // session neither waits for nor holds up other sessions' work.
+    cudaStream_t init = nullptr;
+    e = cudaStreamCreateWithFlags(&init, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMemsetAsync(f->arena, 0, f->arena_bytes, init);
+    int rc = e == cudaSuccess ? afx_fusion_reset(f, init) : note_cuda_error(e);
+    e = init ? cudaStreamSynchronize(init) : cudaSuccess;
+    if (!rc && e != cudaSuccess) rc = note_cuda_error(e);
+    if (init) cudaStreamDestroy(init);
+    f->work.wait_and_clear();  // the reset's mark names the private stream
     if (rc) {
         cudaFree(f->arena);
         delete f;
         return rc;
-    }
-    e = cudaStreamSynchronize(nullptr);  // the reset above; other streams' work is not waited for
-    if (e != cudaSuccess) {
-        note_cuda_error(e);
-        cudaFree(f->arena);
-        delete f;
-        return AFX_ERR_CUDA;
     }
     *out = f;
     return AFX_OK;
@@ -427,7 +497,7 @@ static void drop_graphs(afx_fusion* f) {
 
 int afx_fusion_destroy(afx_fusion* f) {
     if (!f) return AFX_ERR_INVALID_ARGUMENT;
-    cudaDeviceSynchronize();
+    f->work.wait_and_clear();  // the session's own work on every stream it was given
     for (auto& m : f->marks) cudaEventDestroy(m.second);
     for (auto e : f->ev_pool) cudaEventDestroy(e);
     drop_graphs(f);
@@ -476,6 +546,7 @@ int afx_fusion_reset(afx_fusion* f, void* stream) {
     AFX_CUDA(cudaMemsetAsync(f->nmfaces, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->stats, 0, sizeof(FrameStats), st));
     f->frame = 0;
+    f->work.note(st);
     return AFX_OK;
 }
 
@@ -722,6 +793,7 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
         const int rc = enqueue_frame(f, depth_mm, st, f->cur, false);
         if (rc) return rc;
         f->frame++;
+        f->work.note(st);
         return AFX_OK;
     }
     const int cur = f->cur ^ 1;
@@ -746,6 +818,7 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
     f->points = f->points_buf[cur];
     f->npoints = f->npoints_buf[cur];
     f->frame++;
+    f->work.note(st);
     return AFX_OK;
 }
 
@@ -761,6 +834,7 @@ static_assert(sizeof(FrameStats) == sizeof(afx_frame_stats), "statistics layouts
 int afx_fusion_stats_async(afx_fusion* f, afx_frame_stats* out_host, void* stream) {
     if (!f || !out_host) return AFX_ERR_INVALID_ARGUMENT;
     AFX_CUDA(cudaMemcpyAsync(out_host, f->stats, sizeof(FrameStats), cudaMemcpyDeviceToHost, as_stream(stream)));
+    f->work.note(as_stream(stream));
     return AFX_OK;
 }
 
@@ -845,6 +919,7 @@ int afx_fusion_frame_views(afx_fusion* f, float** depth, float** vertices, float
 int afx_fusion_set_transforms(afx_fusion* f, const float* transforms_host, int n, void* stream) {
     if (!f || !transforms_host || n < 0 || n > f->p.node_capacity) return AFX_ERR_INVALID_ARGUMENT;
     AFX_CUDA(cudaMemcpyAsync(f->T, transforms_host, (size_t)n * 64, cudaMemcpyHostToDevice, as_stream(stream)));
+    f->work.note(as_stream(stream));
     return AFX_OK;
 }
 
@@ -869,7 +944,7 @@ int afx_fusion_graph_count(const afx_fusion* f) {
 int afx_fusion_set_tile(afx_fusion* f, int tile) {
     if (!f || tile < 0 || tile >= kMcTiles) return AFX_ERR_INVALID_ARGUMENT;
     if (tile != f->mc_tile) {
-        AFX_CUDA(cudaDeviceSynchronize());  // graphs in flight may still use the old tile
+        AFX_CUDA(f->work.wait_and_clear());  // graphs in flight may still use the old tile
         drop_graphs(f);
         f->mc_tile = tile;
     }
@@ -977,6 +1052,7 @@ struct afx_batch {
     };
     std::map<std::vector<long>, Exec> cache;
     long graph_launches = 0;
+    WorkMarks work;  // streams the batch's graphs were launched on
 };
 
 namespace {
@@ -1062,7 +1138,7 @@ int afx_batch_create(afx_fusion* const* sessions, int n, afx_batch** out) {
 
 int afx_batch_destroy(afx_batch* b) {
     if (!b) return AFX_ERR_INVALID_ARGUMENT;
-    cudaDeviceSynchronize();
+    b->work.wait_and_clear();  // the batch's graph launches
     batch_free(b);
     return AFX_OK;
 }
@@ -1114,8 +1190,10 @@ int afx_batch_process(afx_batch* b, const uint16_t* const* depth_mm, void* strea
     const cudaError_t le = cudaGraphLaunch(it->second.exec, st);
     if (le != cudaSuccess) return batch_fail("launch", le);
     ++b->graph_launches;
+    b->work.note(st);
     for (size_t k = 0; k < members.size(); ++k) {
         afx_fusion* f = b->s[members[k]];
+        f->work.note(st);  // the member's frame ran inside the batch graph on st
         f->replayed += f->glaunches[build[k]][cur[k]];
         f->cur = cur[k];
         f->points = f->points_buf[cur[k]];

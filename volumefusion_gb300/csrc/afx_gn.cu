@@ -18,6 +18,7 @@
 #include <new>
 
 #include "afx_gn.h"
+#include "afx_host.h"
 
 namespace afx {
 
@@ -1232,8 +1233,10 @@ static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 // Cluster size for gn_loop_kernel: 16 CTAs where the device runs non-portable clusters of
 // that size, else the portable 8.
 static int gn_cluster_size() {
-    static int cached = 0;
-    if (!cached) {
+    static ContextOnce once;
+    static int cached_dev[kMaxDevices];
+    once_per_context(once, [](int dev) {
+        int cached = 0;
         cudaFuncSetAttribute(gn_loop_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         cudaFuncSetAttribute(gn_loop_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDsSmem);
         cudaFuncSetAttribute(gn_solve_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
@@ -1258,9 +1261,12 @@ static int gn_cluster_size() {
             }
             cudaGetLastError();
         }
-        if (!cached) cached = 8;
-    }
-    return cached;
+        cached_dev[dev] = cached ? cached : 8;
+        return (int)AFX_OK;
+    });
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return cached_dev[dev] ? cached_dev[dev] : 8;
 }
 
 size_t gn_workspace_size(long m_max, int n_max, int k, int kreg) {
@@ -1366,7 +1372,14 @@ int gn_icp_setup(const GnArgs& a, float* T_pending, const float* T_committed, cu
     const int words = (a.n_max + 31) / 32;
     const size_t smem = (size_t)kGnWarps * words * 4;
     if (smem > 200 * 1024) return AFX_ERR_UNSUPPORTED;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(nbr_discover_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static ContextOnce once;  // the opt-in covers every size accepted above
+    if (smem > 48 * 1024) {
+        const int rc = once_per_context(once, [](int) {
+            return note_cuda_error(
+                cudaFuncSetAttribute(nbr_discover_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        });
+        if (rc) return rc;
+    }
     nbr_discover_kernel<<<nb, 32 * kGnWarps, smem, st>>>(a, words);
     AFX_LAUNCH_CHECK();
     nbr_ref_kernel<<<grid_for((long)a.n_max * kMaxNbr, 256), 256, 0, st>>>(a);

@@ -7,6 +7,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "afx_host.h"
 #include "afx_internal.h"
 
 namespace afx {
@@ -718,7 +719,9 @@ int correspondences_impl(int* corr, unsigned* corr_count, long cap, const float*
     return AFX_OK;
 }
 
-// Per-call device scratch for the stand-alone entry points (error word, node count copy).
+// Device scratch of the stand-alone entry points (error word, node count copy): one per host
+// thread and device, allocated on the thread's first call and kept for the life of the process,
+// so calls from different host threads never share it.
 struct CallScratch {
     int error;
     int n;
@@ -726,12 +729,19 @@ struct CallScratch {
 };
 
 static CallScratch* call_scratch() {
-    static CallScratch* s = nullptr;
-    if (!s) {
-        if (cudaMalloc(&s, sizeof(CallScratch)) != cudaSuccess) return nullptr;
-        cudaMemset(s, 0, sizeof(CallScratch));
+    thread_local CallScratch* s[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+    if (!s[dev]) {
+        CallScratch* p = nullptr;
+        if (cudaMalloc(&p, sizeof(CallScratch)) != cudaSuccess) return nullptr;
+        if (cudaMemset(p, 0, sizeof(CallScratch)) != cudaSuccess) {
+            cudaFree(p);
+            return nullptr;
+        }
+        s[dev] = p;
     }
-    return s;
+    return s[dev];
 }
 
 }  // namespace afx
@@ -828,20 +838,31 @@ static __device__ __align__(256) unsigned char g_corr_static_scratch[kCorrStatic
 
 constexpr int kCorrStaticMaxDevices = 64;
 static std::mutex g_corr_static_mu;
-static void* g_corr_static_ptr[kCorrStaticMaxDevices];
+struct CorrStaticSlot {
+    unsigned long long ctx_id = 0;  // context the address belongs to (0: none yet)
+    void* ptr = nullptr;
+};
+static CorrStaticSlot g_corr_static[kCorrStaticMaxDevices];
 
-// Device address of the scratch array on the current device, looked up once per device.
+// Device address of the scratch array in the current device's context.  The lookup
+// (cudaGetSymbolAddress, which loads the module into the context if needed and allocates
+// nothing) runs on the first call in each context -- once per device unless the device is
+// reset -- and its result is kept with the context's identifier, so an address from a
+// context that has since been destroyed is never reused.
 static int corr_static_scratch(void** out) {
     int dev = 0;
     AFX_CUDA(cudaGetDevice(&dev));
     if (dev < 0 || dev >= kCorrStaticMaxDevices) return AFX_ERR_UNSUPPORTED;
     std::lock_guard<std::mutex> lock(g_corr_static_mu);
-    if (!g_corr_static_ptr[dev]) {
+    CorrStaticSlot& slot = g_corr_static[dev];
+    const unsigned long long id = current_context_id();
+    if (!slot.ptr || id == 0 || id != slot.ctx_id) {
         void* p = nullptr;
         AFX_CUDA(cudaGetSymbolAddress(&p, g_corr_static_scratch));
-        g_corr_static_ptr[dev] = p;
+        slot.ptr = p;
+        slot.ctx_id = current_context_id();  // the lookup above made the context current if it was not
     }
-    *out = g_corr_static_ptr[dev];
+    *out = slot.ptr;
     return AFX_OK;
 }
 

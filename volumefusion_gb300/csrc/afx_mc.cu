@@ -10,6 +10,7 @@
 
 #include <cstring>
 
+#include "afx_host.h"
 #include "afx_internal.h"
 #include "afx_store.cuh"
 #include "afx_tma.h"
@@ -29,24 +30,22 @@ __constant__ int c_corner[8][3] = {{1, 1, 0}, {1, 0, 0}, {0, 0, 0}, {0, 1, 0}, {
 __constant__ int c_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
 static const int kEdgeHost[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6}, {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
 
+// The tables are constant: uploaded once per device context (before the first marching-cubes launch,
+// which is never inside a stream capture: a session's first frame runs eagerly).
 static int upload_tables() {
-    static bool done = false;  // tables are constant; one upload per process and device 0 context
-    static int dev_done = -1;
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (done && dev_done == dev) return AFX_OK;
-    unsigned short et[256];
-    for (int c = 0; c < 256; ++c) {
-        int e = 0;
-        for (int i = 0; i < 12; ++i)
-            if (((c >> kEdgeHost[i][0]) & 1) != ((c >> kEdgeHost[i][1]) & 1)) e |= 1 << i;
-        et[c] = (unsigned short)e;
-    }
-    AFX_CUDA(cudaMemcpyToSymbol(c_edge_table, et, sizeof(et)));
-    AFX_CUDA(cudaMemcpyToSymbol(c_tri_table, kTriTableHost, sizeof(kTriTableHost)));
-    done = true;
-    dev_done = dev;
-    return AFX_OK;
+    static ContextOnce once;
+    return once_per_context(once, [](int) {
+        unsigned short et[256];
+        for (int c = 0; c < 256; ++c) {
+            int e = 0;
+            for (int i = 0; i < 12; ++i)
+                if (((c >> kEdgeHost[i][0]) & 1) != ((c >> kEdgeHost[i][1]) & 1)) e |= 1 << i;
+            et[c] = (unsigned short)e;
+        }
+        AFX_CUDA(cudaMemcpyToSymbol(c_edge_table, et, sizeof(et)));
+        AFX_CUDA(cudaMemcpyToSymbol(c_tri_table, kTriTableHost, sizeof(kTriTableHost)));
+        return (int)AFX_OK;
+    });
 }
 
 struct McArgs {
@@ -527,12 +526,11 @@ template <class TT, class WT, bool kPoints, bool kMesh, int ZR>
 static void mc_launch_tma(const TT* tsdf, const McArgs& a, const CUtensorMap* mt, const CUtensorMap* mw,
                           cudaStream_t st) {
     constexpr int smem = (int)mc_tma_smem(sizeof(TT), ZR);
-    static bool attr = false;  // per instantiation: the dynamic shared memory opt-in
-    if (!attr) {
-        cudaFuncSetAttribute(mc_tma_kernel<TT, WT, kPoints, kMesh, ZR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             smem);
-        attr = true;
-    }
+    static ContextOnce once;  // per instantiation: the dynamic shared memory opt-in
+    once_per_context(once, [](int) {
+        return note_cuda_error(cudaFuncSetAttribute(mc_tma_kernel<TT, WT, kPoints, kMesh, ZR>,
+                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    });
     const dim3 grid((unsigned)((a.vol.dims[0] - 2 + kMcX - 1) / kMcX), (unsigned)((a.vol.dims[1] - 2 + kMcY - 1) / kMcY),
                     (unsigned)((a.vol.dims[2] - 2 + ZR - 1) / ZR));
     mc_tma_kernel<TT, WT, kPoints, kMesh, ZR><<<grid, dim3(kMcX, kMcY), smem, st>>>(*mt, *mw, tsdf, a);
@@ -542,19 +540,23 @@ template <class TT, class WT, bool kPoints, bool kMesh, int ZR>
 static void mc_launch_pipe(const TT* tsdf, const McArgs& a, const CUtensorMap* mt, const CUtensorMap* mw,
                            cudaStream_t st) {
     constexpr int smem = (int)(4 * mc_brick_bytes(sizeof(TT), ZR) + 128);
-    static int per_sm = 0, sms = 0;  // per instantiation: opt-in and resident CTAs per SM
-    if (!per_sm) {
+    static ContextOnce once;  // per instantiation: opt-in and resident CTAs per SM, per device
+    static int per_sm_dev[kMaxDevices], sms_dev[kMaxDevices];
+    once_per_context(once, [](int dev) {
+        int per_sm = 0, sms = 0;
         cudaFuncSetAttribute(mc_pipe_kernel<TT, WT, kPoints, kMesh, ZR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem);
-        int dev = 0;
-        cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mc_pipe_kernel<TT, WT, kPoints, kMesh, ZR>, kMcX * kMcY,
                                                       smem);
-        if (per_sm < 1) per_sm = 1;
-        if (sms < 1) sms = 1;
         cudaGetLastError();
-    }
+        per_sm_dev[dev] = per_sm < 1 ? 1 : per_sm;
+        sms_dev[dev] = sms < 1 ? 1 : sms;
+        return (int)AFX_OK;
+    });
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int per_sm = per_sm_dev[dev] < 1 ? 1 : per_sm_dev[dev], sms = sms_dev[dev] < 1 ? 1 : sms_dev[dev];
     const int tx = (a.vol.dims[0] - 2 + kMcX - 1) / kMcX, ty = (a.vol.dims[1] - 2 + kMcY - 1) / kMcY,
               tz = (a.vol.dims[2] - 2 + ZR - 1) / ZR;
     const long nt = (long)tx * ty * tz;
@@ -854,8 +856,10 @@ size_t sort_unique_workspace_size(long n_max) {
 }
 
 static int sort_cluster_size() {
-    static int cached = 0;
-    if (!cached) {
+    static ContextOnce once;
+    static int cached_dev[kMaxDevices];
+    once_per_context(once, [](int dev) {
+        int cached = 0;
         cudaFuncSetAttribute(sort_unique_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
         const int sizes[2] = {kSortCluster, 8};
         for (int c : sizes) {
@@ -876,9 +880,12 @@ static int sort_cluster_size() {
             }
             cudaGetLastError();
         }
-        if (!cached) cached = 8;
-    }
-    return cached;
+        cached_dev[dev] = cached ? cached : 8;
+        return (int)AFX_OK;
+    });
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return cached_dev[dev] ? cached_dev[dev] : 8;
 }
 
 static int sort_unique_cluster(float* pts, unsigned* count, long n_max, void* ws, size_t ws_bytes, cudaStream_t st,
@@ -1123,12 +1130,11 @@ int sort_unique_volume_impl(float* pts, unsigned* count, long n_max, void* ws, s
     BucketWs w{u, u + nb, u + 2 * nb + 1, u + 3 * nb + 1, u + 4 * nb + 1, u + 5 * nb + 2};
     Key3* keys = reinterpret_cast<Key3*>(ws);  // the cluster sort's first buffer (it rebuilds it from the cloud)
     BucketArgs a{vol.half[0], vol.inv[0], nb};
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(kBucketCap * sizeof(Key3)));
-        attr = true;
-    }
+    static ContextOnce once;
+    once_per_context(once, [](int) {
+        return note_cuda_error(cudaFuncSetAttribute(bucket_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                    (int)(kBucketCap * sizeof(Key3))));
+    });
     AFX_CUDA(cudaMemsetAsync(w.cnt, 0, nb * 4, st));
     AFX_CUDA(cudaMemsetAsync(w.overflow, 0, 4, st));
     bucket_count_kernel<<<grid_for(n_max, 256), 256, 0, st>>>(pts, count, n_max, a, w.cnt);

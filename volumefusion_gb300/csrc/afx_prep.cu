@@ -7,8 +7,10 @@
 
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "afx_common.cuh"
+#include "afx_host.h"
 #include "afx_tma.h"
 
 namespace afx {
@@ -390,9 +392,8 @@ __global__ void remove_without_normals_kernel(const float* normals, float* V, fl
 
 EncodeTiledFn encode_fn() {
     static EncodeTiledFn fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static std::once_flag once;
+    std::call_once(once, [] {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
@@ -401,7 +402,7 @@ EncodeTiledFn encode_fn() {
             fn = reinterpret_cast<EncodeTiledFn>(p);
         else
             cudaGetLastError();
-    }
+    });
     return fn;
 }
 
@@ -420,19 +421,29 @@ static bool make_u16_tile_map(CUtensorMap* map, const uint16_t* base, int width,
     return r == CUDA_SUCCESS;
 }
 
-// Per-thread scratch for the prep launch: centroid accumulators and the error word.
+// Scratch of the stand-alone afx_frame_prep: centroid accumulators (zero between calls: the
+// finalising kernel clears them) and the error word.  One per host thread and device, allocated
+// on the thread's first call and kept for the life of the process, so calls from different host
+// threads never share it; calls from one thread on different streams must not overlap.
 struct PrepScratch {
     unsigned long long acc[4];
     int error;
 };
 
 static PrepScratch* prep_scratch() {
-    static PrepScratch* s = nullptr;  // one per process; calls on different streams must not overlap
-    if (!s) {
-        if (cudaMalloc(&s, sizeof(PrepScratch)) != cudaSuccess) return nullptr;
-        cudaMemset(s, 0, sizeof(PrepScratch));
+    thread_local PrepScratch* s[kMaxDevices] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nullptr;
+    if (!s[dev]) {
+        PrepScratch* p = nullptr;
+        if (cudaMalloc(&p, sizeof(PrepScratch)) != cudaSuccess) return nullptr;
+        if (cudaMemset(p, 0, sizeof(PrepScratch)) != cudaSuccess) {
+            cudaFree(p);
+            return nullptr;
+        }
+        s[dev] = p;
     }
-    return s;
+    return s[dev];
 }
 
 int frame_prep_impl(const uint16_t* mm, int width, int height, const afx_prep_params* p, float* depth, float* vertices,
