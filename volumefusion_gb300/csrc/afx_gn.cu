@@ -523,7 +523,52 @@ struct ClusterSums {
     double warp[kLoopWarps * 4];  // per-warp sums
     double total[4];
     int phase;
+    // PCG scalars, written by lane 0 of warp 0 and read by every thread after a __syncthreads
+    double rz, bnorm2;  // r.z of the current iterate, b.b
+    float alpha, beta;
+    int stop;
 };
+
+// A binary64 value as m * 2^e with m a binary32 in [1, 2): the 53-bit significand rounded to 24
+// bits (nearest, ties to even) with integer operations only.  Zero and subnormal doubles give 0,
+// infinities and NaN their binary32 counterparts (e = 0).
+AFX_D float split_f64(double x, int& e) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int ex = (int)((b >> 52) & 0x7ff);
+    const unsigned long long man = b & 0xFFFFFFFFFFFFFull;
+    e = 0;
+    if (ex == 0) return __uint_as_float(sign);
+    if (ex == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (man ? 0x400000u : 0u));
+    unsigned long long q = (man | (1ull << 52)) >> 29;
+    const unsigned long long rem = man & ((1ull << 29) - 1), half = 1ull << 28;
+    if (rem > half || (rem == half && (q & 1ull))) ++q;
+    int adj = 0;
+    if (q == (1ull << 24)) {
+        q >>= 1;
+        adj = 1;
+    }
+    e = ex - 1023 + adj;
+    return __uint_as_float(sign | (127u << 23) | (unsigned)(q & 0x7FFFFFull));
+}
+
+// (float)(a / b) to within about one binary32 ulp, without binary64 arithmetic: the operands are
+// split exactly into binary32 significands and powers of two (split_f64), the significands divided
+// in binary32 (correctly rounded) and the quotient scaled by the power of two.  The PCG step sizes
+// are binary32 in every use, and this part's binary64 division is slow: every thread of a CTA
+// dividing in binary64 cost more than the cluster barrier of the iteration.
+AFX_D float f32_quotient(double a, double b) {
+    int ea, eb;
+    const float ma = split_f64(a, ea), mb = split_f64(b, eb);
+    return ldexpf(ma / mb, ea - eb);
+}
+
+// pap == 0 or NaN, by the bit pattern (no binary64 comparison).
+AFX_D bool zero_or_nan(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+    return b == 0ull || b > 0x7FF0000000000000ull;
+}
+
 
 // Sums v[0..NV) over every thread of the cluster; all threads of all CTAs get identical totals.
 // Fixed-shape FP64 trees: butterfly within each warp, then over the CTA's warps, then over the
@@ -674,6 +719,7 @@ struct DsLayout {
     float* pf;      // [kDsNodes * 6] full copy of the search direction (each CTA forms it)
     float* x;       // [kDsNpc * 6] own slices
     float* r;
+    float* ap;      // [kDsNpc * 6] own slice of A p
     float* minv;    // [kDsNpc * 36]
     float* blk;     // [kDsBlocks * 36]
     int* col;       // [kDsBlocks] neighbour node of each block
@@ -682,7 +728,7 @@ struct DsLayout {
     int* misc;      // [4]
 };
 
-constexpr size_t kDsSmem = sizeof(float) * ((size_t)kDsNodes * 12 + 2 * kDsNpc * 6 + kDsNpc * 36 + (size_t)kDsBlocks * 36) +
+constexpr size_t kDsSmem = sizeof(float) * ((size_t)kDsNodes * 12 + 3 * kDsNpc * 6 + kDsNpc * 36 + (size_t)kDsBlocks * 36) +
                            sizeof(int) * (kDsBlocks + kDsNpc + 1 + 4) + sizeof(double) * 2 * kDsMaxCta * 4 + 64;
 
 AFX_D DsLayout ds_layout(void* base) {
@@ -697,6 +743,8 @@ AFX_D DsLayout ds_layout(void* base) {
     d.x = f;
     f += kDsNpc * 6;
     d.r = f;
+    f += kDsNpc * 6;
+    d.ap = f;
     f += kDsNpc * 6;
     d.minv = f;
     f += kDsNpc * 36;
@@ -814,8 +862,49 @@ AFX_D bool ds_stage(const GnBuffers& b, int n, const DsLayout& d, ClusterSums& c
     return true;
 }
 
-// One PCG solve (same recurrences and arithmetic as the global-memory path), then
-// T_pending -= [x] for the own nodes.  J^T r is read from b.jtr.
+// FP64 dot products x[i] . y[i] of the CTA's own entries (cnt floats each, in shared memory),
+// summed over the cluster.  Warp 0 alone does binary64 work: lane l accumulates entries l, l + 32,
+// ... with fused multiply-adds (the product of two binary32 values is exact in binary64, so each
+// step rounds once, as product-then-add would), a butterfly gives the CTA's sum, and lane q sends
+// it into slot [ph][rank] of CTA q.  After the cluster barrier warp 0 of every CTA adds the slots in
+// one fixed tree, so all CTAs hold bit-identical totals.  Returns true in lane 0 of warp 0 only,
+// with the totals in t; the caller turns them into the scalars every thread reads after the next
+// __syncthreads.
+template <int NV>
+AFX_D bool ds_dot(const float* const (&x)[NV], const float* const (&y)[NV], int cnt, const DsLayout& d, int& ph,
+                  double (&t)[NV]) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned rank = cluster_rank(), ncta = cluster_size();
+    __syncthreads();  // the staged vectors are complete
+    if (w == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double s = 0.0;
+            for (int o = lane; o < cnt; o += 32) s = fma((double)x[i][o], (double)y[i][o], s);
+            s = warp_sum(s);
+            if (lane < (int)ncta) dsmem_store_f64(d.slot + (ph * kDsMaxCta + rank) * 4 + i, lane, s);
+        }
+    }
+    cluster_barrier();
+    const int p = ph;
+    ph ^= 1;
+    if (w != 0) return false;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        double v = lane < (int)ncta ? d.slot[(p * kDsMaxCta + lane) * 4 + i] : 0.0;
+#pragma unroll
+        for (int o = kDsMaxCta / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        t[i] = v;
+    }
+    return lane == 0;
+}
+
+// One PCG solve (same recurrences as the global-memory path), then T_pending -= [x] for the own
+// nodes.  J^T r is read from b.jtr.  Per iteration: p = z + beta p over all nodes (each CTA keeps a
+// full copy of p and of z), A p of the own rows with up to 32 lanes per row (each summing a fixed
+// stride of the row's blocks, then a butterfly), p.Ap (cluster dot), the own x / r / z updates with
+// z sent to every CTA's copy, r.z (and r.r when a tolerance is set; cluster dot).  The step sizes
+// are formed once per CTA by lane 0 (f32_quotient) and read from shared memory.
 AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, int& ph) {
     const GnBuffers& b = L.g.b;
     const unsigned rank = cluster_rank(), ncta = cluster_size();
@@ -825,11 +914,16 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
     const int grp = lane / 6, ei = lane - 6 * grp;
     const int li = w * 5 + grp;  // kLoopWarps * 5 >= kDsNpc: one own node per lane group
     const bool act = lane < 30 && li < own;
-    const bool live = w * 5 < own;  // this warp owns at least one node
     const int o = li * 6 + ei;
     const int gnode = start + li;
+    const int cnt = own * 6;
+    const bool tol = L.tol > 0;
+    float* zown = d.z + (long)start * 6;
+    float* pown = d.pf + (long)start * 6;
+    // SpMV lanes per row: the largest power of two with every own row covered in one pass
+    int R = 1;
+    while (R < 32 && 2 * R * cnt <= (int)blockDim.x) R <<= 1;
     // x = 0, r = b, z = M^-1 r
-    double d2[2] = {0.0, 0.0};
     {
         const float ji = act ? __ldcg(b.jtr + (long)gnode * 6 + ei) : 0.f;
         float zi = 0.f;
@@ -841,42 +935,67 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
         if (act) {
             d.x[o] = 0.f;
             d.r[o] = ji;
-            for (unsigned q = 0; q < ncta; ++q) dsmem_store_f32(d.z + (long)gnode * 6 + ei, q, zi);
-            d2[0] += (double)ji * (double)zi;
-            d2[1] += (double)ji * (double)ji;
+            zown[o] = zi;
+            for (unsigned q = 0; q < ncta; ++q)
+                if (q != rank) dsmem_store_f32(d.z + (long)gnode * 6 + ei, q, zi);
         }
     }
-    ds_sum<2>(d2, d, cs, ph, live);
-    double rz = d2[0];
-    const double bnorm2 = d2[1];
+    {
+        double t[2];
+        bool lead;
+        if (tol) lead = ds_dot<2>({d.r, d.r}, {zown, d.r}, cnt, d, ph, t);
+        else {
+            double t1[1];
+            lead = ds_dot<1>({d.r}, {zown}, cnt, d, ph, t1);
+            t[0] = t1[0];
+            t[1] = 0.0;
+        }
+        if (lead) {
+            cs.rz = t[0];
+            cs.bnorm2 = t[1];
+            cs.stop = 0;
+        }
+    }
+    __syncthreads();
     float beta = 0.f;
     for (int it = 0; it < L.pcg_iters; ++it) {
         // p = z (first iteration) or z + beta p, formed for all nodes by every CTA from its copies
         for (int i = threadIdx.x; i < n * 6; i += blockDim.x) d.pf[i] = it ? d.z[i] + beta * d.pf[i] : d.z[i];
         __syncthreads();
-        double pap[1] = {0.0};
-        float api = 0.f, pi = 0.f;
-        if (act) {
-            const int r0 = d.rowptr[li], r1 = d.rowptr[li + 1];
-            for (int bk = r0; bk < r1; ++bk) {
-                const float* B = d.blk + bk * 36 + ei * 6;
-                const float* x = d.pf + d.col[bk] * 6;
-                float s = 0.f;
+        // A p of the own rows
+        const int rows_per_pass = (int)blockDim.x / R;
+        for (int base = 0; base < cnt; base += rows_per_pass) {
+            const int q = base + (int)threadIdx.x / R, part = (int)threadIdx.x % R;
+            float acc = 0.f;
+            if (q < cnt) {
+                const int l = q / 6, e = q - 6 * l;
+                const int r1 = d.rowptr[l + 1];
+                for (int bk = d.rowptr[l] + part; bk < r1; bk += R) {
+                    const float* B = d.blk + bk * 36 + e * 6;
+                    const float* xv = d.pf + d.col[bk] * 6;
+                    float s = 0.f;
 #pragma unroll
-                for (int j = 0; j < 6; ++j) s = s + B[j] * x[j];
-                api = api + s;
+                    for (int j = 0; j < 6; ++j) s = s + B[j] * xv[j];
+                    acc = acc + s;
+                }
             }
-            pi = d.pf[(long)gnode * 6 + ei];
-            pap[0] += (double)pi * (double)api;
+            for (int m = R / 2; m > 0; m >>= 1) acc = acc + __shfl_xor_sync(0xffffffffu, acc, m);
+            if (q < cnt && part == 0) d.ap[q] = acc;
         }
-        ds_sum<1>(pap, d, cs, ph, live);
-        if (pap[0] == 0.0 || !(pap[0] == pap[0])) break;
-        const float alpha = (float)(rz / pap[0]);
-        double q2[2] = {0.0, 0.0};
+        {
+            double t[1];
+            if (ds_dot<1>({pown}, {d.ap}, cnt, d, ph, t)) {
+                cs.stop = zero_or_nan(t[0]) ? 1 : 0;
+                cs.alpha = cs.stop ? 0.f : f32_quotient(cs.rz, t[0]);
+            }
+        }
+        __syncthreads();
+        if (cs.stop) break;
+        const float alpha = cs.alpha;
         float rv = 0.f;
         if (act) {
-            d.x[o] = d.x[o] + alpha * pi;
-            rv = d.r[o] - alpha * api;
+            d.x[o] = d.x[o] + alpha * pown[o];
+            rv = d.r[o] - alpha * d.ap[o];
             d.r[o] = rv;
         }
         float zi = 0.f;
@@ -885,15 +1004,31 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
             const float rq = __shfl_sync(0xffffffffu, rv, lane < 30 ? grp * 6 + q : q);
             if (act) zi = zi + d.minv[li * 36 + ei * 6 + q] * rq;
         }
+        // z is read (forming p) before the p.Ap barrier in every CTA, so it can be overwritten here
         if (act) {
-            for (unsigned q = 0; q < ncta; ++q) dsmem_store_f32(d.z + (long)gnode * 6 + ei, q, zi);
-            q2[0] += (double)rv * (double)zi;
-            q2[1] += (double)rv * (double)rv;
+            zown[o] = zi;
+            for (unsigned q = 0; q < ncta; ++q)
+                if (q != rank) dsmem_store_f32(d.z + (long)gnode * 6 + ei, q, zi);
         }
-        ds_sum<2>(q2, d, cs, ph, live);
-        beta = (float)(q2[0] / rz);
-        rz = q2[0];
-        if (L.tol > 0 && q2[1] <= L.tol * L.tol * bnorm2) break;
+        {
+            double t[2];
+            bool lead;
+            if (tol) lead = ds_dot<2>({d.r, d.r}, {zown, d.r}, cnt, d, ph, t);
+            else {
+                double t1[1];
+                lead = ds_dot<1>({d.r}, {zown}, cnt, d, ph, t1);
+                t[0] = t1[0];
+                t[1] = 0.0;
+            }
+            if (lead) {
+                cs.beta = f32_quotient(t[0], cs.rz);
+                cs.rz = t[0];
+                cs.stop = (tol && t[1] <= L.tol * L.tol * cs.bnorm2) ? 1 : 0;
+            }
+        }
+        __syncthreads();
+        beta = cs.beta;
+        if (cs.stop) break;
     }
     // T_pending -= [[x_rot]x, x_t; 0] for the own nodes (updateTransformsKernel,
     // src/MotionOptimization.cu:483-498); x also to global memory for inspection
@@ -1036,8 +1171,8 @@ AFX_D void pcg_global(const LoopArgs& L, int n, ClusterSums& cs) {
                 pap[0] += (double)__ldcg(b.p + o) * (double)api;
             }
         cluster_sum<1>(pap, cs);
-        if (pap[0] == 0.0 || !(pap[0] == pap[0])) break;
-        const float alpha = (float)(rz / pap[0]);
+        if (zero_or_nan(pap[0])) break;
+        const float alpha = f32_quotient(rz, pap[0]);
         // x += alpha p; r -= alpha A p; z = M^-1 r; r.z, r.r
         double q2[2] = {0.0, 0.0};
         for (int base = gw * 5; base < n; base += gstep) {
@@ -1064,7 +1199,7 @@ AFX_D void pcg_global(const LoopArgs& L, int n, ClusterSums& cs) {
             }
         }
         cluster_sum<2>(q2, cs);
-        beta = (float)(q2[0] / rz);
+        beta = f32_quotient(q2[0], rz);
         rz = q2[0];
         if (L.tol > 0 && q2[1] <= L.tol * L.tol * bnorm2) break;
     }
