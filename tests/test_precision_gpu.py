@@ -182,3 +182,29 @@ def test_precision_512_runs_clean_and_stays_near_fp32():
     assert frac > 0.8 and float(q[0]) <= 5e-4, (frac, q)
     s16.close()
     s32.close()
+
+
+@pytest.mark.gpu
+def test_precision_512_error_against_fp64_oracle():
+    """The full-size precision workload (512^3 at 2 mm, about a thousand nodes at frame 1), FP16
+    values with uint16 weights and FP32 storage side by side, frames 0-1 against the binary64
+    oracle run from each session's own state.  Frame 0 (rigid) is bounded as in the small case.  At
+    frame 1 the warp parameters of every arithmetic part: the normal equations of this graph are
+    nearly singular and ten PCG iterations do not converge on them (the binary64 oracle's own
+    binary32-storage twin lands as far from it), so the warp error is reported, and the FP16 form
+    is bounded by the FP32 form's own error plus the binary16 rounding of stored values."""
+    import time
+    from volumefusion_gb300 import configs
+    cfg16 = configs.precision_capsules_512()
+    cfg32 = dict(cfg16, precision="fp32")
+    frames = configs.capsule_frames(cfg16, frames=range(2))
+    t0 = time.time()
+    r16 = _error_vs_fp64(cfg16, frames)
+    r32 = _error_vs_fp64(cfg32, frames)
+    print("\nFP64_ERROR_REPORT_512 " + json.dumps({"config": "precision_capsules_512 512^3 @ 2 mm, frames 0-1",
+                                                    "fp16": r16, "fp32": r32, "seconds": round(time.time() - t0, 1)}))
+    for a, b in zip(r32, r16):
+        assert b["tsdf_p50"] <= 5e-4 and b["tsdf_p99"] <= a["tsdf_p99"] + 5e-4, (a, b)
+        if b["frame"] > 0:
+            assert b["mesh_p50_vox"] <= a["mesh_p50_vox"] + 0.05, (a, b)
+            assert b["mesh_p99_vox"] <= a["mesh_p99_vox"] + 0.5, (a, b)
