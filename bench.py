@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-rigid-stream", action="store_true")
+    ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--served-streams", type=int, default=64)
+    ap.add_argument("--served-seconds", type=float, default=4.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-frames", type=int, default=3)
@@ -391,6 +394,131 @@ def batched_arm(args, stream, barrier, reduce_max, world):
     return out
 
 
+def served_arm(args, rank):
+    """Many depth streams through afx_server: (1) the offered load -- N streams at 30 fps with
+    exponential inter-arrival times (mean 33 ms), sessions drawn from the mixed workload, each
+    stream closing its session after its 30-frame sequence and opening a new one (admission by a
+    150 GB budget); (2) capacity -- the same sessions with frames submitted as fast as their
+    four slots allow; (3) the plain per-stream drop-in -- those sessions' frames one session at
+    a time through FusionSession, nothing overlapping."""
+    import heapq
+
+    import torch
+    from volumefusion_gb300 import configs
+    from volumefusion_gb300.fusion import FusionSession
+    from volumefusion_gb300.serve import Server
+
+    n = args.served_streams
+    pool = configs.session_mix(4 * n, seed=7 + rank)
+    for c in pool:
+        configs.scene_frames(c)  # synthesise outside the timed regions
+    budget = 150 << 30
+    rng = np.random.default_rng(11 + rank)
+    # (1) offered load
+    srv = Server(budget, max_sessions=4 * n)
+    next_cfg = 0
+    streams = []  # [session id, cfg, frames submitted, frames done]
+    for _ in range(n):
+        cfg = pool[next_cfg % len(pool)]
+        next_cfg += 1
+        streams.append([srv.open(cfg), cfg, 0, 0])
+    t0 = time.perf_counter()
+    due = [(t0 + float(rng.exponential(1 / 30.0)), k) for k in range(n)]
+    heapq.heapify(due)
+    lat, done, denied_reopen, peak, errors = [], 0, 0, 0, 0
+    t_end = t0 + args.served_seconds
+    while True:
+        now = time.perf_counter()
+        if now >= t_end and not due:
+            break
+        while due and due[0][0] <= now:
+            t_arr, k = heapq.heappop(due)
+            sid, cfg, sent, _ = streams[k]
+            if sid is None:  # not admitted yet: retry the open
+                sid = streams[k][0] = srv.open(cfg)
+            # a frame that finds the session's sequence complete or its slots full is dropped
+            if sid is not None and sent < 30 and srv.submit(sid, configs.scene_frame(cfg, sent), tag=sent):
+                streams[k][2] += 1
+            if now < t_end:
+                heapq.heappush(due, (t_arr + float(rng.exponential(1 / 30.0)), k))
+        for sid_r, tag, ms, st in srv.poll():
+            lat.append(ms)
+            done += 1
+            errors += st["error"] != 0
+            for k, x in enumerate(streams):
+                if x[0] == sid_r:
+                    x[3] += 1
+                    if x[3] == 30:  # sequence finished: close, open the next session
+                        srv.close_session(sid_r)
+                        cfg = pool[next_cfg % len(pool)]
+                        next_cfg += 1
+                        nsid = srv.open(cfg)
+                        denied_reopen += nsid is None
+                        streams[k] = [nsid, cfg, 0, 0]
+                    break
+        peak = max(peak, srv.usage()["used_bytes"])
+        if not due or due[0][0] > time.perf_counter():
+            time.sleep(0.0002)
+    torch.cuda.synchronize()  # drain: every frame in flight completes
+    while True:
+        r = srv.poll()
+        if not r:
+            break
+        lat += [x[2] for x in r]
+        done += len(r)
+    wall = time.perf_counter() - t0
+    usage = srv.usage()
+    srv.close()
+    offered = {"streams": n, "seconds": round(wall, 3), "frames": done, "frames_per_s": done / wall,
+               "latency_ms_p50": float(np.percentile(lat, 50)) if lat else None,
+               "latency_ms_p99": float(np.percentile(lat, 99)) if lat else None,
+               "peak_bytes": int(peak), "denied_opens": int(usage["denied"]), "frames_with_error_flags": int(errors)}
+    # (2) capacity and (3) plain drop-in on the same sessions and frames
+    cap_cfgs = pool[:n]
+    frames_per = 30
+    srv = Server(budget, max_sessions=n)
+    sids = [srv.open(c) for c in cap_cfgs]
+    sent = [0] * n
+    got = 0
+    want = frames_per * sum(s is not None for s in sids)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    host_s = 0.0  # time the driver loop spends inside submit and poll (host work per frame)
+    while got < want and time.perf_counter() - t0 < 120.0:
+        for k, sid in enumerate(sids):
+            while sid is not None and sent[k] < frames_per:
+                h0 = time.perf_counter()
+                ok = srv.submit(sid, configs.scene_frame(cap_cfgs[k], sent[k]))
+                host_s += time.perf_counter() - h0
+                if not ok:
+                    break
+                sent[k] += 1
+        h0 = time.perf_counter()
+        got += len(srv.poll())
+        host_s += time.perf_counter() - h0
+    cap_s = time.perf_counter() - t0
+    srv.close()
+    served_fps = got / cap_s
+    plain_frames, plain_s = 0, 0.0
+    for c in cap_cfgs:  # creation and teardown outside the timed part
+        s = FusionSession(c)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(frames_per):
+            s.process(configs.scene_frame(c, i))
+            s.stats()  # the per-frame result the plain drop-in hands back
+            plain_frames += 1
+        plain_s += time.perf_counter() - t0
+        s.close()
+    plain_fps = plain_frames / plain_s
+    return {"offered_load": offered,
+            "capacity": {"sessions": int(sum(s is not None for s in sids)), "frames": got, "frames_per_s": served_fps,
+                         "host_busy_frac": host_s / cap_s},
+            "plain_per_stream": {"frames": plain_frames, "frames_per_s": plain_fps,
+                                 "note": "same sessions and frames, one session at a time, host frames"},
+            "capacity_over_plain": served_fps / plain_fps}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -563,6 +691,10 @@ def main():
     if not args.no_batched:
         batched = batched_arm(args, stream, barrier, reduce_max, world)
 
+    served = None
+    if not args.no_served:
+        served = served_arm(args, rank)
+
     # ---- roofline of the dominant stage ----
     per_frame = {k: v / frames for k, v in stage_ms.items()}
     dom = max(per_frame, key=per_frame.get)
@@ -614,6 +746,7 @@ def main():
             "batched": batched,
             "rigid_stream": rigid,
             "rigid_integration": rigid_int,
+            "served": served,
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": sampler.summary(),

@@ -1280,7 +1280,10 @@ __global__ void __launch_bounds__(kLoopThreads, 1) gn_loop_kernel(LoopArgs L) {
     __shared__ ClusterSums cs;
     extern __shared__ double ds_smem[];
     if (threadIdx.x == 0) cs.phase = 0;
-    __syncthreads();
+    // Every CTA of the cluster must be running before any thread touches another CTA's shared
+    // memory (the first such store is in ds_stage).  Under load the CTAs of a cluster need not
+    // start together; a store into a CTA that has not started is an SM fault.
+    cluster_barrier();
     const unsigned rank = cluster_rank(), ncta = cluster_size();
     const int w = threadIdx.x >> 5;
     const long gt = (long)rank * kLoopThreads + threadIdx.x, gstride = (long)ncta * kLoopThreads;
@@ -1338,7 +1341,7 @@ __global__ void __launch_bounds__(kLoopThreads, 1) gn_solve_kernel(LoopArgs L) {
     __shared__ ClusterSums cs;
     extern __shared__ double ds_smem[];
     if (threadIdx.x == 0) cs.phase = 0;
-    __syncthreads();
+    cluster_barrier();  // every CTA running before any access to another CTA's shared memory
     const unsigned rank = cluster_rank(), ncta = cluster_size();
     const long gt = (long)rank * kLoopThreads + threadIdx.x, gstride = (long)ncta * kLoopThreads;
     const int n = min(*a.n_nodes, a.n_max);
