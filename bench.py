@@ -20,6 +20,7 @@ import argparse
 import ctypes as C
 import json
 import os
+import platform
 import subprocess
 import sys
 import threading
@@ -109,6 +110,39 @@ def dist_setup(n):
     return dist
 
 
+def headline_config(cfg, clip, world):
+    """The workload description both arms report (the reference arm times the same steps)."""
+    return {"workload": cfg["name"],
+            "frames": "640x576 capsule pair, 30-frame sequence",
+            "step": "reset + frames 0..%d (frame 0 rigid)" % (clip - 1),
+            "volume": "256^3 FP32 TSDF @ 4 mm (134 MB tsdf+weights, larger than L2)",
+            "graph_radius_mm": 25, "knn": 4, "kreg": 8, "gn": "1 ICP x 5 GN x 10 PCG",
+            "parallelism": "replicas" if world > 1 else "single",
+            "l2": "GPU arm: L2 flushed between steps (256 MiB write)"}
+
+
+def cpu_model():
+    """The host CPU's model name and logical core count."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                name = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not name:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith("model name"):
+                    name = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return {"model": name or platform.processor() or platform.machine(), "nproc": os.cpu_count()}
+
+
 def cpu_baseline(cfg, frames_np, n_frames):
     """Oracle port of the reference path on the host cores (all threads)."""
     from oracle import pyoracle as O
@@ -122,13 +156,10 @@ def cpu_baseline(cfg, frames_np, n_frames):
     return n_frames / dt, dt
 
 
-REF_FRAMES_PER_STEP = 4
-
-
 def run_reference(args):
-    """The reference's CPU path (the oracle's restatement of it) on the host cores.  A step is a
-    bounded sample of the workload: the first REF_FRAMES_PER_STEP frames of the sequence from
-    an empty volume (frame 0 rigid, then non-rigid frames)."""
+    """The reference's CPU path (the oracle's restatement of it) on the host cores, on the GPU
+    arm's workload: a step is the same reset + frames 0..clip-1 of the sequence (frame 0 rigid,
+    then non-rigid frames), all host threads."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
@@ -137,10 +168,12 @@ def run_reference(args):
     frames_np = configs.capsule_frames(cfg)
     from oracle import pyoracle as O
 
+    clip = max(1, min(args.clip, N_FRAMES))
+
     def step():
-        o = O.Fusion(dict(cfg))
         t0 = time.perf_counter()
-        for f in range(REF_FRAMES_PER_STEP):
+        o = O.Fusion(dict(cfg))  # the reset: an empty volume and graph
+        for f in range(clip):
             o.process(frames_np[f])
         dt = time.perf_counter() - t0
         o.close()
@@ -149,20 +182,18 @@ def run_reference(args):
     for _ in range(args.warmup):
         step()
     dt = sum(step() for _ in range(args.steps))
-    n = args.steps * REF_FRAMES_PER_STEP
+    n = args.steps * clip
     fps = n / dt
     cores = os.cpu_count()
+    host = cpu_model()
     line = {
         "impl": "reference", "metric": "nonrigid_frames_per_s_256", "value": fps, "unit": "frames/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": cfg["name"], "frames": "640x576 capsule pair, 30-frame sequence",
-                   "volume": "256^3 FP32 TSDF @ 4 mm", "graph_radius_mm": 25, "knn": 4, "kreg": 8,
-                   "gn": "1 ICP x 5 GN x 10 PCG", "parallelism": "single"},
-        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port",
-                         "sample": "%d steps of the first %d frames of the sequence from an empty volume, after %d "
-                                   "warm-up steps, all host threads (OpenMP)" % (args.steps, REF_FRAMES_PER_STEP,
-                                                                                 args.warmup)},
+        "config": headline_config(cfg, clip, args.gpus),
+        "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": cores, "kind": "port", "cpu": host,
+                         "sample": "%d steps of reset + frames 0..%d (the GPU arm's step), after %d warm-up steps, "
+                                   "all host threads (OpenMP)" % (args.steps, clip - 1, args.warmup)},
         "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -715,7 +746,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and args.cpu_frames > 0:
         v, dt = cpu_baseline(cfg, frames_np, args.cpu_frames)
-        cpu = {"value": v, "unit": "frames/s", "cores": os.cpu_count(), "kind": "port",
+        cpu = {"value": v, "unit": "frames/s", "cores": os.cpu_count(), "kind": "port", "cpu": cpu_model(),
                "sample": "frames 1..%d of the sequence after the rigid frame 0 (%.1f s), all host threads"
                          % (args.cpu_frames, dt)}
 
@@ -724,13 +755,7 @@ def main():
             "metric": "nonrigid_frames_per_s_256", "value": fps, "unit": "frames/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": cfg["name"],
-                       "frames": "640x576 capsule pair, 30-frame sequence",
-                       "step": "reset + frames 0..%d (frame 0 rigid)" % (clip - 1),
-                       "volume": "256^3 FP32 TSDF @ 4 mm (134 MB tsdf+weights, larger than L2)",
-                       "graph_radius_mm": 25, "knn": 4, "kreg": 8, "gn": "1 ICP x 5 GN x 10 PCG",
-                       "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "flushed between steps (256 MiB write)"},
+            "config": headline_config(cfg, clip, world),
             "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": int(frames_np[0].nbytes) * clip,
                     "d2h_bytes_per_step": int(C.sizeof(FrameStats)) * clip,
                     "latency_ms_p50": 1000 * float(np.percentile(lat, 50)),
