@@ -42,6 +42,8 @@ typedef enum afx_status {
 } afx_status;
 
 #define AFX_INVALID_INDEX 0xFFFFFFFFu
+#define AFX_BLEND_LBS 0
+#define AFX_BLEND_DQB 1
 
 const char* afx_status_string(int status);
 int afx_version(void);
@@ -223,6 +225,16 @@ int afx_warp_weights(float* weights, const float* radii, const uint32_t* idx, co
 int afx_warp(float* warped, const float* points, const float* transforms, const uint32_t* idx, const float* weights,
              const unsigned* count, long n_points_max, int k, void* stream);
 
+/* afx_warp with dual-quaternion blending (Kavan et al., "Skinning with dual quaternions", 2007) in
+ * place of the linear blend: each node's rigid part (the unit quaternion of its transform's upper
+ * 3x3, and its translation) as a unit dual quaternion, blended with the weights after aligning
+ * hemispheres with the first valid node, normalised, applied as one rigid motion.  A point whose
+ * weights are all within 1e-5 of zero keeps its position, as in warpKernel.  No counterpart in the
+ * reference, which blends linearly only (src/ComputeCorrespondence.cu:5-30); the blend the session
+ * option `blend = AFX_BLEND_DQB` uses. */
+int afx_warp_dqb(float* warped, const float* points, const float* transforms, const uint32_t* idx,
+                 const float* weights, const unsigned* count, long n_points_max, int k, void* stream);
+
 /* af::runCorrespondencePairsKernel (include/af/ComputeCorrespondence.cuh:19,
  * src/ComputeCorrespondence.cu:83): (vertex, pixel) pairs, ordered by vertex index.
  * *corr_count (device) is overwritten. */
@@ -320,6 +332,10 @@ typedef struct afx_fusion_params {
                                     AFX_PRECISION_FP16: FP16 TSDF values + uint16 weights, 4 B/voxel */
     int warp_mesh;               /* settings.isMeshWarped: warp the output mesh into the live frame
                                     (details::warpMeshGPU, src/VolumeFusion.cu:75-110) */
+    int blend;                   /* AFX_BLEND_LBS (the reference's linear blend of node transforms) or
+                                    AFX_BLEND_DQB (dual-quaternion blending of their rigid parts) for
+                                    every warp: canonical points, voxel centres, output mesh.  The
+                                    Gauss-Newton Jacobian is the linear blend's in both cases. */
 } afx_fusion_params;
 
 #define AFX_PRECISION_FP32 0

@@ -61,6 +61,7 @@ def lib():
             "vfo_filter_disconnected": (None, [u32p, f32p, C.c_int, C.c_int, f32p]),
             "vfo_warp_weights": (None, [f32p, f32p, u32p, f32p, C.c_long, C.c_int, C.c_int]),
             "vfo_warp": (None, [f32p, f32p, C.c_long, f32p, u32p, f32p, C.c_int]),
+            "vfo_warp_dqb": (None, [f32p, f32p, C.c_long, f32p, u32p, f32p, C.c_int]),
             "vfo_correspondences": (C.c_long, [i32p, C.c_long, f32p, C.c_long, f32p, f32p, C.c_int, C.c_int, f32p,
                                                C.c_float]),
             "vfo_residual_depth": (None, [f32p, i32p, C.c_long, f32p, f32p, f32p, C.c_float]),
@@ -302,6 +303,14 @@ def warp(pts, transforms, idx, w):
     return out
 
 
+def warp_dqb(pts, transforms, idx, w):
+    """Dual-quaternion blend of the node transforms (Kavan et al. 2007; no counterpart in the reference)."""
+    idx = np.ascontiguousarray(idx, np.uint32)
+    out = np.empty((len(pts), 3), np.float32)
+    lib().vfo_warp_dqb(out, _f32(pts), len(pts), _f32(transforms), idx, _f32(w), idx.shape[1])
+    return out
+
+
 def correspondences(warped, K, depth, frame_mesh, thr):
     h, w = depth.shape
     m = len(warped)
@@ -436,7 +445,7 @@ class VfoParams(C.Structure):
                 ("icp_iterations", C.c_int), ("gn_iterations", C.c_int), ("lambda_depth", C.c_float),
                 ("lambda_reg", C.c_float), ("energy_min_step", C.c_float), ("corr_thresh", C.c_float),
                 ("solver", C.c_int), ("pcg_iterations", C.c_int), ("pcg_tol", C.c_double), ("integrate", C.c_int),
-                ("node_cap", C.c_int), ("mesh_cap", C.c_long), ("precision", C.c_int)]
+                ("node_cap", C.c_int), ("mesh_cap", C.c_long), ("precision", C.c_int), ("blend", C.c_int)]
 
 
 class Fusion:
@@ -459,6 +468,7 @@ class Fusion:
             setattr(p, key, int(cfg[key]))
         p.pcg_tol = float(cfg.get("pcg_tol", 0.0))
         p.precision = {"fp32": 0, "fp16": 1}[cfg.get("precision", "fp32")]
+        p.blend = {"lbs": 0, "dqb": 1}[cfg.get("blend", "lbs")]
         self.cfg = cfg
         self._p = p
         self.h = self._L.vfo_fusion_create(C.byref(p))

@@ -651,6 +651,102 @@ void vfo_warp_weights(real* w, const real* radii, const uint32_t* idx, const rea
     }
 }
 
+// ---- dual-quaternion blending (no counterpart in the reference) ----
+// Kavan, Collins, Zara, O'Sullivan, "Skinning with dual quaternions" (I3D 2007).  A node's rigid part
+// is the unit quaternion of its transform's upper 3x3 by Shepperd's method (the largest diagonal
+// combination under the square root, then normalised) with the translation T[12..14]; the nodes of
+// a point are blended as sum_j w_j s_j q_j, s_j = -1 for rotation parts in the other hemisphere from
+// the first valid node's, normalised by the rotation part's norm, and applied as one rigid motion.
+// Operation order as written (-ffp-contract=off), the library's too.
+static void dq_of(const real* T, real* q) {
+    const real m00 = T[0], m10 = T[1], m20 = T[2], m01 = T[4], m11 = T[5], m21 = T[6];
+    const real m02 = T[8], m12 = T[9], m22 = T[10];
+    const real tr = (m00 + m11) + m22;
+    real w, x, y, z;
+    if (tr > (real)0) {
+        const real s = std::sqrt(tr + (real)1) * (real)2;
+        w = (real)0.25 * s;
+        x = (m21 - m12) / s;
+        y = (m02 - m20) / s;
+        z = (m10 - m01) / s;
+    } else if (m00 > m11 && m00 > m22) {
+        const real s = std::sqrt((((real)1 + m00) - m11) - m22) * (real)2;
+        w = (m21 - m12) / s;
+        x = (real)0.25 * s;
+        y = (m01 + m10) / s;
+        z = (m02 + m20) / s;
+    } else if (m11 > m22) {
+        const real s = std::sqrt((((real)1 + m11) - m00) - m22) * (real)2;
+        w = (m02 - m20) / s;
+        x = (m01 + m10) / s;
+        y = (real)0.25 * s;
+        z = (m12 + m21) / s;
+    } else {
+        const real s = std::sqrt((((real)1 + m22) - m00) - m11) * (real)2;
+        w = (m10 - m01) / s;
+        x = (m02 + m20) / s;
+        y = (m12 + m21) / s;
+        z = (real)0.25 * s;
+    }
+    const real n = std::sqrt(((w * w + x * x) + y * y) + z * z);
+    w = w / n;
+    x = x / n;
+    y = y / n;
+    z = z / n;
+    const real tx = T[12], ty = T[13], tz = T[14];
+    q[0] = w;
+    q[1] = x;
+    q[2] = y;
+    q[3] = z;
+    q[4] = (real)-0.5 * ((tx * x + ty * y) + tz * z);
+    q[5] = (real)0.5 * ((w * tx + ty * z) - tz * y);
+    q[6] = (real)0.5 * ((w * ty + tz * x) - tx * z);
+    q[7] = (real)0.5 * ((w * tz + tx * y) - ty * x);
+}
+
+// out = p moved by the blend of the k slots (skipping VFO_INVALID_IDX); p when the weights are all
+// within 1e-5 of zero or the blend's rotation part is zero.
+static void dq_point(const real* T, const uint32_t* idx, const real* w, int k, const real* p, real* out) {
+    out[0] = p[0];
+    out[1] = p[1];
+    out[2] = p[2];
+    bool zero = true;
+    for (int j = 0; j < k; ++j)
+        if (!(std::fabs(w[j]) <= (real)1e-5f)) zero = false;
+    if (zero) return;
+    real b[8] = {0, 0, 0, 0, 0, 0, 0, 0}, r0[4] = {0, 0, 0, 0};
+    bool first = true;
+    for (int j = 0; j < k; ++j) {
+        if (idx[j] == VFO_INVALID_IDX) continue;
+        real q[8];
+        dq_of(T + 16 * (size_t)idx[j], q);
+        if (first) {
+            for (int c = 0; c < 4; ++c) r0[c] = q[c];
+            first = false;
+        }
+        const real d = ((r0[0] * q[0] + r0[1] * q[1]) + r0[2] * q[2]) + r0[3] * q[3];
+        const real ws = d < (real)0 ? -w[j] : w[j];
+        for (int c = 0; c < 8; ++c) b[c] = b[c] + ws * q[c];
+    }
+    const real n = std::sqrt(((b[0] * b[0] + b[1] * b[1]) + b[2] * b[2]) + b[3] * b[3]);
+    if (!(n > (real)0)) return;
+    const real rw = b[0] / n, rx = b[1] / n, ry = b[2] / n, rz = b[3] / n;
+    const real ew = b[4] / n, ex = b[5] / n, ey = b[6] / n, ez = b[7] / n;
+    const real cx = ry * p[2] - rz * p[1], cy = rz * p[0] - rx * p[2], cz = rx * p[1] - ry * p[0];
+    const real ccx = ry * cz - rz * cy, ccy = rz * cx - rx * cz, ccz = rx * cy - ry * cx;
+    const real tx = (real)2 * ((rw * ex - ew * rx) + (ry * ez - rz * ey));
+    const real ty = (real)2 * ((rw * ey - ew * ry) + (rz * ex - rx * ez));
+    const real tz = (real)2 * ((rw * ez - ew * rz) + (rx * ey - ry * ex));
+    out[0] = ((p[0] + (real)2 * rw * cx) + (real)2 * ccx) + tx;
+    out[1] = ((p[1] + (real)2 * rw * cy) + (real)2 * ccy) + ty;
+    out[2] = ((p[2] + (real)2 * rw * cz) + (real)2 * ccz) + tz;
+}
+
+void vfo_warp_dqb(real* out, const real* pts, long m, const real* T, const uint32_t* idx, const real* w, int k) {
+#pragma omp parallel for schedule(static)
+    for (long i = 0; i < m; ++i) dq_point(T, idx + i * k, w + i * k, k, pts + 3 * i, out + 3 * i);
+}
+
 void vfo_warp(real* out, const real* pts, long m, const real* T, const uint32_t* idx, const real* w, int k) {
     // warpKernel (src/ComputeCorrespondence.cu:5-30): identity when all weights are zero (isZero, 1e-5)
 #pragma omp parallel for schedule(static)
@@ -1185,12 +1281,12 @@ int vfo_fusion_process(vfo_fusion* f, const uint16_t* depth_mm) {
     vfo_filter_disconnected(gidx.data(), gdist.data(), n, p.kreg, f->radii.data());
     vfo_warp_weights(mw.data(), f->radii.data(), midx.data(), mdist.data(), m, p.knn, n);
     std::vector<real> warped(3 * (size_t)m);
-    vfo_warp(warped.data(), f->mesh.data(), m, f->T.data(), midx.data(), mw.data(), p.knn);
+    (p.blend ? vfo_warp_dqb : vfo_warp)(warped.data(), f->mesh.data(), m, f->T.data(), midx.data(), mw.data(), p.knn);
     // ICP / Gauss-Newton (:434-691)
     std::vector<real> pending(f->T.size());
     f->gn_done = 0;
     for (int icp = 0; icp < p.icp_iterations; ++icp) {
-        vfo_warp(warped.data(), f->mesh.data(), m, f->T.data(), midx.data(), mw.data(), p.knn);
+        (p.blend ? vfo_warp_dqb : vfo_warp)(warped.data(), f->mesh.data(), m, f->T.data(), midx.data(), mw.data(), p.knn);
         std::vector<int> corr(2 * (size_t)m);
         long c = vfo_correspondences(corr.data(), m, warped.data(), m, f->K, f->depth.data(), p.height, p.width,
                                      f->verts.data(), p.corr_thresh);
@@ -1221,7 +1317,8 @@ int vfo_fusion_process(vfo_fusion* f, const uint16_t* depth_mm) {
             if (st) return -4;
             for (int i = 0; i < 6 * n; ++i) xf[i] = (real)x[i];
             vfo_update_transforms(pending.data(), xf.data(), n);
-            vfo_warp(warped.data(), f->mesh.data(), m, pending.data(), midx.data(), mw.data(), p.knn);
+            (p.blend ? vfo_warp_dqb : vfo_warp)(warped.data(), f->mesh.data(), m, pending.data(), midx.data(), mw.data(),
+                                                p.knn);
             f->gn_done = gn + 1;
         }
     }
@@ -1240,7 +1337,17 @@ int vfo_fusion_process(vfo_fusion* f, const uint16_t* depth_mm) {
     vfo_tsdf_vertices(tv.data(), f->vs, f->vsize, p.dims);
     vfo_translate(f->nodes_dev.data(), n, f->c0);
     vfo_translate(tv.data(), S, f->c0);
-    vfo_warp_tsdf(tv.data(), f->T.data(), kidx.data(), kw.data(), kcount.data(), S, p.knn);
+    if (p.blend) {
+        // dual-quaternion blend of each supported voxel's nodes (its kcount slots)
+#pragma omp parallel for schedule(static)
+        for (long i = 0; i < S; ++i) {
+            if (!kcount[i]) continue;
+            real c[3] = {tv[3 * i], tv[3 * i + 1], tv[3 * i + 2]};
+            dq_point(f->T.data(), kidx.data() + i * p.knn, kw.data() + i * p.knn, kcount[i], c, tv.data() + 3 * i);
+        }
+    } else {
+        vfo_warp_tsdf(tv.data(), f->T.data(), kidx.data(), kw.data(), kcount.data(), S, p.knn);
+    }
     vfo_count_collisions(coll.data(), tv.data(), kcount.data(), f->vs, f->vsize, p.dims, I3, f->c0);
     if (p.integrate)
         vfo_integrate_warped(f->tsdf.data(), f->weights.data(), tv.data(), coll.data(), kcount.data(), f->depth.data(),

@@ -74,6 +74,8 @@ void vfo_knn(const VFO_REAL* nodes, int n_nodes, const VFO_REAL* pts, long m, in
 void vfo_filter_disconnected(uint32_t* idx, VFO_REAL* dist, int n_nodes, int k, const VFO_REAL* radii);
 void vfo_warp_weights(VFO_REAL* w, const VFO_REAL* radii, const uint32_t* idx, const VFO_REAL* dist, long m, int k, int n_nodes);
 void vfo_warp(VFO_REAL* out, const VFO_REAL* pts, long m, const VFO_REAL* transforms, const uint32_t* idx, const VFO_REAL* w, int k);
+/* The same with dual-quaternion blending (Kavan et al. 2007; the session option blend = 1). */
+void vfo_warp_dqb(VFO_REAL* out, const VFO_REAL* pts, long m, const VFO_REAL* transforms, const uint32_t* idx, const VFO_REAL* w, int k);
 
 /* ---- projective correspondences (src/ComputeCorrespondence.cu) ---- */
 long vfo_correspondences(int* corr, long cap, const VFO_REAL* warped, long m, const VFO_REAL K[9], const VFO_REAL* depth,
@@ -130,6 +132,7 @@ typedef struct vfo_params {
     int node_cap;
     long mesh_cap;
     int precision;    /* 0 = FP32 volume, 1 = FP16 values + integer weights (the precision form) */
+    int blend;        /* 0 = linear blend (the reference's), 1 = dual-quaternion blend */
 } vfo_params;
 
 typedef struct vfo_fusion vfo_fusion;

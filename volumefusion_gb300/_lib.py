@@ -29,7 +29,7 @@ class FusionParams(C.Structure):
                 ("gn_iterations", i32), ("lambda_depth", f32), ("lambda_reg", f32), ("energy_min_step", f32),
                 ("corr_thresh", f32), ("solver", i32), ("pcg_iterations", i32), ("pcg_tol", f64), ("integrate", i32),
                 ("extract_mesh", i32), ("node_capacity", i32), ("mesh_capacity", i64), ("triangle_capacity", i64),
-                ("precision", i32), ("warp_mesh", i32)]
+                ("precision", i32), ("warp_mesh", i32), ("blend", i32)]
 
 
 class FrameStats(C.Structure):
@@ -75,6 +75,7 @@ SIGNATURES = {
     "afx_filter_disconnected": (i32, [vp, vp, vp, i32, i32, vp, vp]),
     "afx_warp_weights": (i32, [vp, vp, vp, vp, vp, i64, i32, vp, vp]),
     "afx_warp": (i32, [vp, vp, vp, vp, vp, vp, i64, i32, vp]),
+    "afx_warp_dqb": (i32, [vp, vp, vp, vp, vp, vp, i64, i32, vp]),
     "afx_correspondences": (i32, [vp, vp, i64, vp, vp, i64, vp, vp, i32, i32, vp, f32, vp, sz, vp]),
     "afx_correspondences_workspace_size": (sz, [i64]),
     "afx_correspondences_static": (i32, [vp, vp, i64, vp, vp, i64, vp, vp, i32, i32, vp, f32, vp]),

@@ -221,6 +221,13 @@ def runWarpKernel(warpedMesh, mesh, motionGraph, knnIdxs, knnWeights, meshSize):
                          knnIdxs.shape[-1], _stream()), "runWarpKernel")
 
 
+def warpDualQuaternion(warpedMesh, mesh, motionGraph, knnIdxs, knnWeights, meshSize):
+    """runWarpKernel with dual-quaternion blending of the node transforms (afx_warp_dqb; no
+    counterpart in the reference)."""
+    _sync(lib().afx_warp_dqb(_p(warpedMesh), _p(mesh), _p(motionGraph), _p(knnIdxs), _p(knnWeights), None,
+                             int(meshSize), knnIdxs.shape[-1], _stream()), "warpDualQuaternion")
+
+
 def runCorrespondencePairsKernel(corrIdxs, corrIdxsSize, warpedMesh, warpedMeshSize, K, depth, depthDim, frameMesh,
                                  thresholdDist):
     rows, cols = int(depthDim[0]), int(depthDim[1])

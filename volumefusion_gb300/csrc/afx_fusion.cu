@@ -369,7 +369,8 @@ static bool params_valid(const afx_fusion_params& p) {
     return !(p.width < 3 || p.height < 3 || p.dims[0] < 3 || p.dims[1] < 3 || p.dims[2] < 3 || p.knn < 1 ||
              p.knn > 8 || p.kreg < 1 || p.kreg > 8 || p.node_capacity < 1 || p.mesh_capacity < 1 ||
              p.triangle_capacity < 1 || !(p.graph_radius > 0.f) || p.icp_iterations < 0 || p.gn_iterations < 0 ||
-             p.pcg_iterations < 0 || (p.precision != AFX_PRECISION_FP32 && p.precision != AFX_PRECISION_FP16));
+             p.pcg_iterations < 0 || (p.precision != AFX_PRECISION_FP32 && p.precision != AFX_PRECISION_FP16) ||
+             (p.blend != AFX_BLEND_LBS && p.blend != AFX_BLEND_DQB));
 }
 
 size_t afx_fusion_memory_bytes(const afx_fusion_params* params) {
@@ -564,7 +565,7 @@ static int finish_output_mesh(afx_fusion* f, bool nonrigid, cudaStream_t st) {
     rc = knn_impl(f->vidx, f->vdist, f->nodes_host, f->n_nodes, p.node_capacity, f->mverts, f->nmverts, vmax, p.knn, 0,
                   st);
     if (!rc) rc = warp_weights_impl(f->vw, f->radii, f->vidx, f->vdist, f->nmverts, vmax, p.knn, f->n_nodes, st);
-    if (!rc) rc = warp_impl(f->mverts, f->mverts, f->T, f->vidx, f->vw, f->nmverts, vmax, p.knn, st);
+    if (!rc) rc = warp_impl(f->mverts, f->mverts, f->T, f->vidx, f->vw, f->nmverts, vmax, p.knn, st, p.blend);
     return rc;
 }
 
@@ -676,6 +677,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
     g.lam_d = p.lambda_depth;
     g.lam_r = p.lambda_reg;
     g.min_step = p.energy_min_step;
+    g.blend = p.blend;
     g.b = f->gn;
     g.error = f->error;
     stage_mark(f, ST_GN_SETUP, st);
@@ -684,7 +686,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
     const double tol = p.solver == 2 ? p.pcg_tol : 0.0;
     for (int icp = 0; icp < p.icp_iterations; ++icp) {
         // warp with the committed transforms, then projective correspondences (src/VolumeFusion.cu:439-447)
-        rc = warp_impl(f->warped, points, f->T, f->midx, f->mw, npoints, M, p.knn, st);
+        rc = warp_impl(f->warped, points, f->T, f->midx, f->mw, npoints, M, p.knn, st, p.blend);
         if (rc) return rc;
         rc = correspondences_impl(f->corr, f->ncorr, M, f->warped, npoints, M, p.K, f->depth, p.height, p.width,
                                   f->verts, p.corr_thresh, f->corr_of_vertex, f->ws_corr, f->ws_corr_bytes, st);
@@ -720,6 +722,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
     for (int c = 0; c < 3; ++c) wa.per[c] = f->per[c];
     wa.centroid_dev = f->centroid0;
     std::memcpy(wa.Rinv, I3, sizeof(I3));
+    wa.blend = p.blend;
     wa.out = f->wvox;
     wa.out_count = f->wcount;
     wa.coll = f->coll;

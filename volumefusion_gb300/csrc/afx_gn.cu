@@ -17,6 +17,7 @@
 #include <cstring>
 #include <new>
 
+#include "afx_dqb.cuh"
 #include "afx_gn.h"
 #include "afx_host.h"
 
@@ -1230,9 +1231,26 @@ AFX_D void update_transforms_range(float* T, const float* x, int lo, int hi, lon
     }
 }
 
-// Canonical vertices warped by T (warpKernel, src/ComputeCorrespondence.cu:13-30).
+// Canonical vertices warped by T (warpKernel, src/ComputeCorrespondence.cu:13-30, or the dual-quaternion
+// blend of afx_dqb.cuh).  T is written by other CTAs of this launch: read through L2.
 AFX_D void gn_rewarp(const GnArgs& a, const float* points, float* warped, const float* T, long m, long gt,
                      long gstride) {
+    if (a.blend == AFX_BLEND_DQB) {
+        for (long i = gt; i < m; i += gstride) {
+            const float p[3] = {points[3 * i], points[3 * i + 1], points[3 * i + 2]};
+            float o[3];
+            dq_blend_point(
+                [T](uint32_t nb, float* Tn) {
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) Tn[e] = __ldcg(T + 16 * (long)nb + e);
+                },
+                a.midx + i * a.k, a.mw + i * a.k, a.k, AFX_INVALID_INDEX, p, o);
+            __stcg(warped + 3 * i, o[0]);
+            __stcg(warped + 3 * i + 1, o[1]);
+            __stcg(warped + 3 * i + 2, o[2]);
+        }
+        return;
+    }
     for (long i = gt; i < m; i += gstride) {
         const float p[3] = {points[3 * i], points[3 * i + 1], points[3 * i + 2]};
         bool zero = true;

@@ -68,6 +68,7 @@ struct GnArgs {
     int kreg;
     float lam_d, lam_r;
     float min_step;
+    int blend;                // AFX_BLEND_LBS or AFX_BLEND_DQB for the re-warp of the canonical vertices
     GnBuffers b;
     int* error;
 };

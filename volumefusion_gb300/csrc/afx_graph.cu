@@ -7,6 +7,7 @@
 #include <cstring>
 #include <mutex>
 
+#include "afx_dqb.cuh"
 #include "afx_host.h"
 #include "afx_internal.h"
 
@@ -617,9 +618,29 @@ int warp_weights_impl(float* w, const float* radii, const uint32_t* idx, const f
     return AFX_OK;
 }
 
+// The same points moved by the dual-quaternion blend of their nodes (afx_dqb.cuh).
+__global__ void warp_dqb_kernel(float* out, const float* __restrict__ pts, const float* __restrict__ T,
+                                const uint32_t* __restrict__ idx, const float* __restrict__ w, const unsigned* count,
+                                long m_max, int k) {
+    long m = count ? min((long)*count, m_max) : m_max;
+    AFX_GRID_STRIDE(i, m) {
+        const float p[3] = {pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+        float o[3];
+        dq_blend_point(T, idx + i * k, w + i * k, k, AFX_INVALID_INDEX, p, o);
+        out[3 * i] = o[0];
+        out[3 * i + 1] = o[1];
+        out[3 * i + 2] = o[2];
+    }
+}
+
 int warp_impl(float* out, const float* pts, const float* T, const uint32_t* idx, const float* w, const unsigned* count,
-              long m_max, int k, cudaStream_t st) {
+              long m_max, int k, cudaStream_t st, int blend) {
     if (m_max <= 0) return AFX_OK;
+    if (blend == AFX_BLEND_DQB) {
+        warp_dqb_kernel<<<grid_for(m_max, 256), 256, 0, st>>>(out, pts, T, idx, w, count, m_max, k);
+        AFX_LAUNCH_CHECK();
+        return AFX_OK;
+    }
     warp_kernel<<<grid_for(m_max, 256), 256, 0, st>>>(out, pts, T, idx, w, count, m_max, k);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
@@ -803,6 +824,13 @@ int afx_warp(float* warped, const float* points, const float* transforms, const 
              const unsigned* count, long n_points_max, int k, void* stream) {
     if (!warped || !points || !transforms || !idx || !weights || k < 1) return AFX_ERR_INVALID_ARGUMENT;
     return warp_impl(warped, points, transforms, idx, weights, count, n_points_max, k, as_stream(stream));
+}
+
+int afx_warp_dqb(float* warped, const float* points, const float* transforms, const uint32_t* idx,
+                 const float* weights, const unsigned* count, long n_points_max, int k, void* stream) {
+    if (!warped || !points || !transforms || !idx || !weights || k < 1) return AFX_ERR_INVALID_ARGUMENT;
+    return warp_impl(warped, points, transforms, idx, weights, count, n_points_max, k, as_stream(stream),
+                     AFX_BLEND_DQB);
 }
 
 size_t afx_correspondences_workspace_size(long n_points_max) { return corr_ws(n_points_max); }

@@ -12,6 +12,7 @@
 // are touched.
 #include <cstring>
 
+#include "afx_dqb.cuh"
 #include "afx_store.cuh"
 #include "afx_voxel.h"
 
@@ -339,7 +340,11 @@ __global__ void __launch_bounds__(kBrickVox) brick_warp_kernel(WarpArgs a) {
     const float cen[3] = {a.centroid_dev[0], a.centroid_dev[1], a.centroid_dev[2]};
     float c[3] = {p[0] + cen[0], p[1] + cen[1], p[2] + cen[2]};
     float q[3] = {c[0], c[1], c[2]};
-    if (!zero) {  // warpTsdfKernel (src/TSDFWarp.cu:158-190)
+    if (!zero && a.blend == AFX_BLEND_DQB) {  // dual-quaternion blend (afx_dqb.cuh)
+        uint32_t kidx[K];
+        for (int s = 0; s < cnt; ++s) kidx[s] = (uint32_t)ki[s];
+        dq_blend_point(a.transforms, kidx, w, cnt, AFX_INVALID_INDEX, c, q);
+    } else if (!zero) {  // warpTsdfKernel (src/TSDFWarp.cu:158-190)
         q[0] = q[1] = q[2] = 0.f;
         for (int s = 0; s < cnt; ++s) {
             float o[3];

@@ -68,8 +68,9 @@ int knn_impl(uint32_t* idx, float* dist, const float* nodes, const int* n_nodes,
              const unsigned* count, long m_max, int k, int excl, cudaStream_t st);
 int warp_weights_impl(float* w, const float* radii, const uint32_t* idx, const float* dist, const unsigned* count,
                       long m_max, int k, const int* n_nodes, cudaStream_t st);
+// blend: AFX_BLEND_LBS (the reference's linear blend) or AFX_BLEND_DQB (dual quaternions, afx_dqb.cuh)
 int warp_impl(float* out, const float* pts, const float* T, const uint32_t* idx, const float* w, const unsigned* count,
-              long m_max, int k, cudaStream_t st);
+              long m_max, int k, cudaStream_t st, int blend = AFX_BLEND_LBS);
 size_t corr_ws(long m_max);
 int correspondences_impl(int* corr, unsigned* corr_count, long cap, const float* warped, const unsigned* count,
                          long m_max, const float* K, const float* depth, int rows, int cols, const float* frame,

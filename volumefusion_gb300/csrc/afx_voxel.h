@@ -63,6 +63,7 @@ struct WarpArgs {
     int per[3];
     const float* centroid_dev;  // frame-0 centroid (volume translation), device
     float Rinv[9];
+    int blend;                  // AFX_BLEND_LBS or AFX_BLEND_DQB
     // outputs: either compact (session) or dense per-voxel arrays (API)
     WarpedVoxel* out;          // [n_active * 512] or null
     unsigned char* out_count;  // [n_active * 512] or null

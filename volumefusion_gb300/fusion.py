@@ -36,6 +36,7 @@ def params_from_config(cfg, extract_mesh=True, triangle_capacity=None):
     p.triangle_capacity = int(triangle_capacity or cfg.get("triangle_cap", 4_000_000))
     p.precision = {"fp32": 0, "fp16": 1}[cfg.get("precision", "fp32")]
     p.warp_mesh = int(bool(cfg.get("warp_mesh", False)))
+    p.blend = {"lbs": 0, "dqb": 1}[cfg.get("blend", "lbs")]
     return p
 
 
