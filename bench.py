@@ -222,7 +222,8 @@ def stage_bytes(cfg, st):
     return {
         "prep": P * (2.0 + 4.0 + 24.0),
         "marching_cubes": 8.0 * S + 12.0 * st["mesh_points"] * 4 + 48.0 * st["mesh_faces"],
-        "warped_integrate": 16.0 * A if A else None,
+        # 16 B per supported voxel (value + weight read and written) + the collision word (4 B)
+        "warped_integrate": 20.0 * A if A else None,
     }
 
 
@@ -625,6 +626,7 @@ def main():
     stage_ms = s.stage_times(reset=True)
     s.set_timing(False)
     st = s.stats(check_errors=False)
+    st["active_bricks"], st["active_voxels"] = s.support_size()
     s.close()
 
     # ---- end-to-end arm: host buffers through the C ABI, per-frame latency ----
@@ -742,6 +744,20 @@ def main():
             "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peaks else "fallback"}
     if pick != dom:
         roof["note"] = "dominant stage is %s (%.3f ms/frame), latency-bound" % (dom, per_frame[dom])
+    # the dominant kernel, which no bandwidth roofline describes: one cluster launch per frame running
+    # every Gauss-Newton iteration (5) with its PCG (10 iterations, two cluster barriers each)
+    gn_iters = max(1, int(st["gn_iterations_done"]))
+    pcg_iters = gn_iters * 10
+    roof["dominant_kernel"] = {
+        "kernel": "gn_loop_kernel", "ms_per_frame": per_frame.get("gn_loop", 0.0),
+        "bound": "latency: cluster barriers and binary64 reduction chains (1.6 MB of DRAM traffic per launch)",
+        "gn_iterations_last_frame": gn_iters, "pcg_iterations_per_frame": pcg_iters,
+        "us_per_pcg_iteration_upper_bound": 1000.0 * per_frame.get("gn_loop", 0.0) / pcg_iters,
+        "cluster_barriers_per_pcg_iteration": 2}
+    # every stage with an exact byte count, against the same peak
+    roof["stages"] = {k: {"ms_per_frame": per_frame.get(k, 0.0), "algorithmic_bytes": v,
+                          "achieved_gbs": v / (per_frame[k] / 1000.0) / 1e9 if per_frame.get(k) else None}
+                      for k, v in algo.items()}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and args.cpu_frames > 0:

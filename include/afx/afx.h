@@ -389,6 +389,11 @@ int afx_fusion_point_cloud(afx_fusion* f, float** points, unsigned** count);
  * into the live frame.  The canonical point cloud (afx_fusion_point_cloud) is not warped. */
 int afx_fusion_mesh(afx_fusion* f, float** vertices, unsigned** vertex_count, int** faces, unsigned** face_count);
 int afx_fusion_frame_views(afx_fusion* f, float** depth, float** vertices, float** normals);
+/* Size of the last non-rigid frame's voxel support (no counterpart in the reference): the bricks of
+ * 8^3 voxels that some node's support cube touches, and the voxels in them with at least one
+ * supporting node (the reference's knnCount > 0, src/TSDFWarp.cu:61-67).  Synchronises `stream`. */
+int afx_fusion_support_size(afx_fusion* f, unsigned* active_bricks, unsigned long long* supported_voxels,
+                            void* stream);
 /* Overwrite the committed node transforms (host memory), e.g. to replay a trajectory. */
 int afx_fusion_set_transforms(afx_fusion* f, const float* transforms_host, int n, void* stream);
 /* Number of kernels the library launched since the session was created. */

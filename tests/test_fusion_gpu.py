@@ -121,4 +121,6 @@ def test_capsule_sequence_256_runs_clean():
             assert st["correspondences"] > 1000
             assert st["gn_iterations_done"] >= 1
             assert st["mesh_faces"] > 1000
+    nb, nv = s.support_size()
+    assert 0 < nv <= 512 * nb, (nb, nv)
     s.close()

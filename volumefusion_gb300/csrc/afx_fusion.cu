@@ -864,6 +864,44 @@ int afx_fusion_stats(afx_fusion* f, afx_frame_stats* out, void* stream) {
     return AFX_OK;
 }
 
+}  // extern "C"
+
+namespace afx {
+
+// Voxels of the active bricks with at least one supporting node (count slot > 0).
+__global__ void support_count_kernel(const unsigned char* count, const unsigned* n_active, unsigned long long* out) {
+    const long n = (long)*n_active * 512;
+    unsigned long long c = 0;
+    AFX_GRID_STRIDE(i, n) c += count[i] ? 1ull : 0ull;
+    c = warp_sum(c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+}  // namespace afx
+
+extern "C" {
+
+int afx_fusion_support_size(afx_fusion* f, unsigned* active_bricks, unsigned long long* supported_voxels,
+                            void* stream) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    unsigned nb = 0;
+    AFX_CUDA(cudaMemcpyAsync(&nb, f->sup.n_active, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    AFX_CUDA(cudaStreamSynchronize(st));
+    if (active_bricks) *active_bricks = nb;
+    if (supported_voxels) {
+        unsigned long long* cnt = reinterpret_cast<unsigned long long*>(f->acc) + 4;  // spare words of acc's 64 B
+        AFX_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), st));
+        if (nb) {
+            support_count_kernel<<<grid_for((long)nb * 512, 256), 256, 0, st>>>(f->wcount, f->sup.n_active, cnt);
+            AFX_LAUNCH_CHECK();
+        }
+        AFX_CUDA(cudaMemcpyAsync(supported_voxels, cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+        AFX_CUDA(cudaStreamSynchronize(st));
+    }
+    return AFX_OK;
+}
+
 int afx_fusion_tsdf(afx_fusion* f, float** tsdf, float** weights) {
     if (!f) return AFX_ERR_INVALID_ARGUMENT;
     if (f->fmt != kVoxF32) return AFX_ERR_UNSUPPORTED;  // FP16 sessions: afx_fusion_volume

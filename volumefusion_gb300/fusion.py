@@ -156,6 +156,12 @@ class FusionSession:
         return (_wrap_device(d.value, P, torch.float32), _wrap_device(v.value, 3 * P, torch.float32).view(-1, 3),
                 _wrap_device(n.value, 3 * P, torch.float32).view(-1, 3))
 
+    def support_size(self):
+        """(active bricks, supported voxels) of the last non-rigid frame's voxel support."""
+        nb, nv = C.c_uint(0), C.c_ulonglong(0)
+        check(lib().afx_fusion_support_size(self.h, C.byref(nb), C.byref(nv), self._st()), "afx_fusion_support_size")
+        return nb.value, nv.value
+
     def set_transforms(self, T):
         arr = np.ascontiguousarray(T, dtype=np.float32)
         check(lib().afx_fusion_set_transforms(self.h, arr.ctypes.data_as(C.c_void_p), arr.shape[0], self._st()),
