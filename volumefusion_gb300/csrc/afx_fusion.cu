@@ -194,6 +194,10 @@ struct afx_fusion {
     // captured on first use; per-stage timing runs eagerly instead
     bool graphs = true;
     cudaStream_t cap_stream = nullptr;
+    // the voxel support is built on a side stream while the Gauss-Newton stages run (fork after the
+    // graph build, join before the voxel warp); created with the session, outside any capture
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     cudaGraph_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // kept for batch graphs
     unsigned graph_epoch = 0;  // advanced whenever the captured graphs are dropped
@@ -468,6 +472,9 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     // session neither waits for nor holds up other sessions' work.
     cudaStream_t init = nullptr;
     e = cudaStreamCreateWithFlags(&init, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&f->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->ev_fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMemsetAsync(f->arena, 0, f->arena_bytes, init);
     int rc = e == cudaSuccess ? afx_fusion_reset(f, init) : note_cuda_error(e);
     e = init ? cudaStreamSynchronize(init) : cudaSuccess;
@@ -475,6 +482,9 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     if (init) cudaStreamDestroy(init);
     f->work.wait_and_clear();  // the reset's mark names the private stream
     if (rc) {
+        if (f->side) cudaStreamDestroy(f->side);
+        if (f->ev_fork) cudaEventDestroy(f->ev_fork);
+        if (f->ev_join) cudaEventDestroy(f->ev_join);
         cudaFree(f->arena);
         delete f;
         return rc;
@@ -499,10 +509,14 @@ static void drop_graphs(afx_fusion* f) {
 int afx_fusion_destroy(afx_fusion* f) {
     if (!f) return AFX_ERR_INVALID_ARGUMENT;
     f->work.wait_and_clear();  // the session's own work on every stream it was given
+    if (f->side) cudaStreamSynchronize(f->side);  // joined into those streams, unless a frame failed midway
     for (auto& m : f->marks) cudaEventDestroy(m.second);
     for (auto e : f->ev_pool) cudaEventDestroy(e);
     drop_graphs(f);
     if (f->cap_stream) cudaStreamDestroy(f->cap_stream);
+    if (f->side) cudaStreamDestroy(f->side);
+    if (f->ev_fork) cudaEventDestroy(f->ev_fork);
+    if (f->ev_join) cudaEventDestroy(f->ev_join);
     cudaError_t e = cudaFree(f->arena);
     delete f;
     return note_cuda_error(e);
@@ -644,6 +658,19 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
         copy_new_nodes_kernel<<<blocks_for(N, 256), 256, 0, st>>>(f->nodes_dev, f->nodes_host, f->n_old, f->n_nodes, N);
         AFX_LAUNCH_CHECK();
     }
+    // Voxel support (the node -> brick lists) needs only the graph: with stage timing off it is built
+    // on the side stream while the KNN and Gauss-Newton stages run (they read nodes_dev too, and
+    // write none of what the support build touches); the join is before the voxel warp.
+    const bool fork = !f->timing;
+    if (fork) {
+        AFX_CUDA(cudaEventRecord(f->ev_fork, st));
+        AFX_CUDA(cudaStreamWaitEvent(f->side, f->ev_fork, 0));
+        rc = translate_dev_impl(f->nodes_t, f->nodes_dev, nullptr, N, f->centroid0, -1.f, f->side);
+        if (!rc) rc = build_support(f->sup, f->vol, f->per, f->nodes_t, f->radii, f->n_nodes, N, f->error, f->side);
+        const cudaError_t je = cudaEventRecord(f->ev_join, f->side);  // recorded even after a failure: the join
+        if (rc) return rc;
+        if (je != cudaSuccess) return note_cuda_error(je);
+    }
     // KNN and weights (src/VolumeFusion.cu:410-424)
     stage_mark(f, ST_KNN, st);
     rc = knn_impl(f->midx, f->mdist, f->nodes_host, f->n_nodes, N, points, npoints, M, p.knn, 0, st);
@@ -699,10 +726,14 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
     }
     // voxel support, warp, collisions and warped integration (src/VolumeFusion.cu:702-741)
     stage_mark(f, ST_SUPPORT, st);
-    rc = translate_dev_impl(f->nodes_t, f->nodes_dev, nullptr, N, f->centroid0, -1.f, st);
-    if (rc) return rc;
-    rc = build_support(f->sup, f->vol, f->per, f->nodes_t, f->radii, f->n_nodes, N, f->error, st);
-    if (rc) return rc;
+    if (fork) {
+        AFX_CUDA(cudaStreamWaitEvent(st, f->ev_join, 0));
+    } else {
+        rc = translate_dev_impl(f->nodes_t, f->nodes_dev, nullptr, N, f->centroid0, -1.f, st);
+        if (rc) return rc;
+        rc = build_support(f->sup, f->vol, f->per, f->nodes_t, f->radii, f->n_nodes, N, f->error, st);
+        if (rc) return rc;
+    }
     // the reference translates its device graph back in place: p = (p - c) + c (src/VolumeFusion.cu:721)
     rc = translate_dev_impl(f->nodes_dev, f->nodes_t, nullptr, N, f->centroid0, 1.f, st);
     if (rc) return rc;

@@ -248,7 +248,22 @@ AFX_D int nearest_node(const Grid& g, const float* nodes, const float* p, float*
     return bi;
 }
 
+// While the graph has at most kGreedyCache nodes their positions are also kept in shared memory,
+// and the coverage test and the nearest-node search scan them there (the same answers as the grid:
+// every node within r is examined, ties go to the lower index); the grid stays up to date and takes
+// over if the graph outgrows the cache.  The first build of a sequence walks every point of the
+// cloud, and there a grid lookup's chain of dependent global loads set the pace.
+constexpr int kGreedyCache = 1000;  // with the chunk arrays, within the 48 KB of static shared memory
+
+AFX_D bool covered_smem(const float* sn, int n, const float* p, float r) {
+    for (int j = 0; j < n; ++j)
+        if (sqrtf(l2sq_nanoflann(p, sn + 3 * j)) < r) return true;
+    return false;
+}
+
 __global__ void __launch_bounds__(kChunk) graph_greedy_kernel(GraphState s, const Grid* gp) {
+    __shared__ float s_nodes[kGreedyCache * 3];  // node positions while they fit
+    __shared__ int s_ncache;                     // nodes in s_nodes (= all nodes, or -1 once outgrown)
     __shared__ unsigned uncovered[kChunk];
     __shared__ int s_nu;
     __shared__ int s_sel[kChunk];
@@ -261,12 +276,23 @@ __global__ void __launch_bounds__(kChunk) graph_greedy_kernel(GraphState s, cons
     const unsigned nc = *s.ncand;
     const int tid = threadIdx.x, lane = tid & 31;
     if (tid == 0) s_stop = 0;
+    {
+        const int n_start = *s.n_nodes;
+        const bool fits = n_start <= kGreedyCache;
+        if (fits)
+            for (int i = tid; i < 3 * n_start; i += blockDim.x) s_nodes[i] = s.nodes[i];
+        if (tid == 0) s_ncache = fits ? n_start : -1;
+    }
     __syncthreads();
     for (unsigned start = 0; start < nc && !s_stop; start += kChunk) {
         // (a) drop candidates covered by nodes inserted by earlier chunks
         unsigned ci = start + tid;
         bool unc = false;
-        if (ci < nc) unc = !grid_covered(g, s.nodes, s.mesh + 3 * (long)s.cand[ci], s.r);
+        const int ncache = s_ncache;
+        if (ci < nc) {
+            const float* pc = s.mesh + 3 * (long)s.cand[ci];
+            unc = ncache >= 0 ? !covered_smem(s_nodes, ncache, pc, s.r) : !grid_covered(g, s.nodes, pc, s.r);
+        }
         // ordered compaction of the uncovered candidates
         unsigned bal = __ballot_sync(0xffffffffu, unc);
         __shared__ int wcount[kChunk / 32];
@@ -293,19 +319,39 @@ __global__ void __launch_bounds__(kChunk) graph_greedy_kernel(GraphState s, cons
         }
         __syncthreads();
         // (b) in-order resolution against the nodes selected earlier in this chunk (warp 0, all
-        // positions in shared memory)
+        // positions in shared memory), 32 candidates at a time: each lane tests its candidate against
+        // every node selected so far, then the survivors are taken in lane order, each one selected
+        // removing the later survivors within r of it -- the same selections as one candidate at a
+        // time, with one step per selected node instead of one per candidate.
         if (tid < 32) {
             int nsel = 0;
-            for (int u = 0; u < s_nu; ++u) {
-                const float* p = s_upos + 3 * u;
-                bool hit = false;
-                for (int k = lane; k < nsel; k += 32)
-                    if (sqrtf(l2sq_nanoflann(p, s_spos + 3 * k)) < s.r) hit = true;
-                hit = __any_sync(0xffffffffu, hit);
-                if (!hit) {
-                    if (lane < 3) s_spos[3 * nsel + lane] = p[lane];
-                    if (lane == 0) s_sel[nsel] = (int)uncovered[u];
+            const int nu = s_nu;
+            for (int base = 0; base < nu; base += 32) {
+                const int u = base + lane;
+                const bool valid = u < nu;
+                float pu[3] = {0.f, 0.f, 0.f};
+                bool hit = !valid;
+                if (valid) {
+                    pu[0] = s_upos[3 * u];
+                    pu[1] = s_upos[3 * u + 1];
+                    pu[2] = s_upos[3 * u + 2];
+                    for (int k = 0; k < nsel && !hit; ++k)
+                        if (sqrtf(l2sq_nanoflann(pu, s_spos + 3 * k)) < s.r) hit = true;
+                }
+                unsigned live = __ballot_sync(0xffffffffu, !hit);
+                while (live) {
+                    const int j = __ffs(live) - 1;  // the earliest survivor: selected
+                    const float pj[3] = {__shfl_sync(0xffffffffu, pu[0], j), __shfl_sync(0xffffffffu, pu[1], j),
+                                         __shfl_sync(0xffffffffu, pu[2], j)};
+                    if (lane == j) {
+                        s_spos[3 * nsel] = pu[0];
+                        s_spos[3 * nsel + 1] = pu[1];
+                        s_spos[3 * nsel + 2] = pu[2];
+                        s_sel[nsel] = (int)uncovered[u];
+                    }
                     ++nsel;
+                    if (lane > j && !hit && sqrtf(l2sq_nanoflann(pu, pj)) < s.r) hit = true;
+                    live = __ballot_sync(0xffffffffu, !hit) & ~((2u << j) - 1u);
                 }
                 __syncwarp();
             }
@@ -322,7 +368,15 @@ __global__ void __launch_bounds__(kChunk) graph_greedy_kernel(GraphState s, cons
             const float* p = s_spos + 3 * tid;
             float bs = FLT_MAX;
             int j = -1;
-            if (n0 <= kNearestBrute) {  // few nodes: a scan beats expanding rings over a sparse grid
+            if (ncache >= 0) {  // every node in shared memory
+                for (int q = 0; q < n0; ++q) {
+                    const float d = l2sq_nanoflann(p, s_nodes + 3 * q);
+                    if (d < bs) {
+                        bs = d;
+                        j = q;
+                    }
+                }
+            } else if (n0 <= kNearestBrute) {  // few nodes: a scan beats expanding rings over a sparse grid
                 for (int q = 0; q < n0; ++q) {
                     const float d = l2sq_nanoflann(p, s.nodes + 3 * (long)q);
                     if (d < bs) {
@@ -348,6 +402,11 @@ __global__ void __launch_bounds__(kChunk) graph_greedy_kernel(GraphState s, cons
             s.nodes[3 * n + 1] = p[1];
             s.nodes[3 * n + 2] = p[2];
             s.radii[n] = s.r;
+            if (ncache >= 0 && n < kGreedyCache) {
+                s_nodes[3 * n] = p[0];
+                s_nodes[3 * n + 1] = p[1];
+                s_nodes[3 * n + 2] = p[2];
+            }
         }
         __syncthreads();
         // transforms in order (a node may copy from one selected earlier in the chunk): lane e of
@@ -364,6 +423,7 @@ __global__ void __launch_bounds__(kChunk) graph_greedy_kernel(GraphState s, cons
         __syncthreads();
         if (tid == 0) {
             *s.n_nodes = n0 + take;
+            if (s_ncache >= 0) s_ncache = n0 + take <= kGreedyCache ? n0 + take : -1;
             if (take < s_nsel) {
                 atomicOr(s.error, ERRF_CAPACITY);
                 s_stop = 1;
