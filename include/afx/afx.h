@@ -381,6 +381,11 @@ int afx_fusion_tsdf(afx_fusion* f, float** tsdf, float** weights);  /* FP32 sess
 /* Device view of the volume in either storage format: FP32 values + FP32 weights, or (precision
  * form) IEEE FP16 values + uint16 weights; *precision says which. */
 int afx_fusion_volume(afx_fusion* f, void** tsdf, void** weights, int* precision);
+/* After writing the session's volume through these views: the session keeps, per brick of 8^3
+ * voxels, whether any voxel has a weight (marching cubes skips bricks without, which hold no active
+ * cube) and updates it itself when it integrates or loads a volume; this rebuilds it from the
+ * weights.  No counterpart in the reference.  Asynchronous on `stream`. */
+int afx_fusion_volume_changed(afx_fusion* f, void* stream);
 int afx_fusion_graph(afx_fusion* f, float** nodes, float** radii, float** transforms, int** n_nodes);
 int afx_fusion_centroid(afx_fusion* f, float** centroid);
 int afx_fusion_point_cloud(afx_fusion* f, float** points, unsigned** count);

@@ -166,6 +166,7 @@ struct afx_fusion {
     unsigned* nmfaces;
     WarpedVoxel* wvox;
     unsigned char* wcount;
+    unsigned char* occ;    // per 8^3 brick: 1 once any voxel of it has a weight (marching cubes skips the rest)
     FrameStats* stats;
     void* ws_sort;
     size_t ws_sort_bytes;
@@ -363,7 +364,7 @@ static void session_layout(const afx_fusion_params& p, afx_fusion* f) {
     add(p.triangle_capacity * 36); add(p.triangle_capacity * 12); add(64); add(64);
     const long mesh_knn = p.warp_mesh ? p.triangle_capacity * 3 * p.knn * 4 : 0;  // output-mesh warp
     add(mesh_knn); add(mesh_knn); add(mesh_knn);
-    add(nbricks * 512 * sizeof(WarpedVoxel)); add(nbricks * 512);
+    add(nbricks * 512 * sizeof(WarpedVoxel)); add(nbricks * 512); add(nbricks);
     add(sizeof(FrameStats)); add(64);
     add(f->ws_sort_bytes); add(f->ws_graph_bytes); add(f->ws_corr_bytes); add(f->ws_support_bytes); add(f->ws_gn_bytes);
     f->arena_bytes = sz + 4096;
@@ -453,6 +454,7 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     f->vw = (float*)take(mesh_knn);
     f->wvox = (WarpedVoxel*)take(nbricks * 512 * sizeof(WarpedVoxel));
     f->wcount = (unsigned char*)take(nbricks * 512);
+    f->occ = (unsigned char*)take(nbricks);
     f->stats = (FrameStats*)take(sizeof(FrameStats));
     f->frame_dev = (int*)take(64);
     f->ws_sort = take(f->ws_sort_bytes);
@@ -543,6 +545,7 @@ int afx_fusion_reset(afx_fusion* f, void* stream) {
     AFX_LAUNCH_CHECK();
     AFX_CUDA(cudaMemsetAsync(f->weights, 0, f->S * vox_bytes(f->fmt), st));
     AFX_CUDA(cudaMemsetAsync(f->coll, 0, f->S * 4, st));
+    AFX_CUDA(cudaMemsetAsync(f->occ, 0, brick_count_total(f->vol), st));
     AFX_CUDA(cudaMemsetAsync(f->centroid0, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->acc, 0, 64, st));
     AFX_CUDA(cudaMemsetAsync(f->error, 0, 64, st));
@@ -592,7 +595,7 @@ static int extract_frame_mesh(afx_fusion* f, int cur, cudaStream_t st) {
     return mc_fused_impl(f->tsdf, f->weights, f->fmt, f->vol, 0.f, f->points_buf[next], f->npoints_buf[next], f->p.mesh_capacity,
                          mesh ? f->mverts : nullptr, mesh ? f->nmverts : nullptr, f->p.triangle_capacity * 3,
                          mesh ? f->mfaces : nullptr, mesh ? f->nmfaces : nullptr, f->p.triangle_capacity, st, f->error,
-                         f->mc_tile);
+                         f->mc_tile, f->occ);
 }
 
 // Everything a frame does on the device, in stream order on `st`; host state is not changed.
@@ -623,7 +626,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
         stage_mark(f, ST_INTEGRATE_RIGID, st);
         // rigid integration at the frame-0 centroid (src/VolumeFusion.cu:334-336)
         rc = integrate_rigid_impl(f->tsdf, f->weights, f->fmt, f->depth, p.width, p.height, p.delta, f->vol, I3, nullptr, p.K,
-                                  st, f->centroid0);
+                                  st, f->centroid0, f->occ);
         if (rc) return rc;
         stage_mark(f, ST_MC, st);
         rc = extract_frame_mesh(f, cur, st);
@@ -781,6 +784,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
         ia.H = p.height;
         ia.delta = p.delta;
         ia.K = make_intrinsics(p.K);
+        ia.occ = f->occ;
         rc = launch_brick_integrate(ia, wa.bg.n, st);
         if (rc) return rc;
     }
@@ -1314,6 +1318,44 @@ int afx_fusion_save_volume(afx_fusion* f, const char* path, void* stream) {
     return afx_tsdf_save(path, f->p.dims, f->p.volume_size, f->vol.vs, f->p.delta, t.data(), w.data());
 }
 
+}  // extern "C"
+
+namespace afx {
+
+// Brick occupancy of a volume read from a file: bricks holding any voxel with a weight.
+template <class WT>
+__global__ void occ_from_weights_kernel(const WT* weights, Volume vol, int nbx, int nby, unsigned char* occ) {
+    const long S = (long)vol.dims[0] * vol.dims[1] * vol.dims[2];
+    AFX_GRID_STRIDE(i, S) {
+        if (!(weights[i] > (WT)0)) continue;
+        const int x = (int)(i % vol.dims[0]), y = (int)((i / vol.dims[0]) % vol.dims[1]);
+        const int z = (int)(i / ((long)vol.dims[0] * vol.dims[1]));
+        occ[((long)(z >> 3) * nby + (y >> 3)) * nbx + (x >> 3)] = 1;
+    }
+}
+
+static int rebuild_occupancy(afx_fusion* f, cudaStream_t st) {
+    const BrickGrid bg = make_bricks(f->vol);
+    AFX_CUDA(cudaMemsetAsync(f->occ, 0, bg.n, st));
+    if (f->fmt == kVoxF16)
+        occ_from_weights_kernel<<<grid_for(f->S, 256), 256, 0, st>>>(static_cast<const unsigned short*>(f->weights),
+                                                                      f->vol, bg.nb[0], bg.nb[1], f->occ);
+    else
+        occ_from_weights_kernel<<<grid_for(f->S, 256), 256, 0, st>>>(static_cast<const float*>(f->weights), f->vol,
+                                                                      bg.nb[0], bg.nb[1], f->occ);
+    AFX_LAUNCH_CHECK();
+    return AFX_OK;
+}
+
+}  // namespace afx
+
+extern "C" {
+
+int afx_fusion_volume_changed(afx_fusion* f, void* stream) {
+    if (!f) return AFX_ERR_INVALID_ARGUMENT;
+    return rebuild_occupancy(f, as_stream(stream));
+}
+
 int afx_fusion_load_volume(afx_fusion* f, const char* path, void* stream) {
     if (!f || !path) return AFX_ERR_INVALID_ARGUMENT;
     int dims[3];
@@ -1339,6 +1381,8 @@ int afx_fusion_load_volume(afx_fusion* f, const char* path, void* stream) {
         AFX_CUDA(cudaMemcpyAsync(f->tsdf, t.data(), 4 * S, cudaMemcpyHostToDevice, st));
         AFX_CUDA(cudaMemcpyAsync(f->weights, w.data(), 4 * S, cudaMemcpyHostToDevice, st));
     }
+    rc = rebuild_occupancy(f, st);
+    if (rc) return rc;
     AFX_CUDA(cudaStreamSynchronize(st));
     return AFX_OK;
 }

@@ -43,7 +43,14 @@ struct RigidArgs {
     Intrinsics K;
     float delta;
     int W, H;
+    unsigned char* occ;  // brick occupancy, or null
+    int nbx, nby;        // bricks per axis (x, y)
 };
+
+// Marks the 8^3 brick of voxel (x, y, z) as holding a voxel with a weight (many threads may store 1).
+AFX_D void mark_brick(unsigned char* occ, int nbx, int nby, int x, int y, int z) {
+    if (occ) occ[((long)(z >> 3) * nby + (y >> 3)) * nbx + (x >> 3)] = 1;
+}
 
 template <class TT, class WT>
 __global__ void __launch_bounds__(256) integrate_rigid_x4_kernel(TT* __restrict__ tsdf, WT* __restrict__ weights,
@@ -68,6 +75,7 @@ __global__ void __launch_bounds__(256) integrate_rigid_x4_kernel(TT* __restrict_
         if (tsdf_update_value(q, depth, a.W, a.H, a.delta, a.K, &tn[i])) upd |= 1u << i;
     }
     if (!upd) return;
+    mark_brick(a.occ, a.nbx, a.nby, qx * 4, y, z);  // the four voxels share a brick
     const long base = ((long)z * Y + y) * X + qx * 4;
     float tv[4], wv[4];
     vox_get4(tsdf, weights, base, tv, wv);
@@ -89,6 +97,7 @@ __global__ void integrate_rigid_kernel(TT* tsdf, WT* weights, const float* __res
     q[1] = q[1] + (a.t_dev ? a.t_dev[1] : a.t[1]);
     q[2] = q[2] + (a.t_dev ? a.t_dev[2] : a.t[2]);
     if (!tsdf_update_value(q, depth, a.W, a.H, a.delta, a.K, &tn)) return;
+    mark_brick(a.occ, a.nbx, a.nby, x, y, z);
     const long i = ((long)z * Y + y) * X + x;
     float t = vox_get_t(tsdf, i), w = vox_get_w(weights, i);
     tsdf_blend(t, w, tn);
@@ -132,6 +141,8 @@ int integrate_fresh_impl(float* tsdf, float* weights, const float* depth, int W,
     if (!vec) return AFX_ERR_UNSUPPORTED;  // callers fall back to initialise + integrate
     RigidArgs a;
     a.vol = vol;
+    a.occ = nullptr;
+    a.nbx = a.nby = 0;
     for (int i = 0; i < 9; ++i) a.R[i] = R[i];
     for (int i = 0; i < 3; ++i) a.t[i] = t[i];
     a.t_dev = nullptr;
@@ -148,9 +159,15 @@ int integrate_fresh_impl(float* tsdf, float* weights, const float* depth, int W,
 
 int integrate_rigid_impl(void* tsdf, void* weights, int fmt, const float* depth, int W, int H, float delta,
                          const Volume& vol, const float* R, const float* t, const float* K, cudaStream_t st,
-                         const float* t_dev) {
+                         const float* t_dev, unsigned char* occ) {
     RigidArgs a;
     a.vol = vol;
+    a.occ = occ;
+    {
+        const BrickGrid bg = make_bricks(vol);
+        a.nbx = bg.nb[0];
+        a.nby = bg.nb[1];
+    }
     for (int i = 0; i < 9; ++i) a.R[i] = R[i];
     for (int i = 0; i < 3; ++i) a.t[i] = t ? t[i] : 0.f;
     a.t_dev = t_dev;
@@ -397,6 +414,7 @@ __global__ void __launch_bounds__(kBrickVox) brick_integrate_kernel(WarpedIntegr
     float t = vox_get_t(tsdf, v), w = vox_get_w(weights, v);
     tsdf_blend(t, w, tn);
     vox_put(tsdf, weights, v, t, w);
+    if (a.occ) a.occ[b] = 1;
     }();
 }
 

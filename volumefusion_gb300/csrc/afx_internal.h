@@ -28,9 +28,10 @@ int frame_prep_impl(const uint16_t* mm, int width, int height, const afx_prep_pa
                     float* normals, float* centroid, unsigned long long* acc, int* error, cudaStream_t st);
 
 // ---- integration (afx_integrate.cu) ----
+// occ (optional): one byte per 8^3 brick, set to 1 for every brick where a voxel gets a weight
 int integrate_rigid_impl(void* tsdf, void* weights, int fmt, const float* depth, int W, int H, float delta,
                          const Volume& vol, const float* R, const float* t, const float* K, cudaStream_t st,
-                         const float* t_dev = nullptr);
+                         const float* t_dev = nullptr, unsigned char* occ = nullptr);
 // initialise (-1, 0) + rigid integration in one write-only pass (FP32 volumes, X % 4 == 0, 16-byte
 // aligned arrays; AFX_ERR_UNSUPPORTED otherwise)
 int integrate_fresh_impl(float* tsdf, float* weights, const float* depth, int W, int H, float delta, const Volume& vol,
@@ -46,7 +47,9 @@ int sort_unique_volume_impl(float* pts, unsigned* count, long n_max, void* ws, s
                             cudaStream_t st, int* error = nullptr);
 int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
-                  unsigned* face_count, long face_cap, cudaStream_t st, int* error = nullptr, int tile = 0);
+                  unsigned* face_count, long face_cap, cudaStream_t st, int* error = nullptr, int tile = 0,
+                  const unsigned char* occ = nullptr);  // occ: brick occupancy (tiles without an occupied
+                                                       // brick hold no active cube and are skipped)
 // marching-cubes tiles (the session's autotuner picks one): TMA bricks of 16, 8 or 32 cubes along z,
 // the column march from global memory, or a persistent grid with two stages of bricks 8 or 16 deep
 enum { kMcTileTma16 = 0, kMcTileTma8 = 1, kMcTileTma32 = 2, kMcTileColumn = 3, kMcTilePipe8 = 4, kMcTilePipe16 = 5,

@@ -60,7 +60,10 @@ struct McArgs {
     long face_cap;
     int* faces;
     int* error;  // TMA path: set on a tile-load timeout
+    const unsigned char* occ;  // brick occupancy (8^3 voxels), or null: process every tile
+    int nbx, nby, nbz;
 };
+
 
 // getVertex + interpolate (src/MarchingCubes.cu:294-336)
 template <class TT>
@@ -181,6 +184,20 @@ AFX_D void mc_emit(const TT* __restrict__ tsdf, const McArgs& a, int x, int y, i
 // (marchingCubesFullKernel) of each cube.
 constexpr int kMcX = 32, kMcY = 8, kMcZ = 16;
 
+// False when no 8^3 brick holding a cube origin of the tile [x0, x0+32) x [y0, y0+8) x [z0, z0+zr)
+// has a voxel with a weight.  A cube is active only if all eight corners have a weight, its origin
+// corner among them, so such a tile has no active cube.  Every thread evaluates it (same answer).
+AFX_D bool tile_occupied(const McArgs& a, int x0, int y0, int z0, int zr) {
+    if (!a.occ) return true;
+    const int bx1 = min((x0 + kMcX - 1) >> 3, a.nbx - 1), by1 = min((y0 + kMcY - 1) >> 3, a.nby - 1);
+    const int bz1 = min((z0 + zr - 1) >> 3, a.nbz - 1);
+    for (int bz = z0 >> 3; bz <= bz1; ++bz)
+        for (int by = y0 >> 3; by <= by1; ++by)
+            for (int bx = x0 >> 3; bx <= bx1; ++bx)
+                if (__ldg(a.occ + ((long)bz * a.nby + by) * a.nbx + bx)) return true;
+    return false;
+}
+
 // tsdf/weight of the corners (x, y), (x+1, y), (x, y+1), (x+1, y+1) of slice z
 template <class TT, class WT>
 AFX_D void mc_slice(const TT* __restrict__ tsdf, const WT* __restrict__ w, long row0, long X, float t[4],
@@ -202,6 +219,7 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_kernel(const TT* __restrict__ 
     const long X = a.vol.dims[0], XY = X * a.vol.dims[1];
     const int x = blockIdx.x * kMcX + threadIdx.x, y = blockIdx.y * kMcY + threadIdx.y;
     const int z0 = blockIdx.z * kMcZ, z1 = min(z0 + kMcZ, nz);
+    if (!tile_occupied(a, blockIdx.x * kMcX, blockIdx.y * kMcY, z0, kMcZ)) return;  // uniform over the CTA
     const bool col = x < nx && y < ny;
     const long base = (long)y * X + x;
     float t0[4] = {0.f, 0.f, 0.f, 0.f}, w0[4] = {0.f, 0.f, 0.f, 0.f};
@@ -269,6 +287,7 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_tma_kernel(const __grid_consta
     WT* sw = reinterpret_cast<WT*>(mc_raw + pad + kMcBrickBytes);
     const int tid = threadIdx.y * kMcX + threadIdx.x;
     const int x0 = blockIdx.x * kMcX, y0 = blockIdx.y * kMcY, z0 = blockIdx.z * ZR;
+    if (!tile_occupied(a, x0, y0, z0, ZR)) return;  // uniform over the CTA, before any barrier or copy
     if (((mc_smem_u32(st) | mc_smem_u32(sw)) & 127u) != 0u) {  // never expected: refuse rather than fault
         if (tid == 0 && a.error) atomicOr(a.error, ERRF_TMA);
         return;
@@ -599,7 +618,8 @@ static void mc_launch_any(const TT* tsdf, const WT* weights, const McArgs& a, co
 
 int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
-                  unsigned* face_count, long face_cap, cudaStream_t st, int* error, int tile) {
+                  unsigned* face_count, long face_cap, cudaStream_t st, int* error, int tile,
+                  const unsigned char* occ) {
     int rc = upload_tables();
     if (rc) return rc;
     McArgs a;
@@ -614,6 +634,10 @@ int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& 
     a.face_cap = face_cap < vert_cap / 3 ? face_cap : vert_cap / 3;
     a.faces = faces;
     a.error = error;
+    a.occ = occ;
+    a.nbx = (vol.dims[0] + 7) / 8;
+    a.nby = (vol.dims[1] + 7) / 8;
+    a.nbz = (vol.dims[2] + 7) / 8;
     const long ncubes = (long)(vol.dims[0] - 2) * (vol.dims[1] - 2) * (vol.dims[2] - 2);
     if (ncubes <= 0) return AFX_OK;
     const bool P = points != nullptr, M = verts != nullptr;

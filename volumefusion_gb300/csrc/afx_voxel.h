@@ -91,6 +91,7 @@ struct WarpedIntegrateArgs {
     int W, H;
     float delta;
     Intrinsics K;
+    unsigned char* occ;  // brick occupancy (brick index = active brick id), or null
 };
 
 // Workspace layout for the support gather.
