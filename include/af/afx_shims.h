@@ -2,27 +2,36 @@
  * af/afx_shims.h -- header-only C++ forwarding from the reference's af:: operator names to
  * the C ABI in afx/afx.h.
  *
- * A caller written against the reference (include/af/*.cuh, include/af/*.h) keeps its call
- * sites: the functions below take the same arguments in the same order.  Small Eigen values
- * (Vec2i, Vec3i, Vec3f, Mat3f, Mat4f) are accepted through templates -- anything indexable
- * with [] for vectors and exposing column-major .data() for matrices -- so this header does not
- * depend on Eigen.  Like the reference, each call blocks until the GPU work has finished
- * (the reference synchronised after every launch) and throws std::runtime_error on failure
- * (the reference's CUDA_CHECK, src/Helper.cu:7-20).  Callers that want asynchronous launches
- * call the afx_* functions directly with a stream.
+ * A caller written against the reference's headers (include/af/) keeps its call sites: the
+ * functions below take the same arguments in the same order, with the reference's element types.  Buffers of Vec3f, Mat4f, Vec2i, Vecui<K> or Vecf<K> (af/afx_types.h: the
+ * caller's Eigen types when Eigen is included first) are passed as such; a pointer to plain
+ * float / int / unsigned is accepted as well, with K then given explicitly (default
+ * Constants::motionGraphKNN, as the reference's kernels hard-code it).  Value arguments (Vec2i,
+ * Vec3i, Vec3f, Mat3f, Mat4f) are accepted through templates: anything indexable with [] for
+ * vectors and exposing column-major .data() for matrices.
+ *
+ * Like the reference, each call blocks until the GPU work has finished (the reference
+ * synchronised after every launch) and throws std::runtime_error on failure (the reference's
+ * CUDA_CHECK, src/Helper.cu:7-20).  Callers that want asynchronous launches call the afx_*
+ * functions directly with a stream.  The classes (DeviceTsdf, WarpField, MotionGraph,
+ * TSDFVolume, ...) are in af/afx_classes.h.
  */
 #ifndef AF_AFX_SHIMS_H
 #define AF_AFX_SHIMS_H
 
 #include <cuda_runtime_api.h>
 
+#include <climits>
 #include <cstddef>
 #include <cstdint>
+#include <limits>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <utility>
 
 #include "../afx/afx.h"
+#include "afx_types.h"
 
 namespace af {
 namespace detail {
@@ -32,6 +41,10 @@ inline void afx_check(int status, const char* what) {
         throw std::runtime_error(std::string(what) + ": " + afx_status_string(status));
     }
     cudaError_t e = cudaStreamSynchronize(nullptr);
+    if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+inline void cuda_check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
@@ -52,48 +65,139 @@ inline void to_m3(const M& m, float* o) {  // column-major, as Eigen stores it
     const float* d = m.data();
     for (int i = 0; i < 9; ++i) o[i] = d[i];
 }
+template <class M>
+inline void to_m4(const M& m, float* o) {
+    const float* d = m.data();
+    for (int i = 0; i < 16; ++i) o[i] = d[i];
+}
+
+// A buffer of elements T seen as the scalars S it packs: T is S itself or N packed S.
+template <class S, int N, class T>
+inline typename std::conditional<std::is_const<T>::value, const S*, S*>::type flat(T* p) {
+    static_assert(sizeof(T) == N * sizeof(S) || sizeof(T) == sizeof(S),
+                  "element type must be the scalar or N packed scalars (Vec3f, Mat4f, Vec2i, ...)");
+    return reinterpret_cast<typename std::conditional<std::is_const<T>::value, const S*, S*>::type>(p);
+}
+template <int N, class T>
+inline auto ff(T* p) -> decltype(flat<float, N>(p)) {
+    return flat<float, N>(p);
+}
+
+// Neighbour slots per point: the element's length for Vecui<K> / Vecf<K> buffers, else K as given
+// (K <= 0: the reference's Constants::motionGraphKNN).
+template <class T>
+inline int slots(int K) {
+    static_assert(sizeof(T) % 4 == 0, "neighbour buffers hold 4-byte values");
+    const int n = (int)(sizeof(T) / 4);
+    if (n == 1) return K > 0 ? K : (int)Constants::motionGraphKNN;
+    if (K > 0 && K != n) throw std::invalid_argument("af: K differs from the neighbour element's length");
+    return n;
+}
+template <class T>
+inline uint32_t* u32(T* p) {
+    return reinterpret_cast<uint32_t*>(p);
+}
+template <class T>
+inline const uint32_t* u32(const T* p) {
+    return reinterpret_cast<const uint32_t*>(p);
+}
+
+// One int on the device (node counts the afx_* calls read from device memory).
+struct DeviceInt {
+    int* p = nullptr;
+    explicit DeviceInt(int v) {
+        cuda_check(cudaMalloc(reinterpret_cast<void**>(&p), sizeof(int)), "cudaMalloc");
+        cuda_check(cudaMemcpy(p, &v, sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");
+    }
+    ~DeviceInt() { cudaFree(p); }
+    DeviceInt(const DeviceInt&) = delete;
+    DeviceInt& operator=(const DeviceInt&) = delete;
+    int get() const {
+        int v = 0;
+        cuda_check(cudaMemcpy(&v, p, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        return v;
+    }
+};
+
+// Scratch device memory for one call.
+struct Workspace {
+    void* p = nullptr;
+    size_t bytes = 0;
+    explicit Workspace(size_t n) : bytes(n) {
+        if (n) cuda_check(cudaMalloc(&p, n), "cudaMalloc (workspace)");
+    }
+    ~Workspace() { cudaFree(p); }
+    Workspace(const Workspace&) = delete;
+    Workspace& operator=(const Workspace&) = delete;
+};
 
 }  // namespace detail
 
-// include/af/VertexManipulation.cuh
-inline void runFilterDepthKernel(float* depth, unsigned int depthSize, float threshold) {
-    detail::afx_check(afx_filter_depth(depth, depthSize, threshold, nullptr), "runFilterDepthKernel");
+// ---- include/af/VertexManipulation.cuh ----
+
+// fillValue: what replaces rejected values (src/VertexManipulation.cu:6-15).
+inline void runFilterDepthKernel(float* depth, unsigned int depthSize, float threshold,
+                                 float fillValue = std::numeric_limits<float>::infinity()) {
+    detail::afx_check(afx_filter_depth_fill(depth, depthSize, threshold, fillValue, nullptr), "runFilterDepthKernel");
 }
 
-template <class Mat3f>
-inline void runDepthToMeshKernel(float* mesh, const float* cDepth, unsigned int depthWidth, unsigned int depthHeight,
+template <class P3, class Mat3f>
+inline void runDepthToMeshKernel(P3* mesh, const float* cDepth, unsigned int depthWidth, unsigned int depthHeight,
                                  const Mat3f& K) {
     float k[9];
     detail::to_m3(K, k);
-    detail::afx_check(afx_depth_to_mesh(mesh, cDepth, (int)depthWidth, (int)depthHeight, k, nullptr),
+    detail::afx_check(afx_depth_to_mesh(detail::ff<3>(mesh), cDepth, (int)depthWidth, (int)depthHeight, k, nullptr),
                       "runDepthToMeshKernel");
 }
 
-inline void runDepthVerticesNormalsKernel(float* normals, float* vertices, const float* /*depth*/, int h, int w,
+template <class P3, class Q3>
+inline void runDepthVerticesNormalsKernel(P3* normals, Q3* vertices, const float* /*depth*/, int h, int w,
                                           std::pair<float, float> normExclAngleRange) {
-    detail::afx_check(afx_depth_vertices_normals(normals, vertices, h, w, normExclAngleRange.first,
-                                                 normExclAngleRange.second, nullptr),
+    detail::afx_check(afx_depth_vertices_normals(detail::ff<3>(normals), detail::ff<3>(vertices), h, w,
+                                                 normExclAngleRange.first, normExclAngleRange.second, nullptr),
                       "runDepthVerticesNormalsKernel");
 }
 
-inline void runRemoveDepthWithoutNormalsKernel(float* normals, float* vertices, float* depth, int h, int w) {
-    detail::afx_check(afx_remove_depth_without_normals(normals, vertices, depth, h, w, nullptr),
+template <class P3, class Q3>
+inline void runRemoveDepthWithoutNormalsKernel(P3* normals, Q3* vertices, float* depth, int h, int w) {
+    detail::afx_check(afx_remove_depth_without_normals(detail::ff<3>(normals), detail::ff<3>(vertices), depth, h, w,
+                                                       nullptr),
                       "runRemoveDepthWithoutNormalsKernel");
 }
 
-// include/af/BilateralFilter.cuh
+template <class P3, class Vec3f>
+inline void runTranslateKernel(P3* mesh, unsigned int meshSize, const Vec3f& translation) {
+    float t[3];
+    detail::to_f3(translation, t);
+    detail::afx_check(afx_translate(detail::ff<3>(mesh), nullptr, (long)meshSize, t, nullptr), "runTranslateKernel");
+}
+
+// knnWeights[i][j] = exp(-d^2 / 2r^2) of slot j (0 at d >= r), normalised to sum 1
+// (src/VertexManipulation.cu:105-132).
+template <class PW, class PI, class PD>
+inline void runComputeWarpWeightsKernel(PW* knnWeights, const float* cMotionGraphRadiuses, const PI* cKnnIdxs,
+                                        const PD* cKnnDists, const std::size_t cMeshSize, int K = 0) {
+    const int k = detail::slots<PI>(K);
+    detail::DeviceInt all(INT_MAX);  // every stored index is a node (empty slots hold 0xFFFFFFFF)
+    detail::afx_check(afx_warp_weights(reinterpret_cast<float*>(knnWeights), cMotionGraphRadiuses, detail::u32(cKnnIdxs),
+                                       reinterpret_cast<const float*>(cKnnDists), nullptr, (long)cMeshSize, k, all.p,
+                                       nullptr),
+                      "runComputeWarpWeightsKernel");
+}
+
+// ---- include/af/BilateralFilter.cuh ----
 inline void bilateralFilterTextureOpmShared(float* output, const float* input, int height, int width, int r, double sI,
                                             double sS, float thr) {
     detail::afx_check(afx_bilateral_filter(output, input, height, width, r, sI, sS, thr, nullptr),
                       "bilateralFilterTextureOpmShared");
 }
 
-// include/af/TSDFIntegration.cuh
-template <class Vec2i, class Vec3i, class Vec3f, class Mat3f>
+// ---- include/af/TSDFIntegration.cuh ----
+template <class Vec2i, class Vec3i, class Vec3f, class Mat3f, class Vec3t>
 inline void runIntegrateTSDFFromFrameKernel(float* tsdf, float* tsdfWeights, const float* cDepthFrame,
                                             const Vec2i cFrameDims, const float cDelta, const Vec3i cDims,
                                             const Vec3f cVoxelSize, const Vec3f cVolumeSize,
-                                            const Mat3f cVolumeRotate, const Vec3f cVolumeTranslate,
+                                            const Mat3f cVolumeRotate, const Vec3t cVolumeTranslate,
                                             const Mat3f cDepthIntrinsics) {
     int dims[3];
     float vs[3], size[3], R[9], t[3], K[9];
@@ -108,8 +212,8 @@ inline void runIntegrateTSDFFromFrameKernel(float* tsdf, float* tsdfWeights, con
                       "runIntegrateTSDFFromFrameKernel");
 }
 
-template <class Vec3f, class Vec3i, class Mat3f>
-inline void runCountCollisionsPerVoxelKernel(int* collisionCounts, const float* tsdfVertices, const int* cKnnCounts,
+template <class P3, class Vec3f, class Vec3i, class Mat3f>
+inline void runCountCollisionsPerVoxelKernel(int* collisionCounts, const P3* tsdfVertices, const int* cKnnCounts,
                                              const Vec3f cVoxelSize, const Vec3f cVolumeSize, const Vec3i cVolumeDim,
                                              const Mat3f cVolumeRotate, const Vec3f cVolumeTranslate) {
     int dims[3];
@@ -119,12 +223,13 @@ inline void runCountCollisionsPerVoxelKernel(int* collisionCounts, const float* 
     detail::to_f3(cVolumeSize, size);
     detail::to_m3(cVolumeRotate, R);
     detail::to_f3(cVolumeTranslate, t);
-    detail::afx_check(afx_count_collisions(collisionCounts, tsdfVertices, cKnnCounts, vs, size, dims, R, t, nullptr),
+    detail::afx_check(afx_count_collisions(collisionCounts, detail::ff<3>(tsdfVertices), cKnnCounts, vs, size, dims, R,
+                                           t, nullptr),
                       "runCountCollisionsPerVoxelKernel");
 }
 
-template <class Vec2i, class Vec3f, class Vec3i, class Mat3f>
-inline void runIntegrateWarpedTSDFFromFrameKernel(float* tsdf, float* tsdfWeights, const float* cTsdfVertices,
+template <class P3, class Vec2i, class Vec3f, class Vec3i, class Mat3f>
+inline void runIntegrateWarpedTSDFFromFrameKernel(float* tsdf, float* tsdfWeights, const P3* cTsdfVertices,
                                                   const int* collisionCounts, const int* cKnnCounts,
                                                   const float* cDepthFrame, const Vec2i cFrameDims,
                                                   const float cDelta, const Vec3f cVoxelSize,
@@ -139,61 +244,73 @@ inline void runIntegrateWarpedTSDFFromFrameKernel(float* tsdf, float* tsdfWeight
     detail::to_m3(cVolumeRotate, R);
     detail::to_f3(cVolumeTranslate, t);
     detail::to_m3(cDepthIntrinsics, K);
-    detail::afx_check(afx_integrate_warped_tsdf(tsdf, tsdfWeights, cTsdfVertices, collisionCounts, cKnnCounts,
-                                                cDepthFrame, (int)cFrameDims[0], (int)cFrameDims[1], cDelta, vs, size,
-                                                dims, R, t, K, nullptr),
+    detail::afx_check(afx_integrate_warped_tsdf(tsdf, tsdfWeights, detail::ff<3>(cTsdfVertices), collisionCounts,
+                                                cKnnCounts, cDepthFrame, (int)cFrameDims[0], (int)cFrameDims[1],
+                                                cDelta, vs, size, dims, R, t, K, nullptr),
                       "runIntegrateWarpedTSDFFromFrameKernel");
 }
 
-// include/af/TSDFWarp.h (K = number of slots per voxel)
-template <class Vec3f, class Vec3i>
-inline void runTsdfKNNGraph(uint32_t* knnIdxs, float* knnDists, int* knnCounts, const float* cGraph,
-                            const float* cGraphRadiuses, const std::size_t cGraphSize, const Vec3f cVoxelSize,
-                            const Vec3f cVolumeSize, const Vec3i cVolumeDim, const Vec3i cVoxelsPerNode, int K) {
+// ---- include/af/TSDFWarp.h ----
+template <class PI, class PD, class P3, class Vec3f, class Vec3i>
+inline void runTsdfKNNGraph(PI* knnIdxs, PD* knnDists, int* knnCounts, const P3* cGraph, const float* cGraphRadiuses,
+                            const std::size_t cGraphSize, const Vec3f cVoxelSize, const Vec3f cVolumeSize,
+                            const Vec3i cVolumeDim, const Vec3i cVoxelsPerNode, int K = 0) {
+    const int k = detail::slots<PI>(K);
     int dims[3], per[3];
     float vs[3], size[3];
     detail::to_i3(cVolumeDim, dims);
     detail::to_i3(cVoxelsPerNode, per);
     detail::to_f3(cVoxelSize, vs);
     detail::to_f3(cVolumeSize, size);
-    std::size_t bytes = afx_tsdf_knn_workspace_size(dims, (int)cGraphSize, per);
-    void* ws = nullptr;
-    if (cudaMalloc(&ws, bytes) != cudaSuccess) throw std::runtime_error("runTsdfKNNGraph: cudaMalloc");
-    int st = afx_tsdf_knn(knnIdxs, knnDists, knnCounts, cGraph, cGraphRadiuses, (int)cGraphSize, vs, size, dims, per, K,
-                          ws, bytes, nullptr);
-    cudaFree(ws);
-    detail::afx_check(st, "runTsdfKNNGraph");
+    detail::Workspace ws(afx_tsdf_knn_workspace_size(dims, (int)cGraphSize, per));
+    detail::afx_check(afx_tsdf_knn(detail::u32(knnIdxs), reinterpret_cast<float*>(knnDists), knnCounts,
+                                   detail::ff<3>(cGraph), cGraphRadiuses, (int)cGraphSize, vs, size, dims, per, k,
+                                   ws.p, ws.bytes, nullptr),
+                      "runTsdfKNNGraph");
 }
 
-inline void runComputeTsdfWarpWeightsKernel(float* cKnnWeights, const float* cMotionGraphRadiuses,
-                                            const uint32_t* cKnnIdxs, const float* cKnnDists, const int* cKnnCounts,
-                                            const std::size_t cGridSize, int K) {
-    detail::afx_check(afx_tsdf_warp_weights(cKnnWeights, cMotionGraphRadiuses, cKnnIdxs, cKnnDists, cKnnCounts,
-                                            (long)cGridSize, K, nullptr),
+template <class PW, class PI, class PD>
+inline void runComputeTsdfWarpWeightsKernel(PW* cKnnWeights, const float* cMotionGraphRadiuses, const PI* cKnnIdxs,
+                                            const PD* cKnnDists, const int* cKnnCounts, const std::size_t cGridSize,
+                                            int K = 0) {
+    const int k = detail::slots<PI>(K);
+    detail::afx_check(afx_tsdf_warp_weights(reinterpret_cast<float*>(cKnnWeights), cMotionGraphRadiuses,
+                                            detail::u32(cKnnIdxs), reinterpret_cast<const float*>(cKnnDists),
+                                            cKnnCounts, (long)cGridSize, k, nullptr),
                       "runComputeTsdfWarpWeightsKernel");
 }
 
-template <class Vec3f, class Vec3i>
-inline void runGenerateTsdfVerticesKernel(float* tsdfVertices, const Vec3f cVoxelSize, const Vec3f cVolumeSize,
+template <class P3, class Vec3f, class Vec3i>
+inline void runGenerateTsdfVerticesKernel(P3* tsdfVertices, const Vec3f cVoxelSize, const Vec3f cVolumeSize,
                                           const Vec3i cVolumeDim) {
     int dims[3];
     float vs[3], size[3];
     detail::to_i3(cVolumeDim, dims);
     detail::to_f3(cVoxelSize, vs);
     detail::to_f3(cVolumeSize, size);
-    detail::afx_check(afx_tsdf_vertices(tsdfVertices, vs, size, dims, nullptr), "runGenerateTsdfVerticesKernel");
+    detail::afx_check(afx_tsdf_vertices(detail::ff<3>(tsdfVertices), vs, size, dims, nullptr),
+                      "runGenerateTsdfVerticesKernel");
 }
 
-inline void runWarpTsdfKernel(float* tsdfVertices, const float* cMotionGraph, const uint32_t* cKnnIdxs,
-                              const float* cKnnWeights, const int* cKnnCounts, std::size_t gridSize, int K) {
-    detail::afx_check(afx_warp_tsdf(tsdfVertices, cMotionGraph, cKnnIdxs, cKnnWeights, cKnnCounts, (long)gridSize, K,
-                                    nullptr),
+template <class P3, class P16, class PI, class PW, class Vec3f, class Vec3i>
+inline void runWarpTsdfKernel(P3* tsdfVertices, const P16* cMotionGraph, const PI* cKnnIdxs, const PW* cKnnWeights,
+                              const int* cKnnCounts, const Vec3f cVoxelSize, const Vec3f cVolumeSize,
+                              const Vec3i cVolumeDim, int K = 0) {
+    (void)cVoxelSize;
+    (void)cVolumeSize;
+    const int k = detail::slots<PI>(K);
+    const long n = (long)cVolumeDim[0] * (long)cVolumeDim[1] * (long)cVolumeDim[2];
+    detail::afx_check(afx_warp_tsdf(detail::ff<3>(tsdfVertices), detail::ff<16>(cMotionGraph), detail::u32(cKnnIdxs),
+                                    reinterpret_cast<const float*>(cKnnWeights), cKnnCounts, n, k, nullptr),
                       "runWarpTsdfKernel");
 }
 
-// include/af/MarchingCubes.cuh
-template <class Vec3i, class Vec3f>
-inline void runMarchingCubesMeshKernel(float* mesh, unsigned int* meshSize, std::size_t meshCapacity, const float* cTsdf,
+// ---- include/af/MarchingCubes.cuh ----
+// The reference's kernels append at *meshSize without a bound (src/MarchingCubes.cu:510-520); the
+// overloads without a capacity keep that contract: the buffer must hold every point the volume
+// yields (at most 12 per cube).  The overloads with a capacity stop there and report overflow.
+template <class P3, class Vec3i, class Vec3f>
+inline void runMarchingCubesMeshKernel(P3* mesh, unsigned int* meshSize, std::size_t meshCapacity, const float* cTsdf,
                                        const float* cTsdfWeights, const Vec3i cDims, const Vec3f& cVoxelSize,
                                        const Vec3f& cVolSize, const float cIsoValue) {
     int dims[3];
@@ -201,13 +318,27 @@ inline void runMarchingCubesMeshKernel(float* mesh, unsigned int* meshSize, std:
     detail::to_i3(cDims, dims);
     detail::to_f3(cVoxelSize, vs);
     detail::to_f3(cVolSize, size);
-    detail::afx_check(afx_marching_cubes_points(mesh, meshSize, (long)meshCapacity, cTsdf, cTsdfWeights, dims, vs,
-                                                size, cIsoValue, nullptr),
+    detail::afx_check(afx_marching_cubes_points(detail::ff<3>(mesh), meshSize, (long)meshCapacity, cTsdf, cTsdfWeights,
+                                                dims, vs, size, cIsoValue, nullptr),
                       "runMarchingCubesMeshKernel");
 }
 
-template <class Vec3i, class Vec3f>
-inline void runMarchingCubesFullKernel(float* mesh, unsigned int* meshSize, std::size_t meshCapacity, int* faces,
+template <class Vec3i>
+inline std::size_t marching_cubes_bound(const Vec3i& d, int per_cube) {
+    const long c = (long)(d[0] > 1 ? d[0] - 1 : 0) * (long)(d[1] > 1 ? d[1] - 1 : 0) * (long)(d[2] > 1 ? d[2] - 1 : 0);
+    return (std::size_t)(c * per_cube);
+}
+
+template <class P3, class Vec3i, class Vec3f>
+inline void runMarchingCubesMeshKernel(P3* mesh, unsigned int* meshSize, const float* cTsdf, const float* cTsdfWeights,
+                                       const Vec3i cDims, const Vec3f& cVoxelSize, const Vec3f& cVolSize,
+                                       const float cIsoValue) {
+    runMarchingCubesMeshKernel(mesh, meshSize, marching_cubes_bound(cDims, 12), cTsdf, cTsdfWeights, cDims, cVoxelSize,
+                               cVolSize, cIsoValue);
+}
+
+template <class P3, class F3, class Vec3i, class Vec3f>
+inline void runMarchingCubesFullKernel(P3* mesh, unsigned int* meshSize, std::size_t meshCapacity, F3* faces,
                                        unsigned int* facesSize, std::size_t facesCapacity, const float* cTsdf,
                                        const float* cTsdfWeights, const Vec3i cDims, const Vec3f& cVoxelSize,
                                        const Vec3f& cVolSize, const float cIsoValue) {
@@ -216,18 +347,78 @@ inline void runMarchingCubesFullKernel(float* mesh, unsigned int* meshSize, std:
     detail::to_i3(cDims, dims);
     detail::to_f3(cVoxelSize, vs);
     detail::to_f3(cVolSize, size);
-    detail::afx_check(afx_marching_cubes_mesh(mesh, meshSize, (long)meshCapacity, faces, facesSize,
-                                              (long)facesCapacity, cTsdf, cTsdfWeights, dims, vs, size, cIsoValue,
-                                              nullptr),
+    detail::afx_check(afx_marching_cubes_mesh(detail::ff<3>(mesh), meshSize, (long)meshCapacity,
+                                              detail::flat<int, 3>(faces), facesSize, (long)facesCapacity, cTsdf,
+                                              cTsdfWeights, dims, vs, size, cIsoValue, nullptr),
                       "runMarchingCubesFullKernel");
 }
 
-// include/af/ComputeCorrespondence.cuh
-inline void runWarpKernel(float* warpedMesh, const float* cMesh, const float* cMotionGraph, const uint32_t* cKnnIdxs,
-                          const float* cKnnWeights, const std::size_t cMeshSize, int K) {
-    detail::afx_check(afx_warp(warpedMesh, cMesh, cMotionGraph, cKnnIdxs, cKnnWeights, nullptr, (long)cMeshSize, K,
-                               nullptr),
+// Without capacities: at most 5 triangles (15 vertices) per cube.
+template <class P3, class F3, class Vec3i, class Vec3f>
+inline void runMarchingCubesFullKernel(P3* mesh, unsigned int* meshSize, F3* faces, unsigned int* facesSize,
+                                       const float* cTsdf, const float* cTsdfWeights, const Vec3i cDims,
+                                       const Vec3f& cVoxelSize, const Vec3f& cVolSize, const float cIsoValue) {
+    runMarchingCubesFullKernel(mesh, meshSize, marching_cubes_bound(cDims, 15), faces, facesSize,
+                               marching_cubes_bound(cDims, 5), cTsdf, cTsdfWeights, cDims, cVoxelSize, cVolSize,
+                               cIsoValue);
+}
+
+// ---- include/af/ComputeCorrespondence.cuh ----
+template <class P3, class Q3, class P16, class PI, class PW>
+inline void runWarpKernel(P3* warpedMesh, const Q3* cMesh, const P16* cMotionGraph, const PI* cKnnIdxs,
+                          const PW* cKnnWeights, const std::size_t cMeshSize, int K = 0) {
+    const int k = detail::slots<PI>(K);
+    detail::afx_check(afx_warp(detail::ff<3>(warpedMesh), detail::ff<3>(cMesh), detail::ff<16>(cMotionGraph),
+                               detail::u32(cKnnIdxs), reinterpret_cast<const float*>(cKnnWeights), nullptr,
+                               (long)cMeshSize, k, nullptr),
                       "runWarpKernel");
+}
+
+// runWarpKernel with dual-quaternion blending (afx_warp_dqb; no counterpart in the reference).
+template <class P3, class Q3, class P16, class PI, class PW>
+inline void runWarpDualQuaternionKernel(P3* warpedMesh, const Q3* cMesh, const P16* cMotionGraph, const PI* cKnnIdxs,
+                                        const PW* cKnnWeights, const std::size_t cMeshSize, int K = 0) {
+    const int k = detail::slots<PI>(K);
+    detail::afx_check(afx_warp_dqb(detail::ff<3>(warpedMesh), detail::ff<3>(cMesh), detail::ff<16>(cMotionGraph),
+                                   detail::u32(cKnnIdxs), reinterpret_cast<const float*>(cKnnWeights), nullptr,
+                                   (long)cMeshSize, k, nullptr),
+                      "runWarpDualQuaternionKernel");
+}
+
+// One (warped point, pixel) pair per warped point that projects onto a valid pixel whose vertex
+// lies within thresholdDist (src/ComputeCorrespondence.cu:33-80), ordered by point index;
+// cDepthDim = (rows, cols).  *corrIdxsSize (device) receives the pair count: the reference's kernel
+// appends to it, and its callers zero it first.  corrIdxs holds up to cWarpedMeshSize pairs.
+template <class P2, class P3, class Mat3f, class Vec2i, class Q3>
+inline void runCorrespondencePairsKernel(P2* corrIdxs, unsigned int* corrIdxsSize, const P3* cWarpedMesh,
+                                         const std::size_t cWarpedMeshSize, const Mat3f& K,
+                                         const float* const cPtrDepth, const Vec2i cDepthDim,
+                                         const Q3* const cFrameMesh, const float thresholdDist) {
+    float k[9];
+    detail::to_m3(K, k);
+    detail::Workspace ws(afx_correspondences_workspace_size((long)cWarpedMeshSize));
+    detail::afx_check(afx_correspondences(detail::flat<int, 2>(corrIdxs), corrIdxsSize, (long)cWarpedMeshSize,
+                                          detail::ff<3>(cWarpedMesh), nullptr, (long)cWarpedMeshSize, k, cPtrDepth,
+                                          (int)cDepthDim[0], (int)cDepthDim[1], detail::ff<3>(cFrameMesh),
+                                          thresholdDist, ws.p, ws.bytes, nullptr),
+                      "runCorrespondencePairsKernel");
+}
+
+// ---- include/af/MotionOptimization.cuh ----
+// T -= [[x_rot]_x, x_t; 0] per node (src/MotionOptimization.cu:483-506).
+template <class P16, class P6>
+inline void runUpdateTransformsKernel(P16* transforms, const P6* cUpdates, unsigned int transformsSize) {
+    detail::DeviceInt n((int)transformsSize);
+    detail::afx_check(afx_update_transforms(detail::ff<16>(transforms), detail::ff<6>(cUpdates), n.p,
+                                            (int)transformsSize, nullptr),
+                      "runUpdateTransformsKernel");
+}
+
+// The reference's wrapper launches the same subtracting kernel as runUpdateTransformsKernel
+// (src/MotionOptimization.cu:525-531), so this entry point subtracts too.
+template <class P16, class P6>
+inline void runUpdateTransformsReverseKernel(P16* transforms, const P6* cUpdates, unsigned int transformsSize) {
+    runUpdateTransformsKernel(transforms, cUpdates, transformsSize);
 }
 
 /* The reference's whole-frame loop (af::runVolumeFusion, src/VolumeFusion.cu:223) fed frame by frame. */

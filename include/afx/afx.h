@@ -60,6 +60,12 @@ int afx_depth_from_mm(float* depth, const uint16_t* depth_mm, long n, void* stre
 /* af::runFilterDepthKernel (include/af/VertexManipulation.cuh:11, src/VertexManipulation.cu:17):
  * values > threshold, < 1e-4 or NaN become +inf. */
 int afx_filter_depth(float* depth, long n, float threshold, void* stream);
+/* The same with the rejected values set to `fill` (runFilterDepthKernel's fillValue argument,
+ * include/af/VertexManipulation.cuh:11). */
+int afx_filter_depth_fill(float* depth, long n, float threshold, float fill, void* stream);
+
+/* dst[0..n) = value (DeviceTsdf::initDefault, include/af/DeviceTsdf.cuh:23-26: values -1, weights 0). */
+int afx_fill_f32(float* dst, long n, float value, void* stream);
 
 /* af::bilateralFilterTextureOpmShared (include/af/BilateralFilter.cuh:8,
  * src/BilateralFilter.cu:180): radius r, range sigma sigma_i (m), spatial sigma

@@ -1,0 +1,239 @@
+// af_surface_check.cpp -- a C++ caller of the af:: surface (af/afx_classes.h) written the way the
+// reference's own code calls it: DeviceTsdf -> extractPointCloud -> MotionGraph / buildGraph /
+// getKnnData / filterDisconnected -> WarpField (spreadMotionGraph, weighted KNN, warp) ->
+// runCorrespondencePairsKernel -> GaussNewtonSystem -> runUpdateTransformsKernel, plus TSDFVolume
+// integrate / save / load.  It reads one pair of prepared frames from <in_dir> and writes every
+// intermediate result to <out_dir> as raw arrays; tests/test_cpp_surface_gpu.py compares them
+// with the CPU oracle.  Built with AFX_TEST_WITH_EIGEN, the value types are Eigen's.
+#ifdef AFX_TEST_WITH_EIGEN
+#include <Eigen/Core>
+#endif
+#include <af/afx_classes.h>
+
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+namespace {
+
+std::string g_in, g_out;
+
+template <class T>
+std::vector<T> read_raw(const std::string& name) {
+    std::ifstream f(g_in + "/" + name, std::ios::binary | std::ios::ate);
+    if (!f) throw std::runtime_error("cannot read " + name);
+    const std::streamsize bytes = f.tellg();
+    f.seekg(0);
+    std::vector<T> v((std::size_t)bytes / sizeof(T));
+    f.read(reinterpret_cast<char*>(v.data()), (std::streamsize)(v.size() * sizeof(T)));
+    return v;
+}
+
+template <class T>
+void write_raw(const std::string& name, const T* p, std::size_t n) {
+    std::ofstream f(g_out + "/" + name, std::ios::binary);
+    f.write(reinterpret_cast<const char*>(p), (std::streamsize)(n * sizeof(T)));
+}
+template <class T>
+void write_raw(const std::string& name, const std::vector<T>& v) {
+    write_raw(name, v.data(), v.size());
+}
+template <class T>
+std::vector<T> download(const T* d, std::size_t n) {
+    std::vector<T> v(n);
+    af::copyToHost(v.data(), d, n);
+    return v;
+}
+
+int run() {
+    // meta: width, height, fx, fy, cx, cy, dims[3], size[3], delta, radius, corr_thresh,
+    //       lambda_depth, lambda_reg, centroid[3]
+    const std::vector<float> meta = read_raw<float>("meta.bin");
+    const int w = (int)meta[0], h = (int)meta[1];
+    af::Mat3f K = af::Mat3f::Identity();
+    K(0, 0) = meta[2];
+    K(1, 1) = meta[3];
+    K(0, 2) = meta[4];
+    K(1, 2) = meta[5];
+    const af::Vec3i dims((int)meta[6], (int)meta[7], (int)meta[8]);
+    const af::Vec3f size(meta[9], meta[10], meta[11]);
+    const float delta = meta[12], radius = meta[13], corrThresh = meta[14], lamD = meta[15], lamR = meta[16];
+    const af::Vec3f c(meta[17], meta[18], meta[19]);
+    const std::size_t P = (std::size_t)w * (std::size_t)h;
+
+    const std::vector<float> depth0 = read_raw<float>("depth0.bin");
+    const std::vector<float> depth1 = read_raw<float>("depth1.bin");
+    const std::vector<af::Vec3f> verts1 = read_raw<af::Vec3f>("verts1.bin");
+    const std::vector<af::Vec3f> normals1 = read_raw<af::Vec3f>("normals1.bin");
+
+    // 1. DeviceTsdf: integrate frame 0 through the volume pose (identity rotation, centre c)
+    af::CameraModel camera;
+    camera.width = (unsigned)w;
+    camera.height = (unsigned)h;
+    camera.depthIntrinsics = K;
+    af::DeviceDepthImage depth_d((std::size_t)h, (std::size_t)w, camera);
+    depth_d.upload(depth0.data());
+    af::DeviceTsdf<float> tsdf(size, dims, c, af::Mat3f::Identity(), delta);
+    tsdf.integrate(depth_d);
+    write_raw("tsdf.bin", download(tsdf.tsdfPtr(), tsdf.voxelCount()));
+    write_raw("weights.bin", download(tsdf.weightsPtr(), tsdf.voxelCount()));
+
+    // 2. point cloud (marching cubes, sort, unique), then into camera space
+    af::DeviceBufferCounted<af::Vec3f> cloud((unsigned)(tsdf.voxelCount() * 3 / 4));
+    tsdf.extractPointCloud(cloud);
+    write_raw("cloud.bin", cloud.download());
+    af::runTranslateKernel(cloud.bufferPtr(), cloud.size(), c);
+    const std::vector<af::Vec3f> mesh = cloud.download();
+    write_raw("mesh.bin", mesh);
+    const std::size_t m = mesh.size();
+
+    // 3. host MotionGraph through buildGraph / getKnnData / filterDisconnected / warp
+    af::MotionGraph graph;
+    af::buildGraph(graph, mesh, af::Constants::motionGraphKNN, radius);
+    const std::size_t n = graph.graph().size();
+    write_raw("nodes.bin", graph.graph().vec_);
+    write_raw("radii.bin", graph.radiuses());
+    write_raw("transforms.bin", graph.transforms());
+
+    std::vector<af::Vecui<6>> midx;
+    std::vector<af::Vecf<6>> mdist;
+    af::getKnnData(midx, mdist, graph, mesh);
+    write_raw("midx.bin", midx);
+    write_raw("mdist.bin", mdist);
+
+    std::vector<unsigned int> fidx;
+    std::vector<float> fdist;
+    af::getKnnData(fidx, fdist, graph, graph.graph().vec_, 4, true);
+    write_raw("flat_idx.bin", fidx);
+    write_raw("flat_dist.bin", fdist);
+
+    std::vector<af::Vecui<4>> gidx;
+    std::vector<af::Vecf<4>> gdist;
+    af::getKnnData(gidx, gdist, graph, graph.graph().vec_, true);
+    af::filterDisconnected(gidx, gdist, graph);
+    write_raw("gidx.bin", gidx);
+    write_raw("gdist.bin", gdist);
+
+    af::Vecui<6> one_idx;
+    af::Vecf<6> one_dist;
+    graph.knnSearch(one_idx, one_dist, mesh[m / 2]);
+    write_raw("one_idx.bin", one_idx.data(), 6);
+    write_raw("one_dist.bin", one_dist.data(), 6);
+
+    for (std::size_t i = 0; i < n; ++i) {  // a smooth deterministic motion
+        af::Mat4f& T = graph.transforms()[i];
+        T.data()[12] += 0.003f * std::sin(1.3f * (float)i);
+        T.data()[13] += 0.003f * std::cos(0.7f * (float)i);
+        T.data()[14] += 0.002f * std::sin(0.4f * (float)i + 1.0f);
+    }
+    write_raw("transforms_moved.bin", graph.transforms());
+    std::vector<af::Vec3f> warped_host;
+    graph.warp(warped_host, mesh);
+    write_raw("warped_motion_graph.bin", warped_host);
+
+    // 4. WarpField on the device: the same graph, skinning, warp
+    af::Settings settings;
+    settings.motionGraphRadius = radius;
+    af::WarpField field(n + 64, settings);
+    field.spreadMotionGraph(cloud);
+    const std::size_t nf = field.motionGraph_d().count();
+    write_raw("field_nodes.bin", download(field.motionGraph_d().pointsPtr(), nf));
+    af::DeviceKnnWeighted<(int)af::Constants::motionGraphKNN> knn_d(m);
+    field.computePointCloudWeightedKnns(knn_d);
+    write_raw("field_midx.bin", download(knn_d.idxsPtr(), m));
+    write_raw("field_mw.bin", download(knn_d.weightsPtr(), m));
+    field.computeGraphKnns();
+    write_raw("field_gidx.bin", download(field.graphKnnIdxs_d().bufferPtr(), nf));
+    af::copyToDevice(field.motionGraph_d().transformsPtr(), graph.transforms().data(), n);
+    af::DeviceBuffer<af::Vec3f> warped_d((unsigned)m);
+    field.warp(warped_d, cloud, knn_d);
+    write_raw("warped_field.bin", warped_d.download());
+
+    // the stand-alone weights operator on the same neighbours
+    af::DeviceArray<af::Vecf<6>> w2(m);
+    af::runComputeWarpWeightsKernel(w2.get(), field.motionGraph_d().radiusesPtr(), knn_d.idxsPtr(), knn_d.distsPtr(), m);
+    write_raw("weights_op.bin", download(w2.get(), m));
+
+    // 5. correspondences with frame 1
+    af::DeviceArray<float> d1(P);
+    af::copyToDevice(d1.get(), depth1.data(), P);
+    af::DeviceArray<af::Vec3f> v1(P), n1(P);
+    af::copyToDevice(v1.get(), verts1.data(), P);
+    af::copyToDevice(n1.get(), normals1.data(), P);
+    af::DeviceBufferCounted<af::Vec2i> corr_d((unsigned)m);
+    af::runCorrespondencePairsKernel(corr_d.bufferPtr(), corr_d.size_dPtr(), warped_d.bufferPtr(), m, K, d1.get(),
+                                     af::Vec2i(h, w), v1.get(), corrThresh);
+    corr_d.syncHostSize();
+    const std::size_t nc = corr_d.size();
+    write_raw("corr.bin", corr_d.download());
+
+    // 6. Gauss-Newton: build, dense export, 10 PCG iterations, transform update
+    af::DeviceBuffer<af::Vecui<4>> gidx_d((unsigned)n);
+    gidx_d.upload(gidx);
+    af::DeviceArray<unsigned> npts(1);
+    const unsigned mu = (unsigned)m;
+    af::copyToDevice(npts.get(), &mu, 1);
+    af::GaussNewtonSystem gn((long)m + 16, (int)n + 8, 6, 4);
+    gn.build(cloud.bufferPtr(), npts.get(), knn_d.idxsPtr(), knn_d.weightsPtr(), corr_d.bufferPtr(), corr_d.size_dPtr(),
+             v1.get(), n1.get(), warped_d.bufferPtr(), field.motionGraph_d().pointsPtr(),
+             field.motionGraph_d().transformsPtr(), field.motionGraph_d().countPtr(), gidx_d.bufferPtr(), lamD, lamR);
+    const std::size_t dim = 6 * n;
+    af::DeviceArray<float> jtj(dim * dim), jtr(dim), rd(nc ? nc : 1), rr(n * 4 * 3);
+    gn.exportDense((int)n, jtj.get(), jtr.get(), rd.get(), rr.get());
+    write_raw("jtj.bin", download(jtj.get(), dim * dim));
+    write_raw("jtr.bin", download(jtr.get(), dim));
+    write_raw("r_depth.bin", download(rd.get(), nc));
+    write_raw("r_reg.bin", download(rr.get(), n * 12));
+    af::DeviceArray<af::Vec6f> x((std::size_t)gn.nodesMax());
+    gn.solve(x.get(), 10);
+    write_raw("x.bin", download(x.get(), n));
+    af::runUpdateTransformsKernel(field.motionGraph_d().transformsPtr(), x.get(), (unsigned)n);
+    write_raw("transforms_updated.bin", download(field.motionGraph_d().transformsPtr(), n));
+
+    // 7. TSDFVolume: the same frame through pose [I | c], save, load
+    af::TSDFVolume volume(dims, size, K);
+    volume.setDelta(delta);
+    af::Mat4f pose = af::Mat4f::Identity();
+    pose(0, 3) = c[0];
+    pose(1, 3) = c[1];
+    pose(2, 3) = c[2];
+    volume.integrate(pose, depth0.data(), h, w);
+    write_raw("volume_tsdf.bin", volume.tsdf());
+    const std::string path = g_out + "/volume.tsdf";
+    volume.save(path);
+    af::TSDFVolume loaded(af::Vec3i(1, 1, 1), af::Vec3f(1.f, 1.f, 1.f), K);
+    loaded.load(path);
+    const bool same = loaded.tsdf() == volume.tsdf() && loaded.tsdfWeights() == volume.tsdfWeights() &&
+                      loaded.dimensions() == volume.dimensions() && loaded.delta() == volume.delta();
+
+    // 8. depth filter with a fill value (DeviceImage::nullifyUpperBound fills +inf)
+    af::DeviceArray<float> f0(P);
+    af::copyToDevice(f0.get(), depth0.data(), P);
+    af::runFilterDepthKernel(f0.get(), (unsigned)P, 0.9f, 0.0f);
+    write_raw("filtered.bin", download(f0.get(), P));
+
+    std::printf("{\"points\": %zu, \"nodes\": %zu, \"field_nodes\": %zu, \"correspondences\": %zu, "
+                "\"volume_roundtrip\": %s}\n",
+                m, n, nf, nc, same ? "true" : "false");
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc != 3) {
+        std::fprintf(stderr, "usage: %s <in_dir> <out_dir>\n", argv[0]);
+        return 2;
+    }
+    g_in = argv[1];
+    g_out = argv[2];
+    try {
+        return run();
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "error: %s\n", e.what());
+        return 1;
+    }
+}

@@ -122,3 +122,30 @@ void caller(float* tsdf, float* w, const float* depth, int* coll, const int* cnt
     r = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I", os.path.join(ROOT, "include"),
                         "-I", "/usr/local/cuda/include", str(src)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_cpp_surface_builds_and_links(lib, tmp_path):
+    """tests/cpp/af_surface_check.cpp -- DeviceTsdf, MotionGraph, buildGraph, getKnnData,
+    filterDisconnected, WarpField, TSDFVolume, GaussNewtonSystem and the typed run* operators,
+    called the way the reference's code calls them -- compiles warning-free and links against
+    libafx.so (it runs in tests/test_cpp_surface_gpu.py)."""
+    import _cppcaller
+    r = _cppcaller.compile_caller(str(tmp_path / "af_check"))
+    if r is None:
+        pytest.skip("no g++ or CUDA runtime")
+    assert r.returncode == 0, r.stderr
+    assert "warning" not in r.stderr, r.stderr
+    assert os.path.exists(tmp_path / "af_check")
+
+
+def test_cpp_surface_compiles_with_eigen_types_when_present():
+    """The same caller with the reference's own Eigen value types (Vec3f = Eigen::Vector3f, ...)."""
+    tree = os.environ.get("VF_REFERENCE", "")
+    eigen = os.path.join(tree, "third_party", "include", "eigen-master")
+    if not tree or not os.path.isdir(os.path.join(eigen, "Eigen")):
+        pytest.skip("reference tree not given (VF_REFERENCE)")
+    import _cppcaller
+    r = _cppcaller.compile_caller(None, eigen_include=eigen, syntax_only=True)
+    if r is None:
+        pytest.skip("no g++")
+    assert r.returncode == 0, r.stderr

@@ -48,6 +48,8 @@ SIGNATURES = {
     "afx_last_cuda_error": (i32, []),
     "afx_depth_from_mm": (i32, [vp, vp, i64, vp]),
     "afx_filter_depth": (i32, [vp, i64, f32, vp]),
+    "afx_filter_depth_fill": (i32, [vp, i64, f32, f32, vp]),
+    "afx_fill_f32": (i32, [vp, i64, f32, vp]),
     "afx_bilateral_filter": (i32, [vp, vp, i32, i32, i32, f64, f64, f32, vp]),
     "afx_depth_to_mesh": (i32, [vp, vp, i32, i32, vp, vp]),
     "afx_depth_vertices_normals": (i32, [vp, vp, i32, i32, f32, f32, vp]),

@@ -342,6 +342,19 @@ __global__ void filter_depth_kernel(float* d, long n, float thr) {
     if (i < n) d[i] = filter_value(d[i], thr);
 }
 
+// filterDepthKernel with the caller's fill value (src/VertexManipulation.cu:6-15).
+__global__ void filter_depth_fill_kernel(float* d, long n, float thr, float fill) {
+    long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    if (i < n) {
+        const float v = d[i];
+        if (v > thr || v < 1.e-4f || isnan(v)) d[i] = fill;
+    }
+}
+
+__global__ void fill_f32_kernel(float* d, long n, float value) {
+    AFX_GRID_STRIDE(i, n) d[i] = value;
+}
+
 __global__ void bilateral_kernel(float* out, const float* __restrict__ in, int h, int w, BilateralTables T) {
     int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= w || y >= h) return;
@@ -501,6 +514,22 @@ int afx_filter_depth(float* depth, long n, float threshold, void* stream) {
     if (!depth || n < 0) return AFX_ERR_INVALID_ARGUMENT;
     if (n == 0) return AFX_OK;
     filter_depth_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(depth, n, threshold);
+    AFX_LAUNCH_CHECK();
+    return AFX_OK;
+}
+
+int afx_filter_depth_fill(float* depth, long n, float threshold, float fill, void* stream) {
+    if (!depth || n < 0) return AFX_ERR_INVALID_ARGUMENT;
+    if (n == 0) return AFX_OK;
+    filter_depth_fill_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(depth, n, threshold, fill);
+    AFX_LAUNCH_CHECK();
+    return AFX_OK;
+}
+
+int afx_fill_f32(float* dst, long n, float value, void* stream) {
+    if (!dst || n < 0) return AFX_ERR_INVALID_ARGUMENT;
+    if (n == 0) return AFX_OK;
+    fill_f32_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(dst, n, value);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
