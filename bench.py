@@ -156,6 +156,65 @@ def cpu_baseline(cfg, frames_np, n_frames):
     return n_frames / dt, dt
 
 
+def reference_cpu_stages(cfg, frames_np):
+    """The reference's own CPU code for three stages of the path (oracle/_ref/libvfref.so, built from
+    its unchanged sources for this host), each timed once, single-threaded as it is written, on the
+    headline frame: TSDFVolume::integrate of frame 0 into an empty 256^3 volume (src/TSDFVolume.cpp:55),
+    MarchingCubes::computeIsoSurface of that volume (src/MarchingCubes.cpp:297), and af::buildGraph +
+    af::getKnnData<4> on its sorted, de-duplicated point cloud (src/GraphBuilder.cpp:12,
+    include/af/GraphBuilder.h:20)."""
+    path = os.path.join(ROOT, "oracle", "_ref", "libvfref.so")
+    if not os.path.exists(path):
+        return {"unavailable": "oracle/_ref/libvfref.so was not built (reference sources not staged)"}
+    from oracle import pyoracle as O
+    R = C.CDLL(path)
+    R.ref_marching_cubes.restype = C.c_long
+
+    def ptr(a):
+        return a.ctypes.data_as(C.c_void_p)
+
+    K = np.asarray(cfg["K"], np.float32)
+    dims = np.asarray(cfg["dims"], np.int32)
+    size = np.asarray(cfg["volume_size"], np.float32)
+    vs = size / dims.astype(np.float32)
+    S = int(np.prod(dims))
+    depth = O.depth_from_mm(frames_np[0])  # the CPU class reads 0 as "no depth"
+    _, _, _, c = O.frame_prep(frames_np[0], K)
+    pose = np.eye(4, dtype=np.float32)
+    pose[:3, 3] = c
+    t, w = np.empty(S, np.float32), np.empty(S, np.float32)
+    h, wd = depth.shape
+    a = time.perf_counter()
+    R.ref_integrate(ptr(t), ptr(w), ptr(np.ascontiguousarray(depth, np.float32)), wd, h, ptr(O.kcol(K)), ptr(dims),
+                    ptr(size), C.c_float(cfg["delta"]), ptr(np.ascontiguousarray(pose.T).ravel()))
+    t_int = time.perf_counter() - a
+    cap = 4_000_000
+    v = np.empty((cap, 3), np.float32)
+    f = np.empty((cap, 3), np.int32)
+    nf = C.c_long(0)
+    a = time.perf_counter()
+    nv = R.ref_marching_cubes(ptr(t), ptr(w), ptr(dims), ptr(size), C.c_float(0.0), 0, ptr(v), C.c_long(cap), ptr(f),
+                              C.c_long(cap), C.byref(nf))
+    t_mc = time.perf_counter() - a
+    mesh = O.translate(O.sort_unique(O.mc_pointcloud(t, w, dims, vs, size)), c)
+    ncap = 20000
+    nn, rr, TT = np.zeros((ncap, 3), np.float32), np.zeros(ncap, np.float32), np.zeros((ncap, 16), np.float32)
+    a = time.perf_counter()
+    n = R.ref_build_graph(ptr(nn), ptr(rr), ptr(TT), 0, ncap, ptr(mesh), C.c_long(len(mesh)), int(cfg["knn"]),
+                          C.c_float(cfg["graph_radius"]))
+    t_graph = time.perf_counter() - a
+    k = int(cfg["knn"])
+    idx, dist = np.empty((len(mesh), k), np.uint32), np.empty((len(mesh), k), np.float32)
+    a = time.perf_counter()
+    R.ref_knn(ptr(nn), ptr(rr), int(n), ptr(mesh), C.c_long(len(mesh)), k, 0, ptr(idx), ptr(dist))
+    t_knn = time.perf_counter() - a
+    return {"kind": "reference", "cores": 1, "cpu": cpu_model(),
+            "sample": "one call of each on frame 0 of the sequence (%dx%d depth, %d^3 volume)" % (wd, h, dims[0]),
+            "integrate_ms": 1000 * t_int, "marching_cubes_ms": 1000 * t_mc, "triangles": int(nf.value),
+            "vertices": int(nv), "build_graph_ms": 1000 * t_graph, "nodes": int(n), "points": len(mesh),
+            "knn_ms": 1000 * t_knn}
+
+
 def run_reference(args):
     """The reference's CPU path (the oracle's restatement of it) on the host cores, on the GPU
     arm's workload: a step is the same reset + frames 0..clip-1 of the sequence (frame 0 rigid,
@@ -765,6 +824,13 @@ def main():
         cpu = {"value": v, "unit": "frames/s", "cores": os.cpu_count(), "kind": "port", "cpu": cpu_model(),
                "sample": "frames 1..%d of the sequence after the rigid frame 0 (%.1f s), all host threads"
                          % (args.cpu_frames, dt)}
+        ref_stages = reference_cpu_stages(cfg, frames_np)
+        if "unavailable" not in ref_stages:
+            # the same stages on the GPU: the rigid integration kernel alone, and per-frame stage times
+            ref_stages["gpu_ms"] = {"integrate": rigid_int["ms"] if rigid_int else None,
+                                    "marching_cubes": per_frame.get("marching_cubes"),
+                                    "build_graph": per_frame.get("graph"), "knn": per_frame.get("knn")}
+        cpu["reference_stages"] = ref_stages
 
     if rank == 0:
         line = {
