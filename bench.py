@@ -12,8 +12,10 @@ same work.  L2 is flushed (a 256 MiB write) between steps.
   dense_graph : the same sequence with the graph radius lowered to 7 mm (about 1500 nodes),
           device-resident, for the solver at the stated graph size.
 
---impl reference times the reference's CPU path (the oracle port of it: this box has no
-build of the reference) with all host threads.  Under torchrun each rank runs an
+--impl reference times the reference's CPU path (the oracle port of it, with all host threads:
+the reference's own CPU code covers only rigid integration, marching cubes and the graph build,
+its warp, solve and warped integration being GPU code; those three of its own functions are
+timed single-threaded in cpu_baseline.reference_stages).  Under torchrun each rank runs an
 independent replica (the path does not shard); value is the sum over ranks.
 """
 import argparse
@@ -559,6 +561,7 @@ def served_arm(args, rank):
         done += len(r)
     wall = time.perf_counter() - t0
     usage = srv.usage()
+    offered_counters = srv.counters()
     srv.close()
     offered = {"streams": n, "seconds": round(wall, 3), "frames": done, "frames_per_s": done / wall,
                "latency_ms_p50": float(np.percentile(lat, 50)) if lat else None,
@@ -568,27 +571,51 @@ def served_arm(args, rank):
     cap_cfgs = pool[:n]
     frames_per = 30
     srv = Server(budget, max_sessions=n)
-    sids = [srv.open(c) for c in cap_cfgs]
-    sent = [0] * n
-    got = 0
-    want = frames_per * sum(s is not None for s in sids)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    host_s = 0.0  # time the driver loop spends inside submit and poll (host work per frame)
-    while got < want and time.perf_counter() - t0 < 120.0:
-        for k, sid in enumerate(sids):
-            while sid is not None and sent[k] < frames_per:
-                h0 = time.perf_counter()
-                ok = srv.submit(sid, configs.scene_frame(cap_cfgs[k], sent[k]))
-                host_s += time.perf_counter() - h0
-                if not ok:
-                    break
-                sent[k] += 1
-        h0 = time.perf_counter()
-        got += len(srv.poll())
-        host_s += time.perf_counter() - h0
-    cap_s = time.perf_counter() - t0
+
+    def capacity():
+        """All sessions' sequences submitted as fast as their slots allow; (frames, seconds, host s)."""
+        sids = [srv.open(c) for c in cap_cfgs]
+        sent = [0] * n
+        got = 0
+        want = frames_per * sum(s is not None for s in sids)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        host_s = 0.0  # time the driver loop spends inside submit and poll (host work per frame)
+        while got < want and time.perf_counter() - t0 < 120.0:
+            for k, sid in enumerate(sids):
+                while sid is not None and sent[k] < frames_per:
+                    h0 = time.perf_counter()
+                    ok = srv.submit(sid, configs.scene_frame(cap_cfgs[k], sent[k]))
+                    host_s += time.perf_counter() - h0
+                    if not ok:
+                        break
+                    sent[k] += 1
+            h0 = time.perf_counter()
+            got += len(srv.poll())
+            host_s += time.perf_counter() - h0
+        wall = time.perf_counter() - t0
+        for sid in sids:
+            if sid is not None:
+                srv.close_session(sid)
+        srv.poll()
+        return got, wall, host_s, int(sum(s is not None for s in sids))
+
+    def counter_delta(a, b):
+        return {k: b[k] - a[k] if k not in ("idle_sessions", "idle_bytes") else b[k] for k in b}
+
+    c0 = srv.counters()
+    got, cap_s, host_s, n_sessions = capacity()  # fresh sessions: allocation and graph capture inside
+    c1 = srv.counters()
+    got_w, cap_w, host_w, _ = capacity()  # the same sessions reopened: reused, graphs kept
+    c2 = srv.counters()
     srv.close()
+    per_frame = lambda c, frames: {"staging_us": 1000 * c["staging_ms"] / max(frames, 1),  # noqa: E731
+                                   "enqueue_us": 1000 * c["enqueue_ms"] / max(frames, 1),
+                                   "poll_us": 1000 * c["poll_ms"] / max(frames, 1),
+                                   "open_ms_total": c["open_ms"], "opens_fresh": c["opens_fresh"],
+                                   "opens_reused": c["opens_reused"]}
+    warm = {"frames": got_w, "frames_per_s": got_w / cap_w, "host_busy_frac": host_w / cap_w,
+            "host_per_frame": per_frame(counter_delta(c1, c2), got_w)}
     served_fps = got / cap_s
     plain_frames, plain_s = 0, 0.0
     for c in cap_cfgs:  # creation and teardown outside the timed part
@@ -602,9 +629,11 @@ def served_arm(args, rank):
         plain_s += time.perf_counter() - t0
         s.close()
     plain_fps = plain_frames / plain_s
+    offered["server_counters"] = {k: offered_counters[k] for k in ("opens_fresh", "opens_reused", "evictions")}
     return {"offered_load": offered,
-            "capacity": {"sessions": int(sum(s is not None for s in sids)), "frames": got, "frames_per_s": served_fps,
-                         "host_busy_frac": host_s / cap_s},
+            "capacity": {"sessions": n_sessions, "frames": got, "frames_per_s": served_fps,
+                         "host_busy_frac": host_s / cap_s, "host_per_frame": per_frame(counter_delta(c0, c1), got),
+                         "reused_sessions": warm},
             "plain_per_stream": {"frames": plain_frames, "frames_per_s": plain_fps,
                                  "note": "same sessions and frames, one session at a time, host frames"},
             "capacity_over_plain": served_fps / plain_fps}

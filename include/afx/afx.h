@@ -476,7 +476,23 @@ int afx_server_submit(afx_server* s, int session_id, const uint16_t* depth_mm_ho
 int afx_server_poll(afx_server* s, afx_server_result* out, int max_results, int* n_results);
 /* The session's afx_fusion (for its volume, graph, mesh); NULL if unknown. */
 afx_fusion* afx_server_session(afx_server* s, int session_id);
+/* used_bytes: the open sessions' device bytes (idle sessions kept for reuse are counted in
+ * afx_server_counters.idle_bytes; both together stay within the budget). */
 int afx_server_usage(afx_server* s, size_t* used_bytes, int* sessions, long* denied);
+
+/* A closed session stays allocated, idle, and an open with equal parameters reuses it (reset on
+ * its stream; arena, stream, pinned slots and captured frame graphs kept).  Counters since
+ * creation: opens that allocated and opens that reused, idle sessions freed to make room, and the
+ * host time spent inside the calls (staging: the copy into the pinned slot; enqueue: the frame's
+ * launches, statistics copy and event). */
+typedef struct afx_server_counters {
+    long opens_fresh, opens_reused, evictions;
+    int idle_sessions;
+    size_t idle_bytes;
+    long submits, polls, results;
+    double open_ms, staging_ms, enqueue_ms, poll_ms;
+} afx_server_counters;
+int afx_server_get_counters(afx_server* s, afx_server_counters* out);
 
 /* ------------------------------------------------------------------------------------
  * Batched form (no counterpart in the reference): one frame of every session of a batch in one

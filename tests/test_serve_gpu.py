@@ -92,3 +92,55 @@ def test_admission_follows_the_memory_budget():
     u = srv.usage()
     assert u["sessions"] == 0 and u["denied"] == 1 and u["used_bytes"] == 0
     srv.close()
+
+
+@pytest.mark.gpu
+def test_closed_session_is_reused_with_fresh_results():
+    """A closed session is reset and handed out again to an open with equal parameters (arena,
+    stream and captured frame graphs kept); the frames it then fuses give exactly the state a
+    fresh session gives.  An open with other parameters does not take it, and one that needs its
+    memory evicts it."""
+    from volumefusion_gb300.serve import Server, session_bytes
+    mix = _mix_configs()
+    cfg_a, frames_a = mix[0]
+    cfg_c, frames_c = mix[2]
+    srv = Server(8 << 30)
+
+    def run(sid, frames):
+        res = []
+        for i, mm in enumerate(frames):
+            while not srv.submit(sid, mm, tag=i):
+                res += srv.poll()
+        res = _drain(srv, len(frames), res)
+        assert [r[1] for r in res] == list(range(len(frames)))
+        assert all(r[3]["error"] == 0 for r in res)
+
+    sid = srv.open(cfg_a)
+    run(sid, frames_a)
+    fresh = _state(srv, sid, cfg_a)
+    srv.close_session(sid)
+    srv.poll()
+    c = srv.counters()
+    assert c["opens_fresh"] == 1 and c["idle_sessions"] == 1 and srv.usage()["used_bytes"] == 0
+    sid_c = srv.open(cfg_c)  # other parameters: a new session
+    assert srv.counters()["opens_fresh"] == 2 and srv.counters()["idle_sessions"] == 1
+    sid2 = srv.open(cfg_a)  # the idle one, reset
+    c = srv.counters()
+    assert c["opens_reused"] == 1 and c["idle_sessions"] == 0
+    run(sid2, frames_a)
+    again = _state(srv, sid2, cfg_a)
+    for x, y in zip(fresh, again):
+        assert np.array_equal(x, y)
+    run(sid_c, frames_c)
+    srv.close()
+    # a budget that holds one session at a time: the idle session makes room for the next
+    need = max(session_bytes(cfg_a), session_bytes(cfg_c))
+    srv = Server(need + need // 2)
+    sid = srv.open(cfg_a)
+    srv.close_session(sid)
+    assert srv.counters()["idle_sessions"] == 1
+    sid = srv.open(cfg_c)
+    assert sid is not None
+    c = srv.counters()
+    assert c["evictions"] == 1 and c["idle_sessions"] == 0 and c["opens_fresh"] == 2
+    srv.close()

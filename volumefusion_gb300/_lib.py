@@ -42,6 +42,12 @@ class ServerResult(C.Structure):
     _fields_ = [("session_id", i32), ("tag", C.c_uint64), ("latency_ms", f64), ("stats", FrameStats)]
 
 
+class ServerCounters(C.Structure):
+    _fields_ = [("opens_fresh", C.c_long), ("opens_reused", C.c_long), ("evictions", C.c_long),
+                ("idle_sessions", i32), ("idle_bytes", C.c_size_t), ("submits", C.c_long), ("polls", C.c_long),
+                ("results", C.c_long), ("open_ms", f64), ("staging_ms", f64), ("enqueue_ms", f64), ("poll_ms", f64)]
+
+
 SIGNATURES = {
     "afx_status_string": (C.c_char_p, [i32]),
     "afx_version": (i32, []),
@@ -108,6 +114,7 @@ SIGNATURES = {
     "afx_server_poll": (i32, [vp, vp, i32, C.POINTER(i32)]),
     "afx_server_session": (vp, [vp, i32]),
     "afx_server_usage": (i32, [vp, C.POINTER(sz), C.POINTER(i32), C.POINTER(C.c_long)]),
+    "afx_server_get_counters": (i32, [vp, C.POINTER(ServerCounters)]),
     "afx_fusion_create": (i32, [C.POINTER(FusionParams), C.POINTER(vp)]),
     "afx_fusion_destroy": (i32, [vp]),
     "afx_fusion_reset": (i32, [vp, vp]),

@@ -10,6 +10,12 @@
 // slot's pinned buffer and enqueues the frame; poll() returns finished frames with their
 // statistics and their latency from submit() to completion.  A session's results do not
 // depend on what else runs: its kernels touch only its own buffers and reduce in fixed orders.
+//
+// A closed session is kept, idle, for reuse: a later open with equal parameters takes it back
+// after afx_fusion_reset (queued on its stream), so its device arena, pinned slots, stream and
+// captured frame graphs are reused -- no allocation, no device-wide synchronisation from
+// cudaFree, no graph capture.  Idle sessions count against the budget; an open that needs room
+// frees the oldest idle ones first.
 #include <chrono>
 #include <cstring>
 #include <map>
@@ -39,10 +45,35 @@ struct Session {
     cudaStream_t st = nullptr;
     size_t bytes = 0;
     long pixels = 0;
+    afx_fusion_params params{};
     Slot slots[kSlots];
     int head = 0, count = 0;  // ring of in-flight frames
     bool closing = false;
 };
+
+// Field by field (the struct has padding).
+bool params_equal(const afx_fusion_params& a, const afx_fusion_params& b) {
+    static_assert(sizeof(afx_fusion_params) == 208, "afx_fusion_params changed: update params_equal");
+    bool eq = a.width == b.width && a.height == b.height && a.delta == b.delta &&
+              a.depth_threshold == b.depth_threshold && a.bilateral == b.bilateral &&
+              a.bilateral_r == b.bilateral_r && a.sigma_i == b.sigma_i && a.sigma_s == b.sigma_s &&
+              a.bilateral_thr == b.bilateral_thr && a.excl_angle_lo == b.excl_angle_lo &&
+              a.excl_angle_hi == b.excl_angle_hi && a.graph_radius == b.graph_radius && a.knn == b.knn &&
+              a.kreg == b.kreg && a.update_graph == b.update_graph && a.icp_iterations == b.icp_iterations &&
+              a.gn_iterations == b.gn_iterations && a.lambda_depth == b.lambda_depth && a.lambda_reg == b.lambda_reg &&
+              a.energy_min_step == b.energy_min_step && a.corr_thresh == b.corr_thresh && a.solver == b.solver &&
+              a.pcg_iterations == b.pcg_iterations && a.pcg_tol == b.pcg_tol && a.integrate == b.integrate &&
+              a.extract_mesh == b.extract_mesh && a.node_capacity == b.node_capacity &&
+              a.mesh_capacity == b.mesh_capacity && a.triangle_capacity == b.triangle_capacity &&
+              a.precision == b.precision && a.warp_mesh == b.warp_mesh && a.blend == b.blend;
+    for (int i = 0; i < 9; ++i) eq = eq && a.K[i] == b.K[i];
+    for (int i = 0; i < 3; ++i) eq = eq && a.dims[i] == b.dims[i] && a.volume_size[i] == b.volume_size[i];
+    return eq;
+}
+
+double ms_since(Clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+}
 
 void free_session(Session* s) {
     if (!s) return;
@@ -60,12 +91,23 @@ void free_session(Session* s) {
 }  // namespace
 
 struct afx_server {
-    size_t budget = 0, used = 0;
+    size_t budget = 0, used = 0, idle_bytes = 0;  // used: open sessions; idle_bytes: kept for reuse
     int max_sessions = 0;
     int next_id = 1;
     long denied = 0;
     std::map<int, Session*> sessions;
+    std::vector<Session*> idle;  // closed sessions, oldest first
+    afx_server_counters c{};
     std::mutex mu;
+
+    // A closed session with nothing in flight leaves the open set and waits for reuse.
+    void retire(std::map<int, Session*>::iterator it) {
+        Session* x = it->second;
+        sessions.erase(it);
+        used -= x->bytes;
+        idle.push_back(x);
+        idle_bytes += x->bytes;
+    }
 };
 
 extern "C" {
@@ -83,6 +125,7 @@ int afx_server_create(size_t memory_budget_bytes, int max_sessions, afx_server**
 int afx_server_destroy(afx_server* s) {
     if (!s) return AFX_ERR_INVALID_ARGUMENT;
     for (auto& kv : s->sessions) free_session(kv.second);
+    for (Session* x : s->idle) free_session(x);
     delete s;
     return AFX_OK;
 }
@@ -92,13 +135,45 @@ int afx_server_open(afx_server* s, const afx_fusion_params* params, int* session
     const size_t need = afx_fusion_memory_bytes(params);
     if (need == 0) return AFX_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lock(s->mu);
-    if ((int)s->sessions.size() >= s->max_sessions || s->used + need > s->budget) {
+    const Clock::time_point t0 = Clock::now();
+    if ((int)s->sessions.size() >= s->max_sessions) {
+        ++s->denied;
+        return AFX_ERR_NO_MEMORY;
+    }
+    // an idle session with the same parameters: reset it and hand it out again
+    for (size_t i = 0; i < s->idle.size(); ++i) {
+        Session* x = s->idle[i];
+        if (!params_equal(x->params, *params)) continue;
+        const int rc = afx_fusion_reset(x->f, x->st);
+        if (rc) return rc;
+        s->idle.erase(s->idle.begin() + (long)i);
+        s->idle_bytes -= x->bytes;
+        x->closing = false;
+        x->head = x->count = 0;
+        x->id = s->next_id++;
+        s->used += x->bytes;
+        s->sessions[x->id] = x;
+        *session_id = x->id;
+        ++s->c.opens_reused;
+        s->c.open_ms += ms_since(t0);
+        return AFX_OK;
+    }
+    // room for a new one: free idle sessions, oldest first
+    while (!s->idle.empty() && s->used + s->idle_bytes + need > s->budget) {
+        Session* v = s->idle.front();
+        s->idle.erase(s->idle.begin());
+        s->idle_bytes -= v->bytes;
+        free_session(v);
+        ++s->c.evictions;
+    }
+    if (s->used + need > s->budget) {
         ++s->denied;
         return AFX_ERR_NO_MEMORY;
     }
     Session* x = new (std::nothrow) Session();
     if (!x) return AFX_ERR_NO_MEMORY;
     x->pixels = (long)params->width * params->height;
+    x->params = *params;
     int rc = afx_fusion_create(params, &x->f);
     if (rc) {
         delete x;
@@ -120,6 +195,8 @@ int afx_server_open(afx_server* s, const afx_fusion_params* params, int* session
     s->used += need;
     s->sessions[x->id] = x;
     *session_id = x->id;
+    ++s->c.opens_fresh;
+    s->c.open_ms += ms_since(t0);
     return AFX_OK;
 }
 
@@ -132,11 +209,7 @@ int afx_server_close(afx_server* s, int session_id) {
     if (it == s->sessions.end()) return AFX_ERR_INVALID_ARGUMENT;
     Session* x = it->second;
     x->closing = true;
-    if (x->count == 0) {
-        s->used -= x->bytes;
-        s->sessions.erase(it);
-        free_session(x);
-    }
+    if (x->count == 0) s->retire(it);
     return AFX_OK;
 }
 
@@ -152,6 +225,7 @@ int afx_server_submit(afx_server* s, int session_id, const uint16_t* depth_mm_ho
     sl.t_submit = Clock::now();
     sl.tag = tag;
     std::memcpy(sl.staging, depth_mm_host, (size_t)x->pixels * 2);
+    const Clock::time_point t1 = Clock::now();
     int rc = afx_fusion_process_host(x->f, sl.staging, x->st);
     if (rc) return rc;
     rc = afx_fusion_stats_async(x->f, sl.stats, x->st);
@@ -159,6 +233,9 @@ int afx_server_submit(afx_server* s, int session_id, const uint16_t* depth_mm_ho
     const cudaError_t re = cudaEventRecord(sl.done, x->st);
     if (re != cudaSuccess) return afx::note_cuda_error(re);
     ++x->count;
+    ++s->c.submits;
+    s->c.staging_ms += std::chrono::duration<double, std::milli>(t1 - sl.t_submit).count();
+    s->c.enqueue_ms += ms_since(t1);
     return AFX_OK;
 }
 
@@ -167,6 +244,7 @@ int afx_server_poll(afx_server* s, afx_server_result* out, int max_results, int*
     std::lock_guard<std::mutex> lock(s->mu);
     int n = 0;
     const Clock::time_point now = Clock::now();
+    ++s->c.polls;
     for (auto it = s->sessions.begin(); it != s->sessions.end();) {
         Session* x = it->second;
         while (x->count > 0 && n < max_results) {
@@ -183,14 +261,14 @@ int afx_server_poll(afx_server* s, afx_server_result* out, int max_results, int*
             --x->count;
         }
         if (x->closing && x->count == 0) {
-            s->used -= x->bytes;
-            free_session(x);
-            it = s->sessions.erase(it);
+            s->retire(it++);
         } else {
             ++it;
         }
     }
     *n_results = n;
+    s->c.results += n;
+    s->c.poll_ms += ms_since(now);
     return AFX_OK;
 }
 
@@ -208,6 +286,15 @@ int afx_server_usage(afx_server* s, size_t* used_bytes, int* sessions, long* den
     if (used_bytes) *used_bytes = s->used;
     if (sessions) *sessions = (int)s->sessions.size();
     if (denied) *denied = s->denied;
+    return AFX_OK;
+}
+
+int afx_server_get_counters(afx_server* s, afx_server_counters* out) {
+    if (!s || !out) return AFX_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lock(s->mu);
+    *out = s->c;
+    out->idle_sessions = (int)s->idle.size();
+    out->idle_bytes = s->idle_bytes;
     return AFX_OK;
 }
 

@@ -2,13 +2,14 @@
 
 Sessions are admitted while their device memory fits the server's budget; each has its own CUDA
 stream, so frames of different sessions overlap on the device, and frames of one session run in
-order.  submit() returns at once; poll() hands back finished frames with their latency.
+order.  submit() returns at once; poll() hands back finished frames with their latency.  A
+closed session is kept for reuse by a later open with the same configuration.
 """
 import ctypes as C
 
 import numpy as np
 
-from ._lib import AfxError, FrameStats, ServerResult, check, lib
+from ._lib import AfxError, FrameStats, ServerCounters, ServerResult, check, lib
 from .fusion import params_from_config
 
 AFX_ERR_CAPACITY = 2
@@ -75,6 +76,12 @@ class Server:
         used, n, denied = C.c_size_t(0), C.c_int(0), C.c_long(0)
         check(lib().afx_server_usage(self.h, C.byref(used), C.byref(n), C.byref(denied)), "afx_server_usage")
         return {"used_bytes": used.value, "sessions": n.value, "denied": denied.value}
+
+    def counters(self):
+        """Reuse of closed sessions and the host time spent inside the server's calls."""
+        c = ServerCounters()
+        check(lib().afx_server_get_counters(self.h, C.byref(c)), "afx_server_get_counters")
+        return {f[0]: getattr(c, f[0]) for f in ServerCounters._fields_}
 
     def session_handle(self, sid):
         return lib().afx_server_session(self.h, int(sid))
