@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--served-seconds", type=float, default=4.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-gpu", action="store_true", help="skip the reference's own GPU loop")
     ap.add_argument("--cpu-frames", type=int, default=3)
     return ap.parse_args()
 
@@ -215,6 +216,73 @@ def reference_cpu_stages(cfg, frames_np):
             "integrate_ms": 1000 * t_int, "marching_cubes_ms": 1000 * t_mc, "triangles": int(nf.value),
             "vertices": int(nv), "build_graph_ms": 1000 * t_graph, "nodes": int(n), "points": len(mesh),
             "knn_ms": 1000 * t_knn}
+
+
+def reference_gpu_arm(cfg, frames_np, stream, timeout_s=600):
+    """The reference's own per-frame loop on this GPU: af::runVolumeFusion (src/VolumeFusion.cu:223-783)
+    and every kernel, thrust call and cuSOLVER LU it makes, compiled unchanged for sm_103a
+    (oracle/ref_gpu/build.py -> oracle/_ref/libvfref_gpu.so), fed the headline sequence from memory in a
+    child process with a time limit (oracle/ref_gpu/run.py).  Its compile-time constants stay its own
+    (256^3, K = 6 skinning, K_reg = 4, up to 20 Gauss-Newton iterations per ICP iteration with its
+    energy-step break), so this library runs the same sequence with those settings beside it
+    (device-resident frames, same ICP count, radius and weights)."""
+    import torch
+    from volumefusion_gb300.fusion import FusionSession
+    lib_path = os.path.join(ROOT, "oracle", "_ref", "libvfref_gpu.so")
+    build_s = 0.0
+    if not os.path.exists(lib_path):
+        sys.path.insert(0, os.path.join(ROOT, "oracle", "ref_gpu"))
+        try:
+            import build as ref_build
+            t0 = time.perf_counter()
+            ref_build.build()
+            build_s = time.perf_counter() - t0
+        except Exception as e:  # no staged sources, or the compile failed
+            return {"unavailable": "reference GPU build: %s" % str(e).splitlines()[0][:200]}
+    n = len(frames_np)
+    try:
+        p = subprocess.run([sys.executable, os.path.join(ROOT, "oracle", "ref_gpu", "run.py"), "--frames", str(n),
+                            "--runs", "2"], capture_output=True, text=True, timeout=timeout_s)
+    except subprocess.TimeoutExpired:
+        return {"unavailable": "the reference loop did not finish within %d s" % timeout_s}
+    if p.returncode != 0:
+        return {"unavailable": "the reference loop exited with %d: %s" % (p.returncode, p.stderr.strip()[-300:])}
+    runs = json.loads(p.stdout.strip().splitlines()[-1])["runs"]
+    last = runs[-1]
+    if last["rc"] != 0:
+        return {"unavailable": "the reference loop stopped at frame %d: %s %s" % (
+            int(np.count_nonzero(np.asarray(last["frame_ms"]))), last["error"], p.stderr.strip()[-200:])}
+    ms = np.asarray(last["frame_ms"])
+    ref_fps = (n - 1) / (ms[1:].sum() / 1000.0)
+    # this library on the reference's constants, the same frames
+    same = dict(cfg, knn=6, kreg=4, gn_iterations=20, name=cfg["name"] + "_reference_constants")
+    frames_dev = [torch.from_numpy(f.astype(np.int16)).cuda() for f in frames_np]
+    s = FusionSession(same, stream=stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        for step in range(3):
+            s.reset()
+            s.process(frames_dev[0])
+            if step == 2:
+                ev0.record(stream)
+            for f in range(1, n):
+                s.process(frames_dev[f])
+        ev1.record(stream)
+    torch.cuda.synchronize()
+    ours_ms = ev0.elapsed_time(ev1)
+    st = s.stats()
+    s.close()
+    ours_fps = (n - 1) / (ours_ms / 1000.0)
+    return {"kind": "reference GPU loop (af::runVolumeFusion, unchanged, sm_103a)",
+            "frames": "1..%d of the headline sequence (non-rigid), second of two runs" % (n - 1),
+            "frames_per_s": ref_fps, "nodes_last_frame": last.get("nodes"),
+            "ms_per_frame_median": float(np.median(ms[1:])),
+            "ms_per_frame_max": float(ms[1:].max()), "ms_frame0": float(ms[0]), "build_s": build_s,
+            "constants": "256^3, K=6, K_reg=4, <=20 GN iterations per ICP iteration (energy-step break), "
+                         "dense J + cuSOLVER LU, graph build and KNN on the host",
+            "ours_same_constants": {"frames_per_s": ours_fps, "nodes_last_frame": st["n_nodes"],
+                                    "gn_iterations_last_frame": st["gn_iterations_done"]},
+            "ratio_ours_over_reference": ours_fps / ref_fps}
 
 
 def run_reference(args):
@@ -847,6 +915,10 @@ def main():
                           "achieved_gbs": v / (per_frame[k] / 1000.0) / 1e9 if per_frame.get(k) else None}
                       for k, v in algo.items()}
 
+    ref_gpu = None
+    if rank == 0 and world == 1 and not args.no_reference_gpu:
+        ref_gpu = reference_gpu_arm(cfg, frames_np, stream)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and args.cpu_frames > 0:
         v, dt = cpu_baseline(cfg, frames_np, args.cpu_frames)
@@ -883,6 +955,7 @@ def main():
             "rigid_stream": rigid,
             "rigid_integration": rigid_int,
             "served": served,
+            "reference_gpu": ref_gpu,
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": sampler.summary(),

@@ -1,5 +1,6 @@
-"""Stages the reference's CPU sources that oracle/Makefile.ref compiles into oracle/_ref/src/, so
-that a machine without the reference tree can build oracle/_ref/libvfref.so for its own CPU.
+"""Stages the reference's sources that oracle/Makefile.ref and oracle/ref_gpu/build.py compile into
+oracle/_ref/src/, so that a machine without the reference tree can build oracle/_ref/libvfref.so
+(its CPU code) and oracle/_ref/libvfref_gpu.so (its per-frame GPU loop) for itself.
 
 Test and baseline infrastructure only: oracle/_ref/ is git-ignored (never committed) and holds
 the reference's files unchanged, in the reference's own layout (src/, include/af/, the two
@@ -13,7 +14,11 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DEST = os.path.join(HERE, "_ref", "src")
-SOURCES = ["src/TSDFVolume.cpp", "src/MarchingCubes.cpp", "src/GraphBuilder.cpp", "src/MotionGraph.cpp", "src/Mesh.cpp"]
+SOURCES = ["src/TSDFVolume.cpp", "src/MarchingCubes.cpp", "src/GraphBuilder.cpp", "src/MotionGraph.cpp", "src/Mesh.cpp",
+           # the per-frame loop and its CUDA sources, for the reference-GPU baseline (oracle/ref_gpu/build.py)
+           "src/VolumeFusion.cu", "src/TSDFIntegration.cu", "src/TSDFWarp.cu", "src/MarchingCubes.cu",
+           "src/ComputeCorrespondence.cu", "src/VertexManipulation.cu", "src/MotionOptimization.cu",
+           "src/LinearSolver.cu", "src/BilateralFilter.cu", "src/Helper.cu"]
 TREES = ["include/af", "third_party/include/eigen-master/Eigen", "third_party/include/nanoflann"]
 
 
