@@ -350,7 +350,11 @@ def stage_bytes(cfg, st):
     A = st.get("active_voxels", 0)
     return {
         "prep": P * (2.0 + 4.0 + 24.0),
-        "marching_cubes": 8.0 * S + 12.0 * st["mesh_points"] * 4 + 48.0 * st["mesh_faces"],
+        # the reference's kernel reads every voxel (8 B); this one reads the 8^3 bricks that hold a
+        # weighted voxel (the rest cannot contain a cube with all eight weights set), then writes
+        # 12 B per point (with the four edge copies) and 48 B per triangle
+        "marching_cubes": 8.0 * 512 * st.get("occupied_bricks", S // 512) + 12.0 * st["mesh_points"] * 4
+                          + 48.0 * st["mesh_faces"],
         # 16 B per supported voxel (value + weight read and written) + the collision word (4 B)
         "warped_integrate": 20.0 * A if A else None,
     }
@@ -783,6 +787,7 @@ def main():
     s.set_timing(False)
     st = s.stats(check_errors=False)
     st["active_bricks"], st["active_voxels"] = s.support_size()
+    st["occupied_bricks"], st["bricks"] = s.occupied_bricks()
     s.close()
 
     # ---- end-to-end arm: host buffers through the C ABI, per-frame latency ----

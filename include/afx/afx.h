@@ -405,6 +405,10 @@ int afx_fusion_frame_views(afx_fusion* f, float** depth, float** vertices, float
  * supporting node (the reference's knnCount > 0, src/TSDFWarp.cu:61-67).  Synchronises `stream`. */
 int afx_fusion_support_size(afx_fusion* f, unsigned* active_bricks, unsigned long long* supported_voxels,
                             void* stream);
+/* Bricks of 8^3 voxels that hold a voxel with nonzero weight (of *total in the volume): the bricks
+ * marching cubes reads (no counterpart in the reference, whose kernel reads every voxel).
+ * Synchronises `stream`. */
+int afx_fusion_occupied_bricks(afx_fusion* f, unsigned long long* bricks, unsigned long long* total, void* stream);
 /* Overwrite the committed node transforms (host memory), e.g. to replay a trajectory. */
 int afx_fusion_set_transforms(afx_fusion* f, const float* transforms_host, int n, void* stream);
 /* Number of kernels the library launched since the session was created. */

@@ -130,6 +130,7 @@ SIGNATURES = {
     "afx_fusion_frame_views": (i32, [vp, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp)]),
     "afx_fusion_volume_changed": (i32, [vp, vp]),
     "afx_fusion_support_size": (i32, [vp, C.POINTER(C.c_uint), C.POINTER(C.c_ulonglong), vp]),
+    "afx_fusion_occupied_bricks": (i32, [vp, C.POINTER(C.c_ulonglong), C.POINTER(C.c_ulonglong), vp]),
     "afx_fusion_set_transforms": (i32, [vp, vp, i32, vp]),
     "afx_fusion_kernel_launches": (i64, [vp]),
     "afx_copy_device": (i32, [vp, vp, sz, vp]),

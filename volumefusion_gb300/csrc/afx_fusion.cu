@@ -912,9 +912,30 @@ __global__ void support_count_kernel(const unsigned char* count, const unsigned*
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
+__global__ void occ_count_kernel(const unsigned char* occ, long n, unsigned long long* out) {
+    unsigned long long c = 0;
+    AFX_GRID_STRIDE(i, n) c += occ[i] ? 1ull : 0ull;
+    c = warp_sum(c);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
 }  // namespace afx
 
 extern "C" {
+
+int afx_fusion_occupied_bricks(afx_fusion* f, unsigned long long* bricks, unsigned long long* total, void* stream) {
+    if (!f || !bricks) return AFX_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = as_stream(stream);
+    const long n = brick_count_total(f->vol);
+    unsigned long long* cnt = reinterpret_cast<unsigned long long*>(f->acc) + 5;  // spare word of acc's 64 B
+    AFX_CUDA(cudaMemsetAsync(cnt, 0, sizeof(unsigned long long), st));
+    occ_count_kernel<<<grid_for(n, 256), 256, 0, st>>>(f->occ, n, cnt);
+    AFX_LAUNCH_CHECK();
+    AFX_CUDA(cudaMemcpyAsync(bricks, cnt, sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    AFX_CUDA(cudaStreamSynchronize(st));
+    if (total) *total = (unsigned long long)n;
+    return AFX_OK;
+}
 
 int afx_fusion_support_size(afx_fusion* f, unsigned* active_bricks, unsigned long long* supported_voxels,
                             void* stream) {

@@ -162,6 +162,13 @@ class FusionSession:
         check(lib().afx_fusion_support_size(self.h, C.byref(nb), C.byref(nv), self._st()), "afx_fusion_support_size")
         return nb.value, nv.value
 
+    def occupied_bricks(self):
+        """(8^3 bricks holding a weighted voxel, bricks in the volume): what marching cubes reads."""
+        nb, tot = C.c_ulonglong(0), C.c_ulonglong(0)
+        check(lib().afx_fusion_occupied_bricks(self.h, C.byref(nb), C.byref(tot), self._st()),
+              "afx_fusion_occupied_bricks")
+        return nb.value, tot.value
+
     def set_transforms(self, T):
         arr = np.ascontiguousarray(T, dtype=np.float32)
         check(lib().afx_fusion_set_transforms(self.h, arr.ctypes.data_as(C.c_void_p), arr.shape[0], self._st()),
