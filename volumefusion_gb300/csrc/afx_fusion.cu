@@ -167,6 +167,7 @@ struct afx_fusion {
     WarpedVoxel* wvox;
     unsigned char* wcount;
     unsigned char* occ;    // per 8^3 brick: 1 once any voxel of it has a weight (marching cubes skips the rest)
+    unsigned* mc_tiles;    // marching cubes on the persistent grid: count + occupied tiles
     FrameStats* stats;
     void* ws_sort;
     size_t ws_sort_bytes;
@@ -365,6 +366,7 @@ static void session_layout(const afx_fusion_params& p, afx_fusion* f) {
     const long mesh_knn = p.warp_mesh ? p.triangle_capacity * 3 * p.knn * 4 : 0;  // output-mesh warp
     add(mesh_knn); add(mesh_knn); add(mesh_knn);
     add(nbricks * 512 * sizeof(WarpedVoxel)); add(nbricks * 512); add(nbricks);
+    add(mc_tile_ws_words(f->vol) * 4);
     add(sizeof(FrameStats)); add(64);
     add(f->ws_sort_bytes); add(f->ws_graph_bytes); add(f->ws_corr_bytes); add(f->ws_support_bytes); add(f->ws_gn_bytes);
     f->arena_bytes = sz + 4096;
@@ -455,6 +457,7 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     f->wvox = (WarpedVoxel*)take(nbricks * 512 * sizeof(WarpedVoxel));
     f->wcount = (unsigned char*)take(nbricks * 512);
     f->occ = (unsigned char*)take(nbricks);
+    f->mc_tiles = (unsigned*)take(mc_tile_ws_words(f->vol) * 4);
     f->stats = (FrameStats*)take(sizeof(FrameStats));
     f->frame_dev = (int*)take(64);
     f->ws_sort = take(f->ws_sort_bytes);
@@ -595,7 +598,7 @@ static int extract_frame_mesh(afx_fusion* f, int cur, cudaStream_t st) {
     return mc_fused_impl(f->tsdf, f->weights, f->fmt, f->vol, 0.f, f->points_buf[next], f->npoints_buf[next], f->p.mesh_capacity,
                          mesh ? f->mverts : nullptr, mesh ? f->nmverts : nullptr, f->p.triangle_capacity * 3,
                          mesh ? f->mfaces : nullptr, mesh ? f->nmfaces : nullptr, f->p.triangle_capacity, st, f->error,
-                         f->mc_tile, f->occ);
+                         f->mc_tile, f->occ, f->mc_tiles);
 }
 
 // Everything a frame does on the device, in stream order on `st`; host state is not changed.

@@ -48,8 +48,11 @@ int sort_unique_volume_impl(float* pts, unsigned* count, long n_max, void* ws, s
 int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
                   unsigned* face_count, long face_cap, cudaStream_t st, int* error = nullptr, int tile = 0,
-                  const unsigned char* occ = nullptr);  // occ: brick occupancy (tiles without an occupied
-                                                       // brick hold no active cube and are skipped)
+                  const unsigned char* occ = nullptr,   // occ: brick occupancy (tiles without an occupied
+                                                        // brick hold no active cube and are skipped)
+                  unsigned* tile_ws = nullptr);         // mc_tile_ws_words(vol) words: with occ, the
+                                                        // persistent tiles walk a list of occupied tiles
+size_t mc_tile_ws_words(const Volume& vol);
 // marching-cubes tiles (the session's autotuner picks one): TMA bricks of 16, 8 or 32 cubes along z,
 // the column march from global memory, or a persistent grid with two stages of bricks 8 or 16 deep
 enum { kMcTileTma16 = 0, kMcTileTma8 = 1, kMcTileTma32 = 2, kMcTileColumn = 3, kMcTilePipe8 = 4, kMcTilePipe16 = 5,

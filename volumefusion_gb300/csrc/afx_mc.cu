@@ -62,6 +62,8 @@ struct McArgs {
     int* error;  // TMA path: set on a tile-load timeout
     const unsigned char* occ;  // brick occupancy (8^3 voxels), or null: process every tile
     int nbx, nby, nbz;
+    unsigned* tile_count;      // persistent grid: occupied tiles listed here (with occ), or null
+    unsigned* tile_list;
 };
 
 
@@ -400,6 +402,17 @@ AFX_D bool mc_wait(uint32_t bar, uint32_t parity) {
     return false;
 }
 
+// The occupied tiles of the volume (those tile_occupied accepts), in no particular order.
+__global__ void mc_tile_list_kernel(McArgs a, int tx_n, int ty_n, int tz_n, int zr) {
+    const long nt = (long)tx_n * ty_n * tz_n;
+    AFX_GRID_STRIDE(t, nt) {
+        const int tx = (int)(t % tx_n), ty = (int)((t / tx_n) % ty_n), tz = (int)(t / ((long)tx_n * ty_n));
+        if (tile_occupied(a, tx * kMcX, ty * kMcY, tz * zr, zr)) a.tile_list[atomicAdd(a.tile_count, 1u)] = (unsigned)t;
+    }
+}
+
+// Persistent grid over the tiles -- every tile, or with a.tile_list the listed ones -- with two
+// stages of TMA bricks: the next tile's brick loads while this one is classified.
 template <class TT, class WT, bool kPoints, bool kMesh, int ZR>
 __global__ void __launch_bounds__(kMcX * kMcY) mc_pipe_kernel(const __grid_constant__ CUtensorMap map_t,
                                                              const __grid_constant__ CUtensorMap map_w,
@@ -422,12 +435,14 @@ __global__ void __launch_bounds__(kMcX * kMcY) mc_pipe_kernel(const __grid_const
         sw[k] = reinterpret_cast<WT*>(mc_raw + pad + (2 * k + 1) * kBrick);
     }
     const int tid = threadIdx.y * kMcX + threadIdx.x;
-    const long nt = (long)tx_n * ty_n * tz_n;
+    const long nall = (long)tx_n * ty_n * tz_n;
+    const long nt = a.tile_list ? min((long)*a.tile_count, nall) : nall;
     if ((mc_smem_u32(st[0]) & 127u) != 0u) {  // never expected: refuse rather than fault
         if (tid == 0 && a.error) atomicOr(a.error, ERRF_TMA);
         return;
     }
-    auto origin = [&](long t, int& x0, int& y0, int& z0) {
+    auto origin = [&](long i, int& x0, int& y0, int& z0) {  // i-th tile of this launch
+        const long t = a.tile_list ? (long)a.tile_list[i] : i;
         const int tx = (int)(t % tx_n), ty = (int)((t / tx_n) % ty_n), tz = (int)(t / ((long)tx_n * ty_n));
         x0 = tx * kMcX;
         y0 = ty * kMcY;
@@ -580,8 +595,22 @@ static void mc_launch_pipe(const TT* tsdf, const McArgs& a, const CUtensorMap* m
               tz = (a.vol.dims[2] - 2 + ZR - 1) / ZR;
     const long nt = (long)tx * ty * tz;
     const long grid = nt < (long)sms * per_sm ? nt : (long)sms * per_sm;
-    mc_pipe_kernel<TT, WT, kPoints, kMesh, ZR><<<(unsigned)grid, dim3(kMcX, kMcY), smem, st>>>(*mt, *mw, tsdf, a, tx,
+    McArgs b = a;
+    if (a.occ && a.tile_list && a.tile_count) {
+        cudaMemsetAsync(a.tile_count, 0, sizeof(unsigned), st);
+        mc_tile_list_kernel<<<grid_for(nt, 256), 256, 0, st>>>(a, tx, ty, tz, ZR);
+    } else {
+        b.tile_list = nullptr;
+    }
+    mc_pipe_kernel<TT, WT, kPoints, kMesh, ZR><<<(unsigned)grid, dim3(kMcX, kMcY), smem, st>>>(*mt, *mw, tsdf, b, tx,
                                                                                               ty, tz);
+}
+
+// Words of the occupied-tile list for a volume (count + one entry per tile of the shallowest depth).
+size_t mc_tile_ws_words(const Volume& vol) {
+    const long tx = (vol.dims[0] - 2 + kMcX - 1) / kMcX, ty = (vol.dims[1] - 2 + kMcY - 1) / kMcY,
+               tz = (vol.dims[2] - 2 + 8 - 1) / 8;
+    return (size_t)(1 + (tx > 0 ? tx : 0) * (ty > 0 ? ty : 0) * (tz > 0 ? tz : 0));
 }
 
 // tile: kMcTileTma16 (default), kMcTileTma8, kMcTileTma32 (TMA bricks of that many cubes along z),
@@ -619,7 +648,7 @@ static void mc_launch_any(const TT* tsdf, const WT* weights, const McArgs& a, co
 int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& vol, float iso, float* points,
                   unsigned* point_count, long point_cap, float* verts, unsigned* vert_count, long vert_cap, int* faces,
                   unsigned* face_count, long face_cap, cudaStream_t st, int* error, int tile,
-                  const unsigned char* occ) {
+                  const unsigned char* occ, unsigned* tile_ws) {
     int rc = upload_tables();
     if (rc) return rc;
     McArgs a;
@@ -635,6 +664,8 @@ int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& 
     a.faces = faces;
     a.error = error;
     a.occ = occ;
+    a.tile_count = tile_ws;
+    a.tile_list = tile_ws ? tile_ws + 1 : nullptr;
     a.nbx = (vol.dims[0] + 7) / 8;
     a.nby = (vol.dims[1] + 7) / 8;
     a.nbz = (vol.dims[2] + 7) / 8;
