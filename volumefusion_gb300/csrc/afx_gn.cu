@@ -233,6 +233,9 @@ struct JtjStage {
     signed char slot[32][kJtjMaxK];    // -1: diagonal, >= 0: upper block, -2: no contribution
     int own[32];                       // depth rows: the row's own slot, -1 without correspondence;
                                        // reg rows: 1 own edge, 0 incoming edge, -1 skipped
+    unsigned qt[32];                   // depth rows with a correspondence, queued in entry order:
+    unsigned qe[32];                   // node-list position, entry (vertex * k + slot)
+    int qc[32];                        // and correspondence
 };
 
 AFX_D int find_slot(const int* L, int cnt, int b) {
@@ -262,54 +265,48 @@ __global__ void __launch_bounds__(32 * kJtjWarps) jtj_assemble_kernel(GnArgs a) 
         __syncwarp();
         float d0 = 0.f, d1 = 0.f;
         bool touched = false;
-        const unsigned o = a.b.loff[node], e = a.b.loff[node + 1];
-        for (unsigned base = o; base < e; base += 32) {
-            // stage up to 32 depth rows, one per lane
-            const unsigned t = base + lane;
-            if (t < e) {
-                const unsigned ent = a.b.lst[t];
+        // Depth rows: the node list is read 128 entries at a time (4 per lane, their loads in
+        // flight together); entries whose vertex has a correspondence are queued in entry order
+        // and, 32 at a time, staged (one row per lane: the Jacobian block of every slot) and then
+        // accumulated in order.  Entries without a correspondence contribute nothing.
+        auto run_queue = [&](int nq) {
+            if (lane < nq) {
+                const unsigned t = S.qt[lane], ent = S.qe[lane];
                 const long v = ent / k;
                 const int s = (int)(ent % k);
-                const int c = a.corr_of_vertex[v];
-                a.b.jc[t] = c;
-                S.own[lane] = c < 0 ? -1 : s;
-                if (c >= 0) {
-                    const int px = a.corr[2 * (long)c + 1];
-                    const float nrm[3] = {a.normals[3 * (long)px], a.normals[3 * (long)px + 1],
-                                          a.normals[3 * (long)px + 2]};
-                    const float p[3] = {a.mesh[3 * v], a.mesh[3 * v + 1], a.mesh[3 * v + 2]};
-                    float G[3][6];
-                    grad_rows(p, G);
-                    for (int tt = 0; tt < k; ++tt) {
-                        const float wt = a.mw[v * k + tt];
-                        const uint32_t bnode = a.midx[v * k + tt];
-                        int sl = -2;
-                        if (wt != 0.f && bnode >= (uint32_t)node) {
-                            if (bnode == (uint32_t)node) sl = -1;
-                            else {
-                                const int f = find_slot(S.L, cnt, (int)bnode);
-                                if (f >= 0) sl = f;
-                            }
+                const int c = S.qc[lane];
+                S.own[lane] = s;
+                const int px = a.corr[2 * (long)c + 1];
+                const float nrm[3] = {a.normals[3 * (long)px], a.normals[3 * (long)px + 1], a.normals[3 * (long)px + 2]};
+                const float p[3] = {a.mesh[3 * v], a.mesh[3 * v + 1], a.mesh[3 * v + 2]};
+                float G[3][6];
+                grad_rows(p, G);
+                for (int tt = 0; tt < k; ++tt) {
+                    const float wt = a.mw[v * k + tt];
+                    const uint32_t bnode = a.midx[v * k + tt];
+                    int sl = -2;
+                    if (wt != 0.f && bnode >= (uint32_t)node) {
+                        if (bnode == (uint32_t)node) sl = -1;
+                        else {
+                            const int f = find_slot(S.L, cnt, (int)bnode);
+                            if (f >= 0) sl = f;
                         }
-                        S.slot[lane][tt] = (signed char)sl;
-                        if (sl != -2 || tt == s) {
-                            float Jt[6];
-                            jdepth(nrm, wt, G, a.lam_d, Jt);
+                    }
+                    S.slot[lane][tt] = (signed char)sl;
+                    if (sl != -2 || tt == s) {
+                        float Jt[6];
+                        jdepth(nrm, wt, G, a.lam_d, Jt);
 #pragma unroll
-                            for (int q = 0; q < 6; ++q) S.J[lane][tt][q] = Jt[q];
-                            if (tt == s)  // this row's J block, for J^T r
+                        for (int q = 0; q < 6; ++q) S.J[lane][tt][q] = Jt[q];
+                        if (tt == s)  // this row's J block, for J^T r
 #pragma unroll
-                                for (int q = 0; q < 6; ++q) a.b.jrow[(long)t * 6 + q] = Jt[q];
-                        }
+                            for (int q = 0; q < 6; ++q) a.b.jrow[(long)t * 6 + q] = Jt[q];
                     }
                 }
             }
             __syncwarp();
-            // ordered accumulation over the staged rows
-            const int nb = (int)min(32u, e - base);
-            for (int r = 0; r < nb; ++r) {
+            for (int r = 0; r < nq; ++r) {
                 const int s = S.own[r];
-                if (s < 0) continue;
                 touched = true;
                 const float ja0 = S.J[r][s][i0];
                 const float ja1 = has1 ? S.J[r][s][i1] : 0.f;
@@ -329,7 +326,49 @@ __global__ void __launch_bounds__(32 * kJtjWarps) jtj_assemble_kernel(GnArgs a) 
                 }
             }
             __syncwarp();
+        };
+        const unsigned o = a.b.loff[node], e = a.b.loff[node + 1];
+        int qn = 0;  // queued rows (warp-uniform)
+        for (unsigned base = o; base < e; base += 128) {
+            unsigned ent[4];
+            int cj[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const unsigned t = base + (unsigned)(j * 32 + lane);
+                ent[j] = t < e ? a.b.lst[t] : 0u;
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const unsigned t = base + (unsigned)(j * 32 + lane);
+                cj[j] = -1;
+                if (t < e) {
+                    cj[j] = a.corr_of_vertex[ent[j] / k];
+                    a.b.jc[t] = cj[j];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                unsigned bal = __ballot_sync(0xffffffffu, cj[j] >= 0);
+                while (bal) {
+                    unsigned take = bal;
+                    for (int drop = __popc(bal) - (32 - qn); drop > 0; --drop) take &= ~(0x80000000u >> __clz(take));
+                    if (take & (1u << lane)) {
+                        const int pos = qn + __popc(take & ((1u << lane) - 1u));
+                        S.qt[pos] = base + (unsigned)(j * 32 + lane);
+                        S.qe[pos] = ent[j];
+                        S.qc[pos] = cj[j];
+                    }
+                    qn += __popc(take);
+                    bal &= ~take;
+                    __syncwarp();
+                    if (qn == 32) {
+                        run_queue(32);
+                        qn = 0;
+                    }
+                }
+            }
         }
+        if (qn) run_queue(qn);
         // regularisation rows in ascending row order: incoming edges x -> node with x < node,
         // then node's own edges, then incoming edges with x > node (src/MotionOptimization.cu:298-340)
         const unsigned io = a.b.ioff[node], nin = a.b.ioff[node + 1] - io;
