@@ -708,7 +708,8 @@ def served_arm(args, rank):
                          "reused_sessions": warm},
             "plain_per_stream": {"frames": plain_frames, "frames_per_s": plain_fps,
                                  "note": "same sessions and frames, one session at a time, host frames"},
-            "capacity_over_plain": served_fps / plain_fps}
+            "capacity_over_plain": served_fps / plain_fps,
+            "reused_capacity_over_plain": warm["frames_per_s"] / plain_fps}
 
 
 def main():

@@ -52,11 +52,21 @@ inline unsigned blocks_for(long n, int threads) {
 
 // Grid for a grid-stride kernel over at most n items whose live count is read on the device:
 // enough blocks to cover n, capped at kStrideBlocks so that a large capacity with few live
-// items costs a few waves of immediately-exiting blocks, not one block per 256 slots.
-constexpr long kStrideBlocks = 1216;  // 8 blocks per SM on 152 SMs
+// items costs one short wave of immediately-exiting blocks, not one block per 256 slots.  Two
+// blocks per SM cover 78k live items in one pass; the cap is low because a block that only
+// reads the count and exits still costs the GPU its dispatch: with many sessions' frames in
+// flight, kernels of 1216 such blocks ran at 1.1M kernels/s, of 152 blocks at 4.0M kernels/s.
+constexpr long kStrideBlocks = 304;  // 2 blocks per SM on 152 SMs
 inline unsigned grid_for(long n, int threads) {
     long b = (n + threads - 1) / threads;
     return (unsigned)(b < 1 ? 1 : (b > kStrideBlocks ? kStrideBlocks : b));
+}
+// The same for kernels with a long loop per item (one graph node per warp or block): up to 8
+// blocks per SM, so that graphs of thousands of nodes still spread over every SM.
+constexpr long kNodeBlocks = 1216;
+inline unsigned grid_for_nodes(long n, int per_block) {
+    long b = (n + per_block - 1) / per_block;
+    return (unsigned)(b < 1 ? 1 : (b > kNodeBlocks ? kNodeBlocks : b));
 }
 
 // for (i in [start, n)) over the whole grid

@@ -131,12 +131,11 @@ __global__ void __launch_bounds__(256) seg_sort_kernel(unsigned* lst, const unsi
 __global__ void __launch_bounds__(32 * kGnWarps) nbr_discover_kernel(GnArgs a, int words) {
     extern __shared__ unsigned bm[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int node = blockIdx.x * kGnWarps + w;
     const int n = min(*a.n_nodes, a.n_max);
     unsigned* my = bm + (long)w * words;
-    for (int i = lane; i < words; i += 32) my[i] = 0u;
-    __syncwarp();
-    if (node < n) {
+    for (int node = blockIdx.x * kGnWarps + w; node < n; node += gridDim.x * kGnWarps) {
+        for (int i = lane; i < words; i += 32) my[i] = 0u;
+        __syncwarp();
         const unsigned o = a.b.loff[node], e = a.b.loff[node + 1];
         for (unsigned t = o + lane; t < e; t += 32) {
             unsigned ent = a.b.lst[t];
@@ -156,33 +155,33 @@ __global__ void __launch_bounds__(32 * kGnWarps) nbr_discover_kernel(GnArgs a, i
             unsigned x = a.b.ilst[t] / a.kreg;
             if (x != (unsigned)node) atomicOr(my + (x >> 5), 1u << (x & 31));
         }
-    }
-    __syncwarp();
-    if (node >= n) return;
-    // ordered extraction
-    int base = 0;
-    for (int w0 = 0; w0 < words; w0 += 32) {
-        int wi = w0 + lane;
-        unsigned bits = wi < words ? my[wi] : 0u;
-        int c = __popc(bits);
-        int incl = c;
+        __syncwarp();
+        // ordered extraction
+        int base = 0;
+        for (int w0 = 0; w0 < words; w0 += 32) {
+            int wi = w0 + lane;
+            unsigned bits = wi < words ? my[wi] : 0u;
+            int c = __popc(bits);
+            int incl = c;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            int pos = base + incl - c;
+            while (bits) {
+                int bit = __ffs(bits) - 1;
+                bits &= bits - 1;
+                if (pos < kMaxNbr) a.b.nbr[(long)node * kMaxNbr + pos] = wi * 32 + bit;
+                ++pos;
+            }
+            base += __shfl_sync(0xffffffffu, incl, 31);
         }
-        int pos = base + incl - c;
-        while (bits) {
-            int bit = __ffs(bits) - 1;
-            bits &= bits - 1;
-            if (pos < kMaxNbr) a.b.nbr[(long)node * kMaxNbr + pos] = wi * 32 + bit;
-            ++pos;
+        if (lane == 0) {
+            a.b.nbr_cnt[node] = min(base, kMaxNbr);
+            if (base > kMaxNbr) atomicOr(a.error, ERRF_CAPACITY);
         }
-        base += __shfl_sync(0xffffffffu, incl, 31);
-    }
-    if (lane == 0) {
-        a.b.nbr_cnt[node] = min(base, kMaxNbr);
-        if (base > kMaxNbr) atomicOr(a.error, ERRF_CAPACITY);
+        __syncwarp();  // the bitmap is cleared for the warp's next node
     }
 }
 
@@ -455,11 +454,8 @@ __global__ void __launch_bounds__(32 * kJtjWarps) jtj_assemble_kernel(GnArgs a) 
 // Inverse of each diagonal block: Gauss-Jordan with partial pivoting in FP64, one warp per
 // node with lane j < 12 owning column j of [D | I]; stored rounded to FP32 (the preconditioner
 // is applied in FP32).
-__global__ void __launch_bounds__(128) diag_inverse_kernel(GnArgs a) {
+AFX_D void diag_inverse_node(const GnArgs& a, int node) {
     const int lane = threadIdx.x & 31;
-    const int node = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    const int n = min(*a.n_nodes, a.n_max);
-    if (node >= n) return;
     const float* D = a.b.diag + (long)node * 36;
     const bool own = lane < 12;
     double col[6];
@@ -511,6 +507,12 @@ __global__ void __launch_bounds__(128) diag_inverse_kernel(GnArgs a) {
     if (lane >= 6 && lane < 12)
 #pragma unroll
         for (int i = 0; i < 6; ++i) out[i * 6 + lane - 6] = (float)col[i];
+}
+
+__global__ void __launch_bounds__(128) diag_inverse_kernel(GnArgs a) {
+    const int n = min(*a.n_nodes, a.n_max);
+    for (int node = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); node < n; node += gridDim.x * (blockDim.x >> 5))
+        diag_inverse_node(a, node);
 }
 
 // ---- Gauss-Newton loop: one thread-block cluster per ICP iteration ----
@@ -1533,7 +1535,7 @@ int gn_frame_setup(const GnArgs& a, cudaStream_t st) {
         lst_fill_kernel<<<grid_for(mk, 256), 256, 0, st>>>(a);
         AFX_LAUNCH_CHECK();
     }
-    seg_sort_kernel<<<grid_for(a.n_max, 1), 256, 0, st>>>(b.lst, b.loff, a.n_nodes, a.n_max, a.error);
+    seg_sort_kernel<<<grid_for_nodes(a.n_max, 1), 256, 0, st>>>(b.lst, b.loff, a.n_nodes, a.n_max, a.error);
     AFX_LAUNCH_CHECK();
     const long nk = (long)a.n_max * a.kreg;
     in_count_kernel<<<grid_for(nk, 256), 256, 0, st>>>(a);
@@ -1542,7 +1544,7 @@ int gn_frame_setup(const GnArgs& a, cudaStream_t st) {
     if (rc) return rc;
     in_fill_kernel<<<grid_for(nk, 256), 256, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
-    seg_sort_kernel<<<grid_for(a.n_max, 1), 256, 0, st>>>(b.ilst, b.ioff, a.n_nodes, a.n_max, a.error);
+    seg_sort_kernel<<<grid_for_nodes(a.n_max, 1), 256, 0, st>>>(b.ilst, b.ioff, a.n_nodes, a.n_max, a.error);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
@@ -1563,7 +1565,7 @@ int gn_icp_setup(const GnArgs& a, float* T_pending, const float* T_committed, cu
     AFX_LAUNCH_CHECK();
     if (T_pending)
         AFX_CUDA(cudaMemcpyAsync(T_pending, T_committed, (size_t)a.n_max * 64, cudaMemcpyDeviceToDevice, st));
-    const unsigned nb = (unsigned)((a.n_max + kGnWarps - 1) / kGnWarps);
+    const unsigned nb = grid_for_nodes(a.n_max, kGnWarps);  // grid-stride over the live nodes
     const int words = (a.n_max + 31) / 32;
     const size_t smem = (size_t)kGnWarps * words * 4;
     if (smem > 200 * 1024) return AFX_ERR_UNSUPPORTED;
@@ -1579,9 +1581,9 @@ int gn_icp_setup(const GnArgs& a, float* T_pending, const float* T_committed, cu
     AFX_LAUNCH_CHECK();
     nbr_ref_kernel<<<grid_for((long)a.n_max * kMaxNbr, 256), 256, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
-    jtj_assemble_kernel<<<grid_for(a.n_max, kJtjWarps), 32 * kJtjWarps, 0, st>>>(a);
+    jtj_assemble_kernel<<<grid_for_nodes(a.n_max, kJtjWarps), 32 * kJtjWarps, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
-    diag_inverse_kernel<<<(unsigned)((a.n_max + 3) / 4), 128, 0, st>>>(a);
+    diag_inverse_kernel<<<grid_for_nodes(a.n_max, 4), 128, 0, st>>>(a);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }

@@ -575,8 +575,9 @@ int knn_impl(uint32_t* idx, float* dist, const float* nodes, const int* n_nodes,
     if (m_max <= 0) return AFX_OK;
     const int e = excl ? 1 : 0;
     const int kk = k + e;
+    // grid-stride over the live points; the search loop is long, so up to 8 blocks per SM
     const long want = (m_max + kKnnThreads - 1) / kKnnThreads;
-    const unsigned blocks = (unsigned)(want < 4096 ? want : 4096);
+    const unsigned blocks = (unsigned)(want < 1216 ? want : 1216);
 #define AFX_KNN(KK)                                                                                              \
     knn_kernel<KK><<<blocks, kKnnThreads, 0, st>>>(idx, dist, nodes, n_nodes, n_max, pts, count, m_max, k, e); \
     break

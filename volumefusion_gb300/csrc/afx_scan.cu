@@ -1,6 +1,8 @@
 // afx_scan.cu -- exclusive prefix sums used for stream compaction and CSR offsets.
-// Three phases: per-block sums, a single-block scan of those sums, then the block-local
-// scans with their offsets added.  Deterministic (integer arithmetic).
+// Three phases: per-tile sums, a single-block scan of those sums, then the tile-local scans
+// with their offsets added.  Deterministic (integer arithmetic).  The tile phases are
+// grid-stride loops over the tiles that hold live items (the live count is read on the device),
+// on a grid of at most kScanBlocks, so a large capacity with few items costs one short wave.
 #include "afx_internal.h"
 
 namespace afx {
@@ -40,24 +42,30 @@ __device__ __forceinline__ long scan_n(const unsigned* count, long n_max) {
     return count ? min((long)*count, n_max) : n_max;
 }
 
+constexpr long kScanBlocks = 152;
+
 __global__ void __launch_bounds__(kScanThreads) scan_block_sums(const unsigned* in, const unsigned* count, long n_max,
                                                                  unsigned* sums) {
     __shared__ unsigned ws[32];
     const long n = scan_n(count, n_max);
-    const long base = (long)blockIdx.x * kScanTile;
-    unsigned s = 0;
-    if (base < n)
+    const long nt = (n + kScanTile - 1) / kScanTile;
+    for (long tile = blockIdx.x; tile < nt; tile += gridDim.x) {
+        const long base = tile * kScanTile;
+        unsigned s = 0;
         for (int i = 0; i < kScanItems; ++i) {
             long j = base + (long)threadIdx.x * kScanItems + i;
             if (j < n) s += in[j];
         }
-    unsigned tot;
-    block_exclusive_scan(s, ws, &tot);
-    if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+        unsigned tot;
+        block_exclusive_scan(s, ws, &tot);
+        if (threadIdx.x == 0) sums[tile] = tot;
+    }
 }
 
-__global__ void __launch_bounds__(1024) scan_sums_kernel(unsigned* sums, long nblocks, unsigned* total) {
+__global__ void __launch_bounds__(1024) scan_sums_kernel(unsigned* sums, const unsigned* count, long n_max,
+                                                         unsigned* total) {
     __shared__ unsigned ws[32];
+    const long nblocks = (scan_n(count, n_max) + kScanTile - 1) / kScanTile;
     unsigned carry = 0;
     for (long base = 0; base < nblocks; base += blockDim.x) {
         long j = base + threadIdx.x;
@@ -74,20 +82,22 @@ __global__ void __launch_bounds__(kScanThreads) scan_apply(const unsigned* in, u
                                                            long n_max, const unsigned* sums) {
     __shared__ unsigned ws[32];
     const long n = scan_n(count, n_max);
-    const long base = (long)blockIdx.x * kScanTile;
-    if (base >= n) return;
-    unsigned v[kScanItems];
-    unsigned s = 0;
-    for (int i = 0; i < kScanItems; ++i) {
-        long j = base + (long)threadIdx.x * kScanItems + i;
-        v[i] = j < n ? in[j] : 0u;
-        s += v[i];
-    }
-    unsigned e = block_exclusive_scan(s, ws, nullptr) + sums[blockIdx.x];
-    for (int i = 0; i < kScanItems; ++i) {
-        long j = base + (long)threadIdx.x * kScanItems + i;
-        if (j < n) out[j] = e;
-        e += v[i];
+    const long nt = (n + kScanTile - 1) / kScanTile;
+    for (long tile = blockIdx.x; tile < nt; tile += gridDim.x) {
+        const long base = tile * kScanTile;
+        unsigned v[kScanItems];
+        unsigned s = 0;
+        for (int i = 0; i < kScanItems; ++i) {
+            long j = base + (long)threadIdx.x * kScanItems + i;
+            v[i] = j < n ? in[j] : 0u;
+            s += v[i];
+        }
+        unsigned e = block_exclusive_scan(s, ws, nullptr) + sums[tile];
+        for (int i = 0; i < kScanItems; ++i) {
+            long j = base + (long)threadIdx.x * kScanItems + i;
+            if (j < n) out[j] = e;
+            e += v[i];
+        }
     }
 }
 
@@ -99,13 +109,14 @@ int scan_exclusive_dev(const unsigned* in, unsigned* out, const unsigned* count,
         if (total) AFX_CUDA(cudaMemsetAsync(total, 0, sizeof(unsigned), st));
         return AFX_OK;
     }
-    long nb = (n_max + kScanTile - 1) / kScanTile;
+    const long nb = (n_max + kScanTile - 1) / kScanTile;
+    const unsigned grid = (unsigned)(nb < kScanBlocks ? nb : kScanBlocks);
     unsigned* sums = static_cast<unsigned*>(ws);
-    scan_block_sums<<<(unsigned)nb, kScanThreads, 0, st>>>(in, count, n_max, sums);
+    scan_block_sums<<<grid, kScanThreads, 0, st>>>(in, count, n_max, sums);
     AFX_LAUNCH_CHECK();
-    scan_sums_kernel<<<1, 1024, 0, st>>>(sums, nb, total);
+    scan_sums_kernel<<<1, 1024, 0, st>>>(sums, count, n_max, total);
     AFX_LAUNCH_CHECK();
-    scan_apply<<<(unsigned)nb, kScanThreads, 0, st>>>(in, out, count, n_max, sums);
+    scan_apply<<<grid, kScanThreads, 0, st>>>(in, out, count, n_max, sums);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
