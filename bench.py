@@ -53,7 +53,37 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-gpu", action="store_true", help="skip the reference's own GPU loop")
     ap.add_argument("--cpu-frames", type=int, default=3)
+    ap.add_argument("--profile-step", action="store_true",
+                    help="for ncu: the headline session, two warm steps, then one step with the marching-cubes tile "
+                         "--mc-tile; prints the library kernel launches before that step and in it, and exits")
+    ap.add_argument("--mc-tile", type=int, default=4, help="marching-cubes tile of --profile-step (4: the one the "
+                                                            "autotuner picks on this workload)")
     return ap.parse_args()
+
+
+def profile_step(args):
+    """The headline workload as ncu should see it: reset + frames 0..29 twice to warm up (frame graphs
+    captured), the marching-cubes tile fixed (the autotuner would time tiles under the profiler), then one
+    more step.  Prints "<launches before the step> <launches in the step>" for ncu's -s / -c."""
+    import torch
+    from volumefusion_gb300 import configs
+    from volumefusion_gb300.fusion import FusionSession
+    cfg = configs.nonrigid_capsules_256(n_frames=N_FRAMES)
+    frames = [torch.from_numpy(f.astype(np.int16)).cuda() for f in configs.capsule_frames(cfg)]
+    stream = torch.cuda.Stream()
+    s = FusionSession(cfg, stream=stream)
+    with torch.cuda.stream(stream):
+        for step in range(3):
+            if step == 1:
+                torch.cuda.synchronize()
+                s.set_tile(args.mc_tile)
+            l0 = s.kernel_launches()
+            s.reset()
+            for f in frames:
+                s.process(f)
+            torch.cuda.synchronize()
+    print(l0, s.kernel_launches() - l0, flush=True)
+    s.close()
 
 
 class ClockSampler(threading.Thread):
@@ -331,7 +361,7 @@ def run_reference(args):
 def ncu_traffic(stage):
     """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) of the stage's kernel from
     the committed ncu summary of the same workload, or None."""
-    files = {"marching_cubes": "mc_tma_kernel_capsules256.md"}
+    files = {"marching_cubes": "mc_pipe_kernel_capsules256.md"}
     if stage not in files:
         return None
     path = os.path.join(ROOT, "profiles", files[stage])
@@ -716,6 +746,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_step:
+        return profile_step(args)
     import torch
     from volumefusion_gb300 import configs
     from volumefusion_gb300._lib import FrameStats
