@@ -50,6 +50,15 @@ int afx_version(void);
 /* Last CUDA error seen by the library on this thread (cudaError_t value), 0 if none. */
 int afx_last_cuda_error(void);
 
+/* af::CameraDistortion (include/af/CameraModel.h:21-33), filled from depthDistortion.txt
+ * (af::loadCameraDistortion, src/dataset.cpp:44-79: file order k1 k2 p1 p2 k3 k4 k5 k6). */
+typedef struct afx_camera_distortion {
+    float k1, k2, k3, k4, k5, k6;
+    float codx, cody;
+    float p1, p2;
+    int is_distorted;
+} afx_camera_distortion;
+
 /* ------------------------------------------------------------------------------------
  * Depth pre-processing (src/VertexManipulation.cu, src/BilateralFilter.cu)
  * ------------------------------------------------------------------------------------ */
@@ -342,6 +351,10 @@ typedef struct afx_fusion_params {
                                     AFX_BLEND_DQB (dual-quaternion blending of their rigid parts) for
                                     every warp: canonical points, voxel centres, output mesh.  The
                                     Gauss-Newton Jacobian is the linear blend's in both cases. */
+    afx_camera_distortion distortion;  /* the depth camera's distortion; when is_distorted, every frame
+                                    is undistorted as af::loadProcessFrame does (cv::undistort of the
+                                    metres before the filter, src/VolumeFusion.cu:162-180), through a
+                                    map built once at create (AFX_UNDISTORT_LINEAR) */
 } afx_fusion_params;
 
 #define AFX_PRECISION_FP32 0
@@ -551,6 +564,10 @@ typedef struct afx_rigid_stream_params {
     int bilateral, bilateral_r;
     float sigma_i, sigma_s, bilateral_thr;
     long triangle_capacity;
+    afx_camera_distortion distortion[AFX_MAX_CAMERAS]; /* per camera; when is_distorted, the camera's
+                                                 depth is undistorted as CameraData::processNextFrame does
+                                                 (src/MeshRecontructionStream.cu:94-101): the unfiltered
+                                                 metres remapped INTER_NEAREST replace the filtered frame */
 } afx_rigid_stream_params;
 typedef struct afx_rigid_stream afx_rigid_stream;
 void afx_rigid_stream_default_params(afx_rigid_stream_params* p);
@@ -582,6 +599,60 @@ int afx_tsdf_load(const char* path, float* tsdf, float* weights, long n_voxels);
 int afx_fusion_save_volume(afx_fusion* f, const char* path, void* stream);
 int afx_fusion_load_volume(afx_fusion* f, const char* path, void* stream);
 int afx_fusion_save_mesh_ply(afx_fusion* f, const char* path, void* stream);
+
+/* ------------------------------------------------------------------------------------
+ * Depth ingest: image decoding (host) and camera undistortion (device).
+ *
+ * afx_decode_depth_image: cv::imread(file, IMREAD_ANYDEPTH | IMREAD_ANYCOLOR) of a depth frame
+ *   (src/dataset.cpp:168-189, src/KinectReader.cpp:9-21, src/AzureReader.cpp:10-22) from the file's
+ *   bytes in host memory: greyscale 8- or 16-bit PNG (any filter, Adam7 or not) or TIFF (strips;
+ *   none / LZW / Deflate / PackBits; horizontal predictor), to uint16 millimetres in out[height][width]
+ *   (host).  out = NULL returns the size only.  AFX_ERR_UNSUPPORTED for colour or other depths,
+ *   AFX_ERR_INVALID_ARGUMENT for a corrupt file (bad CRC-32 / Adler-32, truncated data),
+ *   AFX_ERR_CAPACITY when capacity < width * height.  The conversion to metres happens in the frame
+ *   preparation on the device (afx_depth_from_mm, afx_frame_prep).
+ * afx_decode_depth_images: n images decoded on up to `threads` host threads; status[i] per image,
+ *   the first non-zero status returned.  widths / heights may be NULL.
+ * afx_depth_file_name: af::insertIntoPattern (src/dataset.cpp:131-150): the run of all the
+ *   pattern's '*' replaced by the zero-padded index.
+ * afx_read_depth_frame: afx_depth_file_name + read + afx_decode_depth_image.
+ * ------------------------------------------------------------------------------------ */
+int afx_decode_depth_image(const uint8_t* data, size_t len, uint16_t* out, long capacity, int* width, int* height);
+int afx_decode_depth_images(int n, const uint8_t* const* data, const size_t* lens, uint16_t* const* outs,
+                            const long* capacities, int* widths, int* heights, int* status, int threads);
+int afx_depth_file_name(const char* pattern, long index, char* out, size_t capacity);
+int afx_read_depth_frame(const char* pattern, long index, uint16_t* out, long capacity, int* width, int* height);
+
+/* The two undistortions of the reference, both with the intrinsics as new camera matrix and
+ * constant-zero borders:
+ *  AFX_UNDISTORT_LINEAR  cv::undistort of the float depth (af::loadProcessFrame,
+ *                        src/VolumeFusion.cu:162-180): fixed-point maps (1/32 pixel) built in stripes
+ *                        of max(1, 4096 / width) rows, bilinear sampling;
+ *  AFX_UNDISTORT_NEAREST cv::initUndistortRectifyMap(..., CV_32FC1) + cv::remap(INTER_NEAREST)
+ *                        (src/MeshRecontructionStream.cu:94-101, src/PointCloudStream.cu:107-116).
+ * afx_undistort_map writes the per-pixel source map (2 x uint32 per pixel, device; build it once per
+ * camera), afx_undistort_depth applies it to a float image (dst must not alias src). */
+#define AFX_UNDISTORT_LINEAR 0
+#define AFX_UNDISTORT_NEAREST 1
+int afx_undistort_map(uint32_t* map, int width, int height, const float K[9], const afx_camera_distortion* d,
+                      int mode, void* stream);
+int afx_undistort_depth(float* dst, const float* src, int width, int height, const uint32_t* map, int mode,
+                        void* stream);
+
+/* af::create_xy_lookup_table (src/CameraCalibration.cpp:261-295): for every pixel (x, y) the ray
+ * (X/Z, Y/Z) of af::transformation_unproject at unit depth -- Brown-Conrady inverse by the closed-form
+ * first guess and up to 20 Gauss-Newton passes (src/CameraCalibration.cpp:106-218) -- or (0, 0) where
+ * the unprojection is invalid.  intrinsics = the af::CameraIntrinsics fields {cx, cy, fx, fy} as the
+ * caller filled them.  table: 2 floats per pixel, device.  AFX_ERR_INVALID_ARGUMENT unless fx, fy > 0. */
+int afx_xy_lookup_table(float* table, int width, int height, const float intrinsics[4],
+                        const afx_camera_distortion* d, void* stream);
+/* af::transformation_unproject / transformation_project (src/CameraCalibration.cpp:220-259) over n
+ * points (device arrays): pixels (2 floats) + depths -> points (3 floats) and valid flags; points ->
+ * pixels and valid flags. */
+int afx_unproject_points(float* points, int* valid, const float* pixels, const float* depths, long n,
+                         const float intrinsics[4], const afx_camera_distortion* d, void* stream);
+int afx_project_points(float* pixels, int* valid, const float* points, long n, const float intrinsics[4],
+                       const afx_camera_distortion* d, void* stream);
 
 /* Stream-ordered device-to-device copy (helper for bindings that hold raw device views). */
 int afx_copy_device(void* dst, const void* src, size_t bytes, void* stream);

@@ -79,6 +79,14 @@ def lib():
             "vfo_count_collisions": (None, [i32p, f32p, i32p, f32p, f32p, i32p, f32p, f32p]),
             "vfo_integrate_warped": (None, [f32p, f32p, f32p, i32p, i32p, f32p, C.c_int, C.c_int, C.c_float, f32p,
                                             f32p, i32p, f32p, f32p, f32p, C.c_int]),
+            "vfo_undistort_map": (None, [u32p, C.c_int, C.c_int, f32p, f32p, C.c_int]),
+            "vfo_undistort_depth": (None, [f32p, f32p, C.c_int, C.c_int, u32p, C.c_int]),
+            "vfo_xy_lookup_table": (None, [f32p, C.c_int, C.c_int, f32p, f32p]),
+            "vfo_bc_unproject": (None, [f32p, i32p, f32p, f32p, C.c_long, f32p, f32p]),
+            "vfo_bc_project": (None, [f32p, i32p, f32p, C.c_long, f32p, f32p]),
+            "vfo_frame_prep_undistorted": (None, [u16p, C.c_int, C.c_int, f32p, C.c_float, C.c_int, C.c_int,
+                                                  C.c_double, C.c_double, C.c_float, C.c_float, C.c_float, u32p,
+                                                  f32p, f32p, f32p, f32p]),
             "vfo_fusion_create": (C.c_void_p, [C.c_void_p]),
             "vfo_fusion_destroy": (None, [C.c_void_p]),
             "vfo_fusion_process": (C.c_int, [C.c_void_p, u16p]),
@@ -436,6 +444,60 @@ def mc_pointcloud64(tsdf, weights, dims, voxel_size, volume_size, iso=0.0):
     return out[:3 * n].reshape(-1, 3)
 
 
+# ---- depth ingest (OpenCV's undistortions and src/CameraCalibration.cpp, restated) ----
+
+def dist_cv(d):
+    """k1 k2 p1 p2 k3 k4 k5 k6 (OpenCV order) from a dict of coefficients."""
+    return [float(d.get(k, 0.0)) for k in ("k1", "k2", "p1", "p2", "k3", "k4", "k5", "k6")]
+
+
+def dist_bc(d):
+    """k1..k6, codx, cody, p1, p2 (af::CameraDistortion order)."""
+    return np.asarray([float(d.get(k, 0.0)) for k in ("k1", "k2", "k3", "k4", "k5", "k6", "codx", "cody", "p1",
+                                                       "p2")], np.float32)
+
+
+def undistort_map(K, d, width, height, mode):
+    """Per-pixel source map (2 uint32 per pixel) of cv::undistort (mode 0) or of
+    initUndistortRectifyMap(CV_32FC1) + remap(INTER_NEAREST) (mode 1)."""
+    out = np.empty(2 * width * height, np.uint32)
+    lib().vfo_undistort_map(out, width, height, kcol(K), np.asarray(dist_cv(d), np.float32), int(mode))
+    return out
+
+
+def undistort_depth(src, umap, mode):
+    src = np.ascontiguousarray(src, np.float32)
+    h, w = src.shape
+    out = np.empty_like(src)
+    lib().vfo_undistort_depth(out.ravel(), src.ravel(), w, h, np.ascontiguousarray(umap, np.uint32), int(mode))
+    return out
+
+
+def xy_lookup_table(intr, d, width, height):
+    out = np.empty((height, width, 2), np.float32)
+    lib().vfo_xy_lookup_table(out.ravel(), width, height, np.asarray(intr, np.float32), dist_bc(d))
+    return out
+
+
+def bc_unproject(pixels, depths, intr, d):
+    pixels = np.ascontiguousarray(pixels, np.float32)
+    depths = np.ascontiguousarray(depths, np.float32)
+    n = depths.size
+    pts = np.empty((n, 3), np.float32)
+    valid = np.empty(n, np.int32)
+    lib().vfo_bc_unproject(pts.ravel(), valid, pixels.ravel(), depths, n, np.asarray(intr, np.float32), dist_bc(d))
+    return pts, valid
+
+
+def bc_project(points, intr, d, out=None):
+    points = np.ascontiguousarray(points, np.float32)
+    n = points.shape[0]
+    px = np.zeros((n, 2), np.float32) if out is None else np.ascontiguousarray(out, np.float32).copy()
+    valid = np.empty(n, np.int32)
+    lib().vfo_bc_project(px.ravel(), valid, points.ravel(), n, np.asarray(intr, np.float32), dist_bc(d))
+    return px, valid
+
+
 class VfoParams(C.Structure):
     _fields_ = [("width", C.c_int), ("height", C.c_int), ("K", C.c_float * 9), ("dims", C.c_int * 3),
                 ("volume_size", C.c_float * 3), ("delta", C.c_float), ("depth_threshold", C.c_float),
@@ -445,7 +507,8 @@ class VfoParams(C.Structure):
                 ("icp_iterations", C.c_int), ("gn_iterations", C.c_int), ("lambda_depth", C.c_float),
                 ("lambda_reg", C.c_float), ("energy_min_step", C.c_float), ("corr_thresh", C.c_float),
                 ("solver", C.c_int), ("pcg_iterations", C.c_int), ("pcg_tol", C.c_double), ("integrate", C.c_int),
-                ("node_cap", C.c_int), ("mesh_cap", C.c_long), ("precision", C.c_int), ("blend", C.c_int)]
+                ("node_cap", C.c_int), ("mesh_cap", C.c_long), ("precision", C.c_int), ("blend", C.c_int),
+                ("distorted", C.c_int), ("dist_cv", C.c_float * 8)]
 
 
 class Fusion:
@@ -469,6 +532,9 @@ class Fusion:
         p.pcg_tol = float(cfg.get("pcg_tol", 0.0))
         p.precision = {"fp32": 0, "fp16": 1}[cfg.get("precision", "fp32")]
         p.blend = {"lbs": 0, "dqb": 1}[cfg.get("blend", "lbs")]
+        if cfg.get("distortion"):
+            p.distorted = 1
+            p.dist_cv[:] = dist_cv(cfg["distortion"])
         self.cfg = cfg
         self._p = p
         self.h = self._L.vfo_fusion_create(C.byref(p))

@@ -5,6 +5,7 @@
 // reference's TSDFVolume::integrate, MarchingCubes::computeIsoSurface/computePointCloud,
 // af::buildGraph, af::getKnnData, af::filterDisconnected and MotionGraph::warp on
 // in-memory inputs.  Nothing here re-implements the reference; it only marshals arrays.
+#include <af/CameraCalibration.h>
 #include <af/GraphBuilder.h>
 #include <af/MarchingCubes.h>
 #include <af/Mesh.h>
@@ -61,9 +62,75 @@ void filter_impl(const MotionGraph& g, unsigned* idx, float* dist, int n) {
         }
 }
 
+af::CameraModel bc_camera(int width, int height, const float* intr, const float* dist) {
+    af::CameraModel cam;
+    cam.width = (unsigned)width;
+    cam.height = (unsigned)height;
+    cam.intrinsics.cx = intr[0];
+    cam.intrinsics.cy = intr[1];
+    cam.intrinsics.fx = intr[2];
+    cam.intrinsics.fy = intr[3];
+    af::CameraDistortion& d = cam.distortion;
+    d.k1 = dist[0];
+    d.k2 = dist[1];
+    d.k3 = dist[2];
+    d.k4 = dist[3];
+    d.k5 = dist[4];
+    d.k6 = dist[5];
+    d.codx = dist[6];
+    d.cody = dist[7];
+    d.p1 = dist[8];
+    d.p2 = dist[9];
+    d.is_distorted = true;
+    return cam;
+}
+
 }  // namespace
 
+namespace af {
+// defined with external linkage in src/CameraCalibration.cpp:220-259 (no header declares them)
+bool transformation_unproject(const af::CameraModel& camera, const Eigen::Vector2f& point2d, const float depth,
+                              Eigen::Vector3f& point3d, int* valid);
+bool transformation_project(const af::CameraModel& camera, const Eigen::Vector3f& point3d, Eigen::Vector2f& point2d,
+                            int* valid);
+}  // namespace af
+
 extern "C" {
+
+// af::create_xy_lookup_table (src/CameraCalibration.cpp:261-295) into table[height][width][2];
+// intr = {cx, cy, fx, fy}, dist = {k1..k6, codx, cody, p1, p2}.  Returns its result (0/1).
+int ref_xy_lookup_table(float* table, int width, int height, const float* intr, const float* dist) {
+    af::CameraModel cam = bc_camera(width, height, intr, dist);
+    cv::Mat t(height, width, table);
+    return af::create_xy_lookup_table(cam, t) ? 1 : 0;
+}
+
+// af::transformation_unproject over n pixels (2 floats) and depths -> points (3 floats), valid.
+void ref_bc_unproject(float* pts, int* valid, const float* px, const float* depth, long n, const float* intr,
+                      const float* dist) {
+    af::CameraModel cam = bc_camera(1, 1, intr, dist);
+    for (long i = 0; i < n; ++i) {
+        Eigen::Vector3f p(0.f, 0.f, 0.f);
+        int v = 0;
+        af::transformation_unproject(cam, Eigen::Vector2f(px[2 * i], px[2 * i + 1]), depth[i], p, &v);
+        for (int c = 0; c < 3; ++c) pts[3 * i + c] = p(c);
+        valid[i] = v;
+    }
+}
+
+// af::transformation_project over n points -> pixels (left as passed in where the reference leaves them).
+void ref_bc_project(float* px, int* valid, const float* pts, long n, const float* intr, const float* dist) {
+    af::CameraModel cam = bc_camera(1, 1, intr, dist);
+    for (long i = 0; i < n; ++i) {
+        Eigen::Vector2f q(px[2 * i], px[2 * i + 1]);
+        int v = 0;
+        af::transformation_project(cam, Eigen::Vector3f(pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]), q, &v);
+        px[2 * i] = q(0);
+        px[2 * i + 1] = q(1);
+        valid[i] = v;
+    }
+}
+
 
 // TSDFVolume::integrate (src/TSDFVolume.cpp:55-171); pose = Mat4f column-major
 void ref_integrate(float* tsdf, float* weights, const float* depth, int width, int height, const float* K,

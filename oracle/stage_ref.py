@@ -15,6 +15,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 DEST = os.path.join(HERE, "_ref", "src")
 SOURCES = ["src/TSDFVolume.cpp", "src/MarchingCubes.cpp", "src/GraphBuilder.cpp", "src/MotionGraph.cpp", "src/Mesh.cpp",
+           "src/CameraCalibration.cpp",
            # the per-frame loop and its CUDA sources, for the reference-GPU baseline (oracle/ref_gpu/build.py)
            "src/VolumeFusion.cu", "src/TSDFIntegration.cu", "src/TSDFWarp.cu", "src/MarchingCubes.cu",
            "src/ComputeCorrespondence.cu", "src/VertexManipulation.cu", "src/MotionOptimization.cu",

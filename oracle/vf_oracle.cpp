@@ -399,6 +399,283 @@ void vfo_centroid(const real* V, long n, real out[3]) {
     for (int c = 0; c < 3; ++c) out[c] = (real)(((double)s[c] / 4294967296.0) / (double)cnt);
 }
 
+// ---- depth ingest (test infrastructure: restatements of OpenCV 4.x and of src/CameraCalibration.cpp) ----
+
+// cvRound on x86-64: nearest, ties to even; NaN and values outside int32 give INT_MIN.
+static int cv_round_d(double v) {
+    return (v >= -2147483648.5 && v < 2147483647.5) ? (int)std::nearbyint(v) : (int)(-2147483647 - 1);
+}
+static int cv_round_f(float v) {
+    return (v >= -2147483648.f && v < 2147483648.f) ? (int)std::nearbyintf(v) : (int)(-2147483647 - 1);
+}
+static uint32_t pack_sxy(int sx, int sy) { return (uint32_t)(uint16_t)(int16_t)sx | ((uint32_t)(uint16_t)(int16_t)sy << 16); }
+
+void vfo_undistort_map(uint32_t* map, int W, int H, const float K[9], const float k_cv[8], int mode) {
+    // the camera matrix the reference builds (src/VolumeFusion.cu:163-170): fx, fy, cx, cy, K(2,2)
+    double A[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    A[0] = K[0];
+    A[4] = K[4];
+    A[2] = K[6];
+    A[5] = K[7];
+    A[8] = K[8];
+    double k[8];
+    for (int q = 0; q < 8; ++q) k[q] = k_cv[q];
+    // cv::undistort (calib3d/src/undistort.dispatch.cpp): stripes of max(1, 4096 / cols) rows, each
+    // with the new camera matrix's cy lowered by the stripe's first row; the stream readers' single
+    // initUndistortRectifyMap is one stripe
+    int stripe = H;
+    if (mode == 0) {
+        stripe = 4096 / W;
+        if (stripe < 1) stripe = 1;
+        if (stripe > H) stripe = H;
+    }
+    for (int i = 0; i < H; ++i) {
+        const int y0 = (i / stripe) * stripe;
+        double Ar[9];
+        std::memcpy(Ar, A, sizeof(Ar));
+        if (mode == 0) Ar[5] = A[5] - (double)y0;
+        // iR = Ar^-1 (cv::invert, DECOMP_LU, closed form for 3 x 3)
+        const double* m = Ar;
+        double ir[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        const double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                           m[2] * (m[3] * m[7] - m[4] * m[6]);
+        if (det != 0.0) {
+            const double d = 1.0 / det;
+            ir[0] = (m[4] * m[8] - m[5] * m[7]) * d;
+            ir[1] = (m[2] * m[7] - m[1] * m[8]) * d;
+            ir[2] = (m[1] * m[5] - m[2] * m[4]) * d;
+            ir[3] = (m[5] * m[6] - m[3] * m[8]) * d;
+            ir[4] = (m[0] * m[8] - m[2] * m[6]) * d;
+            ir[5] = (m[2] * m[3] - m[0] * m[5]) * d;
+            ir[6] = (m[3] * m[7] - m[4] * m[6]) * d;
+            ir[7] = (m[1] * m[6] - m[0] * m[7]) * d;
+            ir[8] = (m[0] * m[4] - m[1] * m[3]) * d;
+        }
+        // initUndistortRectifyMap's row loop: u0, v0, fx, fy from the original camera matrix
+        const double u0 = A[2], v0 = A[5], fx = A[0], fy = A[4];
+        const double k1 = k[0], k2 = k[1], p1 = k[2], p2 = k[3], k3 = k[4], k4 = k[5], k5 = k[6], k6 = k[7];
+        const int row = mode == 0 ? i - y0 : i;
+        double X = row * ir[1] + ir[2], Y = row * ir[4] + ir[5], Wh = row * ir[7] + ir[8];
+        uint32_t* out = map + 2 * (size_t)i * W;
+        for (int j = 0; j < W; ++j, X += ir[0], Y += ir[3], Wh += ir[6]) {
+            const double w = 1. / Wh, x = X * w, y = Y * w;
+            const double x2 = x * x, y2 = y * y;
+            const double r2 = x2 + y2, _2xy = 2 * x * y;
+            const double kr = (1 + ((k3 * r2 + k2) * r2 + k1) * r2) / (1 + ((k6 * r2 + k5) * r2 + k4) * r2);
+            const double xd = x * kr + p1 * _2xy + p2 * (r2 + 2 * x2);
+            const double yd = y * kr + p1 * (r2 + 2 * y2) + p2 * _2xy;
+            const double u = fx * xd + u0, v = fy * yd + v0;
+            if (mode == 0) {  // CV_16SC2 + CV_16UC1, INTER_BITS = 5
+                const int iu = cv_round_d(u * 32.0), iv = cv_round_d(v * 32.0);
+                out[2 * j] = pack_sxy((int)(int16_t)(iu >> 5), (int)(int16_t)(iv >> 5));
+                out[2 * j + 1] = (uint32_t)((iv & 31) * 32 + (iu & 31));
+            } else {  // CV_32FC1, then remap's saturate_cast<short> of each coordinate
+                const int sx = cv_round_f((float)u), sy = cv_round_f((float)v);
+                out[2 * j] = pack_sxy(std::min(std::max(sx, -32768), 32767), std::min(std::max(sy, -32768), 32767));
+                out[2 * j + 1] = 0;
+            }
+        }
+    }
+}
+
+void vfo_undistort_depth(real* dst, const real* src, int W, int H, const uint32_t* map, int mode) {
+    // cv::remap (imgproc/src/imgwarp.cpp): remapBilinear with the float 32 x 32 weight table, or
+    // remapNearest; BORDER_CONSTANT with value 0
+    for (long p = 0; p < (long)W * H; ++p) {
+        const int sx = (int)(int16_t)(uint16_t)(map[2 * p] & 0xFFFF), sy = (int)(int16_t)(uint16_t)(map[2 * p] >> 16);
+        auto at = [&](int x, int y) -> real {
+            return ((unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H) ? src[(long)y * W + x] : (real)0;
+        };
+        if (mode == 0) {
+            const uint32_t f = map[2 * p + 1];
+            const float ax = (float)(f & 31u) * (1.f / 32.f), ay = (float)((f >> 5) & 31u) * (1.f / 32.f);
+            const float bx = 1.f - ax, by = 1.f - ay;
+            const real w0 = by * bx, w1 = by * ax, w2 = ay * bx, w3 = ay * ax;
+            dst[p] = at(sx, sy) * w0 + at(sx + 1, sy) * w1 + at(sx, sy + 1) * w2 + at(sx + 1, sy + 1) * w3;
+        } else {
+            dst[p] = at(sx, sy);
+        }
+    }
+}
+
+namespace {
+
+struct BcCam {
+    float cx, cy, fx, fy, k1, k2, k3, k4, k5, k6, codx, cody, p1, p2;
+};
+
+BcCam bc_cam(const float intr[4], const float d[10]) {
+    return BcCam{intr[0], intr[1], intr[2], intr[3], d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], d[9]};
+}
+
+// transformation_project_internal (src/CameraCalibration.cpp:9-94); false beyond the radius
+bool bc_project(const BcCam& c, float x, float y, float* uv, float* J) {
+    float xp = x - c.codx, yp = y - c.cody;
+    float xp2 = xp * xp, yp2 = yp * yp, xyp = xp * yp;
+    float rs = xp2 + yp2;
+    float max_r = 1.7f;
+    if (rs > max_r * max_r) return false;
+    float rss = rs * rs, rsc = rss * rs;
+    float a = 1.f + c.k1 * rs + c.k2 * rss + c.k3 * rsc;
+    float b = 1.f + c.k4 * rs + c.k5 * rss + c.k6 * rsc;
+    float bi = b != 0.f ? 1.f / b : 1.f;
+    float d = a * bi;
+    float xp_d = xp * d, yp_d = yp * d;
+    float rs_2xp2 = rs + 2.f * xp2, rs_2yp2 = rs + 2.f * yp2;
+    xp_d += rs_2xp2 * c.p2 + 2.f * xyp * c.p1;
+    yp_d += rs_2yp2 * c.p1 + 2.f * xyp * c.p2;
+    uv[0] = (xp_d + c.codx) * c.fx + c.cx;
+    uv[1] = (yp_d + c.cody) * c.fy + c.cy;
+    if (J) {
+        float dudrs = c.k1 + 2.f * c.k2 * rs + 3.f * c.k3 * rss;
+        float dvdrs = c.k4 + 2.f * c.k5 * rs + 3.f * c.k6 * rss;
+        float bis = bi * bi;
+        float dddrs = (dudrs * b - a * dvdrs) * bis;
+        float dddrs_2 = dddrs * 2.f;
+        float xp_dddrs_2 = xp * dddrs_2;
+        float yp_xp_dddrs_2 = yp * xp_dddrs_2;
+        J[0] = c.fx * (d + xp * xp_dddrs_2 + 6.f * xp * c.p2 + 2.f * yp * c.p1);
+        J[1] = c.fx * (yp_xp_dddrs_2 + 2.f * yp * c.p2 + 2.f * xp * c.p1);
+        J[2] = c.fy * (yp_xp_dddrs_2 + 2.f * xp * c.p1 + 2.f * yp * c.p2);
+        J[3] = c.fy * (d + yp * yp * dddrs_2 + 6.f * yp * c.p1 + 2.f * xp * c.p2);
+    }
+    return true;
+}
+
+// transformation_unproject_internal + transformation_iterative_unproject (src/CameraCalibration.cpp:106-218)
+void bc_unproject(const BcCam& c, float u, float v, float* xy, int* valid) {
+    float xp_d = (u - c.cx) / c.fx - c.codx;
+    float yp_d = (v - c.cy) / c.fy - c.cody;
+    float rs = xp_d * xp_d + yp_d * yp_d;
+    float rss = rs * rs, rsc = rss * rs;
+    float a = 1.f + c.k1 * rs + c.k2 * rss + c.k3 * rsc;
+    float b = 1.f + c.k4 * rs + c.k5 * rss + c.k6 * rsc;
+    float ai = a != 0.f ? 1.f / a : 1.f;
+    float di = ai * b;
+    float x = xp_d * di, y = yp_d * di;
+    float two_xy = 2.f * x * y;
+    float xx = x * x, yy = y * y;
+    x -= (yy + 3.f * xx) * c.p2 + two_xy * c.p1;
+    y -= (xx + 3.f * xx) * c.p1 + two_xy * c.p2;  // (xx + 3 xx), as the reference has it
+    x += c.codx;
+    y += c.cody;
+    *valid = 1;
+    float bx = 0.f, by = 0.f, best = std::numeric_limits<float>::max();
+    for (int pass = 0; pass < 20; ++pass) {
+        float p[2], J[4];
+        if (!bc_project(c, x, y, p, J)) {
+            *valid = 0;
+            xy[0] = x;
+            xy[1] = y;
+            return;
+        }
+        float ex = u - p[0], ey = v - p[1];
+        float err = ex * ex + ey * ey;
+        if (err >= best) {
+            x = bx;
+            y = by;
+            break;
+        }
+        best = err;
+        bx = x;
+        by = y;
+        float det = J[0] * J[3] - J[1] * J[2];
+        float inv = 1.f / det;
+        float i0 = inv * J[3], i3 = inv * J[0], i1 = -inv * J[1], i2 = -inv * J[2];
+        if (pass + 1 == 20 || best < 1e-22f) break;
+        x += i0 * ex + i1 * ey;
+        y += i2 * ex + i3 * ey;
+    }
+    if (best > 1e-6f) *valid = 0;
+    xy[0] = x;
+    xy[1] = y;
+}
+
+}  // namespace
+
+void vfo_xy_lookup_table(float* table, int W, int H, const float intr[4], const float dist[10]) {
+    // create_xy_lookup_table (src/CameraCalibration.cpp:261-295)
+    const BcCam c = bc_cam(intr, dist);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            float xy[2];
+            int valid = 0;
+            bc_unproject(c, (float)x, (float)y, xy, &valid);
+            float* o = table + 2 * ((size_t)y * W + x);
+            o[0] = valid ? xy[0] * 1.f : 0.f;
+            o[1] = valid ? xy[1] * 1.f : 0.f;
+        }
+}
+
+void vfo_bc_unproject(float* pts, int* valid, const float* px, const float* depth, long n, const float intr[4],
+                      const float dist[10]) {
+    // transformation_unproject (src/CameraCalibration.cpp:220-243)
+    const BcCam c = bc_cam(intr, dist);
+    for (long i = 0; i < n; ++i) {
+        const float d = depth[i];
+        if (d == 0.f) {
+            pts[3 * i] = pts[3 * i + 1] = pts[3 * i + 2] = 0.f;
+            valid[i] = 0;
+            continue;
+        }
+        float xy[2];
+        bc_unproject(c, px[2 * i], px[2 * i + 1], xy, &valid[i]);
+        pts[3 * i] = xy[0] * d;
+        pts[3 * i + 1] = xy[1] * d;
+        pts[3 * i + 2] = d;
+    }
+}
+
+void vfo_bc_project(float* px, int* valid, const float* pts, long n, const float intr[4], const float dist[10]) {
+    // transformation_project (src/CameraCalibration.cpp:245-259); beyond the radius the pixel is left as it was
+    const BcCam c = bc_cam(intr, dist);
+    for (long i = 0; i < n; ++i) {
+        const float z = pts[3 * i + 2];
+        if (z <= 0.f) {
+            px[2 * i] = px[2 * i + 1] = 0.f;
+            valid[i] = 0;
+            continue;
+        }
+        float uv[2];
+        if (bc_project(c, pts[3 * i] / z, pts[3 * i + 1] / z, uv, nullptr)) {
+            px[2 * i] = uv[0];
+            px[2 * i + 1] = uv[1];
+            valid[i] = 1;
+        } else {
+            valid[i] = 0;
+        }
+    }
+}
+
+static void frame_prep_from_depth(int width, int height, const real* K, real depth_threshold, int bilateral, int r,
+                                  double sigma_i, double sigma_s, real thr, real angle_lo, real angle_hi, real* depth,
+                                  real* vertices, real* normals, real centroid[3]) {
+    long n = (long)width * height;
+    vfo_filter_depth(depth, n, depth_threshold);
+    if (bilateral) {
+        std::vector<real> tmp(depth, depth + n);
+        vfo_bilateral(depth, tmp.data(), height, width, r, sigma_i, sigma_s, thr);
+    }
+    vfo_depth_to_mesh(vertices, depth, width, height, K);
+    vfo_normals(normals, vertices, height, width, angle_lo, angle_hi);
+    vfo_remove_without_normals(normals, vertices, depth, height, width);
+    vfo_centroid(vertices, n, centroid);
+}
+
+void vfo_frame_prep_undistorted(const uint16_t* mm, int width, int height, const real* K, real depth_threshold,
+                                int bilateral, int r, double sigma_i, double sigma_s, real thr, real angle_lo,
+                                real angle_hi, const uint32_t* map, real* depth, real* vertices, real* normals,
+                                real centroid[3]) {
+    // af::loadProcessFrame with a distorted camera (src/VolumeFusion.cu:160-220): metres, cv::undistort,
+    // then the filter and the rest
+    long n = (long)width * height;
+    std::vector<real> metres(n);
+    vfo_depth_from_mm(mm, n, metres.data());
+    vfo_undistort_depth(depth, metres.data(), width, height, map, 0);
+    frame_prep_from_depth(width, height, K, depth_threshold, bilateral, r, sigma_i, sigma_s, thr, angle_lo, angle_hi,
+                          depth, vertices, normals, centroid);
+}
+
 void vfo_frame_prep(const uint16_t* mm, int width, int height, const real* K, real depth_threshold, int bilateral,
                     int r, double sigma_i, double sigma_s, real thr, real angle_lo, real angle_hi, real* depth,
                     real* vertices, real* normals, real centroid[3]) {
@@ -1207,6 +1484,7 @@ struct vfo_fusion {
     int frame = 0;
     std::vector<real> tsdf, weights;
     std::vector<real> depth, verts, normals;
+    std::vector<uint32_t> umap;  // cv::undistort map of a distorted camera
     real c0[3] = {0, 0, 0};
     int n = 0;
     std::vector<real> nodes_host, nodes_dev, radii, T;
@@ -1235,6 +1513,10 @@ vfo_fusion* vfo_fusion_create(const vfo_params* p) {
     f->nodes_dev.resize(3 * (size_t)p->node_cap);
     f->radii.resize(p->node_cap);
     f->T.resize(16 * (size_t)p->node_cap);
+    if (p->distorted) {
+        f->umap.resize(2 * (size_t)f->P);
+        vfo_undistort_map(f->umap.data(), p->width, p->height, p->K, p->dist_cv, 0);
+    }
     return f;
 }
 
@@ -1245,9 +1527,14 @@ int vfo_fusion_process(vfo_fusion* f, const uint16_t* depth_mm) {
     const vfo_params& p = f->p;
     static const real I3[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     real cen[3];
-    vfo_frame_prep(depth_mm, p.width, p.height, f->K, p.depth_threshold, p.bilateral, p.bilateral_r, p.sigma_i,
-                   p.sigma_s, p.bilateral_thr, p.angle_lo, p.angle_hi, f->depth.data(), f->verts.data(),
-                   f->normals.data(), cen);
+    if (p.distorted)
+        vfo_frame_prep_undistorted(depth_mm, p.width, p.height, f->K, p.depth_threshold, p.bilateral, p.bilateral_r,
+                                   p.sigma_i, p.sigma_s, p.bilateral_thr, p.angle_lo, p.angle_hi, f->umap.data(),
+                                   f->depth.data(), f->verts.data(), f->normals.data(), cen);
+    else
+        vfo_frame_prep(depth_mm, p.width, p.height, f->K, p.depth_threshold, p.bilateral, p.bilateral_r, p.sigma_i,
+                       p.sigma_s, p.bilateral_thr, p.angle_lo, p.angle_hi, f->depth.data(), f->verts.data(),
+                       f->normals.data(), cen);
     if (f->frame == 0) {
         std::memcpy(f->c0, cen, 3 * sizeof(real));
         vfo_integrate_rigid(f->tsdf.data(), f->weights.data(), f->depth.data(), p.width, p.height, p.delta, p.dims,

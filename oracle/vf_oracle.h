@@ -109,6 +109,26 @@ void vfo_integrate_warped(VFO_REAL* tsdf, VFO_REAL* weights, const VFO_REAL* ver
                           const VFO_REAL volume_size[3], const int dims[3], const VFO_REAL Rinv[9], const VFO_REAL t[3],
                           const VFO_REAL K[9], int half);
 
+/* ---- depth ingest: the reference's OpenCV undistortions and its Brown-Conrady unprojection ----
+ * vfo_undistort_map: cv::undistort's fixed-point map (mode 0, stripes of max(1, 4096 / W) rows) or
+ *   cv::initUndistortRectifyMap's float map rounded for INTER_NEAREST (mode 1); 2 words per pixel:
+ *   (int16 sx | int16 sy << 16, sub-pixel index fy * 32 + fx).  K column-major (fx, fy, cx, cy, K(2,2)
+ *   used), k_cv = k1 k2 p1 p2 k3 k4 k5 k6.
+ * vfo_undistort_depth: cv::remap through that map, zero border.
+ * vfo_xy_lookup_table / vfo_bc_unproject / vfo_bc_project: src/CameraCalibration.cpp with
+ *   intr = {cx, cy, fx, fy} (af::CameraIntrinsics) and dist = {k1..k6, codx, cody, p1, p2}. */
+void vfo_undistort_map(uint32_t* map, int width, int height, const float K[9], const float k_cv[8], int mode);
+void vfo_undistort_depth(VFO_REAL* dst, const VFO_REAL* src, int width, int height, const uint32_t* map, int mode);
+void vfo_xy_lookup_table(float* table, int width, int height, const float intr[4], const float dist[10]);
+void vfo_bc_unproject(float* points, int* valid, const float* pixels, const float* depths, long n, const float intr[4],
+                      const float dist[10]);
+void vfo_bc_project(float* pixels, int* valid, const float* points, long n, const float intr[4], const float dist[10]);
+/* vfo_frame_prep with the frame's metres sampled through a mode-0 undistortion map before the filter. */
+void vfo_frame_prep_undistorted(const uint16_t* mm, int width, int height, const VFO_REAL K[9], VFO_REAL depth_threshold,
+                                int bilateral, int r, double sigma_i, double sigma_s, VFO_REAL thr, VFO_REAL angle_lo,
+                                VFO_REAL angle_hi, const uint32_t* map, VFO_REAL* depth, VFO_REAL* vertices,
+                                VFO_REAL* normals, VFO_REAL centroid[3]);
+
 /* ---- whole-frame driver mirroring af::runVolumeFusion's per-frame loop (src/VolumeFusion.cu:343-769) ---- */
 typedef struct vfo_params {
     int width, height;
@@ -133,6 +153,8 @@ typedef struct vfo_params {
     long mesh_cap;
     int precision;    /* 0 = FP32 volume, 1 = FP16 values + integer weights (the precision form) */
     int blend;        /* 0 = linear blend (the reference's), 1 = dual-quaternion blend */
+    int distorted;    /* undistort every frame as af::loadProcessFrame does (cv::undistort, linear) */
+    float dist_cv[8]; /* k1 k2 p1 p2 k3 k4 k5 k6 */
 } vfo_params;
 
 typedef struct vfo_fusion vfo_fusion;

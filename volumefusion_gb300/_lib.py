@@ -21,6 +21,12 @@ class PrepParams(C.Structure):
                 ("sigma_s", f32), ("bilateral_thr", f32), ("excl_angle_lo", f32), ("excl_angle_hi", f32)]
 
 
+class CameraDistortion(C.Structure):
+    """af::CameraDistortion (include/af/CameraModel.h:21-33)."""
+    _fields_ = [("k1", f32), ("k2", f32), ("k3", f32), ("k4", f32), ("k5", f32), ("k6", f32), ("codx", f32),
+                ("cody", f32), ("p1", f32), ("p2", f32), ("is_distorted", i32)]
+
+
 class FusionParams(C.Structure):
     _fields_ = [("width", i32), ("height", i32), ("K", f32 * 9), ("dims", i32 * 3), ("volume_size", f32 * 3),
                 ("delta", f32), ("depth_threshold", f32), ("bilateral", i32), ("bilateral_r", i32), ("sigma_i", f32),
@@ -29,7 +35,7 @@ class FusionParams(C.Structure):
                 ("gn_iterations", i32), ("lambda_depth", f32), ("lambda_reg", f32), ("energy_min_step", f32),
                 ("corr_thresh", f32), ("solver", i32), ("pcg_iterations", i32), ("pcg_tol", f64), ("integrate", i32),
                 ("extract_mesh", i32), ("node_capacity", i32), ("mesh_capacity", i64), ("triangle_capacity", i64),
-                ("precision", i32), ("warp_mesh", i32), ("blend", i32)]
+                ("precision", i32), ("warp_mesh", i32), ("blend", i32), ("distortion", CameraDistortion)]
 
 
 class FrameStats(C.Structure):
@@ -148,6 +154,15 @@ SIGNATURES = {
     "afx_fusion_save_volume": (i32, [vp, C.c_char_p, vp]),
     "afx_fusion_load_volume": (i32, [vp, C.c_char_p, vp]),
     "afx_fusion_save_mesh_ply": (i32, [vp, C.c_char_p, vp]),
+    "afx_decode_depth_image": (i32, [vp, sz, vp, i64, C.POINTER(i32), C.POINTER(i32)]),
+    "afx_decode_depth_images": (i32, [i32, vp, vp, vp, vp, vp, vp, vp, i32]),
+    "afx_depth_file_name": (i32, [C.c_char_p, i64, C.c_char_p, sz]),
+    "afx_read_depth_frame": (i32, [C.c_char_p, i64, vp, i64, C.POINTER(i32), C.POINTER(i32)]),
+    "afx_undistort_map": (i32, [vp, i32, i32, vp, vp, i32, vp]),
+    "afx_undistort_depth": (i32, [vp, vp, i32, i32, vp, i32, vp]),
+    "afx_xy_lookup_table": (i32, [vp, i32, i32, vp, vp, vp]),
+    "afx_unproject_points": (i32, [vp, vp, vp, vp, i64, vp, vp, vp]),
+    "afx_project_points": (i32, [vp, vp, vp, i64, vp, vp, vp]),
     "afx_fusion_set_timing": (i32, [vp, i32]),
     "afx_fusion_stage_times": (i32, [vp, C.POINTER(f64), i32, i32]),
 }
@@ -163,7 +178,7 @@ class RigidStreamParams(C.Structure):
                 ("camera_to_world", (f32 * 16) * MAX_CAMERAS), ("dims", i32 * 3), ("volume_size", f32 * 3),
                 ("delta", f32), ("center", f32 * 3), ("rotation", f32 * 9), ("depth_threshold", f32),
                 ("bilateral", i32), ("bilateral_r", i32), ("sigma_i", f32), ("sigma_s", f32), ("bilateral_thr", f32),
-                ("triangle_capacity", i64)]
+                ("triangle_capacity", i64), ("distortion", CameraDistortion * MAX_CAMERAS)]
 
 
 class AfxError(RuntimeError):

@@ -168,6 +168,7 @@ struct afx_fusion {
     unsigned char* wcount;
     unsigned char* occ;    // per 8^3 brick: 1 once any voxel of it has a weight (marching cubes skips the rest)
     unsigned* mc_tiles;    // marching cubes on the persistent grid: count + occupied tiles
+    uint32_t* umap;        // undistortion map of a distorted camera (null otherwise)
     FrameStats* stats;
     void* ws_sort;
     size_t ws_sort_bytes;
@@ -367,6 +368,7 @@ static void session_layout(const afx_fusion_params& p, afx_fusion* f) {
     add(mesh_knn); add(mesh_knn); add(mesh_knn);
     add(nbricks * 512 * sizeof(WarpedVoxel)); add(nbricks * 512); add(nbricks);
     add(mc_tile_ws_words(f->vol) * 4);
+    add(p.distortion.is_distorted ? Pp * 8 : 0);
     add(sizeof(FrameStats)); add(64);
     add(f->ws_sort_bytes); add(f->ws_graph_bytes); add(f->ws_corr_bytes); add(f->ws_support_bytes); add(f->ws_gn_bytes);
     f->arena_bytes = sz + 4096;
@@ -458,6 +460,7 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     f->wcount = (unsigned char*)take(nbricks * 512);
     f->occ = (unsigned char*)take(nbricks);
     f->mc_tiles = (unsigned*)take(mc_tile_ws_words(f->vol) * 4);
+    f->umap = p.distortion.is_distorted ? (uint32_t*)take(Pp * 8) : nullptr;
     f->stats = (FrameStats*)take(sizeof(FrameStats));
     f->frame_dev = (int*)take(64);
     f->ws_sort = take(f->ws_sort_bytes);
@@ -482,6 +485,8 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->ev_join, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMemsetAsync(f->arena, 0, f->arena_bytes, init);
     int rc = e == cudaSuccess ? afx_fusion_reset(f, init) : note_cuda_error(e);
+    if (!rc && f->umap)  // cv::undistort's map, built once: it depends on the camera only
+        rc = undistort_map_impl(f->umap, p.width, p.height, p.K, &p.distortion, AFX_UNDISTORT_LINEAR, init);
     e = init ? cudaStreamSynchronize(init) : cudaSuccess;
     if (!rc && e != cudaSuccess) rc = note_cuda_error(e);
     if (init) cudaStreamDestroy(init);
@@ -623,7 +628,7 @@ static int enqueue_frame(afx_fusion* f, const uint16_t* depth_mm, cudaStream_t s
     pp.excl_angle_hi = p.excl_angle_hi;
     stage_mark(f, ST_PREP, st);
     rc = frame_prep_impl(depth_mm, p.width, p.height, &pp, f->depth, f->verts, f->normals,
-                         f->frame == 0 ? f->centroid0 : f->centroid, f->acc, f->error, st);
+                         f->frame == 0 ? f->centroid0 : f->centroid, f->acc, f->error, st, f->umap);
     if (rc) return rc;
     if (f->frame == 0) {
         stage_mark(f, ST_INTEGRATE_RIGID, st);

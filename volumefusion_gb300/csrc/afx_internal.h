@@ -24,8 +24,16 @@ int scan_exclusive_dev(const unsigned* in, unsigned* out, const unsigned* count,
                        cudaStream_t st);
 
 // ---- prep (afx_prep.cu) ----
+// undistort_map: a cv::undistort map of the frame (afx_undistort_map, AFX_UNDISTORT_LINEAR) to sample the
+// metres through before the filter, or null.
 int frame_prep_impl(const uint16_t* mm, int width, int height, const afx_prep_params* p, float* depth, float* vertices,
-                    float* normals, float* centroid, unsigned long long* acc, int* error, cudaStream_t st);
+                    float* normals, float* centroid, unsigned long long* acc, int* error, cudaStream_t st,
+                    const uint32_t* undistort_map = nullptr);
+// afx_undistort_map / afx_undistort_depth (afx_undistort.cu)
+int undistort_map_impl(uint32_t* map, int width, int height, const float K[9], const afx_camera_distortion* d, int mode,
+                       cudaStream_t st);
+int undistort_apply_impl(float* dst, const float* src, int width, int height, const uint32_t* map, int mode,
+                         cudaStream_t st);
 
 // ---- integration (afx_integrate.cu) ----
 // occ (optional): one byte per 8^3 brick, set to 1 for every brick where a voxel gets a weight

@@ -12,6 +12,7 @@
 #include "afx_common.cuh"
 #include "afx_host.h"
 #include "afx_tma.h"
+#include "afx_undistort.cuh"
 
 namespace afx {
 
@@ -182,11 +183,17 @@ struct PrepArgs {
     float* normals;
     unsigned long long* acc;  // 3 fixed-point sums + count
     int* error;
+    const uint32_t* umap;     // cv::undistort map (kSrc == kSrcUndistort)
 };
+
+// Where the tile's depth comes from: plain loads of the uint16 frame, one TMA tile copy of it, or
+// bilinear samples of its metres through an undistortion map (cv::undistort before the filter,
+// src/VolumeFusion.cu:162-190).
+constexpr int kSrcLoad = 0, kSrcTma = 1, kSrcUndistort = 2;
 
 AFX_D uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
-template <bool kTma>
+template <int kSrc>
 __global__ void __launch_bounds__(kTW * kTH) prep_kernel(const __grid_constant__ CUtensorMap tmap,
                                                          const uint16_t* __restrict__ mm, PrepArgs A) {
     __shared__ alignas(128) uint16_t raw[kInH * kInW];
@@ -202,7 +209,7 @@ __global__ void __launch_bounds__(kTW * kTH) prep_kernel(const __grid_constant__
     const int inW = kTW + 2 * A.xhalo, inH = kTH + 2 * A.halo;
     const int gx0 = x0 - A.xhalo, gy0 = y0 - A.halo;  // global coordinates of raw[0][0]
 
-    if (kTma) {
+    if (kSrc == kSrcTma) {
         if (tid == 0) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&mbar)));
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -243,15 +250,29 @@ __global__ void __launch_bounds__(kTW * kTH) prep_kernel(const __grid_constant__
             }
             return;
         }
-    } else {
+    } else if (kSrc == kSrcLoad) {
         for (int i = tid; i < inW * inH; i += kTW * kTH) {
             int gx = gx0 + i % inW, gy = gy0 + i / inW;
             raw[i] = (gx >= 0 && gx < W && gy >= 0 && gy < H) ? mm[(long)gy * W + gx] : (uint16_t)0;
         }
     }
-    __syncthreads();
-    // metres + range filter (src/dataset.cpp:188, src/VertexManipulation.cu:6-15)
-    for (int i = tid; i < inW * inH; i += kTW * kTH) dep[i] = filter_value((float)raw[i] * 0.001f, A.depth_threshold);
+    if (kSrc == kSrcUndistort) {
+        // metres (src/dataset.cpp:188), cv::undistort (src/VolumeFusion.cu:179), range filter
+        auto metres = [&](int x, int y) { return (float)mm[(long)y * W + x] * 0.001f; };
+        for (int i = tid; i < inW * inH; i += kTW * kTH) {
+            int gx = gx0 + i % inW, gy = gy0 + i / inW;
+            float v = 0.f;
+            if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+                const long p = (long)gy * W + gx;
+                v = remap_linear_at(A.umap[2 * p], A.umap[2 * p + 1], W, H, metres);
+            }
+            dep[i] = filter_value(v, A.depth_threshold);
+        }
+    } else {
+        __syncthreads();
+        // metres + range filter (src/dataset.cpp:188, src/VertexManipulation.cu:6-15)
+        for (int i = tid; i < inW * inH; i += kTW * kTH) dep[i] = filter_value((float)raw[i] * 0.001f, A.depth_threshold);
+    }
     __syncthreads();
     auto at_dep = [&](int gx, int gy) -> float { return dep[(gy - gy0) * inW + (gx - gx0)]; };
     // bilateral filter on the tile plus a one-pixel ring
@@ -460,7 +481,8 @@ static PrepScratch* prep_scratch() {
 }
 
 int frame_prep_impl(const uint16_t* mm, int width, int height, const afx_prep_params* p, float* depth, float* vertices,
-                    float* normals, float* centroid, unsigned long long* acc, int* error, cudaStream_t st) {
+                    float* normals, float* centroid, unsigned long long* acc, int* error, cudaStream_t st,
+                    const uint32_t* undistort_map) {
     if (!mm || !p || !depth || !vertices || !normals || width < 3 || height < 3) return AFX_ERR_INVALID_ARGUMENT;
     if (p->bilateral && (p->bilateral_r < 0 || p->bilateral_r > kMaxBilateralR)) return AFX_ERR_UNSUPPORTED;
     PrepArgs A;
@@ -481,13 +503,17 @@ int frame_prep_impl(const uint16_t* mm, int width, int height, const afx_prep_pa
     A.normals = normals;
     A.acc = acc;
     A.error = error;
+    A.umap = undistort_map;
     CUtensorMap map;
     std::memset(&map, 0, sizeof(map));
     const int inW = kTW + 2 * A.xhalo, inH = kTH + 2 * A.halo;
-    bool tma = make_u16_tile_map(&map, mm, width, height, inW, inH);
     dim3 grid((width + kTW - 1) / kTW, (height + kTH - 1) / kTH), block(kTW, kTH);
-    if (tma) prep_kernel<true><<<grid, block, 0, st>>>(map, mm, A);
-    else prep_kernel<false><<<grid, block, 0, st>>>(map, mm, A);
+    if (undistort_map)
+        prep_kernel<kSrcUndistort><<<grid, block, 0, st>>>(map, mm, A);
+    else if (make_u16_tile_map(&map, mm, width, height, inW, inH))
+        prep_kernel<kSrcTma><<<grid, block, 0, st>>>(map, mm, A);
+    else
+        prep_kernel<kSrcLoad><<<grid, block, 0, st>>>(map, mm, A);
     AFX_LAUNCH_CHECK();
     if (centroid) {
         centroid_finalize_kernel<<<1, 1, 0, st>>>(acc, centroid);
@@ -580,7 +606,7 @@ int afx_frame_prep(const uint16_t* depth_mm, int width, int height, const afx_pr
     PrepScratch* s = prep_scratch();
     if (!s) return AFX_ERR_NO_MEMORY;
     return frame_prep_impl(depth_mm, width, height, params, depth, vertices, normals, centroid, s->acc, &s->error,
-                           as_stream(stream));
+                           as_stream(stream), nullptr);
 }
 
 }  // extern "C"

@@ -53,7 +53,7 @@ struct Session {
 
 // Field by field (the struct has padding).
 bool params_equal(const afx_fusion_params& a, const afx_fusion_params& b) {
-    static_assert(sizeof(afx_fusion_params) == 208, "afx_fusion_params changed: update params_equal");
+    static_assert(sizeof(afx_fusion_params) == 248, "afx_fusion_params changed: update params_equal");
     bool eq = a.width == b.width && a.height == b.height && a.delta == b.delta &&
               a.depth_threshold == b.depth_threshold && a.bilateral == b.bilateral &&
               a.bilateral_r == b.bilateral_r && a.sigma_i == b.sigma_i && a.sigma_s == b.sigma_s &&
@@ -66,6 +66,11 @@ bool params_equal(const afx_fusion_params& a, const afx_fusion_params& b) {
               a.extract_mesh == b.extract_mesh && a.node_capacity == b.node_capacity &&
               a.mesh_capacity == b.mesh_capacity && a.triangle_capacity == b.triangle_capacity &&
               a.precision == b.precision && a.warp_mesh == b.warp_mesh && a.blend == b.blend;
+    const afx_camera_distortion &da = a.distortion, &db = b.distortion;
+    eq = eq && da.is_distorted == db.is_distorted;
+    if (da.is_distorted)  // the coefficients matter only to a distorted camera
+        eq = eq && da.k1 == db.k1 && da.k2 == db.k2 && da.k3 == db.k3 && da.k4 == db.k4 && da.k5 == db.k5 &&
+             da.k6 == db.k6 && da.codx == db.codx && da.cody == db.cody && da.p1 == db.p1 && da.p2 == db.p2;
     for (int i = 0; i < 9; ++i) eq = eq && a.K[i] == b.K[i];
     for (int i = 0; i < 3; ++i) eq = eq && a.dims[i] == b.dims[i] && a.volume_size[i] == b.volume_size[i];
     return eq;

@@ -58,6 +58,8 @@ struct afx_rigid_stream {
     int* faces;      // [triangle_capacity * 3]
     unsigned* counts;  // faces, vertices
     int* error;
+    float* raw;        // [P], a distorted camera's unfiltered metres
+    uint32_t* umap;    // [n_cameras * P * 2], undistortion maps of the distorted cameras
 };
 
 extern "C" {
@@ -102,7 +104,11 @@ int afx_rigid_stream_create(const afx_rigid_stream_params* params, afx_rigid_str
     s->P = (long)p.width * p.height;
     auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
     const size_t nc = (size_t)p.n_cameras, P = (size_t)s->P, S = (size_t)s->S, T = (size_t)p.triangle_capacity;
-    const size_t sizes[] = {nc * P * 4, P * 4, nc * P * 12, S * 4, S * 4, T * 36, T * 12, 64, 64};
+    bool distorted = false;
+    for (int c = 0; c < p.n_cameras; ++c) distorted = distorted || p.distortion[c].is_distorted;
+    const size_t sizes[] = {nc * P * 4, P * 4, nc * P * 12, S * 4, S * 4, T * 36, T * 12, 64, 64,
+                            distorted ? P * 4 : 0, distorted ? nc * P * 8 : 0};
+    constexpr int kBuffers = (int)(sizeof(sizes) / sizeof(sizes[0]));
     size_t total = 0;
     for (size_t x : sizes) total += al(x);
     cudaError_t e = cudaMalloc(&s->arena, total);
@@ -112,8 +118,8 @@ int afx_rigid_stream_create(const afx_rigid_stream_params* params, afx_rigid_str
         return AFX_ERR_NO_MEMORY;
     }
     char* q = static_cast<char*>(s->arena);
-    void* ptr[9];
-    for (int i = 0; i < 9; ++i) {
+    void* ptr[kBuffers];
+    for (int i = 0; i < kBuffers; ++i) {
         ptr[i] = q;
         q += al(sizes[i]);
     }
@@ -126,7 +132,22 @@ int afx_rigid_stream_create(const afx_rigid_stream_params* params, afx_rigid_str
     s->faces = (int*)ptr[6];
     s->counts = (unsigned*)ptr[7];
     s->error = (int*)ptr[8];
+    s->raw = distorted ? (float*)ptr[9] : nullptr;
+    s->umap = distorted ? (uint32_t*)ptr[10] : nullptr;
     e = cudaMemset(s->arena, 0, total);
+    // each distorted camera's cv::initUndistortRectifyMap(CV_32FC1) map, built once
+    // (src/MeshRecontructionStream.cu:97-98 rebuilds the same map every frame)
+    int map_rc = AFX_OK;
+    for (int c = 0; c < p.n_cameras && e == cudaSuccess && !map_rc; ++c)
+        if (p.distortion[c].is_distorted)
+            map_rc = undistort_map_impl(s->umap + (size_t)c * P * 2, p.width, p.height, p.K[c], &p.distortion[c],
+                                        AFX_UNDISTORT_NEAREST, nullptr);
+    if (e == cudaSuccess && !map_rc) e = cudaStreamSynchronize(nullptr);
+    if (map_rc) {
+        cudaFree(s->arena);
+        delete s;
+        return map_rc;
+    }
     if (e != cudaSuccess) {
         cudaFree(s->arena);
         delete s;
@@ -154,8 +175,17 @@ int afx_rigid_stream_process(afx_rigid_stream* s, const uint16_t* const* depth_m
     for (int c = 0; c < p.n_cameras; ++c) {
         float* d = s->depth + c * P;
         float* in = p.bilateral ? s->scratch : d;
-        int rc = afx_depth_from_mm(in, depth_mm[c], P, st);
-        if (!rc) rc = afx_filter_depth(in, P, p.depth_threshold, st);
+        int rc;
+        if (p.distortion[c].is_distorted) {
+            // the filtered device frame is overwritten by the host frame's undistortion: the unfiltered
+            // metres remapped (src/MeshRecontructionStream.cu:91-101)
+            rc = afx_depth_from_mm(s->raw, depth_mm[c], P, st);
+            if (!rc) rc = undistort_apply_impl(in, s->raw, p.width, p.height, s->umap + (size_t)c * P * 2,
+                                               AFX_UNDISTORT_NEAREST, st);
+        } else {
+            rc = afx_depth_from_mm(in, depth_mm[c], P, st);
+            if (!rc) rc = afx_filter_depth(in, P, p.depth_threshold, st);
+        }
         if (!rc && p.bilateral)
             rc = afx_bilateral_filter(d, in, p.height, p.width, p.bilateral_r, p.sigma_i, p.sigma_s, p.bilateral_thr, st);
         float* cloud = s->cloud + 3 * c * P;

@@ -37,6 +37,9 @@ def params_from_config(cfg, extract_mesh=True, triangle_capacity=None):
     p.precision = {"fp32": 0, "fp16": 1}[cfg.get("precision", "fp32")]
     p.warp_mesh = int(bool(cfg.get("warp_mesh", False)))
     p.blend = {"lbs": 0, "dqb": 1}[cfg.get("blend", "lbs")]
+    if cfg.get("distortion"):
+        from .ingest import distortion
+        p.distortion = distortion(cfg["distortion"])
     return p
 
 

@@ -17,9 +17,10 @@ def _colmajor(m):
 class RigidStream:
     def __init__(self, Ks, camera_to_world, width, height, dims, volume_size, delta, center, rotation,
                  depth_threshold=1.2, bilateral=True, bilateral_r=2, sigma_i=0.03, sigma_s=2.0, bilateral_thr=0.09,
-                 triangle_capacity=4_000_000, stream=None):
+                 triangle_capacity=4_000_000, distortions=None, stream=None):
         """Ks: per-camera 3x3 intrinsics; camera_to_world: per-camera 4x4 (inverse of world2camera);
-        center, rotation: the volume pose (settings.tsdfCenter and the rotation settings.tsdfRotation gives)."""
+        center, rotation: the volume pose (settings.tsdfCenter and the rotation settings.tsdfRotation gives);
+        distortions: per camera None or the distortion coefficients (dict of k1..k6, p1, p2)."""
         n = len(Ks)
         assert 1 <= n <= MAX_CAMERAS and len(camera_to_world) == n
         p = RigidStreamParams()
@@ -37,6 +38,11 @@ class RigidStream:
         p.bilateral, p.bilateral_r = int(bool(bilateral)), int(bilateral_r)
         p.sigma_i, p.sigma_s, p.bilateral_thr = float(sigma_i), float(sigma_s), float(bilateral_thr)
         p.triangle_capacity = int(triangle_capacity)
+        if distortions:
+            from .ingest import distortion
+            for c, d in enumerate(distortions):
+                if d:
+                    p.distortion[c] = distortion(d)
         h = C.c_void_p()
         check(lib().afx_rigid_stream_create(C.byref(p), C.byref(h)), "afx_rigid_stream_create")
         self.h, self.params, self.stream, self.n = h, p, stream, n
