@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-rigid-stream", action="store_true")
     ap.add_argument("--no-served", action="store_true")
+    ap.add_argument("--no-ingest", action="store_true")
     ap.add_argument("--served-streams", type=int, default=64)
     ap.add_argument("--served-seconds", type=float, default=4.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -521,6 +522,177 @@ def rigid_stream_arm(args, stream, barrier, reduce_max, world, hbm):
                                   "note": "write-only: 8 B per voxel; outputs (512 MB) larger than L2"}}
 
 
+def encode_depth_png(img, level=1):
+    """16-bit greyscale PNG of a depth frame the way libpng writes it by default: per scanline the
+    filter whose bytes have the smallest sum of absolute values (as signed bytes), zlib at `level`
+    (cv::imwrite's default PNG compression is 1).  Synthetic input for the ingest measurement."""
+    import struct
+    import zlib
+    x = np.ascontiguousarray(img.astype(">u2")).view(np.uint8).reshape(img.shape[0], -1).astype(np.int16)
+    a = np.zeros_like(x)
+    a[:, 2:] = x[:, :-2]
+    b = np.zeros_like(x)
+    b[1:] = x[:-1]
+    c = np.zeros_like(x)
+    c[1:, 2:] = x[:-1, :-2]
+    p = a + b - c
+    pa, pb, pc = np.abs(p - a), np.abs(p - b), np.abs(p - c)
+    paeth = np.where((pa <= pb) & (pa <= pc), a, np.where(pb <= pc, b, c))
+    cand = np.stack([x, x - a, x - b, x - (a + b) // 2, x - paeth]) & 0xFF
+    cost = np.minimum(cand, 256 - cand).sum(axis=2)
+    pick = cost.argmin(axis=0)
+    rows = cand[pick, np.arange(x.shape[0])].astype(np.uint8)
+    raw = np.concatenate([pick.astype(np.uint8)[:, None], rows], axis=1).tobytes()
+
+    def chunk(kind, data):
+        return struct.pack(">I", len(data)) + kind + data + struct.pack(">I", zlib.crc32(kind + data) & 0xFFFFFFFF)
+
+    h, w = img.shape
+    return (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 16, 0, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(raw, level)) + chunk(b"IEND", b""))
+
+
+# A depth camera's distortion for the ingest measurement (rational model, as depthDistortion.txt holds it)
+INGEST_DISTORTION = dict(k1=0.45, k2=-0.05, p1=4e-5, p2=-6e-5, k3=0.003, k4=0.78, k5=0.01, k6=0.0)
+
+
+def ingest_arm(args, cfg, frames_np, stream, barrier):
+    """Depth ingest on the headline frames: host decoding of their PNG files (one thread and all host
+    threads), the cost of undistorting every frame inside the session (cv::undistort before the
+    filter; the undistorted session fuses the same scene seen through a lens with INGEST_DISTORTION),
+    and frames/s from PNG bytes in host memory through decode + fusion."""
+    import concurrent.futures as cf
+    import torch
+    from volumefusion_gb300 import configs, ingest
+    from volumefusion_gb300.fusion import FusionSession
+    clip = max(1, min(args.clip, N_FRAMES))
+    blobs = [encode_depth_png(f) for f in frames_np[:clip]]
+    raw_bytes = int(frames_np[0].nbytes)
+    # one thread
+    for b in blobs[:3]:
+        ingest.decode_depth(b)
+    t0 = time.perf_counter()
+    reps = 3
+    for _ in range(reps):
+        for b in blobs:
+            ingest.decode_depth(b)
+    one = reps * len(blobs) / (time.perf_counter() - t0)
+    # every host thread, batches of the sequence
+    threads = os.cpu_count() or 1
+    outs = [np.empty(frames_np[0].shape, np.uint16) for _ in blobs]
+    batch = blobs * 4
+    outs4 = outs * 4
+    ingest.decode_depth_many(batch, threads=threads, outs=outs4)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ingest.decode_depth_many(batch, threads=threads, outs=outs4)
+    many = reps * len(batch) / (time.perf_counter() - t0)
+    assert all(np.array_equal(o, f) for o, f in zip(outs, frames_np[:clip]))
+    res = {"workload": "the %d headline frames (640x576 uint16) as 16-bit PNG, libpng's default per-row filter "
+                       "choice, zlib level 1; %.0f kB per file" % (clip, np.mean([len(b) for b in blobs]) / 1e3),
+           "decode_one_thread": {"frames_per_s": one, "mb_per_s": one * raw_bytes / 1e6},
+           "decode_all_threads": {"frames_per_s": many, "threads": threads, "mb_per_s": many * raw_bytes / 1e6}}
+    # undistortion inside the session: device-resident frames, with and without a distorted camera
+    dcfg = dict(cfg, distortion=INGEST_DISTORTION)
+    seq = {"plain": frames_np[:clip], "undistorted": configs.capsule_frames(dcfg)[:clip]}
+    per = {}
+    for name, c in (("plain", cfg), ("undistorted", dcfg)):
+        frames_dev = [torch.from_numpy(f.astype(np.int16)).cuda() for f in seq[name]]
+        t_create = time.perf_counter()
+        s = FusionSession(c, stream=stream)
+        create_ms = 1000 * (time.perf_counter() - t_create)
+        with torch.cuda.stream(stream):
+            for _ in range(2):
+                s.reset()
+                for f in frames_dev:
+                    s.process(f)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps = max(1, min(3, args.steps))
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            for _ in range(steps):
+                s.reset()
+                for f in frames_dev:
+                    s.process(f)
+            e1.record(stream)
+        barrier()
+        s.set_timing(True)
+        s.stage_times(reset=True)
+        with torch.cuda.stream(stream):
+            s.reset()
+            for f in frames_dev:
+                s.process(f)
+        barrier()
+        stages = {k: v / clip for k, v in s.stage_times(reset=True).items()}
+        s.set_timing(False)
+        st = s.stats(check_errors=False)
+        per[name] = {"frames_per_s": steps * clip / (e0.elapsed_time(e1) / 1000.0),
+                     "prep_ms_per_frame": stages.get("prep", 0.0), "stage_ms_per_frame": stages,
+                     "create_ms": create_ms, "error": st["error"],
+                     "last_frame": {k: st[k] for k in ("n_nodes", "mesh_points", "correspondences")}}
+        s.close()
+    res["session"] = per
+    # the stand-alone undistortion kernel on one frame (map built once), both modes
+    K = np.asarray(cfg["K"], np.float32)
+    src = torch.from_numpy(frames_np[1].astype(np.float32) * np.float32(0.001)).cuda()
+    H, W = frames_np[0].shape
+    kern = {}
+    for mode, name in ((ingest.LINEAR, "linear"), (ingest.NEAREST, "nearest")):
+        u = ingest.Undistorter(K, INGEST_DISTORTION, W, H, mode=mode)
+        out = torch.empty_like(src)
+        for _ in range(10):
+            u(src, out=out)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n = 200
+        cur = torch.cuda.current_stream()
+        e0.record(cur)
+        for _ in range(n):
+            u(src, out=out)
+        e1.record(cur)
+        torch.cuda.synchronize()
+        us = 1000 * e0.elapsed_time(e1) / n
+        kern[name] = {"us_per_launch": us, "algorithmic_bytes": W * H * 16,
+                      "achieved_gbs": W * H * 16 / (us * 1e-6) / 1e9}
+    res["undistort_kernel"] = kern
+    # PNG bytes in host memory -> decode on a thread pool into pinned buffers -> the session (e2e)
+    ring = 8
+    pinned = [torch.empty(frames_np[0].shape, dtype=torch.int16).pin_memory() for _ in range(ring)]
+    views = [p.numpy().view(np.uint16) for p in pinned]
+    s = FusionSession(cfg, stream=stream)
+    pool = cf.ThreadPoolExecutor(max_workers=min(threads, ring))
+
+    def decode_into(i):
+        ingest.decode_depth_many([blobs[i % clip]], threads=1, outs=[views[i % ring]])
+        return i
+
+    def run(steps):
+        total = steps * clip
+        futs = {i: pool.submit(decode_into, i) for i in range(min(ring - 1, total))}
+        for i in range(total):
+            if i % clip == 0:
+                s.reset()
+            futs.pop(i).result()
+            s.process_host_ptr(pinned[i % ring].data_ptr())
+            s.stats(check_errors=False)
+            j = i + ring - 1
+            if j < total:
+                futs[j] = pool.submit(decode_into, j)
+        return total
+
+    run(1)
+    barrier()
+    t0 = time.perf_counter()
+    n = run(max(1, min(3, args.steps)))
+    barrier()
+    res["e2e_from_png"] = {"frames_per_s": n / (time.perf_counter() - t0), "decode_threads": min(threads, ring),
+                           "note": "PNG bytes in host memory decoded ahead of the session into pinned buffers, each "
+                                   "frame then copied in by afx_fusion_process_host and its statistics read back"}
+    pool.shutdown()
+    s.close()
+    return res
+
+
 def batched_arm(args, stream, barrier, reduce_max, world):
     """16 sessions of uneven size (the config-4 mix: volumes 128^3-384^3, 320x288 or 640x576,
     sphere / torus / capsule) fusing 30-frame sequences: one afx_batch_process per frame of all
@@ -922,6 +1094,10 @@ def main():
     if not args.no_served:
         served = served_arm(args, rank)
 
+    ingest_res = None
+    if not args.no_ingest and rank == 0:
+        ingest_res = ingest_arm(args, cfg, frames_np, stream, barrier)
+
     # ---- roofline of the dominant stage ----
     per_frame = {k: v / frames for k, v in stage_ms.items()}
     dom = max(per_frame, key=per_frame.get)
@@ -993,6 +1169,7 @@ def main():
             "rigid_stream": rigid,
             "rigid_integration": rigid_int,
             "served": served,
+            "ingest": ingest_res,
             "reference_gpu": ref_gpu,
             "roofline": roof,
             "cpu_baseline": cpu,

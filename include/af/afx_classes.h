@@ -8,6 +8,7 @@
  *   TSDFVolume                            include/af/TSDFVolume.h:10-113, src/TSDFVolume.cpp
  *   GaussNewtonSystem                     the Gauss-Newton step of src/VolumeFusion.cu:454-691
  *   the run* operators                    af/afx_shims.h
+ *   depth ingest (loadDepthFrame, DepthUndistorter, create_xy_lookup_table, ...)  af/afx_ingest.h
  *
  * Every computation runs on the GPU through the afx_* entry points; calls block until the GPU
  * work has finished and throw std::runtime_error on failure.  The reference's MotionGraph,
@@ -20,6 +21,7 @@
 #include <string>
 #include <vector>
 
+#include "afx_ingest.h"
 #include "afx_motion_graph.h"
 
 namespace af {

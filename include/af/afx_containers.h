@@ -3,7 +3,7 @@
  *
  *   DeviceBuffer, DeviceBufferCounted     include/af/DeviceBuffer.cuh:36-115
  *   DeviceImage, DeviceDepthImage         include/af/DeviceImage.cuh:12-68
- *   CameraModel                           include/af/CameraModel.h (the fields the path uses)
+ *   CameraIntrinsics, CameraDistortion, CameraModel   include/af/CameraModel.h:14-44
  *   DeviceKnn, DeviceKnnWeighted          include/af/DataTypes.cuh:9-62
  *   DeviceMotionGraph                     include/af/DeviceMotionGraph.cuh:10-33
  *   Settings                              include/af/Settings.h:9-47, defaults src/Settings.cpp:8-41
@@ -184,10 +184,33 @@ private:
     DeviceArray<unsigned int> _size_d;
 };
 
-// ---- include/af/CameraModel.h (the fields the fusion path reads) ----
+// ---- include/af/CameraModel.h:14-44 ----
+struct CameraIntrinsics {
+    float cx{0.f};
+    float cy{0.f};
+    float fx{0.f};
+    float fy{0.f};
+};
+
+struct CameraDistortion {
+    float k1{0.f};
+    float k2{0.f};
+    float k3{0.f};
+    float k4{0.f};
+    float k5{0.f};
+    float k6{0.f};
+    float codx{0.f};
+    float cody{0.f};
+    float p1{0.f};
+    float p2{0.f};
+    bool is_distorted{false};
+};
+
 struct CameraModel {
     unsigned int width{0};
     unsigned int height{0};
+    CameraIntrinsics intrinsics;
+    CameraDistortion distortion;
     Mat3f depthIntrinsics = Mat3f::Identity();
     Mat4f transfW2C = Mat4f::Identity();
 };

@@ -2,7 +2,9 @@
 // reference's own code calls it: DeviceTsdf -> extractPointCloud -> MotionGraph / buildGraph /
 // getKnnData / filterDisconnected -> WarpField (spreadMotionGraph, weighted KNN, warp) ->
 // runCorrespondencePairsKernel -> GaussNewtonSystem -> runUpdateTransformsKernel, plus TSDFVolume
-// integrate / save / load.  It reads one pair of prepared frames from <in_dir> and writes every
+// integrate / save / load, and the depth-ingest functions (loadDepthFrame, loadIntrinsics,
+// loadCameraDistortion, DepthUndistorter, create_xy_lookup_table).  It reads one pair of prepared
+// frames (and a PNG frame with its calibration files) from <in_dir> and writes every
 // intermediate result to <out_dir> as raw arrays; tests/test_cpp_surface_gpu.py compares them
 // with the CPU oracle.  Built with AFX_TEST_WITH_EIGEN, the value types are Eigen's.
 #ifdef AFX_TEST_WITH_EIGEN
@@ -215,9 +217,35 @@ int run() {
     af::runFilterDepthKernel(f0.get(), (unsigned)P, 0.9f, 0.0f);
     write_raw("filtered.bin", download(f0.get(), P));
 
+    // 9. depth ingest: af::loadDepthFrame of a 16-bit PNG by pattern, the calibration files,
+    // cv::undistort on the device, and create_xy_lookup_table
+    af::DeviceDepthImage frame(camera);
+    af::loadDepthFrame(g_in + "/frame-******.depth.png", 3, frame);
+    write_raw("ingest_depth.bin", download(frame.dataPtr(), frame.size()));
+    af::Mat3f Kf;
+    af::loadIntrinsics(g_in + "/depthIntrinsics.txt", Kf);
+    af::CameraDistortion dist;
+    const bool has_dist = af::loadCameraDistortion(g_in + "/depthDistortion.txt", dist);
+    af::DepthUndistorter undistort(Kf, dist, (int)frame.width(), (int)frame.height());
+    undistort.apply(frame);
+    write_raw("ingest_undistorted.bin", download(frame.dataPtr(), frame.size()));
+    af::CameraModel lens;
+    lens.width = (unsigned)frame.width();
+    lens.height = (unsigned)frame.height();
+    lens.intrinsics.cx = Kf(0, 2);
+    lens.intrinsics.cy = Kf(1, 2);
+    lens.intrinsics.fx = Kf(0, 0);
+    lens.intrinsics.fy = Kf(1, 1);
+    lens.distortion = dist;
+    af::DeviceBuffer<af::Vec2f> table(1);
+    const bool table_ok = af::create_xy_lookup_table(lens, table);
+    write_raw("ingest_xy.bin", download(table.bufferPtr(), table.size()));
+
     std::printf("{\"points\": %zu, \"nodes\": %zu, \"field_nodes\": %zu, \"correspondences\": %zu, "
-                "\"volume_roundtrip\": %s}\n",
-                m, n, nf, nc, same ? "true" : "false");
+                "\"volume_roundtrip\": %s, \"ingest\": [%d, %d, %s, %s, \"%s\"]}\n",
+                m, n, nf, nc, same ? "true" : "false", (int)frame.width(), (int)frame.height(),
+                has_dist ? "true" : "false", table_ok ? "true" : "false",
+                af::insertIntoPattern("frame-******.depth.png", 42).c_str());
     return 0;
 }
 

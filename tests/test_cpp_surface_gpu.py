@@ -18,6 +18,10 @@ from oracle import pyoracle as O
 pytestmark = pytest.mark.gpu
 
 
+# depthDistortion.txt order: k1 k2 p1 p2 k3 k4 k5 k6
+INGEST_DIST = (-0.08, 0.02, 4e-4, -3e-4, 0.001, 0.0, 0.0, 0.0)
+
+
 @pytest.fixture(scope="module")
 def run(tmp_path_factory):
     pytest.importorskip("torch")
@@ -48,6 +52,13 @@ def run(tmp_path_factory):
     meta.tofile(inp / "meta.bin")
     for name, a in (("depth0", d0), ("depth1", d1), ("verts1", v1), ("normals1", n1)):
         np.ascontiguousarray(a, np.float32).tofile(inp / (name + ".bin"))
+    # depth ingest inputs: frame 3 as a 16-bit PNG and the two calibration files
+    import _depth_codecs
+    mm3, _ = synth.capsule_pair_frame(16, **cam)
+    (inp / "frame-000003.depth.png").write_bytes(_depth_codecs.png(mm3, 16, -1))
+    (inp / "depthIntrinsics.txt").write_text("%r 0 %r\n0 %r %r\n0 0 1\n" % (float(K[0, 0]), float(K[0, 2]),
+                                                                           float(K[1, 1]), float(K[1, 2])))
+    (inp / "depthDistortion.txt").write_text(" ".join(repr(v) for v in INGEST_DIST))
     p = subprocess.run([exe, str(inp), str(out)], capture_output=True, text=True, timeout=300)
     assert p.returncode == 0, p.stdout + p.stderr
     stats = json.loads(p.stdout.strip().splitlines()[-1])
@@ -57,7 +68,7 @@ def run(tmp_path_factory):
         return a.reshape(-1, cols) if cols else a
 
     return dict(cfg=cfg, K=K, d0=d0, d1=d1, v1=v1, n1=n1, c=c, dims=dims, size=size, vs=size / dims.astype(np.float32),
-                stats=stats, load=load, out=out)
+                stats=stats, load=load, out=out, mm3=mm3)
 
 
 def test_volume_and_point_cloud(run):
@@ -138,3 +149,20 @@ def test_correspondences_and_gauss_newton(run):
     x_o, _ = O.pcg(A, b, 10)
     assert np.linalg.norm(x - x_o) <= 3e-2 * np.linalg.norm(x_o)
     assert np.array_equal(L("transforms_updated", cols=16), O.update_transforms(Tm, x))
+
+
+def test_depth_ingest(run):
+    """loadDepthFrame (PNG by pattern -> metres), the calibration files, cv::undistort on the device
+    and create_xy_lookup_table, from the C++ caller, against the oracle."""
+    w, h, has_dist, table_ok, name = run["stats"]["ingest"]
+    assert (w, h) == (run["cfg"]["width"], run["cfg"]["height"]) and has_dist and table_ok
+    assert name == "frame-000042.depth.png"
+    K = np.asarray(run["K"], np.float32)
+    metres = O.depth_from_mm(run["mm3"])
+    assert np.array_equal(run["load"]("ingest_depth"), metres.ravel())
+    d = dict(zip(("k1", "k2", "p1", "p2", "k3", "k4", "k5", "k6"), INGEST_DIST))
+    d = {k: float(np.float32(v)) for k, v in d.items()}
+    umap = O.undistort_map(K, d, w, h, 0)
+    assert np.array_equal(run["load"]("ingest_undistorted"), O.undistort_depth(metres, umap, 0).ravel())
+    intr = np.array([K[0, 2], K[1, 2], K[0, 0], K[1, 1]], np.float32)
+    assert np.array_equal(run["load"]("ingest_xy").reshape(h, w, 2), O.xy_lookup_table(intr, d, w, h))

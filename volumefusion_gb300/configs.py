@@ -73,7 +73,8 @@ def capsule_frames(cfg, frames=None):
     frames = range(n) if frames is None else frames
     return [synth.capsule_pair_frame(f, n_frames=n, width=cfg["width"], height=cfg["height"],
                                      fx=float(cfg["K"][0, 0]), fy=float(cfg["K"][1, 1]),
-                                     cx=float(cfg["K"][0, 2]), cy=float(cfg["K"][1, 2]))[0] for f in frames]
+                                     cx=float(cfg["K"][0, 2]), cy=float(cfg["K"][1, 2]),
+                                     distortion=cfg.get("distortion"))[0] for f in frames]
 
 
 def small_nonrigid(n_frames=6, dims=(64, 64, 64), voxel=0.008, width=160, height=144):

@@ -48,6 +48,24 @@ def _rays(width, height, K):
     return np.stack([dx, dy, np.ones_like(dx)], axis=-1)
 
 
+def _distorted_rays(width, height, K, dist):
+    """Rays of a camera whose lens follows OpenCV's rational + tangential model (k1..k6, p1, p2): pixel
+    (u, v) sees the normalised point (x, y) that the model maps to ((u - cx) / fx, (v - cy) / fy),
+    found by the fixed-point iteration cv::undistortPoints uses (40 passes in binary64)."""
+    g = {k: float(dist.get(k, 0.0)) for k in ("k1", "k2", "k3", "k4", "k5", "k6", "p1", "p2")}
+    u, v = np.meshgrid(np.arange(width, dtype=np.float64), np.arange(height, dtype=np.float64))
+    xd = (u - K[0, 2]) / K[0, 0]
+    yd = (v - K[1, 2]) / K[1, 1]
+    x, y = xd.copy(), yd.copy()
+    for _ in range(40):
+        r2 = x * x + y * y
+        kr = (1 + ((g["k3"] * r2 + g["k2"]) * r2 + g["k1"]) * r2) / (1 + ((g["k6"] * r2 + g["k5"]) * r2 + g["k4"]) * r2)
+        tx = 2 * g["p1"] * x * y + g["p2"] * (r2 + 2 * x * x)
+        ty = g["p1"] * (r2 + 2 * y * y) + 2 * g["p2"] * x * y
+        x, y = (xd - tx) / kr, (yd - ty) / kr
+    return np.stack([x, y, np.ones_like(x)], axis=-1)
+
+
 def _hit_sphere(d, c, r):
     dd = np.einsum("...i,...i->...", d, d)
     dc = d @ c
@@ -107,12 +125,14 @@ def sphere_frame(width=320, height=288, fx=252.0, fy=252.0, cx=160.0, cy=144.0, 
 
 
 def capsule_pair_frame(frame, n_frames=30, width=640, height=576, fx=504.0, fy=504.0, cx=320.0, cy=288.0,
-                       radius=0.060, length=0.300, joint=(0.0, 0.0, 0.800), max_bend_deg=45.0, seed=0):
+                       radius=0.060, length=0.300, joint=(0.0, 0.0, 0.800), max_bend_deg=45.0, seed=0,
+                       distortion=None):
     """Frame `frame` of the articulated capsule pair: two capsules of the given radius and length
     meeting at `joint`; the second one bends linearly from 0 to max_bend_deg about the camera y
-    axis (its free end swings toward the camera) over n_frames frames."""
+    axis (its free end swings toward the camera) over n_frames frames.  With `distortion` (OpenCV
+    coefficients) the frame is what a camera with that lens sees."""
     K = intrinsics(fx, fy, cx, cy)
-    d = _rays(width, height, K)
+    d = _distorted_rays(width, height, K, distortion) if distortion else _rays(width, height, K)
     j = np.asarray(joint, dtype=np.float64)
     theta = math.radians(max_bend_deg) * (frame / max(n_frames - 1, 1))
     a_end = j + length * np.array([-1.0, 0.0, 0.0])
