@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--no-rigid-stream", action="store_true")
     ap.add_argument("--no-served", action="store_true")
     ap.add_argument("--no-ingest", action="store_true")
+    ap.add_argument("--profile-ingest", action="store_true",
+                    help="run the depth-ingest kernels once at the headline size (for an ncu capture)")
     ap.add_argument("--served-streams", type=int, default=64)
     ap.add_argument("--served-seconds", type=float, default=4.0)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -84,6 +86,29 @@ def profile_step(args):
                 s.process(f)
             torch.cuda.synchronize()
     print(l0, s.kernel_launches() - l0, flush=True)
+    s.close()
+
+
+def profile_ingest(args):
+    """The depth-ingest kernels as ncu should see them, at the headline size: a session with a distorted
+    camera (map built at create) over frames 0..3 of the sequence seen through that lens (frame
+    preparation samples through the cv::undistort map), then the stand-alone remap in both modes."""
+    import torch
+    from volumefusion_gb300 import configs, ingest
+    from volumefusion_gb300.fusion import FusionSession
+    cfg = dict(configs.nonrigid_capsules_256(n_frames=N_FRAMES), distortion=INGEST_DISTORTION)
+    frames = [torch.from_numpy(f.astype(np.int16)).cuda() for f in configs.capsule_frames(cfg, frames=range(4))]
+    s = FusionSession(cfg)
+    for f in frames:
+        s.process(f)
+    torch.cuda.synchronize()
+    K = np.asarray(cfg["K"], np.float32)
+    src = frames[1].float() * 0.001
+    for mode in (ingest.LINEAR, ingest.NEAREST):
+        u = ingest.Undistorter(K, INGEST_DISTORTION, cfg["width"], cfg["height"], mode=mode)
+        u(src)
+    torch.cuda.synchronize()
+    print("ok", s.stats()["error"], flush=True)
     s.close()
 
 
@@ -920,6 +945,8 @@ def main():
         return run_reference(args)
     if args.profile_step:
         return profile_step(args)
+    if args.profile_ingest:
+        return profile_ingest(args)
     import torch
     from volumefusion_gb300 import configs
     from volumefusion_gb300._lib import FrameStats

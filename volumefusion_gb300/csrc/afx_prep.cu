@@ -317,9 +317,11 @@ __global__ void __launch_bounds__(kTW * kTH) prep_kernel(const __grid_constant__
         float* no = A.normals + 3 * p;
         vo[0] = v[0]; vo[1] = v[1]; vo[2] = v[2];
         no[0] = n[0]; no[1] = n[1]; no[2] = n[2];
-        s0 = __double2ll_rn((double)v[0] * 4294967296.0);
-        s1 = __double2ll_rn((double)v[1] * 4294967296.0);
-        s2 = __double2ll_rn((double)v[2] * 4294967296.0);
+        // v * 2^32 is exact in binary32 (a power-of-two scaling of a finite coordinate), so rounding
+        // it to an integer from binary32 gives the binary64 path's value without the FP64 pipe
+        s0 = __float2ll_rn(v[0] * 4294967296.0f);
+        s1 = __float2ll_rn(v[1] * 4294967296.0f);
+        s2 = __float2ll_rn(v[2] * 4294967296.0f);
         cnt = v[2] > 1.e-4f ? 1 : 0;
     }
     s0 = warp_sum(s0);

@@ -19,8 +19,7 @@
 // kr = (1 + ((k3 r2 + k2) r2 + k1) r2) / (1 + ((k6 r2 + k5) r2 + k4) r2), the tangential terms, and
 // u = fx xd + cx, v = fy yd + cy.  The fixed-point map is round(u * 32) split into the integer pixel
 // (arithmetic shift) and the 5 + 5 fractional bits; the float map is rounded to the nearest pixel
-// (ties to even) and saturated to int16 when remapped.  One thread walks one row, as the per-row
-// increments are sequential; the map is built once per camera.
+// (ties to even) and saturated to int16 when remapped.  The map is built once per camera.
 #include <climits>
 #include <cstring>
 
@@ -67,37 +66,61 @@ AFX_D int round_to_int(float v) { return (v >= -2147483648.f && v < 2147483648.f
 AFX_D int saturate_short(int v) { return v < -32768 ? -32768 : (v > 32767 ? 32767 : v); }
 AFX_D uint32_t pack_xy(int sx, int sy) { return (uint32_t)(uint16_t)(int16_t)sx | ((uint32_t)(uint16_t)(int16_t)sy << 16); }
 
-__global__ void undistort_map_kernel(uint32_t* map, MapArgs a) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// One block per row.  The row's homogeneous coordinates are OpenCV's running sums (one addition per
+// column, in column order), so thread 0 walks them kMapChunk columns at a time into shared memory and
+// the block then maps those columns in parallel: the same values, pixel by pixel, as the sequential
+// loop, at the cost of one serial addition chain per row.
+constexpr int kMapChunk = 256;
+
+__global__ void __launch_bounds__(kMapChunk) undistort_map_kernel(uint32_t* map, MapArgs a) {
+    __shared__ double sx[kMapChunk], sy[kMapChunk], sw[kMapChunk];
+    __shared__ double ir[9];
+    const int i = blockIdx.x;  // row
     if (i >= a.height) return;
     const int y0 = (i / a.stripe) * a.stripe;  // first row of this row's stripe
-    double Ar[9];
-    for (int q = 0; q < 9; ++q) Ar[q] = a.A[q];
-    if (a.mode == AFX_UNDISTORT_LINEAR) Ar[5] = a.A[5] - (double)y0;  // cv::undistort: Ar(1,2) = v0 - y
-    double ir[9];
-    inverse3(Ar, ir);
+    if (threadIdx.x == 0) {
+        double Ar[9];
+        for (int q = 0; q < 9; ++q) Ar[q] = a.A[q];
+        if (a.mode == AFX_UNDISTORT_LINEAR) Ar[5] = a.A[5] - (double)y0;  // cv::undistort: Ar(1,2) = v0 - y
+        inverse3(Ar, ir);
+    }
+    __syncthreads();
     const double u0 = a.A[2], v0 = a.A[5], fx = a.A[0], fy = a.A[4];
     const double k1 = a.k[0], k2 = a.k[1], p1 = a.k[2], p2 = a.k[3], k3 = a.k[4], k4 = a.k[5], k5 = a.k[6], k6 = a.k[7];
     const int row = a.mode == AFX_UNDISTORT_LINEAR ? i - y0 : i;
-    double X = row * ir[1] + ir[2], Y = row * ir[4] + ir[5], Wh = row * ir[7] + ir[8];
+    double X = row * ir[1] + ir[2], Y = row * ir[4] + ir[5], Wh = row * ir[7] + ir[8];  // thread 0's running sums
     uint32_t* out = map + 2 * (size_t)i * a.width;
-    for (int j = 0; j < a.width; ++j, X += ir[0], Y += ir[3], Wh += ir[6]) {
-        const double w = 1. / Wh, x = X * w, y = Y * w;
-        const double x2 = x * x, y2 = y * y;
-        const double r2 = x2 + y2, _2xy = 2 * x * y;
-        const double kr = (1 + ((k3 * r2 + k2) * r2 + k1) * r2) / (1 + ((k6 * r2 + k5) * r2 + k4) * r2);
-        const double xd = x * kr + p1 * _2xy + p2 * (r2 + 2 * x2);
-        const double yd = y * kr + p1 * (r2 + 2 * y2) + p2 * _2xy;
-        const double u = fx * xd + u0, v = fy * yd + v0;
-        if (a.mode == AFX_UNDISTORT_LINEAR) {
-            const int iu = round_to_int(u * 32.0), iv = round_to_int(v * 32.0);
-            out[2 * j] = pack_xy((int)(int16_t)(iu >> 5), (int)(int16_t)(iv >> 5));
-            out[2 * j + 1] = (uint32_t)((iv & 31) * 32 + (iu & 31));
-        } else {
-            const float fu = (float)u, fv = (float)v;
-            out[2 * j] = pack_xy(saturate_short(round_to_int(fu)), saturate_short(round_to_int(fv)));
-            out[2 * j + 1] = 0u;
+    for (int j0 = 0; j0 < a.width; j0 += kMapChunk) {
+        const int n = min(kMapChunk, a.width - j0);
+        if (threadIdx.x == 0) {
+            for (int t = 0; t < n; ++t, X += ir[0], Y += ir[3], Wh += ir[6]) {
+                sx[t] = X;
+                sy[t] = Y;
+                sw[t] = Wh;
+            }
         }
+        __syncthreads();
+        const int t = threadIdx.x;
+        if (t < n) {
+            const int j = j0 + t;
+            const double w = 1. / sw[t], x = sx[t] * w, y = sy[t] * w;
+            const double x2 = x * x, y2 = y * y;
+            const double r2 = x2 + y2, _2xy = 2 * x * y;
+            const double kr = (1 + ((k3 * r2 + k2) * r2 + k1) * r2) / (1 + ((k6 * r2 + k5) * r2 + k4) * r2);
+            const double xd = x * kr + p1 * _2xy + p2 * (r2 + 2 * x2);
+            const double yd = y * kr + p1 * (r2 + 2 * y2) + p2 * _2xy;
+            const double u = fx * xd + u0, v = fy * yd + v0;
+            if (a.mode == AFX_UNDISTORT_LINEAR) {
+                const int iu = round_to_int(u * 32.0), iv = round_to_int(v * 32.0);
+                out[2 * j] = pack_xy((int)(int16_t)(iu >> 5), (int)(int16_t)(iv >> 5));
+                out[2 * j + 1] = (uint32_t)((iv & 31) * 32 + (iu & 31));
+            } else {
+                const float fu = (float)u, fv = (float)v;
+                out[2 * j] = pack_xy(saturate_short(round_to_int(fu)), saturate_short(round_to_int(fv)));
+                out[2 * j + 1] = 0u;
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -312,7 +335,7 @@ int undistort_map_impl(uint32_t* map, int width, int height, const float K[9], c
     } else {
         a.stripe = height;
     }
-    undistort_map_kernel<<<(height + 63) / 64, 64, 0, st>>>(map, a);
+    undistort_map_kernel<<<height, kMapChunk, 0, st>>>(map, a);
     AFX_LAUNCH_CHECK();
     return AFX_OK;
 }
