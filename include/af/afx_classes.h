@@ -9,6 +9,7 @@
  *   GaussNewtonSystem                     the Gauss-Newton step of src/VolumeFusion.cu:454-691
  *   the run* operators                    af/afx_shims.h
  *   depth ingest (loadDepthFrame, DepthUndistorter, create_xy_lookup_table, ...)  af/afx_ingest.h
+ *   the dense Gauss-Newton operators and LU solve (runFill_J_*, ..., linearSolverLUStable)  af/afx_gn_dense.h
  *
  * Every computation runs on the GPU through the afx_* entry points; calls block until the GPU
  * work has finished and throw std::runtime_error on failure.  The reference's MotionGraph,
@@ -21,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "afx_gn_dense.h"
 #include "afx_ingest.h"
 #include "afx_motion_graph.h"
 

@@ -28,6 +28,7 @@ using Vec6f = Eigen::Matrix<float, 6, 1>;
 using Vec3d = Eigen::Matrix<double, 3, 1>;
 using Mat3f = Eigen::Matrix<float, 3, 3>;
 using Mat4f = Eigen::Matrix<float, 4, 4>;
+using Mat6f = Eigen::Matrix<float, 6, 6>;
 template <int K>
 using Vecf = Eigen::Matrix<float, K, 1>;
 template <int K>
@@ -104,6 +105,7 @@ using Vec6f = SmallVec<float, 6>;
 using Vec3d = SmallVec<double, 3>;
 using Mat3f = SmallMat<float, 3>;
 using Mat4f = SmallMat<float, 4>;
+using Mat6f = SmallMat<float, 6>;
 template <int K>
 using Vecf = SmallVec<float, K>;
 template <int K>

@@ -313,6 +313,52 @@ int afx_gn_solve(afx_gn* g, float* x, int iterations, double tol, void* stream);
 /* runUpdateTransformsKernel (src/MotionOptimization.cu:483-506): T -= [[x_rot]x, x_t; 0]. */
 int afx_update_transforms(float* transforms, const float* x, const int* n_nodes, int n_nodes_max, void* stream);
 
+/* The reference's dense Gauss-Newton operators, for callers that keep its dense path
+ * (src/VolumeFusion.cu:454-691).  J is rows x width Vec6f (6 floats), row-major; pairs and J^T r
+ * elements are Vec2i (2 ints); a product is a Mat6f (36 floats, column-major); J^T J is dense with
+ * rows jtj_width floats apart.  All arrays are device arrays.
+ *  afx_fill_j_depth / afx_fill_j_mreg: runFill_J_DepthKernel / runFill_J_MRegKernel
+ *    (include/af/MotionOptimization.cuh:9-28); K / Kreg neighbours per vertex / node (<= 8).
+ *  afx_fill_r_depth / afx_fill_r_mreg: runFill_r_DepthKernel / runFill_r_MRegKernel (:30-43).
+ *  afx_jtj_contrib_depth / afx_jtj_contrib_mreg: runComputeJTJAndJTrContribJ*Kernel (:51-68): the
+ *    pairs (with row numbers) and J^T r elements appended after the counters' current values
+ *    (device counters, updated) -- in row order, where the reference's atomics append in a varying
+ *    order.  Workspace: afx_jtj_contrib_workspace_size(rows of the call).
+ *  afx_multiply_jtj_pairs / afx_multiply_jtr_elems: runMultiplyJTJContribPairsKernel /
+ *    runMultiplyJTrContribElemsKernel (:70-82).
+ *  afx_fill_jtj / afx_fill_jtr: runFillJTJKernel / runFillJTrKernel (:84-90).  J^T J is taken as
+ *    square (jtj_width / 6 nodes); pairs naming a node outside J or J^T J are skipped.
+ *  afx_lu_solve: linearSolverLUStable (include/af/LinearSolver.cuh:22, src/LinearSolver.cu:179-223):
+ *    x = A^-1 b by LU with partial pivoting in binary32, A column-major with leading dimension lda
+ *    (left unchanged; factorised in the workspace), ipiv the 1-based pivots; AFX_ERR_SINGULAR where
+ *    getrf would report info != 0.  Synchronises `stream`. */
+int afx_fill_j_depth(float* J, float weight, unsigned rows, unsigned width, const int* corr, unsigned n_corr,
+                     const float* mesh, const uint32_t* knn_idx, const float* knn_w, int K, const float* normals,
+                     void* stream);
+int afx_fill_j_mreg(float* J, float weight, unsigned rows, unsigned width, const float* nodes, unsigned n_nodes,
+                    const uint32_t* knn_idx, int Kreg, void* stream);
+int afx_fill_r_depth(float* r, float weight, const int* corr, unsigned n_corr, const float* warped,
+                     const float* depth_mesh, const float* normals, void* stream);
+int afx_fill_r_mreg(float* r, float weight, const float* nodes, const float* transforms, unsigned n_nodes,
+                    const uint32_t* knn_idx, int Kreg, void* stream);
+size_t afx_jtj_contrib_workspace_size(long rows);
+int afx_jtj_contrib_depth(int* pairs, unsigned* rows, unsigned* n_pairs, int* jtr_elems, unsigned* n_jtr,
+                          const int* corr, unsigned n_corr, const uint32_t* knn_idx, const float* knn_w, int K,
+                          void* workspace, size_t workspace_bytes, void* stream);
+int afx_jtj_contrib_mreg(int* pairs, unsigned* rows, unsigned row_offset, unsigned* n_pairs, int* jtr_elems,
+                         unsigned* n_jtr, unsigned n_nodes, const uint32_t* knn_idx, int Kreg, void* workspace,
+                         size_t workspace_bytes, void* stream);
+int afx_multiply_jtj_pairs(float* out, const int* pairs, const unsigned* rows, unsigned n_pairs, const float* J,
+                           unsigned width, void* stream);
+int afx_multiply_jtr_elems(float* out, const int* elems, unsigned n_elems, const float* J, const float* r,
+                           unsigned width, void* stream);
+int afx_fill_jtj(float* JTJ, const int* coords, const float* elems, unsigned n_elems, unsigned jtj_width,
+                 void* stream);
+int afx_fill_jtr(float* JTr, const int* coords, const float* elems, unsigned n_elems, void* stream);
+size_t afx_lu_solve_workspace_size(int n, int lda);
+int afx_lu_solve(float* x, const float* A, int n, int lda, const float* b, int* ipiv, void* workspace,
+                 size_t workspace_bytes, void* stream);
+
 /* ------------------------------------------------------------------------------------
  * Whole-frame session: af::runVolumeFusion's per-frame loop (src/VolumeFusion.cu:223-769)
  * with all state (TSDF, motion graph, solver) resident on the device.

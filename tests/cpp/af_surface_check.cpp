@@ -12,6 +12,7 @@
 #endif
 #include <af/afx_classes.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <fstream>
@@ -189,6 +190,108 @@ int run() {
     write_raw("jtr.bin", download(jtr.get(), dim));
     write_raw("r_depth.bin", download(rd.get(), nc));
     write_raw("r_reg.bin", download(rr.get(), n * 12));
+    // 6b. the reference's dense sequence (src/VolumeFusion.cu:454-660) through the dense operators,
+    // its thrust sort + reduce_by_key done on the host as a stable sort and sequential sums
+    {
+        const unsigned hD = (unsigned)nc, hR = (unsigned)(n * 4 * 3), rowsJ = hD + hR;
+        af::DeviceArray<af::Vec6f> J((std::size_t)rowsJ * n);
+        af::DeviceArray<float> r(rowsJ);
+        af::detail::cuda_check(cudaMemset(J.get(), 0, sizeof(af::Vec6f) * (std::size_t)rowsJ * n), "memset");
+        af::detail::cuda_check(cudaMemset(r.get(), 0, sizeof(float) * rowsJ), "memset");
+        af::runFill_J_DepthKernel(J.get(), lamD, hD, (unsigned)n, corr_d.bufferPtr(), hD, cloud.bufferPtr(),
+                                  knn_d.idxsPtr(), knn_d.weightsPtr(), v1.get(), n1.get());
+        af::runFill_r_DepthKernel(r.get(), lamD, corr_d.bufferPtr(), hD, warped_d.bufferPtr(), v1.get(), n1.get());
+        af::runFill_r_MRegKernel(r.get() + hD, lamR, field.motionGraph_d().pointsPtr(),
+                                 field.motionGraph_d().transformsPtr(), (unsigned)n, gidx_d.bufferPtr());
+        af::runFill_J_MRegKernel(J.get() + (std::size_t)hD * n, lamR, hR, (unsigned)n, field.motionGraph_d().pointsPtr(),
+                                 field.motionGraph_d().transformsPtr(), (unsigned)n, gidx_d.bufferPtr());
+        const unsigned maxPairs = hD * (af::combinations(6, 2) + 6) + hR * 3, maxElems = hD * 6 + hR * 2;
+        af::DeviceArray<af::Vec2i> pairs(maxPairs), elems(maxElems);
+        af::DeviceArray<unsigned> rows(maxPairs), counts(2);
+        af::detail::cuda_check(cudaMemset(counts.get(), 0, 8), "memset");
+        af::runComputeJTJAndJTrContribJDepthKernel(pairs.get(), rows.get(), counts.get(), elems.get(), counts.get() + 1,
+                                                   corr_d.bufferPtr(), hD, knn_d.idxsPtr(), knn_d.weightsPtr());
+        af::runComputeJTJAndJTrContribJMRegKernel(pairs.get(), rows.get(), hD, counts.get(), elems.get(), counts.get() + 1,
+                                                  (unsigned)n, gidx_d.bufferPtr());
+        const std::vector<unsigned> cnt = download(counts.get(), 2);
+        std::vector<af::Vec2i> P = download(pairs.get(), cnt[0]), E = download(elems.get(), cnt[1]);
+        std::vector<unsigned> R = download(rows.get(), cnt[0]);
+        std::vector<unsigned> order(cnt[0]);
+        for (unsigned i = 0; i < cnt[0]; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](unsigned a, unsigned b) {
+            return P[a][0] < P[b][0] || (P[a][0] == P[b][0] && P[a][1] < P[b][1]);
+        });
+        std::vector<af::Vec2i> sp(cnt[0]);
+        std::vector<unsigned> sr(cnt[0]);
+        for (unsigned i = 0; i < cnt[0]; ++i) {
+            sp[i] = P[order[i]];
+            sr[i] = R[order[i]];
+        }
+        af::DeviceArray<af::Vec2i> sp_d(cnt[0]);
+        af::DeviceArray<unsigned> sr_d(cnt[0]);
+        af::DeviceArray<af::Mat6f> prod_d(cnt[0]);
+        af::copyToDevice(sp_d.get(), sp.data(), sp.size());
+        af::copyToDevice(sr_d.get(), sr.data(), sr.size());
+        af::runMultiplyJTJContribPairsKernel(prod_d.get(), sp_d.get(), sr_d.get(), cnt[0], J.get(), (unsigned)n);
+        std::vector<float> prod(36 * (std::size_t)cnt[0]);
+        af::copyToHost(prod.data(), reinterpret_cast<const float*>(prod_d.get()), prod.size());
+        std::vector<af::Vec2i> coords;
+        std::vector<float> sums;
+        for (unsigned i = 0; i < cnt[0]; ++i) {
+            if (!coords.empty() && coords.back()[0] == sp[i][0] && coords.back()[1] == sp[i][1]) {
+                float* s = sums.data() + sums.size() - 36;
+                for (int e = 0; e < 36; ++e) s[e] = s[e] + prod[36 * (std::size_t)i + e];
+            } else {
+                coords.push_back(sp[i]);
+                sums.insert(sums.end(), prod.begin() + 36 * (std::size_t)i, prod.begin() + 36 * (std::size_t)(i + 1));
+            }
+        }
+        std::vector<unsigned> eorder(cnt[1]);
+        for (unsigned i = 0; i < cnt[1]; ++i) eorder[i] = i;
+        std::stable_sort(eorder.begin(), eorder.end(), [&](unsigned a, unsigned b) { return E[a][1] < E[b][1]; });
+        std::vector<af::Vec2i> se(cnt[1]);
+        for (unsigned i = 0; i < cnt[1]; ++i) se[i] = E[eorder[i]];
+        af::DeviceArray<af::Vec2i> se_d(cnt[1]);
+        af::DeviceArray<af::Vec6f> eprod_d(cnt[1]);
+        af::copyToDevice(se_d.get(), se.data(), se.size());
+        af::runMultiplyJTrContribElemsKernel(eprod_d.get(), se_d.get(), cnt[1], J.get(), r.get(), (unsigned)n);
+        std::vector<float> eprod(6 * (std::size_t)cnt[1]);
+        af::copyToHost(eprod.data(), reinterpret_cast<const float*>(eprod_d.get()), eprod.size());
+        std::vector<af::Vec2i> ecoords;
+        std::vector<float> esums;
+        for (unsigned i = 0; i < cnt[1]; ++i) {
+            if (!ecoords.empty() && ecoords.back()[1] == se[i][1]) {
+                float* s = esums.data() + esums.size() - 6;
+                for (int e = 0; e < 6; ++e) s[e] = s[e] + eprod[6 * (std::size_t)i + e];
+            } else {
+                ecoords.push_back(se[i]);
+                esums.insert(esums.end(), eprod.begin() + 6 * (std::size_t)i, eprod.begin() + 6 * (std::size_t)(i + 1));
+            }
+        }
+        std::vector<float> eye(dim * dim, 0.f);  // runInitIdentityKernel
+        for (std::size_t i = 0; i < dim; ++i) eye[i * dim + i] = 1.f;
+        af::DeviceArray<float> jtj2(dim * dim), jtr2(dim), x2(dim);
+        af::copyToDevice(jtj2.get(), eye.data(), eye.size());
+        af::detail::cuda_check(cudaMemset(jtr2.get(), 0, sizeof(float) * dim), "memset");
+        af::DeviceArray<af::Vec2i> c_d(coords.size()), ec_d(ecoords.size());
+        af::DeviceArray<float> s_d(sums.size()), es_d(esums.size());
+        af::copyToDevice(c_d.get(), coords.data(), coords.size());
+        af::copyToDevice(s_d.get(), sums.data(), sums.size());
+        af::copyToDevice(ec_d.get(), ecoords.data(), ecoords.size());
+        af::copyToDevice(es_d.get(), esums.data(), esums.size());
+        af::runFillJTJKernel(jtj2.get(), c_d.get(), reinterpret_cast<const af::Mat6f*>(s_d.get()), (unsigned)coords.size(),
+                             (unsigned)dim);
+        af::runFillJTrKernel(reinterpret_cast<af::Vec6f*>(jtr2.get()), ec_d.get(),
+                             reinterpret_cast<const af::Vec6f*>(es_d.get()), (unsigned)ecoords.size());
+        write_raw("jtj_dense_ops.bin", download(jtj2.get(), dim * dim));
+        write_raw("jtr_dense_ops.bin", download(jtr2.get(), dim));
+        write_raw("r_dense_ops.bin", download(r.get(), rowsJ));
+        af::DeviceArray<int> ipiv(dim);
+        const bool solved = af::linearSolverLUStable(nullptr, (int)dim, jtj2.get(), (int)dim, jtr2.get(), ipiv.get(), x2.get());
+        if (!solved) throw std::runtime_error("linearSolverLUStable failed");
+        write_raw("x_lu.bin", download(x2.get(), dim));
+    }
+
     af::DeviceArray<af::Vec6f> x((std::size_t)gn.nodesMax());
     gn.solve(x.get(), 10);
     write_raw("x.bin", download(x.get(), n));

@@ -166,3 +166,28 @@ def test_depth_ingest(run):
     assert np.array_equal(run["load"]("ingest_undistorted"), O.undistort_depth(metres, umap, 0).ravel())
     intr = np.array([K[0, 2], K[1, 2], K[0, 0], K[1, 1]], np.float32)
     assert np.array_equal(run["load"]("ingest_xy").reshape(h, w, 2), O.xy_lookup_table(intr, d, w, h))
+
+
+def test_dense_operator_sequence(run):
+    """The reference's dense Gauss-Newton sequence from the C++ caller (runFill_J_* / runFill_r_*,
+    runComputeJTJAndJTrContrib*, runMultiply*, runFillJTJKernel / runFillJTrKernel with a host-side
+    stable sort and sequential sums, then linearSolverLUStable): residuals, J^T J and J^T r equal the
+    oracle's restatement of that sequence bit for bit (which the reference's own kernels pin), and
+    the LU solution solves the system."""
+    cfg, L = run["cfg"], run["load"]
+    mesh, nodes = L("mesh", cols=3), L("nodes", cols=3)
+    Tm = L("transforms_moved", cols=16)
+    midx, mw = L("midx", np.uint32, 6), L("field_mw", cols=6)
+    corr = L("corr", np.int32, 2)
+    gidx = L("gidx", np.uint32, 4)
+    lam_d, lam_r = np.float32(cfg["lambda_depth"]), np.float32(cfg["lambda_reg"])
+    rd = O.residual_depth(corr, L("warped_field", cols=3), run["v1"], run["n1"], lam_d)
+    rr = O.residual_reg(nodes, Tm, gidx, lam_r)
+    A, b, _ = O.assemble(corr, mesh, midx, mw, run["n1"], lam_d, nodes, gidx, lam_r, rd, rr)
+    n = len(nodes)
+    assert np.array_equal(L("r_dense_ops"), np.concatenate([rd, rr]))
+    assert np.array_equal(L("jtj_dense_ops").reshape(6 * n, 6 * n), A)
+    assert np.array_equal(L("jtr_dense_ops"), b)
+    x = L("x_lu").astype(np.float64)
+    A64, b64 = A.astype(np.float64), b.astype(np.float64)
+    assert np.linalg.norm(A64 @ x - b64) <= 1e-4 * np.linalg.norm(b64)

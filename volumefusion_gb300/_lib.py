@@ -163,6 +163,19 @@ SIGNATURES = {
     "afx_xy_lookup_table": (i32, [vp, i32, i32, vp, vp, vp]),
     "afx_unproject_points": (i32, [vp, vp, vp, vp, i64, vp, vp, vp]),
     "afx_project_points": (i32, [vp, vp, vp, i64, vp, vp, vp]),
+    "afx_fill_j_depth": (i32, [vp, f32, C.c_uint, C.c_uint, vp, C.c_uint, vp, vp, vp, i32, vp, vp]),
+    "afx_fill_j_mreg": (i32, [vp, f32, C.c_uint, C.c_uint, vp, C.c_uint, vp, i32, vp]),
+    "afx_fill_r_depth": (i32, [vp, f32, vp, C.c_uint, vp, vp, vp, vp]),
+    "afx_fill_r_mreg": (i32, [vp, f32, vp, vp, C.c_uint, vp, i32, vp]),
+    "afx_jtj_contrib_workspace_size": (sz, [i64]),
+    "afx_jtj_contrib_depth": (i32, [vp, vp, vp, vp, vp, vp, C.c_uint, vp, vp, i32, vp, sz, vp]),
+    "afx_jtj_contrib_mreg": (i32, [vp, vp, C.c_uint, vp, vp, vp, C.c_uint, vp, i32, vp, sz, vp]),
+    "afx_multiply_jtj_pairs": (i32, [vp, vp, vp, C.c_uint, vp, C.c_uint, vp]),
+    "afx_multiply_jtr_elems": (i32, [vp, vp, C.c_uint, vp, vp, C.c_uint, vp]),
+    "afx_fill_jtj": (i32, [vp, vp, vp, C.c_uint, C.c_uint, vp]),
+    "afx_fill_jtr": (i32, [vp, vp, vp, C.c_uint, vp]),
+    "afx_lu_solve_workspace_size": (sz, [i32, i32]),
+    "afx_lu_solve": (i32, [vp, vp, i32, i32, vp, vp, vp, sz, vp]),
     "afx_fusion_set_timing": (i32, [vp, i32]),
     "afx_fusion_stage_times": (i32, [vp, C.POINTER(f64), i32, i32]),
 }

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libafx.so")
 SOURCES = ["afx_prep.cu", "afx_integrate.cu", "afx_scan.cu", "afx_mc.cu", "afx_graph.cu", "afx_gn.cu",
-           "afx_fusion.cu", "afx_serve.cu", "afx_io.cu", "afx_stream.cu", "afx_decode.cu", "afx_undistort.cu"]
+           "afx_fusion.cu", "afx_serve.cu", "afx_io.cu", "afx_stream.cu", "afx_decode.cu", "afx_undistort.cu", "afx_gn_dense.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 FLAGS = [ARCH, "-O3", "-lineinfo", "-fmad=false", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler",
          "-fno-fast-math", "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
