@@ -282,8 +282,8 @@ def _sort_dev(pts, fn, *extra):
 
 def test_volume_sort_equals_general_sort():
     """The column-bucket sort + unique of a marching-cubes cloud gives the general sort's result bit
-    for bit: on a real cloud, with +0/-0 twins, and with one column too large for shared memory (the
-    device falls back to the general sort)."""
+    for bit: on a real cloud, with +0/-0 twins, and with columns too large for shared memory (their
+    CTA sorts runs of 8192 and merges them: 2 runs, and 5 runs over three merge rounds)."""
     import ctypes as C
 
     from volumefusion_gb300 import configs
@@ -307,7 +307,11 @@ def test_volume_sort_equals_general_sort():
     dims = (C.c_int * 3)(*cfg["dims"])
     f3 = lambda a: (C.c_float * 3)(*[float(x) for x in a])  # noqa: E731
     extra = (dims, f3(vs), f3(cfg["volume_size"]))
-    for case in (raw, np.concatenate([raw, neg, twins, raw[:500]]), np.concatenate([raw, column])):
+    big = np.stack([np.full(40000, -half + np.float32(60.25) * vs[0], np.float32),
+                    (rng.integers(0, 150, 40000) * vs[1] - half).astype(np.float32),
+                    (rng.integers(0, 150, 40000) * vs[2] - half).astype(np.float32)], axis=1)
+    for case in (raw, np.concatenate([raw, neg, twins, raw[:500]]), np.concatenate([raw, column]),
+                 np.concatenate([raw, column, big, big[:7000]])):
         case = case[rng.permutation(len(case))]
         a = _sort_dev(case, "general")
         b = _sort_dev(case, "volume", *extra)

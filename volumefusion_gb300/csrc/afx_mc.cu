@@ -986,8 +986,9 @@ static int sort_unique_cluster(float* pts, unsigned* count, long n_max, void* ws
 // Pipeline: count per bucket, scan, scatter (order within a bucket arbitrary), one CTA per bucket
 // sorting it in shared memory and counting its unique points, scan of those counts, ordered
 // compaction back into the cloud.  A bucket larger than kBucketCap (a surface lying along one x
-// column) raises a flag on the device; the bucket kernels then stand down and the cluster sort above
-// runs instead, on the untouched cloud.
+// column) is sorted by its CTA in runs of kBucketCap in shared memory that are then merged pairwise
+// in global memory (merge path, ties from the left run first) between the key buffer and the second
+// buffer of the workspace, so one crowded column no longer sends the whole cloud to the cluster sort.
 // ------------------------------------------------------------------------------------
 
 constexpr int kBucketCap = 8192;  // keys per bucket sorted in shared memory (96 KB)
@@ -1099,15 +1100,37 @@ AFX_D void bucket_bitonic(Key3* g, unsigned m, Key3* sk) {
     __syncthreads();
 }
 
-// One CTA per bucket (at most kBucketCap points): sort it in place and count its unique points.
-__global__ void __launch_bounds__(kBucketThreads) bucket_sort_kernel(Key3* keys, const unsigned* off, unsigned* ucnt,
-                                                                   const unsigned* overflow, long n_max, int* error) {
+// Stable merge of the sorted runs A[0, la) and B[0, lb) into out by the whole CTA: each thread finds
+// where its share of the output starts on the merge path (binary search: the first i with
+// B[k - i - 1] < A[i]) and merges its share sequentially.
+AFX_D void cta_merge(const Key3* A, unsigned la, const Key3* B, unsigned lb, Key3* out) {
+    const unsigned total = la + lb, per = (total + blockDim.x - 1) / blockDim.x;
+    const unsigned k0 = min(total, threadIdx.x * per), k1 = min(total, k0 + per);
+    if (k0 >= k1) return;
+    unsigned lo = k0 > lb ? k0 - lb : 0u, hi = min(k0, la);
+    while (lo < hi) {
+        const unsigned mid = (lo + hi) >> 1;
+        if (key_less(B[k0 - mid - 1], A[mid])) hi = mid;
+        else lo = mid + 1;
+    }
+    unsigned i = lo, j = k0 - lo;
+    for (unsigned k = k0; k < k1; ++k) {
+        const bool takeA = i < la && (j >= lb || !key_less(B[j], A[i]));
+        out[k] = takeA ? A[i++] : B[j++];
+    }
+}
+
+// One CTA per bucket: sort it in place (in shared memory, or in runs merged through `scratch` when it
+// holds more than kBucketCap points) and count its unique points.
+__global__ void __launch_bounds__(kBucketThreads) bucket_sort_kernel(Key3* keys, Key3* scratch, const unsigned* off,
+                                                                   unsigned* ucnt, const unsigned* overflow, long n_max,
+                                                                   int* error) {
     extern __shared__ Key3 sk[];
     __shared__ unsigned wsum[kBucketThreads / 32];
     if (*overflow) return;
     const int b = blockIdx.x;
     const unsigned lo = off[b], n = off[b + 1] - lo;
-    if (lo > off[b + 1] || (long)off[b + 1] > n_max || n > (unsigned)kBucketCap) {  // never expected: skip, flag
+    if (lo > off[b + 1] || (long)off[b + 1] > n_max) {  // never expected: skip, flag
         if (threadIdx.x == 0) {
             ucnt[b] = 0;
             if (error) atomicOr(error, ERRF_INDEX);
@@ -1119,7 +1142,26 @@ __global__ void __launch_bounds__(kBucketThreads) bucket_sort_kernel(Key3* keys,
         return;
     }
     Key3* g = keys + lo;
-    bucket_bitonic(g, n, sk);
+    if (n <= (unsigned)kBucketCap) {
+        bucket_bitonic(g, n, sk);
+    } else {
+        for (unsigned c0 = 0; c0 < n; c0 += kBucketCap) bucket_bitonic(g + c0, min((unsigned)kBucketCap, n - c0), sk);
+        Key3 *src = g, *dst = scratch + lo;
+        for (unsigned L = kBucketCap; L < n; L *= 2) {
+            for (unsigned s0 = 0; s0 < n; s0 += 2 * L) {
+                const unsigned la = min(L, n - s0), lb = min(L, n - s0 - la);
+                cta_merge(src + s0, la, src + s0 + la, lb, dst + s0);
+            }
+            __syncthreads();
+            Key3* t = src;
+            src = dst;
+            dst = t;
+        }
+        if (src != g) {
+            for (unsigned i = threadIdx.x; i < n; i += blockDim.x) g[i] = src[i];
+            __syncthreads();
+        }
+    }
     unsigned c = 0;
     for (unsigned i = threadIdx.x; i < n; i += blockDim.x) c += (i == 0 || !key_same_point(g[i - 1], g[i])) ? 1u : 0u;
     c = warp_sum(c);
@@ -1193,11 +1235,12 @@ int sort_unique_volume_impl(float* pts, unsigned* count, long n_max, void* ws, s
     AFX_CUDA(cudaMemsetAsync(w.cnt, 0, nb * 4, st));
     AFX_CUDA(cudaMemsetAsync(w.overflow, 0, 4, st));
     bucket_count_kernel<<<grid_for(n_max, 256), 256, 0, st>>>(pts, count, n_max, a, w.cnt);
-    small_scan_kernel<<<1, 1024, 0, st>>>(w.cnt, nb, w.off, w.cursor, kBucketCap, w.overflow, nullptr, nullptr);
+    small_scan_kernel<<<1, 1024, 0, st>>>(w.cnt, nb, w.off, w.cursor, 0xffffffffu, nullptr, nullptr, nullptr);
     bucket_scatter_kernel<<<grid_for(n_max, 256), 256, 0, st>>>(pts, count, n_max, a, w.cursor, keys, w.overflow,
                                                                  error);
-    bucket_sort_kernel<<<nb, kBucketThreads, kBucketCap * sizeof(Key3), st>>>(keys, w.off, w.ucnt, w.overflow, n_max,
-                                                                              error);
+    Key3* scratch = reinterpret_cast<Key3*>(static_cast<char*>(ws) + al(n_max * sizeof(Key3)));  // the second buffer
+    bucket_sort_kernel<<<nb, kBucketThreads, kBucketCap * sizeof(Key3), st>>>(keys, scratch, w.off, w.ucnt, w.overflow,
+                                                                              n_max, error);
     small_scan_kernel<<<1, 1024, 0, st>>>(w.ucnt, nb, w.uoff, nullptr, 0xffffffffu, nullptr, count, w.overflow);
     bucket_compact_kernel<<<nb, kBucketThreads, 0, st>>>(keys, w.off, w.uoff, pts, n_max, w.overflow, error);
     AFX_LAUNCH_CHECK();
