@@ -318,3 +318,35 @@ def test_volume_sort_equals_general_sort():
         assert a.shape == b.shape and len(a) > 0
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
     assert np.array_equal(_sort_dev(raw, "volume", *extra), O.sort_unique(raw))
+
+
+def test_knn_large_graph(af):
+    """KNN over a graph of several node tiles (4332 nodes) gives the oracle's lists (the K smallest
+    (distance, index) pairs) bit for bit: nodes on a jittered lattice with duplicates and equidistant
+    pairs, queries inside and outside the node cloud, K = 4 and 6, and the graph's own 8-NN excluding
+    the closest."""
+    rng = np.random.default_rng(12)
+    g = np.stack(np.meshgrid(np.arange(18), np.arange(16), np.arange(14), indexing="ij"), -1).reshape(-1, 3)
+    nodes = (g * 0.01 + rng.normal(0, 0.002, g.shape)).astype(np.float32)
+    nodes = nodes[rng.permutation(len(nodes))]
+    nodes[100:140] = nodes[:40]  # duplicates: equal distances, resolved by index
+    nodes = np.concatenate([nodes, (g[:300] * 0.01).astype(np.float32)])  # exact lattice points (ties)
+    n = len(nodes)
+    assert n > 2048
+    pts = np.concatenate([(rng.random((6000, 3)) * [0.19, 0.17, 0.15] - 0.01),
+                          (rng.random((500, 3)) * 0.6 - 0.2),  # many far outside the cloud
+                          (g[:300] * 0.01 + 0.005)]).astype(np.float32)  # equidistant to lattice neighbours
+    nodes_g, n_g = cu(nodes), cu(np.array([n], np.int32))
+    for k in (4, 6):
+        idx = torch.empty((len(pts), k), dtype=torch.int32, device="cuda")
+        dist = torch.empty((len(pts), k), dtype=torch.float32, device="cuda")
+        af.getKnnData(idx, dist, nodes_g, n_g, cu(pts))
+        io, do = O.knn(nodes, pts, k)
+        assert np.array_equal(host(idx).view(np.uint32), io), k
+        assert np.array_equal(host(dist), do), k
+    gi = torch.empty((n, 8), dtype=torch.int32, device="cuda")
+    gd = torch.empty((n, 8), dtype=torch.float32, device="cuda")
+    af.getKnnData(gi, gd, nodes_g, n_g, nodes_g, excludeClosest=True)
+    gio, gdo = O.knn(nodes, nodes, 8, exclude_closest=True)
+    assert np.array_equal(host(gi).view(np.uint32), gio)
+    assert np.array_equal(host(gd), gdo)
