@@ -201,6 +201,11 @@ struct afx_fusion {
     // graph build, join before the voxel warp); created with the session, outside any capture
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+    // host frames (afx_fusion_process_host): two device input buffers filled on a copy stream, so the
+    // next frame's copy overlaps the frame in flight
+    uint16_t* in_buf[2] = {nullptr, nullptr};
+    cudaStream_t copy_st = nullptr;
+    cudaEvent_t ev_in_ready[2] = {nullptr, nullptr}, ev_in_free[2] = {nullptr, nullptr};
     cudaGraphExec_t gexec[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     cudaGraph_t graph[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // kept for batch graphs
     unsigned graph_epoch = 0;  // advanced whenever the captured graphs are dropped
@@ -357,6 +362,7 @@ static void session_layout(const afx_fusion_params& p, afx_fusion* f) {
     const long vb = (long)vox_bytes(f->fmt);
     add(S * vb); add(S * vb); add(S * 4);                // tsdf weights coll
     add(Pp * 2); add(Pp * 4); add(Pp * 12); add(Pp * 12);  // frame buffers
+    add(Pp * 2); add(Pp * 2);                              // host-frame input buffers
     add(64); add(64); add(64); add(64); add(64);          // centroids acc error epoch
     add(M * 12); add(64); add(M * 12); add(64); add(64);  // point-cloud double buffer + used count
     add(N * 12); add(N * 12); add(N * 12); add(N * 4); add(N * 64); add(N * 64); add(64); add(64);
@@ -416,6 +422,8 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     f->weights = take(S * vox_bytes(f->fmt));
     f->coll = (unsigned*)take(S * 4);
     f->depth_mm = (uint16_t*)take(Pp * 2);
+    f->in_buf[0] = (uint16_t*)take(Pp * 2);
+    f->in_buf[1] = (uint16_t*)take(Pp * 2);
     f->depth = (float*)take(Pp * 4);
     f->verts = (float*)take(Pp * 12);
     f->normals = (float*)take(Pp * 12);
@@ -483,6 +491,11 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&f->side, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->ev_fork, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->ev_join, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&f->copy_st, cudaStreamNonBlocking);
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+        e = cudaEventCreateWithFlags(&f->ev_in_ready[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f->ev_in_free[k], cudaEventDisableTiming);
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(f->arena, 0, f->arena_bytes, init);
     int rc = e == cudaSuccess ? afx_fusion_reset(f, init) : note_cuda_error(e);
     if (!rc && f->umap)  // cv::undistort's map, built once: it depends on the camera only
@@ -495,6 +508,11 @@ int afx_fusion_create(const afx_fusion_params* params, afx_fusion** out) {
         if (f->side) cudaStreamDestroy(f->side);
         if (f->ev_fork) cudaEventDestroy(f->ev_fork);
         if (f->ev_join) cudaEventDestroy(f->ev_join);
+        if (f->copy_st) cudaStreamDestroy(f->copy_st);
+        for (int k = 0; k < 2; ++k) {
+            if (f->ev_in_ready[k]) cudaEventDestroy(f->ev_in_ready[k]);
+            if (f->ev_in_free[k]) cudaEventDestroy(f->ev_in_free[k]);
+        }
         cudaFree(f->arena);
         delete f;
         return rc;
@@ -527,6 +545,14 @@ int afx_fusion_destroy(afx_fusion* f) {
     if (f->side) cudaStreamDestroy(f->side);
     if (f->ev_fork) cudaEventDestroy(f->ev_fork);
     if (f->ev_join) cudaEventDestroy(f->ev_join);
+    if (f->copy_st) {
+        cudaStreamSynchronize(f->copy_st);  // a host frame's copy, if the caller never ran its frame
+        cudaStreamDestroy(f->copy_st);
+    }
+    for (int k = 0; k < 2; ++k) {
+        if (f->ev_in_ready[k]) cudaEventDestroy(f->ev_in_ready[k]);
+        if (f->ev_in_free[k]) cudaEventDestroy(f->ev_in_free[k]);
+    }
     cudaError_t e = cudaFree(f->arena);
     delete f;
     return note_cuda_error(e);
@@ -868,11 +894,21 @@ int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream) {
     return AFX_OK;
 }
 
+// The frame is copied into one of two input buffers on the session's copy stream (after the frame
+// that last read that buffer) and the frame waits for the copy: a caller that submits the next frame
+// before the current one finishes gets its copy overlapped with the current frame's kernels.
 int afx_fusion_process_host(afx_fusion* f, const uint16_t* depth_mm_host, void* stream) {
     if (!f || !depth_mm_host) return AFX_ERR_INVALID_ARGUMENT;
     cudaStream_t st = as_stream(stream);
-    AFX_CUDA(cudaMemcpyAsync(f->depth_mm, depth_mm_host, f->P * 2, cudaMemcpyHostToDevice, st));
-    return afx_fusion_process(f, f->depth_mm, stream);
+    const int k = f->frame & 1;
+    AFX_CUDA(cudaStreamWaitEvent(f->copy_st, f->ev_in_free[k], 0));
+    AFX_CUDA(cudaMemcpyAsync(f->in_buf[k], depth_mm_host, f->P * 2, cudaMemcpyHostToDevice, f->copy_st));
+    AFX_CUDA(cudaEventRecord(f->ev_in_ready[k], f->copy_st));
+    AFX_CUDA(cudaStreamWaitEvent(st, f->ev_in_ready[k], 0));
+    int rc = afx_fusion_process(f, f->in_buf[k], stream);
+    const cudaError_t e = cudaEventRecord(f->ev_in_free[k], st);  // the buffer is free once this frame is done
+    if (!rc && e != cudaSuccess) rc = note_cuda_error(e);
+    return rc;
 }
 
 static_assert(sizeof(FrameStats) == sizeof(afx_frame_stats), "statistics layouts differ");
