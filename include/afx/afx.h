@@ -434,7 +434,10 @@ int afx_fusion_reset(afx_fusion* f, void* stream);
  * non-rigid loop.  depth_mm is a device pointer (use afx_fusion_process_host for host
  * memory).  Asynchronous on `stream`. */
 int afx_fusion_process(afx_fusion* f, const uint16_t* depth_mm, void* stream);
-/* Same, from host memory: copies the frame to the device on `stream` first. */
+/* Same, from host memory: the frame is copied into one of two session input buffers on the
+ * session's own copy stream, and the frame on `stream` waits for that copy, so frames submitted back
+ * to back overlap each copy with the frame before it.  A pinned host buffer must stay unchanged until
+ * its frame has run (pageable memory is staged before the call returns). */
 int afx_fusion_process_host(afx_fusion* f, const uint16_t* depth_mm_host, void* stream);
 /* Enqueue a copy of the last frame's statistics into host memory (pinned for an asynchronous
  * copy); the values are there once `stream` has passed this point. */
