@@ -47,8 +47,10 @@ __global__ void fill_j_depth_kernel(float* J, float lam, unsigned width, const i
         for (int i = 0; i < K; ++i) {
             const float w = knn_w[v * K + i];
             if (w < 1.e-4f) continue;
+            const uint32_t node = knn_idx[v * K + i];
+            if (node >= width) continue;  // not a column of J
             const float nw[3] = {n[0] * w, n[1] * w, n[2] * w};
-            float* o = J + 6 * ((long)c * width + knn_idx[v * K + i]);
+            float* o = J + 6 * ((long)c * width + node);
 #pragma unroll
             for (int q = 0; q < 6; ++q) o[q] = (nw[0] * G[0][q] + (nw[1] * G[1][q] + nw[2] * G[2][q])) * lam;
         }
