@@ -1209,7 +1209,7 @@ def main():
             "last_frame_stats": {k: st[k] for k in ("n_nodes", "mesh_points", "correspondences", "gn_iterations_done",
                                                 "mesh_faces", "error")},
             "mc_tile": {"chosen": tile, "ms_per_tile": [round(x, 4) for x in tile_ms],
-                        "tiles": ["tma16", "tma8", "tma32", "column", "pipe8", "pipe16"]},
+                        "tiles": ["tma16", "tma8", "tma32", "column", "pipe8", "pipe16", "pipe4"]},
             "dense_graph": dense,
             "precision": precision,
             "batched": batched,

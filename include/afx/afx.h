@@ -487,8 +487,8 @@ int afx_fusion_graph_count(const afx_fusion* f);
 /* Marching-cubes tile of the session (no counterpart in the reference): AFX_MC_TILE_TMA16 (default:
  * a CTA's brick of 32x8x16 cubes brought into shared memory by TMA), AFX_MC_TILE_TMA8,
  * AFX_MC_TILE_TMA32 (8 or 32 cubes along z), AFX_MC_TILE_COLUMN (column march from global memory),
- * AFX_MC_TILE_PIPE8 / AFX_MC_TILE_PIPE16 (a persistent grid whose CTAs keep two bricks of 8 or 16
- * cubes in flight).  Results are the same with every tile (point and triangle sets; triangle order
+ * AFX_MC_TILE_PIPE8 / AFX_MC_TILE_PIPE16 / AFX_MC_TILE_PIPE4 (a persistent grid whose CTAs keep two
+ * bricks of 8, 16 or 4 cubes in flight).  Results are the same with every tile (point and triangle sets; triangle order
  * may differ).  afx_fusion_autotune times each tile on the session's current volume (call it after
  * a few frames), keeps the fastest and returns it in *tile (and the best time of each tile in
  * ms[AFX_MC_TILES] if given); it re-extracts the current frame's mesh and blocks on `stream`.
@@ -499,7 +499,8 @@ int afx_fusion_graph_count(const afx_fusion* f);
 #define AFX_MC_TILE_COLUMN 3
 #define AFX_MC_TILE_PIPE8 4
 #define AFX_MC_TILE_PIPE16 5
-#define AFX_MC_TILES 6
+#define AFX_MC_TILE_PIPE4 6
+#define AFX_MC_TILES 7
 int afx_fusion_set_tile(afx_fusion* f, int tile);
 int afx_fusion_get_tile(const afx_fusion* f);
 int afx_fusion_autotune(afx_fusion* f, int* tile, float* ms, void* stream);

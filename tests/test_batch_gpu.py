@@ -63,7 +63,7 @@ def test_every_mc_tile_gives_the_same_surface_and_autotune_picks_one():
     cfg = configs.small_nonrigid(n_frames=5)
     frames = configs.small_frames(cfg)
     ref = None
-    for tile in range(6):
+    for tile in range(7):
         s = FusionSession(cfg)
         s.set_tile(tile)
         for mm in frames:

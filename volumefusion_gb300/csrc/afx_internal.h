@@ -63,8 +63,8 @@ int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& 
 size_t mc_tile_ws_words(const Volume& vol);
 // marching-cubes tiles (the session's autotuner picks one): TMA bricks of 16, 8 or 32 cubes along z,
 // the column march from global memory, or a persistent grid with two stages of bricks 8 or 16 deep
-enum { kMcTileTma16 = 0, kMcTileTma8 = 1, kMcTileTma32 = 2, kMcTileColumn = 3, kMcTilePipe8 = 4, kMcTilePipe16 = 5,
-       kMcTiles = 6 };
+enum { kMcTileTma16 = 0, kMcTileTma8 = 1, kMcTileTma32 = 2, kMcTileColumn = 3, kMcTilePipe8 = 4, kMcTilePipe16 = 5, kMcTilePipe4 = 6,
+       kMcTiles = 7 };
 int translate_impl(float* pts, const unsigned* count, long n_max, const float* t, cudaStream_t st);
 // pts += sign * t_dev (t_dev in device memory); dst may differ from src
 int translate_dev_impl(float* dst, const float* src, const unsigned* count, long n_max, const float* t_dev, float sign,

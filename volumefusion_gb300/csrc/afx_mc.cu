@@ -606,15 +606,16 @@ static void mc_launch_pipe(const TT* tsdf, const McArgs& a, const CUtensorMap* m
                                                                                               ty, tz);
 }
 
-// Words of the occupied-tile list for a volume (count + one entry per tile of the shallowest depth).
+// Words of the occupied-tile list for a volume (count + one entry per tile of the shallowest depth, 4).
 size_t mc_tile_ws_words(const Volume& vol) {
     const long tx = (vol.dims[0] - 2 + kMcX - 1) / kMcX, ty = (vol.dims[1] - 2 + kMcY - 1) / kMcY,
-               tz = (vol.dims[2] - 2 + 8 - 1) / 8;
+               tz = (vol.dims[2] - 2 + 4 - 1) / 4;
     return (size_t)(1 + (tx > 0 ? tx : 0) * (ty > 0 ? ty : 0) * (tz > 0 ? tz : 0));
 }
 
 // tile: kMcTileTma16 (default), kMcTileTma8, kMcTileTma32 (TMA bricks of that many cubes along z),
-// kMcTilePipe8 / kMcTilePipe16 (persistent grid with two stages of bricks 8 or 16 cubes deep) or
+// kMcTilePipe8 / kMcTilePipe16 / kMcTilePipe4 (persistent grid with two stages of bricks 8, 16 or 4
+// cubes deep) or
 // kMcTileColumn (column march from global memory, 16 cubes along z).  mt/mw are the maps encoded for
 // that depth, or null (then the column march runs).
 template <class TT, class WT, bool kPoints, bool kMesh>
@@ -622,6 +623,8 @@ static void mc_launch(const TT* tsdf, const WT* weights, const McArgs& a, const 
                       int tile, cudaStream_t st) {
     if (mt && tile == kMcTilePipe8) {
         mc_launch_pipe<TT, WT, kPoints, kMesh, 8>(tsdf, a, mt, mw, st);
+    } else if (mt && tile == kMcTilePipe4) {
+        mc_launch_pipe<TT, WT, kPoints, kMesh, 4>(tsdf, a, mt, mw, st);
     } else if (mt && tile == kMcTilePipe16) {
         mc_launch_pipe<TT, WT, kPoints, kMesh, 16>(tsdf, a, mt, mw, st);
     } else if (mt && tile == kMcTileTma8) {
@@ -677,7 +680,7 @@ int mc_fused_impl(const void* tsdf, const void* weights, int fmt, const Volume& 
     CUtensorMap mt, mw;
     const bool f16 = fmt == kVoxF16;
     const size_t elem = vox_bytes(fmt);
-    const int zr = (tile == kMcTileTma8 || tile == kMcTilePipe8) ? 8 : tile == kMcTileTma32 ? 32 : 16;
+    const int zr = (tile == kMcTileTma8 || tile == kMcTilePipe8) ? 8 : tile == kMcTilePipe4 ? 4 : tile == kMcTileTma32 ? 32 : 16;
     const bool tma = error && tile != kMcTileColumn &&
                      make_volume_map(&mt, tsdf, vol, f16 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 :
                                                            CU_TENSOR_MAP_DATA_TYPE_FLOAT32, elem, zr) &&

@@ -210,7 +210,7 @@ class FusionSession:
 
     def autotune(self):
         """Time every marching-cubes tile on the current volume and keep the fastest: (tile, ms per tile)."""
-        t, ms = C.c_int(0), (C.c_float * 6)()
+        t, ms = C.c_int(0), (C.c_float * 7)()
         check(lib().afx_fusion_autotune(self.h, C.byref(t), ms, self._st()), "afx_fusion_autotune")
         return t.value, list(ms)
 
