@@ -60,8 +60,9 @@ def parse():
     ap.add_argument("--profile-step", action="store_true",
                     help="for ncu: the headline session, two warm steps, then one step with the marching-cubes tile "
                          "--mc-tile; prints the library kernel launches before that step and in it, and exits")
-    ap.add_argument("--mc-tile", type=int, default=4, help="marching-cubes tile of --profile-step (4: the one the "
-                                                            "autotuner picks on this workload)")
+    ap.add_argument("--mc-tile", type=int, default=6, help="marching-cubes tile of --profile-step (6, the persistent "
+                                                            "grid of 4-deep bricks: the one the autotuner picks on "
+                                                            "this workload)")
     return ap.parse_args()
 
 
