@@ -693,6 +693,10 @@ def ingest_arm(args, cfg, frames_np, stream, barrier):
         ingest.decode_depth_many([blobs[i % clip]], threads=1, outs=[views[i % ring]])
         return i
 
+    from volumefusion_gb300._lib import FrameStats, lib as _afx_lib
+    stats_host = torch.empty(clip * C.sizeof(FrameStats), dtype=torch.uint8).pin_memory()
+    slot_done = [None] * ring  # event after the frame that last read each pinned slot
+
     def run(steps):
         total = steps * clip
         futs = {i: pool.submit(decode_into, i) for i in range(min(ring - 1, total))}
@@ -701,10 +705,20 @@ def ingest_arm(args, cfg, frames_np, stream, barrier):
                 s.reset()
             futs.pop(i).result()
             s.process_host_ptr(pinned[i % ring].data_ptr())
-            s.stats(check_errors=False)
+            rc = _afx_lib().afx_fusion_stats_async(s.h, C.c_void_p(stats_host.data_ptr() + (i % clip) * C.sizeof(FrameStats)),
+                                                   C.c_void_p(stream.cuda_stream))
+            if rc:
+                raise RuntimeError("afx_fusion_stats_async failed: %d" % rc)
+            ev = torch.cuda.Event()
+            ev.record(stream)
+            slot_done[i % ring] = ev
             j = i + ring - 1
             if j < total:
+                prev = slot_done[j % ring]  # the frame that last read slot j % ring
+                if prev is not None:
+                    prev.synchronize()
                 futs[j] = pool.submit(decode_into, j)
+        stream.synchronize()
         return total
 
     run(1)
@@ -713,8 +727,10 @@ def ingest_arm(args, cfg, frames_np, stream, barrier):
     n = run(max(1, min(3, args.steps)))
     barrier()
     res["e2e_from_png"] = {"frames_per_s": n / (time.perf_counter() - t0), "decode_threads": min(threads, ring),
-                           "note": "PNG bytes in host memory decoded ahead of the session into pinned buffers, each "
-                                   "frame then copied in by afx_fusion_process_host and its statistics read back"}
+                           "note": "PNG bytes in host memory decoded on host threads ahead of the session into a ring "
+                                   "of pinned buffers (a buffer is refilled once the frame that read it has run); "
+                                   "frames submitted back to back through afx_fusion_process_host, each frame's "
+                                   "statistics read into pinned memory"}
     pool.shutdown()
     s.close()
     return res
