@@ -143,8 +143,8 @@ def test_lu_solve():
     wsn = L.afx_lu_solve_workspace_size(n, n)
     ws = torch.empty(wsn, dtype=torch.uint8, device="cuda")
     s = torch.cuda.current_stream().cuda_stream
-    _ok(L.afx_lu_solve(x.data_ptr(), A.data_ptr(), n, n, jtr.data_ptr(), piv.data_ptr(), ws.data_ptr(), wsn, s),
-        "afx_lu_solve")
+    from volumefusion_gb300 import af
+    assert af.linearSolverLUStable(None, n, A, n, jtr, piv, x)
     A64 = G["jtj"].astype(np.float64)
     b64 = G["jtr"].astype(np.float64)
     x64 = np.linalg.solve(A64, b64)
@@ -169,3 +169,38 @@ def test_lu_solve():
     ws8 = torch.empty(w8, dtype=torch.uint8, device="cuda")
     rc = L.afx_lu_solve(x8.data_ptr(), S.data_ptr(), 8, 8, b.data_ptr(), p8.data_ptr(), ws8.data_ptr(), w8, s)
     assert rc == 4  # AFX_ERR_SINGULAR
+    assert af.linearSolverLUStable(None, 8, S, 8, b, p8, x8) is False
+
+
+def test_dense_operators_python_names():
+    """The same sequence through volumefusion_gb300.af's reference-named wrappers gives the same
+    residuals and J^T J (the first two steps and the J^T J scatter)."""
+    from volumefusion_gb300 import af
+    G = _g()
+    r_ref, jtj_ref, _, (P, R, E, hD) = _system(G)
+    K = G["K"]
+    d1, v1, n1, _ = O.frame_prep(G["mm1"], K)
+    corr, nodes, T, gidx = G["corr"], G["nodes"], G["T"], G["gidx"]
+    Cn, n = len(corr), len(nodes)
+    hR = n * 4 * 3
+    J = torch.zeros((hD + hR, n, 6), dtype=torch.float32, device="cuda")
+    r = torch.zeros(hD + hR, dtype=torch.float32, device="cuda")
+    corr_d, mesh_d = _dev(corr, np.int32), _dev(G["mesh"], np.float32)
+    midx_d, mw_d = _dev(G["midx"], np.uint32), _dev(G["mw"], np.float32)
+    n1_d, v1_d = _dev(n1.reshape(-1, 3), np.float32), _dev(v1.reshape(-1, 3), np.float32)
+    warped_d, nodes_d = _dev(G["warped"], np.float32), _dev(nodes, np.float32)
+    T_d, gidx_d = _dev(T, np.float32), _dev(gidx, np.uint32)
+    af.runFill_J_DepthKernel(J, 1.0, hD, n, corr_d, Cn, mesh_d, midx_d, mw_d, v1_d, n1_d)
+    af.runFill_r_DepthKernel(r, 1.0, corr_d, Cn, warped_d, v1_d, n1_d)
+    af.runFill_r_MRegKernel(r[hD:], float(np.float32(np.sqrt(200.0))), nodes_d, T_d, n, gidx_d)
+    af.runFill_J_MRegKernel(J[hD:], float(np.float32(np.sqrt(200.0))), hR, n, nodes_d, T_d, n, gidx_d)
+    assert np.array_equal(r.cpu().numpy(), r_ref)
+    pairs = torch.zeros((len(P) + 8, 2), dtype=torch.int32, device="cuda")
+    rows = torch.zeros(len(P) + 8, dtype=torch.int32, device="cuda")
+    elems = torch.zeros((len(E) + 8, 2), dtype=torch.int32, device="cuda")
+    npairs = torch.zeros(1, dtype=torch.int32, device="cuda")
+    nelems = torch.zeros(1, dtype=torch.int32, device="cuda")
+    af.runComputeJTJAndJTrContribJDepthKernel(pairs, rows, npairs, elems, nelems, corr_d, Cn, midx_d, mw_d)
+    af.runComputeJTJAndJTrContribJMRegKernel(pairs, rows, hD, npairs, elems, nelems, n, gidx_d)
+    assert int(npairs.item()) == len(P) and int(nelems.item()) == len(E)
+    assert np.array_equal(pairs[:len(P)].cpu().numpy(), P) and np.array_equal(rows[:len(P)].cpu().numpy(), R)

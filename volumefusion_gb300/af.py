@@ -288,3 +288,82 @@ class GaussNewtonSystem:
 def runUpdateTransformsKernel(transforms, x, n_nodes):
     _sync(lib().afx_update_transforms(_p(transforms), _p(x), _p(n_nodes), transforms.shape[0], _stream()),
           "runUpdateTransformsKernel")
+
+
+# ---- include/af/MotionOptimization.cuh, include/af/LinearSolver.cuh: the dense Gauss-Newton path ----
+# J: (rows, width, 6) float tensor; pairs / elements: (n, 2) int32; rows: (n,) int32; products:
+# (n, 36) (Mat6f, column-major) or (n, 6); counters: (1,) int32 device counters appended after.
+
+def runFill_J_DepthKernel(jDepth, energyWeight, jDepthHeight, jDepthWidth, corrIdxs, corrIdxsSize, canonMesh,
+                          knnIdxs, knnWeights, depthMesh, depthMeshNormals):
+    K = knnIdxs.shape[-1]
+    _sync(lib().afx_fill_j_depth(_p(jDepth), float(energyWeight), int(jDepthHeight), int(jDepthWidth), _p(corrIdxs),
+                                 int(corrIdxsSize), _p(canonMesh), _p(knnIdxs), _p(knnWeights), int(K),
+                                 _p(depthMeshNormals), _stream()), "runFill_J_DepthKernel")
+
+
+def runFill_J_MRegKernel(jMReg, energyWeight, jMRegHeight, jMRegWidth, graph, graphTransforms, graphSize, knnIdxs):
+    _sync(lib().afx_fill_j_mreg(_p(jMReg), float(energyWeight), int(jMRegHeight), int(jMRegWidth), _p(graph),
+                                int(graphSize), _p(knnIdxs), int(knnIdxs.shape[-1]), _stream()), "runFill_J_MRegKernel")
+
+
+def runFill_r_DepthKernel(rDepth, energyWeight, corrIdxs, corrIdxsSize, canonMeshWarped, depthMesh, depthMeshNormals):
+    _sync(lib().afx_fill_r_depth(_p(rDepth), float(energyWeight), _p(corrIdxs), int(corrIdxsSize),
+                                 _p(canonMeshWarped), _p(depthMesh), _p(depthMeshNormals), _stream()),
+          "runFill_r_DepthKernel")
+
+
+def runFill_r_MRegKernel(rMReg, energyWeight, graph, graphTransforms, graphSize, knnIdxs):
+    _sync(lib().afx_fill_r_mreg(_p(rMReg), float(energyWeight), _p(graph), _p(graphTransforms), int(graphSize),
+                                _p(knnIdxs), int(knnIdxs.shape[-1]), _stream()), "runFill_r_MRegKernel")
+
+
+def runComputeJTJAndJTrContribJDepthKernel(jTJContribPairs, rowNumbers, jTJContribPairsSize, jTrContribElems,
+                                           jTrContribElemsSize, corrIdxs, corrIdxsSize, knnIdxs, knnWeights):
+    ws = _workspace(lib().afx_jtj_contrib_workspace_size(int(corrIdxsSize)))
+    _sync(lib().afx_jtj_contrib_depth(_p(jTJContribPairs), _p(rowNumbers), _p(jTJContribPairsSize),
+                                      _p(jTrContribElems), _p(jTrContribElemsSize), _p(corrIdxs), int(corrIdxsSize),
+                                      _p(knnIdxs), _p(knnWeights), int(knnIdxs.shape[-1]), _p(ws), ws.numel(),
+                                      _stream()), "runComputeJTJAndJTrContribJDepthKernel")
+
+
+def runComputeJTJAndJTrContribJMRegKernel(jTJContribPairs, rowNumbers, rowNumberOffset, jTJContribPairsSize,
+                                          jTrContribElems, jTrContribElemsSize, graphSize, knnIdxs):
+    ws = _workspace(lib().afx_jtj_contrib_workspace_size(int(graphSize)))
+    _sync(lib().afx_jtj_contrib_mreg(_p(jTJContribPairs), _p(rowNumbers), int(rowNumberOffset),
+                                     _p(jTJContribPairsSize), _p(jTrContribElems), _p(jTrContribElemsSize),
+                                     int(graphSize), _p(knnIdxs), int(knnIdxs.shape[-1]), _p(ws), ws.numel(),
+                                     _stream()), "runComputeJTJAndJTrContribJMRegKernel")
+
+
+def runMultiplyJTJContribPairsKernel(multipliedContribPairs, jTJContribPairs, rowNumbers, jTJContribPairsSize, J,
+                                     jWidth):
+    _sync(lib().afx_multiply_jtj_pairs(_p(multipliedContribPairs), _p(jTJContribPairs), _p(rowNumbers),
+                                       int(jTJContribPairsSize), _p(J), int(jWidth), _stream()),
+          "runMultiplyJTJContribPairsKernel")
+
+
+def runMultiplyJTrContribElemsKernel(multipliedJTrContribElems, jTrContribElems, jTrContribElemsSize, J, r, jWidth):
+    _sync(lib().afx_multiply_jtr_elems(_p(multipliedJTrContribElems), _p(jTrContribElems), int(jTrContribElemsSize),
+                                       _p(J), _p(r), int(jWidth), _stream()), "runMultiplyJTrContribElemsKernel")
+
+
+def runFillJTJKernel(JTJ, jTJElemsCoords, jTJElems, jTJElemsSize, jTJWidth):
+    _sync(lib().afx_fill_jtj(_p(JTJ), _p(jTJElemsCoords), _p(jTJElems), int(jTJElemsSize), int(jTJWidth), _stream()),
+          "runFillJTJKernel")
+
+
+def runFillJTrKernel(JTr, jTrElemsCoordinates, jTrElems, jTrElemsSize):
+    _sync(lib().afx_fill_jtr(_p(JTr), _p(jTrElemsCoordinates), _p(jTrElems), int(jTrElemsSize), _stream()),
+          "runFillJTrKernel")
+
+
+def linearSolverLUStable(handle, n, Acopy, lda, b, ipiv, x):
+    """x = A^-1 b (A column-major with leading dimension lda, left unchanged); False where getrf would
+    fail.  `handle` stands in for the cuSOLVER handle and is not used."""
+    ws = _workspace(lib().afx_lu_solve_workspace_size(int(n), int(lda)))
+    st = lib().afx_lu_solve(_p(x), _p(Acopy), int(n), int(lda), _p(b), _p(ipiv), _p(ws), ws.numel(), _stream())
+    if st == 4:  # AFX_ERR_SINGULAR
+        return False
+    _sync(st, "linearSolverLUStable")
+    return True
