@@ -220,3 +220,46 @@ def test_oracle_undistort_linear_is_a_convex_blend():
     out = O.undistort_depth(np.full((60, 80), 1.5, np.float32), m.ravel(), 0)
     assert np.all(out[inside] == np.float32(1.5))
     assert np.all(out[~inside] <= 1.5)
+
+
+def test_decoder_survives_corrupt_files():
+    """Random byte changes and truncations of valid PNG / TIFF files (PNG chunk CRCs recomputed for most,
+    so the damage reaches the inflater and the filters): every call returns a status, and a file that
+    still decodes gives an image of the size its header states."""
+    import ctypes as C
+    from volumefusion_gb300._lib import lib
+    rng = np.random.default_rng(21)
+    img = ((np.cumsum(rng.integers(0, 4, (30, 40)), axis=1) * 7) % 65536).astype(np.uint16)
+    bases = [D.png(img, 16, -1), D.png(img, 16, 4, level=0), D.png(img, 16, 2, interlace=True),
+             D.tiff(img, 16, 5, 2, rows_per_strip=7), D.tiff(img, 16, 8, 1, rows_per_strip=13, big_endian=True),
+             D.tiff(img, 16, 32773)]
+
+    def fix_crcs(b):
+        b, pos = bytearray(b), 8
+        while pos + 12 <= len(b):
+            ln = struct.unpack(">I", bytes(b[pos:pos + 4]))[0]
+            if pos + 12 + ln > len(b):
+                break
+            b[pos + 8 + ln:pos + 12 + ln] = struct.pack(">I", zlib.crc32(bytes(b[pos + 4:pos + 8 + ln])) & 0xFFFFFFFF)
+            pos += 12 + ln
+        return bytes(b)
+
+    out = np.zeros(1 << 20, np.uint16)
+    w, h = C.c_int(), C.c_int()
+    seen = set()
+    for it in range(3000):
+        b = bytearray(bases[it % len(bases)])
+        for _ in range(int(rng.integers(1, 6))):
+            b[int(rng.integers(0, len(b)))] = int(rng.integers(0, 256))
+        if rng.random() < 0.3:
+            b = b[:int(rng.integers(1, len(b)))]
+        b = bytes(b)
+        if b[:4] == b"\x89PNG" and rng.random() < 0.7:
+            b = fix_crcs(b)
+        buf = np.frombuffer(b, np.uint8)
+        rc = lib().afx_decode_depth_image(buf.ctypes.data, buf.size, out.ctypes.data, out.size, C.byref(w), C.byref(h))
+        assert rc in (0, 1, 2, 6), rc
+        if rc == 0:
+            assert 0 < w.value * h.value <= out.size
+        seen.add(rc)
+    assert {0, 1} <= seen
