@@ -1074,6 +1074,10 @@ def main():
     last = FrameStats.from_buffer_copy(bytes(stats_host[(clip - 1) * C.sizeof(FrameStats):].numpy()))
     if last.error:
         raise RuntimeError("frame error flags in the end-to-end run: %d" % last.error)
+    # Gauss-Newton iterations (each with one PCG solve) over the step's frames
+    fsz = C.sizeof(FrameStats)
+    raw_stats = bytes(stats_host.numpy())
+    gn_step = sum(FrameStats.from_buffer_copy(raw_stats[f * fsz:(f + 1) * fsz]).gn_iterations_done for f in range(clip))
     lat = []
     run_e2e(args.steps, lat)
     barrier()
@@ -1177,14 +1181,14 @@ def main():
     if pick != dom:
         roof["note"] = "dominant stage is %s (%.3f ms/frame), latency-bound" % (dom, per_frame[dom])
     # the dominant kernel, which no bandwidth roofline describes: one cluster launch per frame running
-    # every Gauss-Newton iteration (5) with its PCG (10 iterations, two cluster barriers each)
-    gn_iters = max(1, int(st["gn_iterations_done"]))
-    pcg_iters = gn_iters * 10
+    # every Gauss-Newton iteration (up to 5) with its PCG (10 iterations, two cluster barriers each)
+    pcg_mean = max(1e-9, 10.0 * gn_step / clip)
     roof["dominant_kernel"] = {
         "kernel": "gn_loop_kernel", "ms_per_frame": per_frame.get("gn_loop", 0.0),
-        "bound": "latency: cluster barriers and binary64 reduction chains (1.6 MB of DRAM traffic per launch)",
-        "gn_iterations_last_frame": gn_iters, "pcg_iterations_per_frame": pcg_iters,
-        "us_per_pcg_iteration_upper_bound": 1000.0 * per_frame.get("gn_loop", 0.0) / pcg_iters,
+        "bound": "latency: cluster barriers and the dot products' reduction chains (1.6 MB of DRAM traffic per launch)",
+        "gn_iterations_last_frame": int(st["gn_iterations_done"]), "gn_iterations_per_step": gn_step,
+        "pcg_iterations_per_frame_mean": pcg_mean,
+        "us_per_pcg_iteration_upper_bound": 1000.0 * per_frame.get("gn_loop", 0.0) / pcg_mean,
         "cluster_barriers_per_pcg_iteration": 2}
     # every stage with an exact byte count, against the same peak
     roof["stages"] = {k: {"ms_per_frame": per_frame.get(k, 0.0), "algorithmic_bytes": v,

@@ -134,14 +134,18 @@ def test_global_memory_pcg_on_a_tiled_system():
     for c in range(copies):
         assert np.array_equal(x[c], x[0]), c
         assert np.linalg.norm(x[c] - x_o) <= 3e-2 * np.linalg.norm(x_o)
-    # the same solve through the shared-memory path (the single system): the two paths sum in
-    # different orders, and on this stiff system (condition number ~5e6) binary32 iterates part by
-    # about 1e-3 relative
+    # the same solve through the shared-memory path (the single system): the two paths sum their
+    # dot products in different orders and arithmetics (binary64 here, double-binary32 there), so a
+    # step size can round to a neighbouring binary32 value.  This system is stiff (condition number
+    # ~5e6): in a binary32 emulation of these ten iterations, moving the first step size by one ulp
+    # moves x by 2.2e-2 relative (1.1e-2 for the third or fourth).  Both paths are held to the
+    # oracle's binary64 PCG at 3e-2 above and in the test before; here they agree within the same.
     g1 = af.GaussNewtonSystem(m + 16, n + 8, 4, 8)
     g1.build(cu(s["mesh"]), cnt(m), cu(s["midx"].view(np.int32)), cu(s["mw"]), cu(s["corr"]), cnt(nc), cu(s["v1"]),
              cu(s["n1"]), cu(s["warped"]), cu(s["nodes"]), cu(s["T"]), cnt(n), cu(s["gidx"].view(np.int32)),
              s["lam_d"], s["lam_r"])
     x1 = g1.solve(10)[:6 * n].cpu().numpy()
-    assert np.linalg.norm(x[0] - x1) <= 1e-2 * np.linalg.norm(x1)
+    assert np.linalg.norm(x1 - x_o) <= 3e-2 * np.linalg.norm(x_o)
+    assert np.linalg.norm(x[0] - x1) <= 3e-2 * np.linalg.norm(x1)
     g.close()
     g1.close()

@@ -11,8 +11,8 @@
 // Diagonal blocks without any contribution keep the identity (runInitIdentityKernel).
 // J^T J depends only on the canonical geometry, weights and correspondences, so it is
 // assembled once per ICP iteration; J^T r is rebuilt every Gauss-Newton iteration.
-// The solve is a block-Jacobi PCG in one cooperative kernel: FP32 block SpMV, FP64 dot
-// products and FP64 6x6 block inverses.
+// The solve is a block-Jacobi PCG in one cooperative kernel: FP32 block SpMV, dot products in
+// double-binary32 (shared-memory path) or FP64 (global-memory path), FP64 6x6 block inverses.
 #include <cfloat>
 #include <cstring>
 #include <new>
@@ -528,7 +528,7 @@ __global__ void __launch_bounds__(128) diag_inverse_kernel(GnArgs a) {
 // are stored with st.global.cg and loaded with ld.global.cg, i.e. always from L2.
 // Per iteration:
 //   residuals + energies -> energy test and commit -> J^T r -> PCG (x = 0, block-Jacobi,
-//   FP32 block SpMV, FP64 dots, two cluster barriers per PCG iteration)
+//   FP32 block SpMV, double-float or FP64 dots, two cluster barriers per PCG iteration)
 //   -> T_pending -= [[x_rot]x, x_t; 0] -> re-warp the canonical vertices with T_pending.
 
 constexpr int kLoopThreads = 512;
@@ -560,13 +560,63 @@ AFX_D double dsmem_load(const double* p, unsigned rank) {
     return v;
 }
 
+// Double-binary32 ("double-float") arithmetic: a value is the unevaluated sum hi + lo of two
+// binary32 numbers with |lo| <= ulp(hi) / 2, about 48 significant bits.  A sum is the accurate
+// double-float addition of Hida, Li and Bailey's QD library (2001): Knuth's TwoSum (the exact
+// rounding error of a binary32 sum) on the high and the low parts, then Dekker's Fast2Sum to
+// renormalise; a product of two binary32 values is exact as p + fma(x, y, -p).  TwoSum's error term
+// is exact whatever the operand order, so df_add(a, b) and df_add(b, a) agree bit for bit and
+// every lane of a butterfly ends with the same total.  On this part a dependent binary64 add takes
+// ~150-200 cycles; a double-float add is a chain of ~8 binary32 operations.
+struct DF {
+    float hi, lo;
+};
+
+AFX_D DF two_sum(float a, float b) {
+    const float s = a + b, v = s - a;
+    return {s, (a - (s - v)) + (b - v)};
+}
+
+AFX_D DF fast_two_sum(float a, float b) {
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+
+AFX_D DF df_add(DF a, DF b) {
+    DF s = two_sum(a.hi, b.hi);
+    const DF t = two_sum(a.lo, b.lo);
+    s = fast_two_sum(s.hi, s.lo + t.hi);
+    return fast_two_sum(s.hi, s.lo + t.lo);
+}
+
+AFX_D DF df_prod(float x, float y) {
+    const float p = x * y;
+    return {p, fmaf(x, y, -p)};
+}
+
+AFX_D DF df_shfl_xor(DF v, int o) {
+    return {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+}
+
+// a / b rounded to binary32 (within about half an ulp): the binary32 quotient of the high parts,
+// corrected once by the remainder, which fma forms exactly.
+AFX_D float df_quotient(DF a, DF b) {
+    const float q = a.hi / b.hi;
+    if (q == 0.f || !isfinite(q)) return q;
+    const float r = (fmaf(-q, b.hi, a.hi) + a.lo) - q * b.lo;
+    return q + r / b.hi;
+}
+
+AFX_D bool df_zero_or_nan(DF v) { return v.hi == 0.f || v.hi != v.hi; }
+
 struct ClusterSums {
     double slot[2][4];            // this CTA's block sums, double-buffered across calls
     double warp[kLoopWarps * 4];  // per-warp sums
     double total[4];
     int phase;
     // PCG scalars, written by lane 0 of warp 0 and read by every thread after a __syncthreads
-    double rz, bnorm2;  // r.z of the current iterate, b.b
+    double rz, bnorm2;  // r.z of the current iterate, b.b (global-memory path)
+    DF rz_df, bn_df;    // the same in the shared-memory path
     float alpha, beta;
     int stop;
 };
@@ -812,6 +862,19 @@ AFX_D void dsmem_store_f64(double* local, unsigned rank, double v) {
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
     asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(ra), "d"(v) : "memory");
 }
+// A double-float into an 8-byte slot of CTA `rank` (hi at the lower address), and back from this
+// CTA's own slot.
+AFX_D void dsmem_store_df(double* local, unsigned rank, DF v) {
+    unsigned a = (unsigned)__cvta_generic_to_shared(local), ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+    asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(ra), "f"(v.hi), "f"(v.lo) : "memory");
+}
+AFX_D DF lds_df(const double* local) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(local);
+    DF v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.hi), "=f"(v.lo) : "r"(a) : "memory");
+    return v;
+}
 
 // Cluster sum through the slot arrays: the CTA's block total is written into slot[ph][rank] of
 // every CTA; after the barrier each CTA adds the slots in rank order.
@@ -904,27 +967,27 @@ AFX_D bool ds_stage(const GnBuffers& b, int n, const DsLayout& d, ClusterSums& c
     return true;
 }
 
-// FP64 dot products x[i] . y[i] of the CTA's own entries (cnt floats each, in shared memory),
-// summed over the cluster.  Warp 0 alone does binary64 work: lane l accumulates entries l, l + 32,
-// ... with fused multiply-adds (the product of two binary32 values is exact in binary64, so each
-// step rounds once, as product-then-add would), a butterfly gives the CTA's sum, and lane q sends
-// it into slot [ph][rank] of CTA q.  After the cluster barrier warp 0 of every CTA adds the slots in
-// one fixed tree, so all CTAs hold bit-identical totals.  Returns true in lane 0 of warp 0 only,
-// with the totals in t; the caller turns them into the scalars every thread reads after the next
-// __syncthreads.
+// Dot products x[i] . y[i] of the CTA's own entries (cnt floats each, in shared memory), summed
+// over the cluster in double-float arithmetic (about 48 bits; each product enters exactly).  Warp 0
+// alone does the work: lane l accumulates entries l, l + 32, ..., a butterfly gives the CTA's sum,
+// and lane q sends it into slot [ph][rank] of CTA q.  After the cluster barrier warp 0 of every CTA
+// adds the slots in one fixed tree, so all CTAs hold bit-identical totals.  Returns true in lane 0
+// of warp 0 only, with the totals in t; the caller turns them into the scalars every thread reads
+// after the next __syncthreads.
 template <int NV>
 AFX_D bool ds_dot(const float* const (&x)[NV], const float* const (&y)[NV], int cnt, const DsLayout& d, int& ph,
-                  double (&t)[NV]) {
+                  DF (&t)[NV]) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned rank = cluster_rank(), ncta = cluster_size();
     __syncthreads();  // the staged vectors are complete
     if (w == 0) {
 #pragma unroll
         for (int i = 0; i < NV; ++i) {
-            double s = 0.0;
-            for (int o = lane; o < cnt; o += 32) s = fma((double)x[i][o], (double)y[i][o], s);
-            s = warp_sum(s);
-            if (lane < (int)ncta) dsmem_store_f64(d.slot + (ph * kDsMaxCta + rank) * 4 + i, lane, s);
+            DF s = {0.f, 0.f};
+            for (int o = lane; o < cnt; o += 32) s = df_add(s, df_prod(x[i][o], y[i][o]));
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_xor(s, o));
+            if (lane < (int)ncta) dsmem_store_df(d.slot + (ph * kDsMaxCta + rank) * 4 + i, lane, s);
         }
     }
     cluster_barrier();
@@ -933,9 +996,10 @@ AFX_D bool ds_dot(const float* const (&x)[NV], const float* const (&y)[NV], int 
     if (w != 0) return false;
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-        double v = lane < (int)ncta ? d.slot[(p * kDsMaxCta + lane) * 4 + i] : 0.0;
+        DF v = {0.f, 0.f};
+        if (lane < (int)ncta) v = lds_df(d.slot + (p * kDsMaxCta + lane) * 4 + i);
 #pragma unroll
-        for (int o = kDsMaxCta / 2; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        for (int o = kDsMaxCta / 2; o > 0; o >>= 1) v = df_add(v, df_shfl_xor(v, o));
         t[i] = v;
     }
     return lane == 0;
@@ -946,7 +1010,7 @@ AFX_D bool ds_dot(const float* const (&x)[NV], const float* const (&y)[NV], int 
 // full copy of p and of z), A p of the own rows with up to 32 lanes per row (each summing a fixed
 // stride of the row's blocks, then a butterfly), p.Ap (cluster dot), the own x / r / z updates with
 // z sent to every CTA's copy, r.z (and r.r when a tolerance is set; cluster dot).  The step sizes
-// are formed once per CTA by lane 0 (f32_quotient) and read from shared memory.
+// are formed once per CTA by lane 0 (df_quotient) and read from shared memory.
 AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, int& ph) {
     const GnBuffers& b = L.g.b;
     const unsigned rank = cluster_rank(), ncta = cluster_size();
@@ -982,19 +1046,21 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
                 if (q != rank) dsmem_store_f32(d.z + (long)gnode * 6 + ei, q, zi);
         }
     }
+    // tol^2 in binary32, for the stopping test of lane 0 of warp 0
+    const float tol2 = (tol && threadIdx.x == 0) ? (float)(L.tol * L.tol) : 0.f;
     {
-        double t[2];
+        DF t[2];
         bool lead;
         if (tol) lead = ds_dot<2>({d.r, d.r}, {zown, d.r}, cnt, d, ph, t);
         else {
-            double t1[1];
+            DF t1[1];
             lead = ds_dot<1>({d.r}, {zown}, cnt, d, ph, t1);
             t[0] = t1[0];
-            t[1] = 0.0;
+            t[1] = {0.f, 0.f};
         }
         if (lead) {
-            cs.rz = t[0];
-            cs.bnorm2 = t[1];
+            cs.rz_df = t[0];
+            cs.bn_df = t[1];
             cs.stop = 0;
         }
     }
@@ -1025,10 +1091,10 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
             if (q < cnt && part == 0) d.ap[q] = acc;
         }
         {
-            double t[1];
+            DF t[1];
             if (ds_dot<1>({pown}, {d.ap}, cnt, d, ph, t)) {
-                cs.stop = zero_or_nan(t[0]) ? 1 : 0;
-                cs.alpha = cs.stop ? 0.f : f32_quotient(cs.rz, t[0]);
+                cs.stop = df_zero_or_nan(t[0]) ? 1 : 0;
+                cs.alpha = cs.stop ? 0.f : df_quotient(cs.rz_df, t[0]);
             }
         }
         __syncthreads();
@@ -1053,19 +1119,19 @@ AFX_D void pcg_ds(const LoopArgs& L, int n, const DsLayout& d, ClusterSums& cs, 
                 if (q != rank) dsmem_store_f32(d.z + (long)gnode * 6 + ei, q, zi);
         }
         {
-            double t[2];
+            DF t[2];
             bool lead;
             if (tol) lead = ds_dot<2>({d.r, d.r}, {zown, d.r}, cnt, d, ph, t);
             else {
-                double t1[1];
+                DF t1[1];
                 lead = ds_dot<1>({d.r}, {zown}, cnt, d, ph, t1);
                 t[0] = t1[0];
-                t[1] = 0.0;
+                t[1] = {0.f, 0.f};
             }
             if (lead) {
-                cs.beta = f32_quotient(t[0], cs.rz);
-                cs.rz = t[0];
-                cs.stop = (tol && t[1] <= L.tol * L.tol * cs.bnorm2) ? 1 : 0;
+                cs.beta = df_quotient(t[0], cs.rz_df);
+                cs.rz_df = t[0];
+                cs.stop = (tol && t[1].hi <= tol2 * cs.bn_df.hi) ? 1 : 0;
             }
         }
         __syncthreads();
