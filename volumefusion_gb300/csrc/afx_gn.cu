@@ -615,52 +615,10 @@ struct ClusterSums {
     double total[4];
     int phase;
     // PCG scalars, written by lane 0 of warp 0 and read by every thread after a __syncthreads
-    double rz, bnorm2;  // r.z of the current iterate, b.b (global-memory path)
-    DF rz_df, bn_df;    // the same in the shared-memory path
+    DF rz_df, bn_df;  // r.z of the current iterate, b.b (shared-memory path)
     float alpha, beta;
     int stop;
 };
-
-// A binary64 value as m * 2^e with m a binary32 in [1, 2): the 53-bit significand rounded to 24
-// bits (nearest, ties to even) with integer operations only.  Zero and subnormal doubles give 0,
-// infinities and NaN their binary32 counterparts (e = 0).
-AFX_D float split_f64(double x, int& e) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-    const unsigned sign = (unsigned)(b >> 63) << 31;
-    const int ex = (int)((b >> 52) & 0x7ff);
-    const unsigned long long man = b & 0xFFFFFFFFFFFFFull;
-    e = 0;
-    if (ex == 0) return __uint_as_float(sign);
-    if (ex == 0x7ff) return __uint_as_float(sign | 0x7f800000u | (man ? 0x400000u : 0u));
-    unsigned long long q = (man | (1ull << 52)) >> 29;
-    const unsigned long long rem = man & ((1ull << 29) - 1), half = 1ull << 28;
-    if (rem > half || (rem == half && (q & 1ull))) ++q;
-    int adj = 0;
-    if (q == (1ull << 24)) {
-        q >>= 1;
-        adj = 1;
-    }
-    e = ex - 1023 + adj;
-    return __uint_as_float(sign | (127u << 23) | (unsigned)(q & 0x7FFFFFull));
-}
-
-// (float)(a / b) to within about one binary32 ulp, without binary64 arithmetic: the operands are
-// split exactly into binary32 significands and powers of two (split_f64), the significands divided
-// in binary32 (correctly rounded) and the quotient scaled by the power of two.  The PCG step sizes
-// are binary32 in every use, and this part's binary64 division is slow: every thread of a CTA
-// dividing in binary64 cost more than the cluster barrier of the iteration.
-AFX_D float f32_quotient(double a, double b) {
-    int ea, eb;
-    const float ma = split_f64(a, ea), mb = split_f64(b, eb);
-    return ldexpf(ma / mb, ea - eb);
-}
-
-// pap == 0 or NaN, by the bit pattern (no binary64 comparison).
-AFX_D bool zero_or_nan(double v) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
-    return b == 0ull || b > 0x7FF0000000000000ull;
-}
-
 
 // Sums v[0..NV) over every thread of the cluster; all threads of all CTAs get identical totals.
 // Fixed-shape FP64 trees: butterfly within each warp, then over the CTA's warps, then over the
@@ -698,6 +656,68 @@ AFX_D void cluster_sum(double (&v)[NV], ClusterSums& cs) {
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < NV; ++i) v[i] = cs.total[i];
+    if (threadIdx.x == 0) cs.phase = ph ^ 1;
+}
+
+// Double-floats in this CTA's shared memory and in CTA `rank`'s (8-byte slots, hi first).
+AFX_D void sts_df(double* local, DF v) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(local);
+    asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.hi), "f"(v.lo) : "memory");
+}
+AFX_D DF lds_df_local(const double* local) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(local);
+    DF v;
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.hi), "=f"(v.lo) : "r"(a) : "memory");
+    return v;
+}
+AFX_D DF dsmem_load_df(const double* p, unsigned rank) {
+    unsigned local = (unsigned)__cvta_generic_to_shared(p), remote;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(remote) : "r"(local), "r"(rank));
+    DF v;
+    asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.hi), "=f"(v.lo) : "r"(remote) : "memory");
+    return v;
+}
+
+// cluster_sum in double-float arithmetic: the same fixed-shape trees (warp butterfly, the CTA's
+// warps, the CTAs by rank) with df_add, so every thread of every CTA gets identical totals.
+// Contains one cluster barrier.
+template <int NV>
+AFX_D void cluster_sum_df(DF (&v)[NV], ClusterSums& cs) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+        DF s = v[i];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s = df_add(s, df_shfl_xor(s, o));
+        if (lane == 0) sts_df(&cs.warp[w * 4 + i], s);
+    }
+    __syncthreads();
+    const int ph = cs.phase;
+    if (w == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            DF s = {0.f, 0.f};
+            if (lane < kLoopWarps) s = lds_df_local(&cs.warp[lane * 4 + i]);
+#pragma unroll
+            for (int o = kLoopWarps / 2; o > 0; o >>= 1) s = df_add(s, df_shfl_xor(s, o));
+            if (lane == 0) sts_df(&cs.slot[ph][i], s);
+        }
+    }
+    cluster_barrier();
+    if (w == 0) {
+        const unsigned ncta = cluster_size();
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            DF t = {0.f, 0.f};
+            if (lane < (int)ncta) t = dsmem_load_df(&cs.slot[ph][i], lane);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) t = df_add(t, df_shfl_xor(t, o));
+            if (lane == 0) sts_df(&cs.total[i], t);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = lds_df_local(&cs.total[i]);
     if (threadIdx.x == 0) cs.phase = ph ^ 1;
 }
 
@@ -862,19 +882,13 @@ AFX_D void dsmem_store_f64(double* local, unsigned rank, double v) {
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
     asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(ra), "d"(v) : "memory");
 }
-// A double-float into an 8-byte slot of CTA `rank` (hi at the lower address), and back from this
-// CTA's own slot.
+// A double-float into an 8-byte slot of CTA `rank` (hi at the lower address).
 AFX_D void dsmem_store_df(double* local, unsigned rank, DF v) {
     unsigned a = (unsigned)__cvta_generic_to_shared(local), ra;
     asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
     asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(ra), "f"(v.hi), "f"(v.lo) : "memory");
 }
-AFX_D DF lds_df(const double* local) {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(local);
-    DF v;
-    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.hi), "=f"(v.lo) : "r"(a) : "memory");
-    return v;
-}
+
 
 // Cluster sum through the slot arrays: the CTA's block total is written into slot[ph][rank] of
 // every CTA; after the barrier each CTA adds the slots in rank order.
@@ -997,7 +1011,7 @@ AFX_D bool ds_dot(const float* const (&x)[NV], const float* const (&y)[NV], int 
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
         DF v = {0.f, 0.f};
-        if (lane < (int)ncta) v = lds_df(d.slot + (p * kDsMaxCta + lane) * 4 + i);
+        if (lane < (int)ncta) v = lds_df_local(d.slot + (p * kDsMaxCta + lane) * 4 + i);
 #pragma unroll
         for (int o = kDsMaxCta / 2; o > 0; o >>= 1) v = df_add(v, df_shfl_xor(v, o));
         t[i] = v;
@@ -1233,7 +1247,7 @@ AFX_D void pcg_global(const LoopArgs& L, int n, ClusterSums& cs) {
     const bool glane = lane < 30;
     const int gstep = nw * 5;
     // x = 0, r = b, z = M^-1 r; rz = r.z, bb = b.b
-    double d2[2] = {0.0, 0.0};
+    DF d2[2] = {{0.f, 0.f}, {0.f, 0.f}};
     for (int base = gw * 5; base < n; base += gstep) {  // warp-uniform trip count
         const int node = base + grp;
         const bool act = glane && node < n;
@@ -1250,14 +1264,15 @@ AFX_D void pcg_global(const LoopArgs& L, int n, ClusterSums& cs) {
             __stcg(b.x + o, 0.f);
             __stcg(b.r + o, ji);
             __stcg(b.z + o, zi);
-            d2[0] += (double)ji * (double)zi;
-            d2[1] += (double)ji * (double)ji;
+            d2[0] = df_add(d2[0], df_prod(ji, zi));
+            d2[1] = df_add(d2[1], df_prod(ji, ji));
         }
     }
-    cluster_sum<2>(d2, cs);
+    cluster_sum_df<2>(d2, cs);
     // six lanes per node (entry i = lane % 6 of node group lane / 6, five groups per warp)
-    double rz = d2[0];
-    const double bnorm2 = d2[1];
+    DF rz = d2[0];
+    const DF bnorm2 = d2[1];
+    const float tol2 = L.tol > 0 ? (float)(L.tol * L.tol) : 0.f;
     float beta = 0.f;
     for (int it = 0; it < L.pcg_iters; ++it) {
         // p = z (first iteration) or z + beta p for the own entries, then A p once all are written
@@ -1270,19 +1285,19 @@ AFX_D void pcg_global(const LoopArgs& L, int n, ClusterSums& cs) {
             }
         }
         cluster_barrier();
-        double pap[1] = {0.0};
+        DF pap[1] = {{0.f, 0.f}};
         if (glane)
             for (int node = gw * 5 + grp; node < n; node += gstep) {
                 const long o = (long)node * 6 + ei;
                 const float api = spmv_entry(b, node, ei, b.p);
                 __stcg(b.ap + o, api);
-                pap[0] += (double)__ldcg(b.p + o) * (double)api;
+                pap[0] = df_add(pap[0], df_prod(__ldcg(b.p + o), api));
             }
-        cluster_sum<1>(pap, cs);
-        if (zero_or_nan(pap[0])) break;
-        const float alpha = f32_quotient(rz, pap[0]);
+        cluster_sum_df<1>(pap, cs);
+        if (df_zero_or_nan(pap[0])) break;
+        const float alpha = df_quotient(rz, pap[0]);
         // x += alpha p; r -= alpha A p; z = M^-1 r; r.z, r.r
-        double q2[2] = {0.0, 0.0};
+        DF q2[2] = {{0.f, 0.f}, {0.f, 0.f}};
         for (int base = gw * 5; base < n; base += gstep) {
             const int node = base + grp;
             const bool act = glane && node < n;
@@ -1302,14 +1317,14 @@ AFX_D void pcg_global(const LoopArgs& L, int n, ClusterSums& cs) {
             }
             if (act) {
                 __stcg(b.z + o, zi);
-                q2[0] += (double)rv * (double)zi;
-                q2[1] += (double)rv * (double)rv;
+                q2[0] = df_add(q2[0], df_prod(rv, zi));
+                q2[1] = df_add(q2[1], df_prod(rv, rv));
             }
         }
-        cluster_sum<2>(q2, cs);
-        beta = f32_quotient(q2[0], rz);
+        cluster_sum_df<2>(q2, cs);
+        beta = df_quotient(q2[0], rz);
         rz = q2[0];
-        if (L.tol > 0 && q2[1] <= L.tol * L.tol * bnorm2) break;
+        if (L.tol > 0 && q2[1].hi <= tol2 * bnorm2.hi) break;
     }
 }
 
