@@ -60,8 +60,8 @@ def nonrigid_capsules_256(n_frames=30, dims=(256, 256, 256), voxel=0.004):
 
 def precision_capsules_512(n_frames=30, graph_radius=0.009):
     """The capsule sequence in the precision form: 512^3 at 2 mm (the same 1.024 m cube) with FP16
-    TSDF values and uint16 weights (4 B/voxel, 537 MB), FP32 Jacobian/J^T J, FP64 PCG dot products
-    and 6x6 block inverses.  A 9 mm graph radius gives a graph that grows to ~6000 nodes over the
+    TSDF values and uint16 weights (4 B/voxel, 537 MB), FP32 Jacobian/J^T J, PCG dot products in
+    double-binary32 (about 48 bits) and FP64 6x6 block inverses.  A 9 mm graph radius gives a graph that grows to ~6000 nodes over the
     sequence (measured on the GPU: 11630 nodes at 6.5 mm, and node count goes as 1/r^2)."""
     cfg = nonrigid_capsules_256(n_frames=n_frames, dims=(512, 512, 512), voxel=0.002)
     cfg.update(name="precision_capsules_512", graph_radius=graph_radius, precision="fp16")
