@@ -9,6 +9,7 @@ import pytest
 torch = pytest.importorskip("torch")
 
 from oracle import pyoracle as O  # noqa: E402
+from _gn_system import gn_system  # noqa: E402
 
 pytestmark = pytest.mark.gpu
 
@@ -18,34 +19,7 @@ def cu(a, dtype=None):
     return (t.to(dtype) if dtype is not None else t).cuda()
 
 
-def _system(k, kreg, frame=14):
-    from volumefusion_gb300 import configs, synth
-    cfg = configs.small_nonrigid(n_frames=30)
-    mm0, K = synth.capsule_pair_frame(12, width=cfg["width"], height=cfg["height"], fx=float(cfg["K"][0, 0]),
-                                      fy=float(cfg["K"][1, 1]), cx=float(cfg["K"][0, 2]), cy=float(cfg["K"][1, 2]))
-    mm1, _ = synth.capsule_pair_frame(frame, width=cfg["width"], height=cfg["height"], fx=float(cfg["K"][0, 0]),
-                                      fy=float(cfg["K"][1, 1]), cx=float(cfg["K"][0, 2]), cy=float(cfg["K"][1, 2]))
-    d0, v0, n0, c = O.frame_prep(mm0, K)
-    dims = np.asarray(cfg["dims"], np.int32)
-    size = np.asarray(cfg["volume_size"], np.float32)
-    vs = size / dims.astype(np.float32)
-    S = int(np.prod(dims))
-    t0, w0 = np.full(S, -1, np.float32), np.zeros(S, np.float32)
-    O.integrate_rigid(t0, w0, d0, cfg["delta"], dims, vs, size, np.eye(3), c, K)
-    mesh = O.translate(O.sort_unique(O.mc_pointcloud(t0, w0, dims, vs, size)), c)
-    nodes, radii, T = O.build_graph(mesh, k, cfg["graph_radius"])
-    rng = np.random.default_rng(11)
-    T = T.copy()
-    T[:, 12:15] += rng.normal(0, 0.003, (len(T), 3)).astype(np.float32)
-    midx, mdist = O.knn(nodes, mesh, k)
-    mw = O.warp_weights(radii, midx, mdist)
-    warped = O.warp(mesh, T, midx, mw)
-    d1, v1, n1, _ = O.frame_prep(mm1, K)
-    corr = O.correspondences(warped, K, d1, v1, cfg["corr_thresh"])
-    gidx, gdist = O.knn(nodes, nodes, kreg, exclude_closest=True)
-    gidx, gdist = O.filter_disconnected(gidx, gdist, radii)
-    return dict(mesh=mesh, nodes=nodes, T=T, midx=midx, mw=mw, warped=warped, v1=v1, n1=n1, corr=corr, gidx=gidx,
-                lam_d=np.float32(cfg["lambda_depth"]), lam_r=np.float32(cfg["lambda_reg"]))
+_system = gn_system
 
 
 @pytest.mark.parametrize("k,kreg", [(6, 4), (4, 8)])
@@ -135,11 +109,11 @@ def test_global_memory_pcg_on_a_tiled_system():
         assert np.array_equal(x[c], x[0]), c
         assert np.linalg.norm(x[c] - x_o) <= 3e-2 * np.linalg.norm(x_o)
     # the same solve through the shared-memory path (the single system): the two paths sum their
-    # dot products in different orders and arithmetics (binary64 here, double-binary32 there), so a
-    # step size can round to a neighbouring binary32 value.  This system is stiff (condition number
-    # ~5e6): in a binary32 emulation of these ten iterations, moving the first step size by one ulp
-    # moves x by 2.2e-2 relative (1.1e-2 for the third or fourth).  Both paths are held to the
-    # oracle's binary64 PCG at 3e-2 above and in the test before; here they agree within the same.
+    # SpMV rows and dot products in different orders, so a step size can round to a neighbouring
+    # binary32 value.  This system is stiff (condition number ~5e6): one ulp of one early step size
+    # moves ten binary32 PCG iterations by several 1e-3 relative, up to 2.2e-2 depending on the SpMV's
+    # summation order (tests/test_pcg_sensitivity.py).  Both paths are held to the oracle's binary64
+    # PCG at 3e-2 above and in the test before; here they agree within the same.
     g1 = af.GaussNewtonSystem(m + 16, n + 8, 4, 8)
     g1.build(cu(s["mesh"]), cnt(m), cu(s["midx"].view(np.int32)), cu(s["mw"]), cu(s["corr"]), cnt(nc), cu(s["v1"]),
              cu(s["n1"]), cu(s["warped"]), cu(s["nodes"]), cu(s["T"]), cnt(n), cu(s["gidx"].view(np.int32)),
