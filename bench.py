@@ -163,12 +163,29 @@ class ClockSampler(threading.Thread):
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def dist_setup(n):
+def dist_setup(n, backend="nccl"):
+    """The process group of an N-replica run launched by torchrun (one rank per GPU), or None."""
     if n <= 1 or "RANK" not in os.environ:
         return None
     import torch.distributed as dist
-    dist.init_process_group("nccl")
+    dist.init_process_group(backend)
     return dist
+
+
+def max_over_ranks(x, dist, device):
+    """The largest x over the ranks, on every rank (x itself without a process group): the timed
+    region of an N-replica run is the slowest rank's."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if dist:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, max_seconds):
+    """Units per second of the whole job: every replica processes units_per_rank in the timed
+    region, which lasts as long as the slowest rank (weak scaling)."""
+    return world * units_per_rank / max_seconds
 
 
 def headline_config(cfg, clip, world):
@@ -989,10 +1006,7 @@ def main():
             dist.barrier()
 
     def reduce_max(x):
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        if dist:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return max_over_ranks(x, dist, "cuda")
 
     def run_device(session, steps):
         """`steps` passes over the sequence, each from an empty volume."""
@@ -1027,7 +1041,7 @@ def main():
     launches = s.kernel_launches() - l0
     ms = reduce_max(ev0.elapsed_time(ev1))
     frames = args.steps * clip
-    fps = world * frames / (ms / 1000.0)
+    fps = whole_job_rate(frames, world, ms / 1000.0)
     # per-stage breakdown: the same number of steps again, with CUDA events around each stage
     s.set_timing(True)
     s.stage_times(reset=True)
@@ -1070,7 +1084,7 @@ def main():
     t0 = time.perf_counter()
     run_e2e(args.steps)
     barrier()
-    e2e_fps = world * frames / reduce_max(time.perf_counter() - t0)
+    e2e_fps = whole_job_rate(frames, world, reduce_max(time.perf_counter() - t0))
     last = FrameStats.from_buffer_copy(bytes(stats_host[(clip - 1) * C.sizeof(FrameStats):].numpy()))
     if last.error:
         raise RuntimeError("frame error flags in the end-to-end run: %d" % last.error)
