@@ -914,7 +914,7 @@ def served_arm(args, rank):
         want = frames_per * sum(s is not None for s in sids)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        host_s = 0.0  # time the driver loop spends inside submit and poll (host work per frame)
+        host_s = 0.0  # time the submitting loop spends inside submit and poll (host work per frame)
         while got < want and time.perf_counter() - t0 < 120.0:
             for k, sid in enumerate(sids):
                 while sid is not None and sent[k] < frames_per:
