@@ -224,6 +224,7 @@ def cpu_model():
 def cpu_baseline(cfg, frames_np, n_frames):
     """Oracle port of the reference path on the host cores (all threads)."""
     from oracle import pyoracle as O
+    O.set_threads(os.cpu_count() or 1)
     o = O.Fusion(dict(cfg))
     o.process(frames_np[0])
     t0 = time.perf_counter()
@@ -371,6 +372,7 @@ def run_reference(args):
     cfg = configs.nonrigid_capsules_256(n_frames=N_FRAMES)
     frames_np = configs.capsule_frames(cfg)
     from oracle import pyoracle as O
+    O.set_threads(os.cpu_count() or 1)  # every host thread, whatever the launcher set
 
     clip = max(1, min(args.clip, N_FRAMES))
 
@@ -388,7 +390,7 @@ def run_reference(args):
     dt = sum(step() for _ in range(args.steps))
     n = args.steps * clip
     fps = n / dt
-    cores = os.cpu_count()
+    cores = O.threads()
     host = cpu_model()
     line = {
         "impl": "reference", "metric": "nonrigid_frames_per_s_256", "value": fps, "unit": "frames/s",
@@ -1216,7 +1218,8 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline and args.cpu_frames > 0:
         v, dt = cpu_baseline(cfg, frames_np, args.cpu_frames)
-        cpu = {"value": v, "unit": "frames/s", "cores": os.cpu_count(), "kind": "port", "cpu": cpu_model(),
+        from oracle import pyoracle as O
+        cpu = {"value": v, "unit": "frames/s", "cores": O.threads(), "kind": "port", "cpu": cpu_model(),
                "sample": "frames 1..%d of the sequence after the rigid frame 0 (%.1f s), all host threads"
                          % (args.cpu_frames, dt)}
         ref_stages = reference_cpu_stages(cfg, frames_np)

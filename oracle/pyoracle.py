@@ -37,6 +37,8 @@ def lib():
         L = C.CDLL(LIB_PATH)
         sig = {
             "vfo_expf": (C.c_float, [C.c_float]),
+            "vfo_set_threads": (None, [C.c_int]),
+            "vfo_threads": (C.c_int, []),
             "vfo_f2i_rz": (C.c_int, [C.c_float]),
             "vfo_depth_from_mm": (None, [u16p, C.c_long, f32p]),
             "vfo_filter_depth": (None, [f32p, C.c_long, C.c_float]),
@@ -165,6 +167,17 @@ def kcol(K):
 
 
 I3 = kcol(np.eye(3))
+
+
+def set_threads(n):
+    """OpenMP threads of the oracle's parallel loops for later calls from this thread (a launcher
+    such as torchrun may have set OMP_NUM_THREADS=1 for its processes)."""
+    lib().vfo_set_threads(int(n))
+
+
+def threads():
+    """OpenMP threads the oracle's parallel loops use now."""
+    return int(lib().vfo_threads())
 
 
 def expf(x):

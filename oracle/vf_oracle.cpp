@@ -205,6 +205,10 @@ struct P3 {
 
 extern "C" {
 
+void vfo_set_threads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
+
+int vfo_threads(void) { return omp_get_max_threads(); }
+
 // Own exp: Cody-Waite range reduction x = k*ln2 + r (ln2 split into a 16-bit head and
 // a tail), then a degree-7 Taylor polynomial for e^r by Horner with fused
 // multiply-adds, then scaling by 2^k in two exact steps.  Faithful (<= 1 ulp).

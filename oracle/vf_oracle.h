@@ -37,6 +37,11 @@ extern "C" {
 float vfo_expf(float x);
 int vfo_f2i_rz(VFO_REAL x);
 
+/* OpenMP threads of the oracle's parallel loops (n < 1: one), and the current count.  A launcher
+ * may have set OMP_NUM_THREADS for its processes; a caller that wants every host thread sets it. */
+void vfo_set_threads(int n);
+int vfo_threads(void);
+
 /* ---- frame preparation (src/VertexManipulation.cu, src/BilateralFilter.cu) ---- */
 void vfo_depth_from_mm(const uint16_t* mm, long n, VFO_REAL* out);
 void vfo_filter_depth(VFO_REAL* depth, long n, VFO_REAL threshold);

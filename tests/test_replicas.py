@@ -1,9 +1,9 @@
 """bench.py's N-replica path on the CPU, launched the way an N-GPU run is (torchrun, one process per
 rank, rendezvous on 127.0.0.1), with the gloo backend and world size 2: the timed region is the
 slowest rank's on every rank, `value` is the whole job's rate (weak scaling: every replica fuses the
-same sequence), and the reference arm runs and prints on rank 0 alone while the other ranks exit 0
-without work.  The path does not shard inside a session, so there is no data-path collective to
-test: replicas only."""
+same sequence), and the reference arm runs and prints on rank 0 alone, on every host thread, while
+the other ranks exit 0 without work.  The path does not shard inside a session, so there is no
+data-path collective to test: replicas only."""
 import json
 import os
 import socket
@@ -39,10 +39,10 @@ def _json_lines(text):
     return out
 
 
-def test_slowest_rank_and_whole_job_rate_gloo():
-    p = _torchrun([os.path.join("tests", "_replica_worker.py")])
+def test_slowest_rank_and_whole_job_rate_gloo(tmp_path):
+    p = _torchrun([os.path.join("tests", "_replica_worker.py"), str(tmp_path)])
     assert p.returncode == 0, p.stdout + p.stderr
-    lines = sorted(_json_lines(p.stdout), key=lambda d: d["rank"])
+    lines = [json.loads((tmp_path / ("rank%d.json" % r)).read_text()) for r in range(2)]
     assert [d["rank"] for d in lines] == [0, 1]
     for d in lines:
         assert d["world"] == 2
@@ -58,3 +58,5 @@ def test_reference_arm_prints_once_from_rank_zero():
     d = lines[0]
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+    # torchrun sets OMP_NUM_THREADS=1 for its processes; the reference arm still uses every host thread
+    assert d["cpu_baseline"]["cores"] == os.cpu_count()
